@@ -1,0 +1,229 @@
+/*
+ * tk_heff.h -- C ABI of the GB300 two-site H_eff library (libtk_heff.so).
+ *
+ * Every entry point takes plain pointers and sizes.  Host-side structures
+ * (tk_qindex, tk_bst, tk_env) describe tensors in the reference's own
+ * formats; device buffers are passed as raw device pointers and streams as
+ * the `cudaStream_t` value cast to `void*` (NULL = legacy default stream).
+ * Errors are reported as tk_status codes, never by aborting; the message of
+ * the last failure on the calling thread is returned by tk_last_error().
+ *
+ * Reference interfaces replaced (paths inside kyungminlee/tensorkraft-design):
+ *   build_heff_two_site        tk-dmrg/src/environments/mod.rs:491-602
+ *   Environment (dense)        tk-dmrg/src/environments/mod.rs:24-103
+ *   BlockSparseTensor          tk-symmetry/src/block_sparse.rs:21-159
+ *   FlatBlockStorage           tk-symmetry/src/flat_storage.rs:14-167
+ *   QIndex / PackedSectorKey   tk-symmetry/src/sector_key.rs:18-148
+ *   LinAlgBackend::gemm        tk-linalg/src/traits.rs:114-121
+ *   SparseLinAlgBackend        tk-linalg/src/traits.rs:190-205
+ *   IterativeEigensolver       tk-dmrg/src/eigensolver/mod.rs:22-55
+ *   LanczosSolver              tk-dmrg/src/eigensolver/mod.rs:58-164
+ *   LinAlgError / DmrgError    tk-linalg/src/error.rs:5-39, tk-dmrg/src/error.rs:9-59
+ */
+#ifndef TK_HEFF_H
+#define TK_HEFF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  TK_ERR_CUDA carries the failing CUDA call and its message
+ * in tk_last_error(), the same (op, detail) pair as LinAlgError::CudaError
+ * (tk-linalg/src/error.rs:30-31). */
+typedef int32_t tk_status;
+#define TK_OK                   0
+#define TK_ERR_INVALID_ARG      1
+#define TK_ERR_SECTOR_MISMATCH  2
+#define TK_ERR_OOM              3
+#define TK_ERR_CUDA             4
+#define TK_ERR_TIMEOUT          5
+#define TK_ERR_CANCELLED        6
+#define TK_ERR_UNSUPPORTED      7
+
+/* Quantum-number kinds (tk-symmetry/src/builtins.rs:12-152).  TK_QN_U1U1 is
+ * new: (N, 2Sz) with 8 bits per component, component 0 in the low byte. */
+#define TK_QN_U1      1
+#define TK_QN_Z2      2
+#define TK_QN_U1Z2    3
+#define TK_QN_U1WIDE  4
+#define TK_QN_U1U1    5
+
+/* LegDirection (tk-symmetry/src/quantum_number.rs:49-54). */
+#define TK_LEG_INCOMING 0
+#define TK_LEG_OUTGOING 1
+
+/* Arithmetic of the sector GEMMs inside one matvec. */
+#define TK_PREC_FP64    0  /* FP64 throughout */
+#define TK_PREC_BF16X3  1  /* operands split into bf16 hi+lo, three products, fp32 accumulation */
+
+typedef struct tk_ctx tk_ctx;
+typedef struct tk_heff2_plan tk_heff2_plan;
+
+/* QIndex: sectors sorted by quantum number, charges are `ncomp` int32 per
+ * sector (ncomp = 2 for U1Z2 and U1U1, else 1). */
+typedef struct {
+    int32_t n_sectors;
+    const int32_t* charges;
+    const int64_t* dims;
+} tk_qindex;
+
+/* BlockSparseTensor in FlatBlockStorage form, host memory.  Keys ascending,
+ * packed as PackedSectorKey (leg l at bits l*BIT_WIDTH); each block
+ * row-major with the dims its key selects in `legs`. */
+typedef struct {
+    int32_t qn_kind;
+    int32_t rank;
+    const tk_qindex* legs;
+    const int8_t* leg_dirs;
+    const int32_t* flux;
+    int64_t n_blocks;
+    const uint64_t* keys;
+    const int64_t* block_offsets;
+    const double* data;
+} tk_bst;
+
+/* Environment: dense (bra, w, ket) row-major, host memory. */
+typedef struct {
+    tk_qindex bra;
+    tk_qindex mpo;
+    tk_qindex ket;
+    const double* data;
+} tk_env;
+
+/* Library context bound to one CUDA device. */
+tk_status tk_ctx_create(int32_t device, tk_ctx** out);
+void tk_ctx_destroy(tk_ctx* ctx);
+/* Message of the last failure on this thread ("" if none). */
+const char* tk_last_error(void);
+/* Library version, for the loader check. */
+int32_t tk_version(void);
+
+/*
+ * Two-site H_eff plan: replaces build_heff_two_site
+ * (tk-dmrg/src/environments/mod.rs:491-602).  Uploads the non-zero sector
+ * slabs of L and R, fuses W_i*W_j, and flattens every sector GEMM of one
+ * matvec into device task tables.  `psi_flux` selects the two-site sectors
+ * with q(s_i)+q(s_j)+q(a_L)-q(a_R) == psi_flux; NULL keeps every sector
+ * combination, which makes the plan equal to the reference's dense matrix
+ * on every input.  The plan owns all device memory it uses.
+ */
+tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r,
+                               const tk_bst* w_i, const tk_bst* w_j,
+                               const int32_t* psi_flux, int32_t precision,
+                               tk_heff2_plan** out);
+void tk_heff2_plan_destroy(tk_heff2_plan* plan);
+
+/* dense_dim = d_i*d_j*D_L*D_R (the closure's `dim`); block_dim = length of
+ * the block-layout vector; n_blocks = two-site blocks. */
+tk_status tk_heff2_dims(const tk_heff2_plan* plan, int64_t* dense_dim, int64_t* block_dim,
+                        int64_t* n_blocks);
+/* The two-site block layout: packed keys (ascending) and element offsets. */
+tk_status tk_heff2_blocks(const tk_heff2_plan* plan, uint64_t* keys, int64_t* offsets);
+/* Algorithmic FP64 flops and bytes of one matvec, from the sector tables. */
+tk_status tk_heff2_cost(const tk_heff2_plan* plan, double* flops, double* bytes);
+tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
+
+/* Per-stage kernel timing for roofline reports (no reference counterpart;
+ * observability in the spirit of DMRGStats, tk-dmrg/src/sweep/mod.rs:85-111):
+ * runs `reps` complete matvecs y = H_eff x on `stream` -- the same launches
+ * as tk_heff2_apply -- with a CUDA event before, between and after the
+ * three stages, waits for each, and writes the mean milliseconds of stage 1
+ * (L x psi GEMMs), stage 2 (W_i W_j combine) and stage 3 (x R GEMMs) to
+ * ms[0..2] and the algorithmic flops of each stage to flops[0..2]. */
+tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream,
+                           int32_t reps, float* ms, double* flops);
+
+/* y = H_eff x on device vectors in the block layout; stream-ordered. */
+tk_status tk_heff2_apply(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream);
+/* The closure `Fn(&[f64], &mut [f64])`: host vectors in the dense
+ * (s_i, s_j, a_L, a_R) layout of length dense_dim; y fully overwritten.
+ * Synchronous. */
+tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y);
+/* Same on host vectors in the block layout (FlatBlockStorage), synchronous. */
+tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double* y);
+/* Dense <-> block layout conversion on the host. */
+tk_status tk_heff2_dense_to_flat(const tk_heff2_plan* plan, const double* dense, double* flat);
+tk_status tk_heff2_flat_to_dense(const tk_heff2_plan* plan, const double* flat, double* dense);
+
+/*
+ * Lanczos lowest eigenpair on the device: replaces
+ * LanczosSolver::lowest_eigenpair (tk-dmrg/src/eigensolver/mod.rs:80-164).
+ * Same start vector ((i*7+13)%97)/97-0.5 when x0 is NULL, full
+ * re-orthogonalisation, Sturm bisection for the eigenvalue; the Ritz vector
+ * is solved for (the reference leaves it unsolved) and the residual
+ * ||H x - E x|| is computed with an FP64 matvec.  With a split-precision
+ * plan, `refine` FP64 correction steps follow.  Vectors are in the block
+ * layout on the device.
+ */
+typedef struct {
+    int32_t krylov_dim;
+    int32_t max_restarts;
+    double tol;
+    int32_t refine;
+} tk_lanczos_cfg;
+
+typedef struct {
+    double eigenvalue;
+    double residual_norm;
+    int32_t converged;
+    int32_t matvec_count;
+    int32_t fp64_matvec_count;
+    int32_t restarts;
+} tk_eigen_result;
+
+tk_status tk_lanczos_lowest(tk_heff2_plan* plan, const tk_lanczos_cfg* cfg, const double* x0_dev,
+                            double* evec_dev, tk_eigen_result* out, void* stream);
+
+/*
+ * LinAlgBackend::gemm (tk-linalg/src/traits.rs:114-121) on device memory:
+ * C = alpha*op(A)*op(B) + beta*C with element strides as in MatRef/MatMut
+ * (tk-core/src/matview.rs:12-33).  `is_conjugated` is a no-op for f64.
+ */
+typedef struct {
+    const double* data;
+    int64_t rows, cols, row_stride, col_stride;
+    int32_t is_conjugated;
+} tk_mat;
+
+typedef struct {
+    double* data;
+    int64_t rows, cols, row_stride, col_stride;
+} tk_mat_mut;
+
+tk_status tk_gemm_f64(tk_ctx* ctx, double alpha, const tk_mat* a, const tk_mat* b, double beta,
+                      tk_mat_mut* c, void* stream);
+
+/*
+ * SparseLinAlgBackend::block_gemm (tk-linalg/src/traits.rs:200-204,
+ * tk-linalg/src/device/faer.rs:390-575) for rank-2 tensors: task per
+ * compatible (key_a, key_b) pair, contributions to the same output key
+ * summed, output keys ascending.  Host tensors in, host tensor out; `out`
+ * arrays are allocated by the library and released by tk_bst_free.
+ */
+typedef struct {
+    int32_t qn_kind;
+    int32_t rank;
+    tk_qindex legs[2];
+    int8_t leg_dirs[2];
+    int32_t flux[2];
+    int64_t n_blocks;
+    uint64_t* keys;
+    int64_t* block_offsets;
+    double* data;
+    int64_t total;
+} tk_bst_out;
+
+tk_status tk_block_gemm_f64(tk_ctx* ctx, const tk_bst* a, const tk_bst* b, tk_bst_out* out);
+void tk_bst_free(tk_bst_out* t);
+
+/* SparseLinAlgBackend::spmv (tk-linalg/src/traits.rs:193-198): y = A x for
+ * a rank-2 host tensor and host vectors (y fully overwritten). */
+tk_status tk_spmv_f64(tk_ctx* ctx, const tk_bst* a, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TK_HEFF_H */

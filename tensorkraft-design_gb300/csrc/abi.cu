@@ -1,0 +1,366 @@
+// abi.cu -- C ABI of libtk_heff (declared in include/tk_heff.h).
+//
+// Owns the CUDA context handling, device buffers and launch sequences.  All
+// entry points return status codes; failures leave a message retrievable with
+// tk_last_error() on the same thread.  Nothing here aborts or traps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "tc_gemm.cuh"
+#include "tk_internal.hpp"
+#include "tk_plan.cuh"
+
+namespace tk {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+tk_status cuda_fail(const char* op, cudaError_t e) {
+    set_error(std::string(op) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
+}
+
+namespace {
+
+// Switches to the context's device for the duration of a call and restores
+// the caller's current device afterwards.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = (cudaSetDevice(dev) == cudaSuccess);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+
+#define TK_CUDA(op)                                  \
+    do {                                             \
+        cudaError_t e_ = (op);                       \
+        if (e_ != cudaSuccess) return cuda_fail(#op, e_); \
+    } while (0)
+
+}  // namespace
+}  // namespace tk
+
+using namespace tk;
+
+
+extern "C" {
+
+int32_t tk_version(void) { return 1; }
+
+const char* tk_last_error(void) { return g_last_error.c_str(); }
+
+tk_status tk_ctx_create(int32_t device, tk_ctx** out) {
+    if (!out) {
+        set_error("tk_ctx_create: null out");
+        return TK_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return cuda_fail("cudaGetDeviceCount", e);
+    if (device < 0 || device >= n) {
+        set_error("tk_ctx_create: device index out of range");
+        return TK_ERR_INVALID_ARG;
+    }
+    tk_ctx* c = new (std::nothrow) tk_ctx;
+    if (!c) {
+        set_error("tk_ctx_create: host allocation failed");
+        return TK_ERR_OOM;
+    }
+    c->device = device;
+    *out = c;
+    return TK_OK;
+}
+
+void tk_ctx_destroy(tk_ctx* ctx) { delete ctx; }
+
+tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                               const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
+                               tk_heff2_plan** out) {
+    if (!ctx || !env_l || !env_r || !w_i || !w_j || !out) {
+        set_error("tk_heff2_plan_create: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    if (precision != TK_PREC_FP64 && precision != TK_PREC_BF16X3) {
+        set_error("tk_heff2_plan_create: unknown precision");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::unique_ptr<tk_heff2_plan> p(new (std::nothrow) tk_heff2_plan);
+    if (!p) {
+        set_error("tk_heff2_plan_create: host allocation failed");
+        return TK_ERR_OOM;
+    }
+    std::string err;
+    tk_status st = build_heff2_tables(*env_l, *env_r, *w_i, *w_j, psi_flux, kF64TileM, kF64TileN, p->host, err);
+    if (st != TK_OK) {
+        set_error("tk_heff2_plan_create: " + err);
+        return st;
+    }
+    DeviceGuard g(ctx->device);
+    if (!g.ok) {
+        set_error("tk_heff2_plan_create: cudaSetDevice failed");
+        return TK_ERR_CUDA;
+    }
+    p->device = ctx->device;
+    const Heff2Tables& H = p->host;
+    TK_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    TK_CUDA(p->lbuf.upload(H.lbuf));
+    TK_CUDA(p->rbuf.upload(H.rbuf));
+    TK_CUDA(p->t1.alloc((size_t)std::max<int64_t>(H.t1_total, 1)));
+    TK_CUDA(p->t2.alloc((size_t)std::max<int64_t>(H.t2_total, 1)));
+    TK_CUDA(p->g1.upload(H.g1));
+    TK_CUDA(p->g3.upload(H.g3));
+    TK_CUDA(p->jobs.upload(H.jobs));
+    TK_CUDA(p->terms.upload(H.terms));
+    p->n_jobs = (int)H.jobs.size();
+    p->precision = TK_PREC_FP64;
+    if (precision != TK_PREC_FP64) {
+        tk_status s2 = tk_heff2_set_precision(p.get(), precision);
+        if (s2 != TK_OK) return s2;
+    }
+    *out = p.release();
+    return TK_OK;
+}
+
+void tk_heff2_plan_destroy(tk_heff2_plan* plan) {
+    if (!plan) return;
+    DeviceGuard g(plan->device);
+    delete plan;
+}
+
+tk_status tk_heff2_dims(const tk_heff2_plan* plan, int64_t* dense_dim, int64_t* block_dim, int64_t* n_blocks) {
+    if (!plan) {
+        set_error("tk_heff2_dims: null plan");
+        return TK_ERR_INVALID_ARG;
+    }
+    const Heff2Tables& H = plan->host;
+    if (dense_dim) *dense_dim = H.d_i * H.d_j * H.d_l * H.d_r;
+    if (block_dim) *block_dim = H.total;
+    if (n_blocks) *n_blocks = (int64_t)H.keys.size();
+    return TK_OK;
+}
+
+tk_status tk_heff2_blocks(const tk_heff2_plan* plan, uint64_t* keys, int64_t* offsets) {
+    if (!plan) {
+        set_error("tk_heff2_blocks: null plan");
+        return TK_ERR_INVALID_ARG;
+    }
+    const Heff2Tables& H = plan->host;
+    if (keys) std::copy(H.keys.begin(), H.keys.end(), keys);
+    if (offsets) std::copy(H.blk_off.begin(), H.blk_off.end(), offsets);
+    return TK_OK;
+}
+
+tk_status tk_heff2_cost(const tk_heff2_plan* plan, double* flops, double* bytes) {
+    if (!plan) {
+        set_error("tk_heff2_cost: null plan");
+        return TK_ERR_INVALID_ARG;
+    }
+    const Heff2Tables& H = plan->host;
+    if (flops) *flops = H.g1.flops + H.comb_flops + H.g3.flops;
+    if (bytes) *bytes = H.alg_bytes;
+    return TK_OK;
+}
+
+tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision) {
+    if (!plan) {
+        set_error("tk_heff2_set_precision: null plan");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (precision == TK_PREC_FP64) {
+        plan->precision = precision;
+        return TK_OK;
+    }
+    if (precision != TK_PREC_BF16X3) {
+        set_error("tk_heff2_set_precision: unknown precision");
+        return TK_ERR_INVALID_ARG;
+    }
+    DeviceGuard g(plan->device);
+    if (!plan->tc) {
+        std::string err;
+        std::unique_ptr<TcPlan, TcPlanDeleter> tc;
+        tk_status st = tc_plan_create(plan->host, plan->lbuf.p, plan->rbuf.p, tc, err);
+        if (st != TK_OK) {
+            set_error("tk_heff2_set_precision: " + err);
+            return st;
+        }
+        plan->tc = std::move(tc);
+    }
+    plan->precision = precision;
+    return TK_OK;
+}
+
+// The FP64 matvec: three stream-ordered launches.
+static tk_status apply_fp64(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s) {
+    TK_CUDA(launch_gemm_f64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p, x, p->t1.p, s));
+    TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
+    TK_CUDA(launch_gemm_f64(p->g3.tiles.p, p->g3.n_tiles, p->g3.tasks.p, p->g3.segs.p, p->t2.p, p->rbuf.p, y, s));
+    return TK_OK;
+}
+
+tk_status tk_heff2_apply_prec(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s, int precision) {
+    if (precision == TK_PREC_BF16X3) {
+        std::string err;
+        cudaError_t e = tc_apply(*p->tc, p->host, p->jobs.p, p->n_jobs, p->terms.p, x, y, s, err);
+        if (e != cudaSuccess) return cuda_fail(err.c_str(), e);
+        return TK_OK;
+    }
+    return apply_fp64(p, x, y, s);
+}
+
+tk_status tk_heff2_apply(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream) {
+    if (!plan || (!x_dev && plan->host.total > 0) || (!y_dev && plan->host.total > 0)) {
+        set_error("tk_heff2_apply: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (plan->host.total == 0) return TK_OK;
+    DeviceGuard g(plan->device);
+    return tk_heff2_apply_prec(plan, x_dev, y_dev, (cudaStream_t)stream, plan->precision);
+}
+
+static tk_status ensure_host_staging(tk_heff2_plan* p) {
+    size_t n = (size_t)std::max<int64_t>(p->host.total, 1);
+    if (!p->hx.p) TK_CUDA(p->hx.alloc(n));
+    if (!p->hy.p) TK_CUDA(p->hy.alloc(n));
+    if (!p->pin_x) TK_CUDA(cudaMallocHost(&p->pin_x, sizeof(double) * n));
+    if (!p->pin_y) TK_CUDA(cudaMallocHost(&p->pin_y, sizeof(double) * n));
+    return TK_OK;
+}
+
+tk_status tk_heff2_dense_to_flat(const tk_heff2_plan* plan, const double* dense, double* flat) {
+    if (!plan || !dense || !flat) {
+        set_error("tk_heff2_dense_to_flat: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    const Heff2Tables& H = plan->host;
+    for (const SubMap& m : H.submaps)
+        for (int32_t r = 0; r < m.rows; ++r)
+            std::memcpy(flat + m.flat_off + (int64_t)r * m.cols, dense + m.dense_off + (int64_t)r * H.d_r,
+                        sizeof(double) * m.cols);
+    return TK_OK;
+}
+
+tk_status tk_heff2_flat_to_dense(const tk_heff2_plan* plan, const double* flat, double* dense) {
+    if (!plan || !dense || !flat) {
+        set_error("tk_heff2_flat_to_dense: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    const Heff2Tables& H = plan->host;
+    std::memset(dense, 0, sizeof(double) * (size_t)(H.d_i * H.d_j * H.d_l * H.d_r));
+    for (const SubMap& m : H.submaps)
+        for (int32_t r = 0; r < m.rows; ++r)
+            std::memcpy(dense + m.dense_off + (int64_t)r * H.d_r, flat + m.flat_off + (int64_t)r * m.cols,
+                        sizeof(double) * m.cols);
+    return TK_OK;
+}
+
+tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double* y) {
+    if (!plan || !x || !y) {
+        set_error("tk_heff2_apply_host_flat: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    const int64_t n = plan->host.total;
+    if (n == 0) return TK_OK;
+    DeviceGuard g(plan->device);
+    tk_status st = ensure_host_staging(plan);
+    if (st != TK_OK) return st;
+    cudaStream_t s = plan->stream;
+    TK_CUDA(cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, plan->precision);
+    if (st != TK_OK) return st;
+    TK_CUDA(cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    TK_CUDA(cudaStreamSynchronize(s));
+    return TK_OK;
+}
+
+tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {
+    if (!plan || !x || !y) {
+        set_error("tk_heff2_apply_host: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    DeviceGuard g(plan->device);
+    tk_status st = ensure_host_staging(plan);
+    if (st != TK_OK) return st;
+    tk_heff2_dense_to_flat(plan, x, plan->pin_x);
+    const int64_t n = plan->host.total;
+    cudaStream_t s = plan->stream;
+    if (n > 0) {
+        TK_CUDA(cudaMemcpyAsync(plan->hx.p, plan->pin_x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, plan->precision);
+        if (st != TK_OK) return st;
+        TK_CUDA(cudaMemcpyAsync(plan->pin_y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        TK_CUDA(cudaStreamSynchronize(s));
+    }
+    return tk_heff2_flat_to_dense(plan, plan->pin_y, y);
+}
+
+}  // extern "C"
+
+extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream,
+                                      int32_t reps, float* ms, double* flops) {
+    if (!plan || !x_dev || !y_dev || !ms || reps < 1) {
+        set_error("tk_heff2_profile: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    DeviceGuard g(plan->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    tk_heff2_plan* p = plan;
+    const Heff2Tables& H = p->host;
+    if (flops) {
+        flops[0] = H.g1.flops;
+        flops[1] = H.comb_flops;
+        flops[2] = H.g3.flops;
+    }
+    cudaEvent_t ev[4];
+    for (int i = 0; i < 4; ++i) TK_CUDA(cudaEventCreate(&ev[i]));
+    struct EvFree {
+        cudaEvent_t* e;
+        ~EvFree() {
+            for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+        }
+    } evf{ev};
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int r = 0; r < reps; ++r) {
+        TK_CUDA(cudaEventRecord(ev[0], s));
+        for (int stage = 0; stage < 3; ++stage) {
+            if (p->precision == TK_PREC_BF16X3) {
+                std::string err;
+                cudaError_t e = tc_apply_stage(*p->tc, p->host, p->jobs.p, p->n_jobs, p->terms.p, x_dev, y_dev, s,
+                                               stage, err);
+                if (e != cudaSuccess) return cuda_fail(err.c_str(), e);
+            } else if (stage == 0) {
+                TK_CUDA(launch_gemm_f64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p, x_dev,
+                                        p->t1.p, s));
+            } else if (stage == 1) {
+                TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
+            } else {
+                TK_CUDA(launch_gemm_f64(p->g3.tiles.p, p->g3.n_tiles, p->g3.tasks.p, p->g3.segs.p, p->t2.p, p->rbuf.p,
+                                        y_dev, s));
+            }
+            TK_CUDA(cudaEventRecord(ev[stage + 1], s));
+        }
+        TK_CUDA(cudaEventSynchronize(ev[3]));
+        for (int stage = 0; stage < 3; ++stage) {
+            float t = 0.f;
+            TK_CUDA(cudaEventElapsedTime(&t, ev[stage], ev[stage + 1]));
+            acc[stage] += t;
+        }
+    }
+    for (int stage = 0; stage < 3; ++stage) ms[stage] = (float)(acc[stage] / reps);
+    return TK_OK;
+}

@@ -1,0 +1,595 @@
+// plan.cpp -- host-side sector bookkeeping for the two-site H_eff.
+//
+// Integer work only: decodes the reference-format inputs (dense
+// environments, block-sparse MPO tensors), enumerates the two-site sectors,
+// finds the non-zero environment slabs and flattens every sector GEMM of one
+// matvec into task tables that the device kernels walk.
+//
+// Reference semantics followed (kyungminlee/tensorkraft-design):
+//   tk-dmrg/src/environments/mod.rs:491-602  which (L, W_i, W_j, R) entries meet
+//       which (in, out) pair: in=(s_i,s_j,a_L,a_R), out=(s'_i,s'_j,a'_L,a'_R),
+//       L(a'_L, w_L, a_L), R(a'_R, w_R, a_R), w_mid paired by quantum number
+//       with the block-local index (:532, :545), physical and MPO-bond offsets
+//       from the MPO's QIndex order (:518-538).
+//   tk-symmetry/src/flux.rs:43-234  sector enumeration (DFS order, last leg solved).
+//   tk-symmetry/src/block_sparse.rs:40-84  blocks sorted by packed key.
+//   tk-symmetry/src/flat_storage.rs:95-130  blocks back to back, row-major.
+//   tk-linalg/src/tasks.rs:172-174  LPT order (heaviest work first).
+#include <algorithm>
+#include <array>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <unordered_map>
+
+#include "tk_internal.hpp"
+
+namespace tk {
+
+int qn_ncomp(int kind) { return (kind == TK_QN_U1Z2 || kind == TK_QN_U1U1) ? 2 : 1; }
+
+int qn_bits(int kind) {
+    switch (kind) {
+    case TK_QN_U1: return 8;
+    case TK_QN_Z2: return 1;
+    case TK_QN_U1Z2: return 9;
+    case TK_QN_U1WIDE: return 16;
+    case TK_QN_U1U1: return 16;
+    default: return -1;
+    }
+}
+
+bool qn_kind_valid(int kind) { return qn_bits(kind) > 0; }
+
+Qn qn_fuse(int kind, const Qn& a, const Qn& b) {
+    Qn r;
+    switch (kind) {
+    case TK_QN_Z2: r.c[0] = a.c[0] ^ b.c[0]; break;
+    case TK_QN_U1Z2: r.c[0] = a.c[0] + b.c[0]; r.c[1] = a.c[1] ^ b.c[1]; break;
+    case TK_QN_U1U1: r.c[0] = a.c[0] + b.c[0]; r.c[1] = a.c[1] + b.c[1]; break;
+    default: r.c[0] = a.c[0] + b.c[0]; break;
+    }
+    return r;
+}
+
+Qn qn_dual(int kind, const Qn& a) {
+    Qn r;
+    switch (kind) {
+    case TK_QN_Z2: r.c[0] = a.c[0]; break;
+    case TK_QN_U1Z2: r.c[0] = -a.c[0]; r.c[1] = a.c[1]; break;
+    case TK_QN_U1U1: r.c[0] = -a.c[0]; r.c[1] = -a.c[1]; break;
+    default: r.c[0] = -a.c[0]; break;
+    }
+    return r;
+}
+
+bool qn_less(const Qn& a, const Qn& b) {
+    if (a.c[0] != b.c[0]) return a.c[0] < b.c[0];
+    return a.c[1] < b.c[1];
+}
+
+static int32_t low_signed(uint64_t v, int bits) {
+    uint64_t m = (1ull << bits) - 1;
+    v &= m;
+    return (v >> (bits - 1)) ? (int32_t)((int64_t)v - (int64_t)(1ull << bits)) : (int32_t)v;
+}
+
+uint64_t qn_pack(int kind, const Qn& q) {
+    switch (kind) {
+    case TK_QN_U1: return (uint64_t)((uint32_t)q.c[0] & 0xFFu);
+    case TK_QN_Z2: return (uint64_t)(q.c[0] != 0);
+    case TK_QN_U1Z2: return (uint64_t)((uint32_t)q.c[0] & 0xFFu) | ((uint64_t)(q.c[1] != 0) << 8);
+    case TK_QN_U1WIDE: return (uint64_t)((uint32_t)q.c[0] & 0xFFFFu);
+    case TK_QN_U1U1: return (uint64_t)((uint32_t)q.c[0] & 0xFFu) | ((uint64_t)((uint32_t)q.c[1] & 0xFFu) << 8);
+    default: return 0;
+    }
+}
+
+Qn qn_unpack(int kind, uint64_t b) {
+    Qn q;
+    switch (kind) {
+    case TK_QN_U1: q.c[0] = low_signed(b, 8); break;
+    case TK_QN_Z2: q.c[0] = (int32_t)(b & 1); break;
+    case TK_QN_U1Z2: q.c[0] = low_signed(b, 8); q.c[1] = (int32_t)((b >> 8) & 1); break;
+    case TK_QN_U1WIDE: q.c[0] = low_signed(b, 16); break;
+    case TK_QN_U1U1: q.c[0] = low_signed(b, 8); q.c[1] = low_signed(b >> 8, 8); break;
+    default: break;
+    }
+    return q;
+}
+
+uint64_t key_pack(int kind, const Qn* qns, int rank) {
+    int bw = qn_bits(kind);
+    uint64_t mask = (bw >= 64) ? ~0ull : ((1ull << bw) - 1);
+    uint64_t key = 0;
+    for (int i = 0; i < rank; ++i) key |= (qn_pack(kind, qns[i]) & mask) << (i * bw);
+    return key;
+}
+
+void key_unpack(int kind, uint64_t key, int rank, Qn* qns) {
+    int bw = qn_bits(kind);
+    uint64_t mask = (1ull << bw) - 1;
+    for (int i = 0; i < rank; ++i) qns[i] = qn_unpack(kind, (key >> (i * bw)) & mask);
+}
+
+int QIndex::find(const Qn& x) const {
+    for (size_t s = 0; s < q.size(); ++s)
+        if (q[s] == x) return (int)s;
+    return -1;
+}
+
+bool QIndex::same_as(const QIndex& o) const {
+    if (q.size() != o.q.size()) return false;
+    for (size_t s = 0; s < q.size(); ++s)
+        if (q[s] != o.q[s] || dim[s] != o.dim[s]) return false;
+    return true;
+}
+
+bool qindex_from_abi(int kind, const tk_qindex& in, QIndex& out, std::string& err) {
+    int nc = qn_ncomp(kind);
+    if (in.n_sectors < 0 || (in.n_sectors > 0 && (!in.charges || !in.dims))) {
+        err = "QIndex: null charges/dims";
+        return false;
+    }
+    out.q.resize(in.n_sectors);
+    out.dim.resize(in.n_sectors);
+    out.off.resize(in.n_sectors);
+    out.total = 0;
+    for (int s = 0; s < in.n_sectors; ++s) {
+        Qn q;
+        for (int k = 0; k < nc; ++k) q.c[k] = in.charges[s * nc + k];
+        out.q[s] = q;
+        if (in.dims[s] <= 0) {
+            err = "QIndex: sector with non-positive dimension";
+            return false;
+        }
+        out.dim[s] = in.dims[s];
+        out.off[s] = out.total;
+        out.total += in.dims[s];
+        if (s > 0 && !qn_less(out.q[s - 1], q)) {
+            err = "QIndex: sectors not strictly sorted by quantum number";
+            return false;
+        }
+    }
+    return true;
+}
+
+namespace {
+
+struct Bst4 {
+    int kind = 0;
+    QIndex legs[4];
+    std::vector<uint64_t> keys;
+    std::vector<int64_t> offs;
+    const double* data = nullptr;
+};
+
+bool bst4_from_abi(const tk_bst& t, Bst4& o, const char* name, std::string& err) {
+    if (t.rank != 4 || !t.legs) {
+        err = std::string(name) + ": MPO site tensor must have rank 4 (s_in, s_out, w_L, w_R)";
+        return false;
+    }
+    if (!qn_kind_valid(t.qn_kind)) {
+        err = std::string(name) + ": unknown quantum-number kind";
+        return false;
+    }
+    o.kind = t.qn_kind;
+    for (int l = 0; l < 4; ++l)
+        if (!qindex_from_abi(t.qn_kind, t.legs[l], o.legs[l], err)) {
+            err = std::string(name) + ": " + err;
+            return false;
+        }
+    if (t.n_blocks < 0 || (t.n_blocks > 0 && (!t.keys || !t.block_offsets || !t.data))) {
+        err = std::string(name) + ": null block arrays";
+        return false;
+    }
+    o.keys.assign(t.keys, t.keys + t.n_blocks);
+    o.offs.assign(t.block_offsets, t.block_offsets + t.n_blocks);
+    o.data = t.data;
+    for (int64_t b = 1; b < t.n_blocks; ++b)
+        if (o.keys[b - 1] >= o.keys[b]) {
+            err = std::string(name) + ": sector keys not strictly ascending";
+            return false;
+        }
+    return true;
+}
+
+// Dense MPO tensor (d, d, wl, wr) in global indices, following the offsets
+// the reference reads (environments/mod.rs:518-538, `unwrap_or(0)` for absent
+// sectors is an error here).
+bool mpo_dense(const Bst4& w, std::vector<double>& out, std::string& err) {
+    int64_t d0 = w.legs[0].total, d1 = w.legs[1].total, d2 = w.legs[2].total, d3 = w.legs[3].total;
+    out.assign((size_t)(d0 * d1 * d2 * d3), 0.0);
+    for (size_t b = 0; b < w.keys.size(); ++b) {
+        Qn q[4];
+        key_unpack(w.kind, w.keys[b], 4, q);
+        int s[4];
+        for (int l = 0; l < 4; ++l) {
+            s[l] = w.legs[l].find(q[l]);
+            if (s[l] < 0) {
+                err = "MPO block key names a sector missing from its QIndex";
+                return false;
+            }
+        }
+        int64_t n0 = w.legs[0].dim[s[0]], n1 = w.legs[1].dim[s[1]], n2 = w.legs[2].dim[s[2]], n3 = w.legs[3].dim[s[3]];
+        const double* blk = w.data + w.offs[b];
+        for (int64_t i0 = 0; i0 < n0; ++i0)
+            for (int64_t i1 = 0; i1 < n1; ++i1)
+                for (int64_t i2 = 0; i2 < n2; ++i2)
+                    for (int64_t i3 = 0; i3 < n3; ++i3) {
+                        int64_t g0 = w.legs[0].off[s[0]] + i0, g1 = w.legs[1].off[s[1]] + i1;
+                        int64_t g2 = w.legs[2].off[s[2]] + i2, g3 = w.legs[3].off[s[3]] + i3;
+                        out[((g0 * d1 + g1) * d2 + g2) * d3 + g3] += blk[((i0 * n1 + i1) * n2 + i2) * n3 + i3];
+                    }
+    }
+    return true;
+}
+
+// enumerate_valid_sectors (flux.rs:43-234) for the two-site tensor, directions
+// (In, In, In, Out): q(s_i) + q(s_j) + q(a_L) - q(a_R) == flux.
+void enumerate4(int kind, const QIndex* legs, const Qn& flux, std::vector<std::array<int, 4>>& out) {
+    for (int a = 0; a < legs[0].n(); ++a)
+        for (int b = 0; b < legs[1].n(); ++b)
+            for (int c = 0; c < legs[2].n(); ++c) {
+                Qn part = qn_fuse(kind, qn_fuse(kind, legs[0].q[a], legs[1].q[b]), legs[2].q[c]);
+                // Outgoing last leg: required = dual(flux (+) dual(partial)) = partial (+) dual(flux)
+                Qn req = qn_dual(kind, qn_fuse(kind, flux, qn_dual(kind, part)));
+                int d = legs[3].find(req);
+                if (d >= 0) out.push_back({a, b, c, d});
+            }
+}
+
+}  // namespace
+
+static void add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n, const std::vector<int64_t>& kseg) {
+    const GemmTask& t = g.tasks[task_id];
+    int64_t ktot = 0;
+    for (int64_t k : kseg) ktot += k;
+    for (int m0 = 0; m0 < t.M; m0 += tile_m)
+        for (int n0 = 0; n0 < t.N; n0 += tile_n) g.tiles.push_back({task_id, m0, n0, 0});
+    (void)ktot;
+}
+
+static void lpt_order(GemmTable& g, int tile_m, int tile_n) {
+    // Cost of a tile = (rows) x (cols) x (total K); heaviest first.
+    std::vector<double> ktot(g.tasks.size(), 0.0);
+    for (size_t t = 0; t < g.tasks.size(); ++t)
+        for (int s = g.tasks[t].seg_begin; s < g.tasks[t].seg_end; ++s) ktot[t] += g.segs[s].K;
+    auto cost = [&](const GemmTile& x) {
+        const GemmTask& t = g.tasks[x.task];
+        double rm = std::min(tile_m, t.M - x.m0), rn = std::min(tile_n, t.N - x.n0);
+        return (ktot[x.task] + 1.0) * rm * rn;
+    };
+    std::stable_sort(g.tiles.begin(), g.tiles.end(),
+                     [&](const GemmTile& a, const GemmTile& b) { return cost(a) > cost(b); });
+}
+
+tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi,
+                             const tk_bst& wj_abi, const int32_t* psi_flux, int tile_m, int tile_n,
+                             Heff2Tables& T, std::string& err) {
+    Bst4 wi, wj;
+    if (!bst4_from_abi(wi_abi, wi, "W_i", err)) return TK_ERR_INVALID_ARG;
+    if (!bst4_from_abi(wj_abi, wj, "W_j", err)) return TK_ERR_INVALID_ARG;
+    if (wi.kind != wj.kind) {
+        err = "W_i and W_j use different quantum-number kinds";
+        return TK_ERR_INVALID_ARG;
+    }
+    const int kind = wi.kind;
+    T.kind = kind;
+    QIndex lbra, lmpo, lket, rbra, rmpo, rket;
+    if (!qindex_from_abi(kind, envL.bra, lbra, err) || !qindex_from_abi(kind, envL.mpo, lmpo, err) ||
+        !qindex_from_abi(kind, envL.ket, lket, err) || !qindex_from_abi(kind, envR.bra, rbra, err) ||
+        !qindex_from_abi(kind, envR.mpo, rmpo, err) || !qindex_from_abi(kind, envR.ket, rket, err)) {
+        err = "environment: " + err;
+        return TK_ERR_INVALID_ARG;
+    }
+    if (!envL.data || !envR.data) {
+        err = "environment: null data";
+        return TK_ERR_INVALID_ARG;
+    }
+    // The reference loops a'_L over the ket dimension (mod.rs:503, :559): the
+    // bra and ket bases must agree.
+    if (!lbra.same_as(lket) || !rbra.same_as(rket)) {
+        err = "environment bra and ket QIndex differ";
+        return TK_ERR_SECTOR_MISMATCH;
+    }
+    if (!wi.legs[0].same_as(wi.legs[1]) || !wj.legs[0].same_as(wj.legs[1])) {
+        err = "MPO s_in and s_out QIndex differ";
+        return TK_ERR_SECTOR_MISMATCH;
+    }
+    if (!wi.legs[2].same_as(lmpo) || !wj.legs[3].same_as(rmpo)) {
+        err = "MPO bond QIndex does not match the environment's MPO leg";
+        return TK_ERR_SECTOR_MISMATCH;
+    }
+    if (!wi.legs[3].same_as(wj.legs[2])) {
+        err = "W_i right bond and W_j left bond QIndex differ";
+        return TK_ERR_SECTOR_MISMATCH;
+    }
+    const QIndex& PI = wi.legs[0];
+    const QIndex& PJ = wj.legs[0];
+    const QIndex& QA = lket;
+    const QIndex& QB = rket;
+    const QIndex& WL = lmpo;
+    const QIndex& WR = rmpo;
+    const int64_t d_i = PI.total, d_j = PJ.total, d_l = QA.total, d_r = QB.total;
+    const int64_t nwl = WL.total, nwm = wi.legs[3].total, nwr = WR.total;
+    T.d_i = d_i; T.d_j = d_j; T.d_l = d_l; T.d_r = d_r; T.nwl = nwl; T.nwr = nwr;
+    const int nA = QA.n(), nB = QB.n();
+    const int64_t P = d_i * d_j;
+
+    // --- fused two-site operator W_ij[p][p'][wl][wr] = sum_wm W_i W_j ---------
+    std::vector<double> Wi, Wj;
+    if (!mpo_dense(wi, Wi, err) || !mpo_dense(wj, Wj, err)) return TK_ERR_SECTOR_MISMATCH;
+    std::vector<double> Wij((size_t)(P * P * nwl * nwr), 0.0);
+    for (int64_t si = 0; si < d_i; ++si)
+        for (int64_t so = 0; so < d_i; ++so)
+            for (int64_t sj = 0; sj < d_j; ++sj)
+                for (int64_t to = 0; to < d_j; ++to)
+                    for (int64_t wl = 0; wl < nwl; ++wl)
+                        for (int64_t wm = 0; wm < nwm; ++wm) {
+                            double a = Wi[((si * d_i + so) * nwl + wl) * nwm + wm];
+                            if (a == 0.0) continue;
+                            for (int64_t wr = 0; wr < nwr; ++wr) {
+                                double b = Wj[((sj * d_j + to) * nwm + wm) * nwr + wr];
+                                if (b == 0.0) continue;
+                                Wij[(((si * d_j + sj) * P + (so * d_j + to)) * nwl + wl) * nwr + wr] += a * b;
+                            }
+                        }
+
+    // --- two-site blocks ---------------------------------------------------------
+    std::vector<std::array<int, 4>> tuples;
+    QIndex legs4[4] = {PI, PJ, QA, QB};
+    if (psi_flux) {
+        Qn f;
+        for (int k = 0; k < qn_ncomp(kind); ++k) f.c[k] = psi_flux[k];
+        enumerate4(kind, legs4, f, tuples);
+    } else {
+        for (int a = 0; a < PI.n(); ++a)
+            for (int b = 0; b < PJ.n(); ++b)
+                for (int c = 0; c < nA; ++c)
+                    for (int d = 0; d < nB; ++d) tuples.push_back({a, b, c, d});
+    }
+    if (4 * qn_bits(kind) > 64) {
+        err = "rank-4 sector key exceeds 64 bits";
+        return TK_ERR_UNSUPPORTED;
+    }
+    std::vector<std::pair<uint64_t, std::array<int, 4>>> kb;
+    kb.reserve(tuples.size());
+    for (auto& t : tuples) {
+        Qn q[4] = {PI.q[t[0]], PJ.q[t[1]], QA.q[t[2]], QB.q[t[3]]};
+        kb.push_back({key_pack(kind, q, 4), t});
+    }
+    std::sort(kb.begin(), kb.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    // state -> (sector, local)
+    std::vector<int> secI(d_i), secJ(d_j);
+    std::vector<int64_t> locI(d_i), locJ(d_j);
+    for (int s = 0; s < PI.n(); ++s)
+        for (int64_t k = 0; k < PI.dim[s]; ++k) { secI[PI.off[s] + k] = s; locI[PI.off[s] + k] = k; }
+    for (int s = 0; s < PJ.n(); ++s)
+        for (int64_t k = 0; k < PJ.dim[s]; ++k) { secJ[PJ.off[s] + k] = s; locJ[PJ.off[s] + k] = k; }
+
+    // sub-block (p, A, B) -> flat offset
+    std::vector<int64_t> sub((size_t)(P * nA * nB), -1);
+    auto SUB = [&](int64_t p, int a, int b) -> int64_t& { return sub[((size_t)p * nA + a) * nB + b]; };
+    T.keys.clear();
+    T.blk_off.clear();
+    T.submaps.clear();
+    int64_t off = 0;
+    for (auto& e : kb) {
+        const auto& t = e.second;
+        T.keys.push_back(e.first);
+        T.blk_off.push_back(off);
+        int64_t ni = PI.dim[t[0]], nj = PJ.dim[t[1]], DA = QA.dim[t[2]], DB = QB.dim[t[3]];
+        for (int64_t li = 0; li < ni; ++li)
+            for (int64_t lj = 0; lj < nj; ++lj) {
+                int64_t p = (PI.off[t[0]] + li) * d_j + (PJ.off[t[1]] + lj);
+                int64_t fo = off + (li * nj + lj) * DA * DB;
+                SUB(p, t[2], t[3]) = fo;
+                T.submaps.push_back({p * d_l * d_r + QA.off[t[2]] * d_r + QB.off[t[3]], fo, (int32_t)DA, (int32_t)DB});
+            }
+        off += ni * nj * DA * DB;
+    }
+    T.total = off;
+
+    // --- non-zero environment slabs -------------------------------------------
+    // L slab (A', ws, A) as [(a', w)][a]; R slab (B', ws, B) as [b'][(w, b)].
+    const int nWL = WL.n(), nWR = WR.n();
+    std::vector<int64_t> lblk((size_t)nA * nWL * nA, -1), rblk((size_t)nB * nWR * nB, -1);
+    T.lbuf.clear();
+    T.rbuf.clear();
+    for (int ap = 0; ap < nA; ++ap)
+        for (int ws = 0; ws < nWL; ++ws)
+            for (int a = 0; a < nA; ++a) {
+                bool nz = false;
+                for (int64_t i = 0; i < QA.dim[ap] && !nz; ++i)
+                    for (int64_t w = 0; w < WL.dim[ws] && !nz; ++w) {
+                        const double* row = envL.data + ((QA.off[ap] + i) * nwl + WL.off[ws] + w) * d_l + QA.off[a];
+                        for (int64_t j = 0; j < QA.dim[a]; ++j)
+                            if (row[j] != 0.0) { nz = true; break; }
+                    }
+                if (!nz) continue;
+                lblk[((size_t)ap * nWL + ws) * nA + a] = (int64_t)T.lbuf.size();
+                for (int64_t i = 0; i < QA.dim[ap]; ++i)
+                    for (int64_t w = 0; w < WL.dim[ws]; ++w) {
+                        const double* row = envL.data + ((QA.off[ap] + i) * nwl + WL.off[ws] + w) * d_l + QA.off[a];
+                        T.lbuf.insert(T.lbuf.end(), row, row + QA.dim[a]);
+                    }
+            }
+    for (int bp = 0; bp < nB; ++bp)
+        for (int ws = 0; ws < nWR; ++ws)
+            for (int b = 0; b < nB; ++b) {
+                bool nz = false;
+                for (int64_t i = 0; i < QB.dim[bp] && !nz; ++i)
+                    for (int64_t w = 0; w < WR.dim[ws] && !nz; ++w) {
+                        const double* row = envR.data + ((QB.off[bp] + i) * nwr + WR.off[ws] + w) * d_r + QB.off[b];
+                        for (int64_t j = 0; j < QB.dim[b]; ++j)
+                            if (row[j] != 0.0) { nz = true; break; }
+                    }
+                if (!nz) continue;
+                rblk[((size_t)bp * nWR + ws) * nB + b] = (int64_t)T.rbuf.size();
+                for (int64_t i = 0; i < QB.dim[bp]; ++i)
+                    for (int64_t w = 0; w < WR.dim[ws]; ++w) {
+                        const double* row = envR.data + ((QB.off[bp] + i) * nwr + WR.off[ws] + w) * d_r + QB.off[b];
+                        T.rbuf.insert(T.rbuf.end(), row, row + QB.dim[b]);
+                    }
+            }
+
+    // --- stage 1: T1(p, A', ws, B) = sum_A Lslab(A', ws, A) * psi(p, A, B) -----
+    std::vector<int64_t> t1((size_t)P * nA * nWL * nB, -1);
+    auto T1I = [&](int64_t p, int ap, int ws, int b) -> int64_t& {
+        return t1[(((size_t)p * nA + ap) * nWL + ws) * nB + b];
+    };
+    T.g1 = GemmTable();
+    off = 0;
+    for (int64_t p = 0; p < P; ++p)
+        for (int ap = 0; ap < nA; ++ap)
+            for (int ws = 0; ws < nWL; ++ws)
+                for (int b = 0; b < nB; ++b) {
+                    int seg0 = (int)T.g1.segs.size();
+                    std::vector<int64_t> ks;
+                    for (int a = 0; a < nA; ++a) {
+                        int64_t lo = lblk[((size_t)ap * nWL + ws) * nA + a];
+                        int64_t so = SUB(p, a, b);
+                        if (lo < 0 || so < 0) continue;
+                        GemmSeg s{};
+                        s.a_off = lo; s.a_rs = (int32_t)QA.dim[a]; s.a_cs = 1;
+                        s.b_off = so; s.b_rs = (int32_t)QB.dim[b]; s.b_cs = 1;
+                        s.K = (int32_t)QA.dim[a];
+                        T.g1.segs.push_back(s);
+                        ks.push_back(s.K);
+                    }
+                    if (ks.empty()) continue;
+                    GemmTask tk{};
+                    tk.M = (int32_t)(QA.dim[ap] * WL.dim[ws]);
+                    tk.N = (int32_t)QB.dim[b];
+                    tk.c_off = off; tk.c_rs = tk.N; tk.c_cs = 1;
+                    tk.seg_begin = seg0; tk.seg_end = (int)T.g1.segs.size();
+                    tk.alpha = 1.0; tk.beta = 0.0;
+                    for (int64_t k : ks) T.g1.flops += 2.0 * tk.M * tk.N * (double)k;
+                    T1I(p, ap, ws, b) = off;
+                    off += (int64_t)tk.M * tk.N;
+                    T.g1.tasks.push_back(tk);
+                    add_tiles(T.g1, (int)T.g1.tasks.size() - 1, tile_m, tile_n, ks);
+                }
+    T.t1_total = off;
+
+    // --- stage 2: T2(p', A', wsr, B)[a'][w][b] = sum W_ij * T1 -----------------
+    std::vector<int> wl_sec(nwl), wr_sec(nwr);
+    std::vector<int64_t> wl_loc(nwl), wr_loc(nwr);
+    for (int s = 0; s < nWL; ++s)
+        for (int64_t k = 0; k < WL.dim[s]; ++k) { wl_sec[WL.off[s] + k] = s; wl_loc[WL.off[s] + k] = k; }
+    for (int s = 0; s < nWR; ++s)
+        for (int64_t k = 0; k < WR.dim[s]; ++k) { wr_sec[WR.off[s] + k] = s; wr_loc[WR.off[s] + k] = k; }
+    // non-zero W_ij terms grouped by (p', wr)
+    struct Term { int64_t p; int64_t wl; double c; };
+    std::vector<std::vector<Term>> byout((size_t)(P * nwr));
+    int64_t nterms = 0;
+    for (int64_t p = 0; p < P; ++p)
+        for (int64_t po = 0; po < P; ++po)
+            for (int64_t wl = 0; wl < nwl; ++wl)
+                for (int64_t wr = 0; wr < nwr; ++wr) {
+                    double c = Wij[((p * P + po) * nwl + wl) * nwr + wr];
+                    if (c != 0.0) { byout[po * nwr + wr].push_back({p, wl, c}); ++nterms; }
+                }
+    T.n_wij_terms = nterms;
+    std::vector<int64_t> t2((size_t)P * nA * nWR * nB, -1);
+    auto T2I = [&](int64_t p, int ap, int ws, int b) -> int64_t& {
+        return t2[(((size_t)p * nA + ap) * nWR + ws) * nB + b];
+    };
+    T.jobs.clear();
+    T.terms.clear();
+    T.comb_flops = 0.0;
+    off = 0;
+    for (int64_t po = 0; po < P; ++po)
+        for (int ap = 0; ap < nA; ++ap)
+            for (int ws = 0; ws < nWR; ++ws)
+                for (int b = 0; b < nB; ++b) {
+                    // consumed by stage 3 only if some R slab (B', ws, B) exists and
+                    // the output sub-block (p', A', B') exists
+                    bool used = false;
+                    for (int bp = 0; bp < nB && !used; ++bp)
+                        if (rblk[((size_t)bp * nWR + ws) * nB + b] >= 0 && SUB(po, ap, bp) >= 0) used = true;
+                    if (!used) continue;
+                    int64_t dws = WR.dim[ws];
+                    size_t job0 = T.jobs.size();
+                    bool any = false;
+                    for (int64_t wlc = 0; wlc < dws; ++wlc) {
+                        int64_t wr = WR.off[ws] + wlc;
+                        CombJob j{};
+                        j.rows = (int32_t)QA.dim[ap];
+                        j.cols = (int32_t)QB.dim[b];
+                        j.term_begin = (int32_t)T.terms.size();
+                        for (const Term& tm : byout[po * nwr + wr]) {
+                            int64_t src = T1I(tm.p, ap, wl_sec[tm.wl], b);
+                            if (src < 0) continue;
+                            CombTerm ct{};
+                            ct.in_off = src + wl_loc[tm.wl] * QB.dim[b];
+                            ct.in_rs = (int32_t)(WL.dim[wl_sec[tm.wl]] * QB.dim[b]);
+                            ct.coef = tm.c;
+                            T.terms.push_back(ct);
+                            T.comb_flops += 2.0 * j.rows * j.cols;
+                        }
+                        j.term_end = (int32_t)T.terms.size();
+                        if (j.term_end > j.term_begin) any = true;
+                        j.out_off = wlc * QB.dim[b];  // relative; fixed below
+                        j.out_rs = (int32_t)(dws * QB.dim[b]);
+                        T.jobs.push_back(j);
+                    }
+                    if (!any) {
+                        T.terms.resize(T.jobs[job0].term_begin);
+                        T.jobs.resize(job0);
+                        continue;
+                    }
+                    for (size_t k = job0; k < T.jobs.size(); ++k) T.jobs[k].out_off += off;
+                    T2I(po, ap, ws, b) = off;
+                    off += QA.dim[ap] * dws * QB.dim[b];
+                }
+    T.t2_total = off;
+
+    // --- stage 3: y(p', A', B') = sum_{ws, B} T2(p', A', ws, B) * Rslab(B', ws, B)^T
+    T.g3 = GemmTable();
+    for (int64_t po = 0; po < P; ++po)
+        for (int ap = 0; ap < nA; ++ap)
+            for (int bp = 0; bp < nB; ++bp) {
+                int64_t yo = SUB(po, ap, bp);
+                if (yo < 0) continue;
+                int seg0 = (int)T.g3.segs.size();
+                std::vector<int64_t> ks;
+                for (int ws = 0; ws < nWR; ++ws)
+                    for (int b = 0; b < nB; ++b) {
+                        int64_t ro = rblk[((size_t)bp * nWR + ws) * nB + b];
+                        int64_t to = T2I(po, ap, ws, b);
+                        if (ro < 0 || to < 0) continue;
+                        int32_t K = (int32_t)(WR.dim[ws] * QB.dim[b]);
+                        GemmSeg s{};
+                        s.a_off = to; s.a_rs = K; s.a_cs = 1;
+                        s.b_off = ro; s.b_rs = 1; s.b_cs = K;
+                        s.K = K;
+                        T.g3.segs.push_back(s);
+                        ks.push_back(K);
+                    }
+                GemmTask tk{};
+                tk.M = (int32_t)QA.dim[ap];
+                tk.N = (int32_t)QB.dim[bp];
+                tk.c_off = yo; tk.c_rs = tk.N; tk.c_cs = 1;
+                tk.seg_begin = seg0; tk.seg_end = (int)T.g3.segs.size();
+                tk.alpha = 1.0; tk.beta = 0.0;
+                for (int64_t k : ks) T.g3.flops += 2.0 * tk.M * tk.N * (double)k;
+                T.g3.tasks.push_back(tk);
+                add_tiles(T.g3, (int)T.g3.tasks.size() - 1, tile_m, tile_n, ks);
+            }
+    lpt_order(T.g1, tile_m, tile_n);
+    lpt_order(T.g3, tile_m, tile_n);
+    // Algorithmic bytes: psi in, y out, the block-sparse L, R and W_ij terms, FP64.
+    T.alg_bytes = 8.0 * (2.0 * (double)T.total + (double)T.lbuf.size() + (double)T.rbuf.size() + (double)nterms);
+    // Index ranges must fit the kernels' 32-bit strides and counts.
+    if (T.g1.tiles.size() > (size_t)INT32_MAX || T.g3.tiles.size() > (size_t)INT32_MAX ||
+        T.terms.size() > (size_t)INT32_MAX || T.g1.segs.size() > (size_t)INT32_MAX) {
+        err = "sector tables exceed 32-bit index range";
+        return TK_ERR_UNSUPPORTED;
+    }
+    return TK_OK;
+}
+
+}  // namespace tk

@@ -1,0 +1,31 @@
+// tc_gemm.cuh -- split-precision (bf16x3) sector-GEMM path on tcgen05 tensor cores.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+
+#include "tk_internal.hpp"
+
+namespace tk {
+
+struct TcPlan;
+struct TcPlanDeleter {
+    void operator()(TcPlan* p) const;
+};
+
+// Builds the split operands of L and R (constant across matvecs) and the
+// tile tables of both GEMM stages.
+tk_status tc_plan_create(const Heff2Tables& host, const double* d_lbuf, const double* d_rbuf,
+                         std::unique_ptr<TcPlan, TcPlanDeleter>& out, std::string& err);
+
+// One split-precision matvec, stream-ordered.
+cudaError_t tc_apply(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs, int n_jobs,
+                     const CombTerm* d_terms, const double* x, double* y, cudaStream_t s, std::string& err);
+
+// One stage of the split-precision matvec (0: L x psi, 1: combine, 2: x R), for profiling.
+cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs, int n_jobs,
+                           const CombTerm* d_terms, const double* x, double* y, cudaStream_t s, int stage,
+                           std::string& err);
+
+}  // namespace tk

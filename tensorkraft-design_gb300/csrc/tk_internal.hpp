@@ -1,0 +1,132 @@
+// tk_internal.hpp -- shared types of libtk_heff: quantum-number arithmetic,
+// flattened sector-GEMM task tables, and the host-side plan description.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tk_heff.h"
+
+// Library context: the CUDA device it is bound to.
+struct tk_ctx {
+    int device = 0;
+};
+
+namespace tk {
+
+// ---------------------------------------------------------------------------
+// Quantum numbers.  Semantics of tk-symmetry/src/builtins.rs:12-152: U(1)
+// components add and negate, Z2 components xor and are self-dual; packing
+// truncates each U(1) component to its bit field (Rust `as u8` / `as u16`).
+// Order is lexicographic over components (derived Ord on the tuple structs).
+// ---------------------------------------------------------------------------
+struct Qn {
+    int32_t c[2] = {0, 0};
+    bool operator==(const Qn& o) const { return c[0] == o.c[0] && c[1] == o.c[1]; }
+    bool operator!=(const Qn& o) const { return !(*this == o); }
+};
+
+int qn_ncomp(int kind);
+int qn_bits(int kind);
+bool qn_kind_valid(int kind);
+Qn qn_fuse(int kind, const Qn& a, const Qn& b);
+Qn qn_dual(int kind, const Qn& a);
+bool qn_less(const Qn& a, const Qn& b);
+uint64_t qn_pack(int kind, const Qn& q);
+Qn qn_unpack(int kind, uint64_t bits);
+// PackedSectorKey::pack (tk-symmetry/src/sector_key.rs:31-46).
+uint64_t key_pack(int kind, const Qn* qns, int rank);
+void key_unpack(int kind, uint64_t key, int rank, Qn* qns);
+
+// QIndex (tk-symmetry/src/sector_key.rs:96-148), owned copy.
+struct QIndex {
+    std::vector<Qn> q;
+    std::vector<int64_t> dim;
+    std::vector<int64_t> off;
+    int64_t total = 0;
+    int find(const Qn& x) const;  // sector index or -1 (offset_of / dim_of)
+    bool same_as(const QIndex& o) const;
+    int n() const { return (int)q.size(); }
+};
+// Copies a tk_qindex; checks sectors are strictly sorted with positive dims.
+bool qindex_from_abi(int kind, const tk_qindex& in, QIndex& out, std::string& err);
+
+// ---------------------------------------------------------------------------
+// Sector-GEMM tables.  One launch of the grouped GEMM kernel walks a tile
+// list; each tile belongs to a task (one output block) whose K dimension is a
+// list of segments (one per contributing sector pair), so contributions to
+// one output block are summed in registers without atomics.
+//   A(i,k) = A[a_off + i*a_rs + k*a_cs],  B(k,j) = B[b_off + k*b_rs + j*b_cs]
+//   C(i,j) = alpha * sum_seg A*B + beta * C   (C not read when beta == 0)
+// ---------------------------------------------------------------------------
+struct GemmSeg {
+    int64_t a_off, b_off;
+    int32_t a_rs, a_cs, b_rs, b_cs;
+    int32_t K, pad;
+};
+struct GemmTask {
+    int64_t c_off;
+    int32_t c_rs, c_cs;
+    int32_t M, N;
+    int32_t seg_begin, seg_end;
+    double alpha, beta;
+};
+struct GemmTile {
+    int32_t task, m0, n0, pad;
+};
+// Channel combine (W_i*W_j applied between the two GEMM stages):
+//   out[out_off + r*out_rs + c] = sum_t coef_t * in[in_off_t + r*in_rs_t + c]
+struct CombJob {
+    int64_t out_off;
+    int32_t out_rs, rows, cols, term_begin, term_end, pad;
+};
+struct CombTerm {
+    int64_t in_off;
+    int32_t in_rs, pad;
+    double coef;
+};
+
+// Host description of one dense<->flat sub-block copy (one state pair).
+struct SubMap {
+    int64_t dense_off, flat_off;
+    int32_t rows, cols;  // rows = D_A (dense row stride D_R), cols = D_B
+};
+
+struct GemmTable {
+    std::vector<GemmTask> tasks;
+    std::vector<GemmSeg> segs;
+    std::vector<GemmTile> tiles;
+    double flops = 0.0;
+};
+
+// Everything the device needs for one two-site H_eff, built on the host.
+struct Heff2Tables {
+    int kind = 0;
+    int64_t d_i = 0, d_j = 0, d_l = 0, d_r = 0, nwl = 0, nwr = 0;
+    // two-site block layout (FlatBlockStorage order: ascending packed key)
+    std::vector<uint64_t> keys;
+    std::vector<int64_t> blk_off;
+    int64_t total = 0;
+    std::vector<SubMap> submaps;
+    // non-zero sector slabs of L ([(a',w)][a]) and R ([b'][(w,b)])
+    std::vector<double> lbuf, rbuf;
+    // stage 1: T1 = L * psi ; stage 2: T2 = W_ij (x) T1 ; stage 3: y = T2 * R^T
+    GemmTable g1, g3;
+    std::vector<CombJob> jobs;
+    std::vector<CombTerm> terms;
+    int64_t t1_total = 0, t2_total = 0;
+    double comb_flops = 0.0;
+    double alg_bytes = 0.0;
+    // split-precision operand geometry (filled by the tensor-core path)
+    int64_t n_wij_terms = 0;
+};
+
+// Builds the tables; returns TK_OK or an error code with `err` set.
+tk_status build_heff2_tables(const tk_env& L, const tk_env& R, const tk_bst& wi, const tk_bst& wj,
+                             const int32_t* psi_flux, int tile_m, int tile_n, Heff2Tables& out,
+                             std::string& err);
+
+// Thread-local last-error message.
+void set_error(const std::string& msg);
+
+}  // namespace tk

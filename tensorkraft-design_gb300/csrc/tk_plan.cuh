@@ -1,0 +1,94 @@
+// tk_plan.cuh -- device-side state of a two-site H_eff plan.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "tc_gemm.cuh"
+#include "tk_internal.hpp"
+
+namespace tk {
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        reset();
+        n = count;
+        if (count == 0) return cudaSuccess;
+        return cudaMalloc(&p, sizeof(T) * count);
+    }
+    cudaError_t upload(const std::vector<T>& v) {
+        cudaError_t e = alloc(v.size());
+        if (e != cudaSuccess || v.empty()) return e;
+        return cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+    }
+};
+
+struct DevGemm {
+    DevBuf<GemmTask> tasks;
+    DevBuf<GemmSeg> segs;
+    DevBuf<GemmTile> tiles;
+    int n_tiles = 0;
+    cudaError_t upload(const GemmTable& g) {
+        cudaError_t e;
+        if ((e = tasks.upload(g.tasks)) != cudaSuccess) return e;
+        if ((e = segs.upload(g.segs)) != cudaSuccess) return e;
+        if ((e = tiles.upload(g.tiles)) != cudaSuccess) return e;
+        n_tiles = (int)g.tiles.size();
+        return cudaSuccess;
+    }
+};
+
+
+struct LanczosGraph;
+struct LanczosGraphDeleter {
+    void operator()(LanczosGraph* g) const;
+};
+
+}  // namespace tk
+
+struct tk_heff2_plan {
+    int device = 0;
+    int precision = TK_PREC_FP64;
+    tk::Heff2Tables host;
+    tk::DevBuf<double> lbuf, rbuf, t1, t2;
+    tk::DevGemm g1, g3;
+    tk::DevBuf<tk::CombJob> jobs;
+    tk::DevBuf<tk::CombTerm> terms;
+    int n_jobs = 0;
+    // host-call staging (allocated on first host call)
+    tk::DevBuf<double> hx, hy;
+    double* pin_x = nullptr;
+    double* pin_y = nullptr;
+    cudaStream_t stream = nullptr;
+    // split-precision operands and state (tensor-core path)
+    std::unique_ptr<tk::TcPlan, tk::TcPlanDeleter> tc;
+    // Lanczos workspace (allocated on first use)
+    tk::DevBuf<double> lz_basis, lz_w, lz_scal, lz_part, lz_vec;
+    int lz_cap_k = 0;
+    std::unique_ptr<tk::LanczosGraph, tk::LanczosGraphDeleter> lz_graph;
+    ~tk_heff2_plan() {
+        if (pin_x) cudaFreeHost(pin_x);
+        if (pin_y) cudaFreeHost(pin_y);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+// Dispatches one matvec in the requested precision (stream-ordered).
+extern "C" tk_status tk_heff2_apply_prec(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s, int precision);
+
+namespace tk {
+tk_status cuda_fail(const char* op, cudaError_t e);
+}
