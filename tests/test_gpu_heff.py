@@ -112,13 +112,21 @@ def test_exact_environments_ground_energy(lib_built):
 def test_empty_and_tiny(lib_built):
     """Boundary environments (1x1x1) and a single-sector bond."""
     p = exact_problem(models.heisenberg(), 2, 0, (0,))
-    plan = p.plan()
-    assert plan.block_dim == 2  # |up,down>, |down,up>
     H = oracle_dense_literal(p)
-    x = np.random.default_rng(0).standard_normal(plan.dense_dim)
+    x = np.random.default_rng(0).standard_normal(H.shape[0])
+    # all sectors: the reference's dense closure exactly
+    plan_all = p.plan(all_sectors=True)
+    assert plan_all.block_dim == 4
     y = np.zeros_like(x)
-    plan.apply_host(x, y)
+    plan_all.apply_host(x, y)
     assert rel_err(y, H @ x) < TOL
+    # flux 0: the Sz = 0 sector |up,down>, |down,up> only (projected closure)
+    plan = p.plan()
+    assert plan.block_dim == 2
+    sel = plan.flat_to_dense(np.ones(2)) != 0
+    xs = np.where(sel, x, 0.0)
+    plan.apply_host(x, y)
+    assert rel_err(y, np.where(sel, H @ xs, 0.0)) < TOL
 
 
 def test_sector_mismatch_reported(lib_built):
