@@ -113,6 +113,21 @@ void key_unpack(int kind, uint64_t key, int rank, Qn* qns) {
     for (int i = 0; i < rank; ++i) qns[i] = qn_unpack(kind, (key >> (i * bw)) & mask);
 }
 
+uint16_t f32_to_bf16_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+float bf16_bits_to_f32(uint16_t b) {
+    uint32_t u = (uint32_t)b << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
 int QIndex::find(const Qn& x) const {
     for (size_t s = 0; s < q.size(); ++s)
         if (q[s] == x) return (int)s;
@@ -579,6 +594,193 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                 T.g3.tasks.push_back(tk);
                 add_tiles(T.g3, (int)T.g3.tasks.size() - 1, tile_m, tile_n, ks);
             }
+    // --- split-precision regrouping (tensor-core stacks) ---------------------
+    {
+        TcTables& C = T.tc;
+        C = TcTables();
+        const int BK = kTcBK;
+        auto kchunks = [&](int64_t K) { return (int32_t)((K + BK - 1) / BK); };
+        std::vector<double> lq64, rq64;
+        // T1 pieces: key (p, A', ws, B) -> (offset of channel-0 row, row stride per a')
+        struct Piece { uint64_t key; int64_t off; int32_t rs; };
+        std::vector<Piece> pieces;
+        auto pkey = [&](int64_t p, int ap, int ws, int b) -> uint64_t {
+            return (((uint64_t)p * nA + ap) * nWL + ws) * nB + b;
+        };
+        int64_t t1off = 0;
+        // stage 1: one stack per ket sector A
+        for (int a = 0; a < nA; ++a) {
+            std::vector<std::pair<int, int>> lp;   // (A', ws)
+            std::vector<int64_t> lrow;
+            int64_t rows = 0;
+            for (int ap = 0; ap < nA; ++ap)
+                for (int ws = 0; ws < nWL; ++ws)
+                    if (lblk[((size_t)ap * nWL + ws) * nA + a] >= 0) {
+                        lp.push_back({ap, ws});
+                        lrow.push_back(rows);
+                        rows += QA.dim[ap] * WL.dim[ws];
+                    }
+            std::vector<std::pair<int64_t, int>> xp;  // (p, B)
+            std::vector<int64_t> xcol;
+            int64_t cols = 0;
+            for (int64_t p = 0; p < P; ++p)
+                for (int b = 0; b < nB; ++b)
+                    if (SUB(p, a, b) >= 0) {
+                        xp.push_back({p, b});
+                        xcol.push_back(cols);
+                        cols += QB.dim[b];
+                    }
+            if (rows == 0 || cols == 0) continue;
+            const int64_t K = QA.dim[a];
+            const int32_t kch = kchunks(K);
+            const int64_t lb = C.lq_rows, xb = C.xq_rows;
+            C.lq_rows += kch * rows;
+            C.xq_rows += kch * cols;
+            lq64.resize((size_t)C.lq_rows * BK, 0.0);
+            for (size_t i = 0; i < lp.size(); ++i) {
+                int ap = lp[i].first, ws = lp[i].second;
+                const double* src = T.lbuf.data() + lblk[((size_t)ap * nWL + ws) * nA + a];
+                int64_t nr = QA.dim[ap] * WL.dim[ws];
+                for (int64_t r = 0; r < nr; ++r)
+                    for (int64_t k = 0; k < K; ++k)
+                        lq64[(size_t)(lb + (k / BK) * rows + lrow[i] + r) * BK + (k % BK)] = src[r * K + k];
+            }
+            for (size_t i = 0; i < xp.size(); ++i) {
+                TcSplitJob j{};
+                j.src = SUB(xp[i].first, a, xp[i].second);
+                j.rows = (int32_t)K;
+                j.cols = (int32_t)QB.dim[xp[i].second];
+                j.xrow = (int32_t)(xb + xcol[i]);
+                j.cstride = (int32_t)cols;
+                C.split.push_back(j);
+            }
+            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
+                for (int64_t n0 = 0; n0 < cols; n0 += kTcBN) {
+                    TcTile t{};
+                    t.a_row = (int32_t)(lb + m0); t.a_cs = (int32_t)rows;
+                    t.b_row = (int32_t)(xb + n0); t.b_cs = (int32_t)cols;
+                    t.kch = kch;
+                    t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
+                    t.n_valid = (int32_t)std::min<int64_t>(kTcBN, cols - n0);
+                    t.mode = 0;
+                    t.out_off = t1off + m0 * cols + n0;
+                    t.ldc = (int32_t)cols;
+                    C.tiles1.push_back(t);
+                    C.mma_flops += 2.0 * kTcBM * kTcBN * (double)kch * BK;
+                }
+            for (size_t i = 0; i < lp.size(); ++i)
+                for (size_t jx = 0; jx < xp.size(); ++jx)
+                    pieces.push_back({pkey(xp[jx].first, lp[i].first, lp[i].second, xp[jx].second),
+                                      t1off + lrow[i] * cols + xcol[jx], (int32_t)(WL.dim[lp[i].second] * cols)});
+            t1off += rows * cols;
+        }
+        C.t1_total = t1off;
+        std::sort(pieces.begin(), pieces.end(), [](const Piece& x, const Piece& y) { return x.key < y.key; });
+        // stage 3: one stack per bra sector B' of R
+        for (int bp = 0; bp < nB; ++bp) {
+            std::vector<std::pair<int64_t, int>> yp;  // (p', A')
+            std::vector<int64_t> yr;
+            int64_t rows = 0;
+            for (int64_t p = 0; p < P; ++p)
+                for (int ap = 0; ap < nA; ++ap)
+                    if (SUB(p, ap, bp) >= 0) {
+                        yp.push_back({p, ap});
+                        yr.push_back(rows);
+                        rows += QA.dim[ap];
+                    }
+            if (rows == 0) continue;
+            std::vector<std::pair<int, int>> rp;  // (ws, B)
+            std::vector<int64_t> rk;
+            int64_t K = 0;
+            for (int ws = 0; ws < nWR; ++ws)
+                for (int b = 0; b < nB; ++b)
+                    if (rblk[((size_t)bp * nWR + ws) * nB + b] >= 0) {
+                        rp.push_back({ws, b});
+                        rk.push_back(K);
+                        K += WR.dim[ws] * QB.dim[b];
+                    }
+            const int32_t kch = kchunks(K);
+            const int64_t NB = QB.dim[bp];
+            const int64_t rbase = C.rq_rows, t2b = C.t2q_rows, yb = (int64_t)C.yrow.size();
+            C.rq_rows += kch * NB;
+            C.t2q_rows += kch * rows;
+            rq64.resize((size_t)C.rq_rows * BK, 0.0);
+            for (size_t i = 0; i < rp.size(); ++i) {
+                int ws = rp[i].first, b = rp[i].second;
+                const double* src = T.rbuf.data() + rblk[((size_t)bp * nWR + ws) * nB + b];
+                int64_t len = WR.dim[ws] * QB.dim[b];
+                for (int64_t r = 0; r < NB; ++r)
+                    for (int64_t kk = 0; kk < len; ++kk) {
+                        int64_t k = rk[i] + kk;
+                        rq64[(size_t)(rbase + (k / BK) * NB + r) * BK + (k % BK)] = src[r * len + kk];
+                    }
+            }
+            for (size_t i = 0; i < yp.size(); ++i) {
+                int64_t po = yp[i].first;
+                int ap = yp[i].second;
+                int64_t yo = SUB(po, ap, bp);
+                for (int64_t r = 0; r < QA.dim[ap]; ++r) C.yrow.push_back(yo + r * NB);
+                for (size_t ri = 0; ri < rp.size(); ++ri) {
+                    int ws = rp[ri].first, b = rp[ri].second;
+                    for (int64_t wloc = 0; wloc < WR.dim[ws]; ++wloc) {
+                        int64_t wr = WR.off[ws] + wloc;
+                        TcCombJob j{};
+                        j.t2row = (int32_t)(t2b + yr[i]);
+                        j.cstride = (int32_t)rows;
+                        j.k0 = (int32_t)(rk[ri] + wloc * QB.dim[b]);
+                        j.rows = (int32_t)QA.dim[ap];
+                        j.cols = (int32_t)QB.dim[b];
+                        j.term_begin = (int32_t)C.terms.size();
+                        for (const Term& tm : byout[po * nwr + wr]) {
+                            uint64_t key = pkey(tm.p, ap, wl_sec[tm.wl], b);
+                            auto it = std::lower_bound(pieces.begin(), pieces.end(), key,
+                                                       [](const Piece& x, uint64_t k) { return x.key < k; });
+                            for (; it != pieces.end() && it->key == key; ++it) {
+                                TcCombTerm ct{};
+                                ct.in_off = it->off + wl_loc[tm.wl] * (int64_t)(it->rs / WL.dim[wl_sec[tm.wl]]);
+                                ct.in_rs = it->rs;
+                                ct.coef = (float)tm.c;
+                                C.terms.push_back(ct);
+                            }
+                        }
+                        j.term_end = (int32_t)C.terms.size();
+                        if (j.term_end > j.term_begin) C.jobs.push_back(j);
+                    }
+                }
+            }
+            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
+                for (int64_t n0 = 0; n0 < NB; n0 += kTcBN) {
+                    TcTile t{};
+                    t.a_row = (int32_t)(t2b + m0); t.a_cs = (int32_t)rows;
+                    t.b_row = (int32_t)(rbase + n0); t.b_cs = (int32_t)NB;
+                    t.kch = kch;
+                    t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
+                    t.n_valid = (int32_t)std::min<int64_t>(kTcBN, NB - n0);
+                    t.mode = 1;
+                    t.out_off = yb + m0;
+                    t.ldc = 0;
+                    t.n0 = (int32_t)n0;
+                    C.tiles3.push_back(t);
+                    C.mma_flops += 2.0 * kTcBM * kTcBN * (double)kch * BK;
+                }
+        }
+        // split the constant operands into bf16 hi + lo
+        auto split = [](const std::vector<double>& v, std::vector<uint16_t>& hi, std::vector<uint16_t>& lo) {
+            hi.resize(v.size());
+            lo.resize(v.size());
+            for (size_t i = 0; i < v.size(); ++i) {
+                uint16_t h = f32_to_bf16_bits((float)v[i]);
+                hi[i] = h;
+                lo[i] = f32_to_bf16_bits((float)(v[i] - (double)bf16_bits_to_f32(h)));
+            }
+        };
+        split(lq64, C.lq_hi, C.lq_lo);
+        split(rq64, C.rq_hi, C.rq_lo);
+        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
+            err = "tensor-core operand rows exceed 32 bits";
+            return TK_ERR_UNSUPPORTED;
+        }
+    }
     lpt_order(T.g1, tile_m, tile_n);
     lpt_order(T.g3, tile_m, tile_n);
     // Algorithmic bytes: psi in, y out, the block-sparse L, R and W_ij terms, FP64.

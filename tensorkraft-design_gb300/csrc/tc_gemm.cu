@@ -1,30 +1,443 @@
-// tc_gemm.cu -- split-precision (bf16x3) sector-GEMM path on tcgen05 tensor cores.
+// tc_gemm.cu -- split-precision (bf16x3) sector GEMMs on tcgen05 tensor cores.
+//
+// Every FP64 operand x is split into bf16 hi = rn(x) and lo = rn(x - hi);
+// a product a*b is evaluated as hi_a*hi_b + hi_a*lo_b + lo_a*hi_b with fp32
+// accumulation in tensor memory (the lo*lo term, ~2^-16 relative, is dropped).
+//
+// One matvec = four launches on one stream:
+//   split_psi_kernel   psi (fp64, FlatBlockStorage) -> stage-1 B operand, hi/lo,
+//                      transposed through shared memory into K-major chunks
+//   tc_gemm_kernel     stage 1, T1 = L_stack(A) * psi_A        (fp32 out)
+//   combine_tc_kernel  W_i*W_j channel combine, T1 -> stage-3 A operand hi/lo
+//   tc_gemm_kernel     stage 3, y = T2_stack(B') * R_stack(B')^T (fp64 out via a row table)
+//
+// tc_gemm_kernel: one CTA (4 warps) per 128 x 64 output tile.  Warp 0 lane 0
+// streams 64-wide K chunks of A_hi, A_lo, B_hi, B_lo with TMA (128-byte
+// swizzle) into a two-stage shared-memory ring; warp 1 allocates 64 TMEM
+// columns and lane 0 issues three tcgen05.mma (kind::f16, bf16 in, fp32
+// accumulate, M=128, N=64, K=16) per 16-wide K step; all four warps read the
+// accumulator back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and
+// store it.  Every mbarrier wait is bounded: on timeout the kernel records an
+// error word, drains what it issued (again bounded), frees its TMEM and exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
 #include "tc_gemm.cuh"
+#include "tk_plan.cuh"
 
 namespace tk {
 
+namespace {
+
+constexpr int NST = 2;                              // pipeline stages
+constexpr int A_BYTES = kTcBM * kTcBK * 2;          // 16 KB (one of hi / lo)
+constexpr int B_BYTES = kTcBN * kTcBK * 2;          // 8 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr int SMEM_BYTES = NST * STAGE_BYTES + 1024 + 256;
+constexpr int TMEM_COLS = kTcBN;                    // fp32 accumulator 128 lanes x 64 columns
+constexpr long WAIT_LIMIT = 1L << 22;               // bounded mbarrier polls
+
+// error word codes
+constexpr int ERR_FULL_TIMEOUT = 1, ERR_EMPTY_TIMEOUT = 2, ERR_DONE_TIMEOUT = 3;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; false (and the error word set) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+    for (long i = 0; i < WAIT_LIMIT; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicCAS(err, 0, code);
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row core groups 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: fp32 accumulate, bf16 A and B, both
+// K-major, N>>3 at bit 17, M>>4 at bit 24.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcBN >> 3) << 17) |
+                            ((uint32_t)(kTcBM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void store_out(const TcTile& t, int row, int col, float v, float* out32, double* out64,
+                                          const int64_t* rowtab) {
+    if (t.mode == 0)
+        out32[t.out_off + (int64_t)row * t.ldc + col] = v;
+    else
+        out64[rowtab[t.out_off + row] + t.n0 + col] = (double)v;
+}
+
+__global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restrict__ tiles,
+                                                         const __grid_constant__ CUtensorMap mAh,
+                                                         const __grid_constant__ CUtensorMap mAl,
+                                                         const __grid_constant__ CUtensorMap mBh,
+                                                         const __grid_constant__ CUtensorMap mBl,
+                                                         float* __restrict__ out32, double* __restrict__ out64,
+                                                         const int64_t* __restrict__ rowtab, int* err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
+    uint64_t* empty = full + NST;
+    uint64_t* done = empty + NST;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    const TcTile t = tiles[blockIdx.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (t.kch == 0) {  // no K: the tile is zero
+        for (int e = threadIdx.x; e < t.m_valid * t.n_valid; e += blockDim.x)
+            store_out(t, e / t.n_valid, e % t.n_valid, 0.f, out32, out64, rowtab);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        // producer: TMA loads of the K chunks
+        for (int c = 0; c < t.kch && ok; ++c) {
+            const int s = c % NST;
+            if (c >= NST) ok = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
+            if (!ok) break;
+            uint8_t* st = smem + s * STAGE_BYTES;
+            mbar_expect_tx(&full[s], STAGE_BYTES);
+            const int ya = t.a_row + c * t.a_cs, yb = t.b_row + c * t.b_cs;
+            tma_load_2d(st, &mAh, 0, ya, &full[s]);
+            tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[s]);
+            tma_load_2d(st + 2 * A_BYTES, &mBh, 0, yb, &full[s]);
+            tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mBl, 0, yb, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer: three bf16 products per 16-wide K step
+        for (int c = 0; c < t.kch && ok; ++c) {
+            const int s = c % NST;
+            ok = mbar_wait(&full[s], (c / NST) & 1, err, ERR_FULL_TIMEOUT);
+            if (!ok) break;
+            fence_after();
+            const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+            const uint64_t ah = sw128_desc(sa), al = sw128_desc(sa + A_BYTES);
+            const uint64_t bh = sw128_desc(sa + 2 * A_BYTES), bl = sw128_desc(sa + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < kTcBK / 16; ++kk) {
+                const uint64_t adv = (uint64_t)((kk * 32) >> 4);  // 16 bf16 = 32 bytes along K
+                mma_bf16(tmem, ah + adv, bh + adv, (c | kk) != 0);
+                mma_bf16(tmem, ah + adv, bl + adv, 1u);
+                mma_bf16(tmem, al + adv, bh + adv, 1u);
+            }
+            mma_commit(&empty[s]);
+        }
+        mma_commit(done);
+    }
+    __syncwarp();
+    // epilogue: thread r owns accumulator row r (TMEM lane r)
+    const bool have = mbar_wait(done, 0, err, ERR_DONE_TIMEOUT);
+    fence_after();
+    // tcgen05.ld is warp-collective: decide per warp
+    const bool go = __all_sync(0xffffffffu, have && (*(volatile int*)err == 0));
+    if (go) {
+        const int row = threadIdx.x;
+        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < kTcBN; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + c0, v);
+            if (row < t.m_valid) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (c0 + j < t.n_valid) store_out(t, row, c0 + j, v[j], out32, out64, rowtab);
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+__device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+    hi = __float2bfloat16_rn((float)x);
+    lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+}
+
+// psi sub-block (D_A x D_B, row-major fp64) -> B operand rows (one per column b),
+// 64-wide K chunks over a; transposed through a 64 x 32 shared tile.
+__global__ void __launch_bounds__(256) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
+                                                        const double* __restrict__ x, __nv_bfloat16* __restrict__ xh,
+                                                        __nv_bfloat16* __restrict__ xl) {
+    const TcSplitJob j = jobs[blockIdx.x];
+    __shared__ double tile[64][33];
+    for (int a0 = 0; a0 < j.rows; a0 += 64)
+        for (int b0 = 0; b0 < j.cols; b0 += 32) {
+            __syncthreads();
+            for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
+                const int a = e >> 5, b = e & 31;
+                double v = 0.0;
+                if (a0 + a < j.rows && b0 + b < j.cols) v = x[j.src + (int64_t)(a0 + a) * j.cols + b0 + b];
+                tile[a][b] = v;
+            }
+            __syncthreads();
+            const int64_t rowbase = (int64_t)j.xrow + (int64_t)(a0 >> 6) * j.cstride;
+            for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
+                const int b = e >> 6, a = e & 63;
+                if (a0 + a < j.rows && b0 + b < j.cols) {
+                    __nv_bfloat16 h, l;
+                    split2(tile[a][b], h, l);
+                    const int64_t idx = ((rowbase + b0 + b) << 6) + a;
+                    xh[idx] = h;
+                    xl[idx] = l;
+                }
+            }
+        }
+}
+
+__global__ void __launch_bounds__(256) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+                                                         const TcCombTerm* __restrict__ terms,
+                                                         const float* __restrict__ t1, __nv_bfloat16* __restrict__ th,
+                                                         __nv_bfloat16* __restrict__ tl) {
+    const TcCombJob j = jobs[blockIdx.x];
+    __shared__ TcCombTerm st[32];
+    const int nterm = j.term_end - j.term_begin;
+    const int n = j.rows * j.cols;
+    // accumulate in registers over term chunks of 32; elements strided by block
+    for (int e0 = 0; e0 < n; e0 += blockDim.x) {
+        const int e = e0 + threadIdx.x;
+        const int r = e < n ? e / j.cols : 0, c = e < n ? e - r * j.cols : 0;
+        float acc = 0.f;
+        for (int t0 = 0; t0 < nterm; t0 += 32) {
+            const int tn = min(32, nterm - t0);
+            __syncthreads();
+            if (threadIdx.x < tn) st[threadIdx.x] = terms[j.term_begin + t0 + threadIdx.x];
+            __syncthreads();
+            if (e < n)
+                for (int t = 0; t < tn; ++t) acc = fmaf(st[t].coef, t1[st[t].in_off + (int64_t)r * st[t].in_rs + c], acc);
+        }
+        if (e < n) {
+            const int k = j.k0 + c;
+            const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
+            const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+            th[idx] = h;
+            tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
+        }
+    }
+}
+
+template <class T>
+cudaError_t put(T** dst, const std::vector<T>& v) {
+    *dst = nullptr;
+    if (v.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)dst, sizeof(T) * v.size());
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+}
+
+bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string& err) {
+    std::memset(m, 0, sizeof(*m));
+    if (rows <= 0) return true;
+    cuuint64_t dims[2] = {(cuuint64_t)kTcBK, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kTcBK * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = cuTensorMapEncodeTiled(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
+                                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        const char* s = nullptr;
+        cuGetErrorString(r, &s);
+        err = std::string("cuTensorMapEncodeTiled: ") + (s ? s : "error");
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+
 struct TcPlan {
-    int unused = 0;
+    __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
+    __nv_bfloat16 *xh = nullptr, *xl = nullptr, *th = nullptr, *tl = nullptr;
+    float* t1 = nullptr;
+    TcTile *tiles1 = nullptr, *tiles3 = nullptr;
+    TcSplitJob* split = nullptr;
+    TcCombJob* jobs = nullptr;
+    TcCombTerm* terms = nullptr;
+    int64_t* yrow = nullptr;
+    int* err = nullptr;
+    int n1 = 0, n3 = 0, nsplit = 0, njobs = 0;
+    CUtensorMap mLh, mLl, mXh, mXl, mTh, mTl, mRh, mRl;
+    ~TcPlan() {
+        void* ps[] = {lh, ll, rh, rl, xh, xl, th, tl, t1, tiles1, tiles3, split, jobs, terms, yrow, err};
+        for (void* p : ps)
+            if (p) cudaFree(p);
+    }
 };
 
 void TcPlanDeleter::operator()(TcPlan* p) const { delete p; }
 
-tk_status tc_plan_create(const Heff2Tables&, const double*, const double*, std::unique_ptr<TcPlan, TcPlanDeleter>&,
-                         std::string& err) {
-    err = "split-precision path not built";
-    return TK_ERR_UNSUPPORTED;
+tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
+                         std::unique_ptr<TcPlan, TcPlanDeleter>& out, std::string& err) {
+    const TcTables& C = host.tc;
+    std::unique_ptr<TcPlan, TcPlanDeleter> p(new TcPlan);
+    cudaError_t e = cudaSuccess;
+    auto bf = [](const std::vector<uint16_t>& v) {
+        return std::vector<__nv_bfloat16>(reinterpret_cast<const __nv_bfloat16*>(v.data()),
+                                          reinterpret_cast<const __nv_bfloat16*>(v.data()) + v.size());
+    };
+    auto zeros = [&](__nv_bfloat16** d, int64_t rows) -> cudaError_t {
+        *d = nullptr;
+        if (rows <= 0) return cudaSuccess;
+        cudaError_t r = cudaMalloc((void**)d, sizeof(__nv_bfloat16) * kTcBK * (size_t)rows);
+        if (r != cudaSuccess) return r;
+        return cudaMemset(*d, 0, sizeof(__nv_bfloat16) * kTcBK * (size_t)rows);
+    };
+    if ((e = put(&p->lh, bf(C.lq_hi))) != cudaSuccess || (e = put(&p->ll, bf(C.lq_lo))) != cudaSuccess ||
+        (e = put(&p->rh, bf(C.rq_hi))) != cudaSuccess || (e = put(&p->rl, bf(C.rq_lo))) != cudaSuccess ||
+        (e = zeros(&p->xh, C.xq_rows)) != cudaSuccess || (e = zeros(&p->xl, C.xq_rows)) != cudaSuccess ||
+        (e = zeros(&p->th, C.t2q_rows)) != cudaSuccess || (e = zeros(&p->tl, C.t2q_rows)) != cudaSuccess ||
+        (e = put(&p->tiles1, C.tiles1)) != cudaSuccess || (e = put(&p->tiles3, C.tiles3)) != cudaSuccess ||
+        (e = put(&p->split, C.split)) != cudaSuccess || (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
+        (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess) {
+        err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
+    }
+    if ((e = cudaMalloc((void**)&p->t1, sizeof(float) * (size_t)std::max<int64_t>(C.t1_total, 1))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&p->err, sizeof(int))) != cudaSuccess || (e = cudaMemset(p->err, 0, sizeof(int))) != cudaSuccess) {
+        err = std::string("tensor-core workspace: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
+    }
+    p->n1 = (int)C.tiles1.size();
+    p->n3 = (int)C.tiles3.size();
+    p->nsplit = (int)C.split.size();
+    p->njobs = (int)C.jobs.size();
+    if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
+        !make_map(&p->mXh, p->xh, C.xq_rows, kTcBN, err) || !make_map(&p->mXl, p->xl, C.xq_rows, kTcBN, err) ||
+        !make_map(&p->mTh, p->th, C.t2q_rows, kTcBM, err) || !make_map(&p->mTl, p->tl, C.t2q_rows, kTcBM, err) ||
+        !make_map(&p->mRh, p->rh, C.rq_rows, kTcBN, err) || !make_map(&p->mRl, p->rl, C.rq_rows, kTcBN, err))
+        return TK_ERR_CUDA;
+    if ((e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)) !=
+        cudaSuccess) {
+        err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+        return TK_ERR_CUDA;
+    }
+    out = std::move(p);
+    return TK_OK;
 }
 
-cudaError_t tc_apply(TcPlan&, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double*, double*,
-                     cudaStream_t, std::string& err) {
-    err = "split-precision path not built";
-    return cudaErrorNotSupported;
+cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double* x,
+                           double* y, cudaStream_t s, int stage, std::string& err) {
+    if (stage == 0) {
+        if (tc.nsplit > 0) split_psi_kernel<<<tc.nsplit, 256, 0, s>>>(tc.split, x, tc.xh, tc.xl);
+        if (tc.n1 > 0)
+            tc_gemm_kernel<<<tc.n1, 128, SMEM_BYTES, s>>>(tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl, tc.t1, nullptr,
+                                                          nullptr, tc.err);
+    } else if (stage == 1) {
+        if (tc.njobs > 0) combine_tc_kernel<<<tc.njobs, 256, 0, s>>>(tc.jobs, tc.terms, tc.t1, tc.th, tc.tl);
+    } else {
+        if (tc.n3 > 0)
+            tc_gemm_kernel<<<tc.n3, 128, SMEM_BYTES, s>>>(tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl, nullptr, y,
+                                                          tc.yrow, tc.err);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) err = "tensor-core stage launch";
+    return e;
 }
 
-cudaError_t tc_apply_stage(TcPlan&, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double*, double*,
-                           cudaStream_t, int, std::string& err) {
-    err = "split-precision path not built";
-    return cudaErrorNotSupported;
+cudaError_t tc_apply(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs, int n_jobs, const CombTerm* d_terms,
+                     const double* x, double* y, cudaStream_t s, std::string& err) {
+    for (int stage = 0; stage < 3; ++stage) {
+        cudaError_t e = tc_apply_stage(tc, host, d_jobs, n_jobs, d_terms, x, y, s, stage, err);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
+
+int* tc_error_word(TcPlan& tc) { return tc.err; }
 
 }  // namespace tk

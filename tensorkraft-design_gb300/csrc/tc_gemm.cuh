@@ -29,3 +29,8 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables& host, const CombJob* d
                            std::string& err);
 
 }  // namespace tk
+
+namespace tk {
+// Device error word of the tensor-core kernels (0 = no bounded wait ran out).
+int* tc_error_word(TcPlan& tc);
+}  // namespace tk

@@ -99,6 +99,57 @@ struct GemmTable {
     double flops = 0.0;
 };
 
+// ---------------------------------------------------------------------------
+// Split-precision (tensor-core) tables.  Both GEMM stages are regrouped into
+// "stacks" that share one operand:
+//   stage 1, one stack per ket sector A of L: rows = every L slab (A', ws, A)
+//     stacked, columns = every psi sub-block (p, A, B) side by side, K = D_A;
+//   stage 3, one stack per bra sector B' of R: rows = every y sub-block
+//     (p', A', B') stacked, columns = D_B', K = every R slab (B', ws, B)
+//     concatenated.
+// Operands are bf16 (hi, lo) pairs stored K-major in 64-element chunks: a
+// stack's chunk c occupies `cstride` consecutive rows of 64 bf16 starting at
+// row base + c*cstride, so one 2D TMA tensor map covers a whole buffer.
+// K beyond a stack's extent is zero in both operands.
+// ---------------------------------------------------------------------------
+constexpr int kTcBM = 128;  // rows per tensor-core tile (UMMA M)
+constexpr int kTcBN = 64;   // columns per tensor-core tile (UMMA N)
+constexpr int kTcBK = 64;   // K chunk (128 bytes of bf16: one swizzle atom)
+
+struct TcTile {
+    int32_t a_row, a_cs;     // A operand row of chunk 0 at this tile's m0; rows between chunks
+    int32_t b_row, b_cs;     // B operand row of chunk 0 at this tile's n0; rows between chunks
+    int32_t kch, m_valid, n_valid, mode;  // mode 0: fp32 row-major out; 1: fp64 out through a row table
+    int64_t out_off;         // mode 0: element offset of (m0, n0); mode 1: row-table index of m0
+    int32_t ldc, n0;         // mode 0: row stride; mode 1: column offset added to the row table
+};
+// psi sub-block -> stage-1 B operand (transposed into K-major chunks), hi/lo split.
+struct TcSplitJob {
+    int64_t src;             // flat offset of the (D_A x D_B) sub-block
+    int32_t rows, cols;      // D_A (becomes K), D_B (becomes N)
+    int32_t xrow, cstride;   // operand row of chunk 0 for column 0; rows between chunks
+};
+// T1 (fp32) -> stage-3 A operand (K-major chunks), hi/lo split.
+struct TcCombJob {
+    int32_t t2row, cstride;  // operand row of chunk 0 for slab row 0; rows between chunks
+    int32_t k0, rows, cols, term_begin, term_end, pad;
+};
+struct TcCombTerm {
+    int64_t in_off;
+    int32_t in_rs;
+    float coef;
+};
+struct TcTables {
+    int64_t lq_rows = 0, rq_rows = 0, xq_rows = 0, t2q_rows = 0, t1_total = 0;
+    std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
+    std::vector<TcTile> tiles1, tiles3;
+    std::vector<TcSplitJob> split;
+    std::vector<TcCombJob> jobs;
+    std::vector<TcCombTerm> terms;
+    std::vector<int64_t> yrow;  // y element offset of every stage-3 operand row
+    double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
+};
+
 // Everything the device needs for one two-site H_eff, built on the host.
 struct Heff2Tables {
     int kind = 0;
@@ -117,9 +168,14 @@ struct Heff2Tables {
     int64_t t1_total = 0, t2_total = 0;
     double comb_flops = 0.0;
     double alg_bytes = 0.0;
-    // split-precision operand geometry (filled by the tensor-core path)
     int64_t n_wij_terms = 0;
+    // split-precision (tensor-core) regrouping of the same work
+    TcTables tc;
 };
+
+// bf16 bit pattern of a float, round to nearest even (NaN kept quiet).
+uint16_t f32_to_bf16_bits(float f);
+float bf16_bits_to_f32(uint16_t b);
 
 // Builds the tables; returns TK_OK or an error code with `err` set.
 tk_status build_heff2_tables(const tk_env& L, const tk_env& R, const tk_bst& wi, const tk_bst& wj,
