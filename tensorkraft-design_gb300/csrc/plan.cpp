@@ -280,6 +280,74 @@ static void lpt_order(GemmTable& g, int tile_m, int tile_n) {
                      [&](const GemmTile& a, const GemmTile& b) { return cost(a) > cost(b); });
 }
 
+// Every device access the tables can produce, checked against its buffer on
+// the host: a table fault becomes an error code instead of a device fault.
+static bool validate_tables(const Heff2Tables& T, std::string& err) {
+    auto gemm_ok = [&](const GemmTable& g, int64_t na, int64_t nb, int64_t nc, const char* name) {
+        for (const GemmTile& tl : g.tiles) {
+            if (tl.task < 0 || (size_t)tl.task >= g.tasks.size()) { err = std::string(name) + ": tile task"; return false; }
+            const GemmTask& t = g.tasks[tl.task];
+            if (tl.m0 < 0 || tl.m0 >= t.M || tl.n0 < 0 || tl.n0 >= t.N) { err = std::string(name) + ": tile origin"; return false; }
+        }
+        for (const GemmTask& t : g.tasks) {
+            if (t.M <= 0 || t.N <= 0) { err = std::string(name) + ": empty task"; return false; }
+            int64_t cmax = t.c_off + (int64_t)(t.M - 1) * t.c_rs + (int64_t)(t.N - 1) * t.c_cs;
+            if (t.c_off < 0 || cmax >= nc) { err = std::string(name) + ": output range"; return false; }
+            if (t.seg_begin < 0 || t.seg_end < t.seg_begin || (size_t)t.seg_end > g.segs.size()) { err = std::string(name) + ": segments"; return false; }
+            for (int s = t.seg_begin; s < t.seg_end; ++s) {
+                const GemmSeg& sg = g.segs[s];
+                int64_t amax = sg.a_off + (int64_t)(t.M - 1) * sg.a_rs + (int64_t)(sg.K - 1) * sg.a_cs;
+                int64_t bmax = sg.b_off + (int64_t)(sg.K - 1) * sg.b_rs + (int64_t)(t.N - 1) * sg.b_cs;
+                if (sg.K <= 0 || sg.a_off < 0 || sg.b_off < 0 || amax >= na || bmax >= nb) { err = std::string(name) + ": operand range"; return false; }
+            }
+        }
+        return true;
+    };
+    if (!gemm_ok(T.g1, (int64_t)T.lbuf.size(), T.total, T.t1_total, "stage 1")) return false;
+    if (!gemm_ok(T.g3, T.t2_total, (int64_t)T.rbuf.size(), T.total, "stage 3")) return false;
+    for (const CombJob& j : T.jobs) {
+        if (j.rows <= 0 || j.cols <= 0 || j.out_off < 0 || j.out_off + (int64_t)(j.rows - 1) * j.out_rs + j.cols - 1 >= T.t2_total ||
+            j.term_begin < 0 || j.term_end < j.term_begin || (size_t)j.term_end > T.terms.size()) { err = "combine job range"; return false; }
+        for (int t = j.term_begin; t < j.term_end; ++t) {
+            const CombTerm& c = T.terms[t];
+            if (c.in_off < 0 || c.in_off + (int64_t)(j.rows - 1) * c.in_rs + j.cols - 1 >= T.t1_total) { err = "combine term range"; return false; }
+        }
+    }
+    const TcTables& C = T.tc;
+    for (const TcTile& t : C.tiles1) {
+        if (t.mode != 0 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
+            t.out_off < 0 || t.out_off + (int64_t)(t.m_valid - 1) * t.ldc + t.n_valid - 1 >= C.t1_total ||
+            t.a_row < 0 || t.b_row < 0) { err = "tensor-core stage 1 tile"; return false; }
+    }
+    for (const TcTile& t : C.tiles3) {
+        if (t.mode != 1 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
+            t.out_off < 0 || t.out_off + t.m_valid - 1 >= (int64_t)C.yrow.size() || t.a_row < 0 || t.b_row < 0) {
+            err = "tensor-core stage 3 tile";
+            return false;
+        }
+        for (int r = 0; r < t.m_valid; ++r) {
+            int64_t y0 = C.yrow[t.out_off + r];
+            if (y0 < 0 || y0 + t.n0 + t.n_valid - 1 >= T.total) { err = "tensor-core stage 3 output row"; return false; }
+        }
+    }
+    for (const TcSplitJob& j : C.split) {
+        int64_t imax = (((int64_t)j.xrow + (int64_t)((j.rows - 1) >> 6) * j.cstride + j.cols - 1) << 6) + 63;
+        if (j.rows <= 0 || j.cols <= 0 || j.src < 0 || j.src + (int64_t)j.rows * j.cols > T.total || j.xrow < 0 ||
+            imax >= C.xq_rows * kTcBK) { err = "tensor-core split job"; return false; }
+    }
+    for (const TcCombJob& j : C.jobs) {
+        int64_t kmax = (int64_t)j.k0 + j.cols - 1;
+        int64_t imax = (((int64_t)j.t2row + (kmax >> 6) * j.cstride + j.rows - 1) << 6) + 63;
+        if (j.rows <= 0 || j.cols <= 0 || j.k0 < 0 || j.t2row < 0 || imax >= C.t2q_rows * kTcBK || j.term_begin < 0 ||
+            j.term_end < j.term_begin || (size_t)j.term_end > C.terms.size()) { err = "tensor-core combine job"; return false; }
+        for (int t = j.term_begin; t < j.term_end; ++t) {
+            const TcCombTerm& c = C.terms[t];
+            if (c.in_off < 0 || c.in_off + (int64_t)(j.rows - 1) * c.in_rs + j.cols - 1 >= C.t1_total) { err = "tensor-core combine term"; return false; }
+        }
+    }
+    return true;
+}
+
 tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi,
                              const tk_bst& wj_abi, const int32_t* psi_flux, int tile_m, int tile_n,
                              Heff2Tables& T, std::string& err) {
@@ -790,6 +858,10 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
         T.terms.size() > (size_t)INT32_MAX || T.g1.segs.size() > (size_t)INT32_MAX) {
         err = "sector tables exceed 32-bit index range";
         return TK_ERR_UNSUPPORTED;
+    }
+    if (!validate_tables(T, err)) {
+        err = "internal table check failed: " + err;
+        return TK_ERR_INVALID_ARG;
     }
     return TK_OK;
 }

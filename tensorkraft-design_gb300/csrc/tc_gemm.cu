@@ -20,6 +20,7 @@
 // store it.  Every mbarrier wait is bounded: on timeout the kernel records an
 // error word, drains what it issued (again bounded), frees its TMEM and exits.
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -319,20 +320,36 @@ cudaError_t put(T** dst, const std::vector<T>& v) {
     return cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so the
+// library does not link libcuda directly.
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn(std::string& err) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (fn) return fn;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+        err = "cuTensorMapEncodeTiled entry point unavailable";
+        return nullptr;
+    }
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return fn;
+}
+
 bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string& err) {
     std::memset(m, 0, sizeof(*m));
     if (rows <= 0) return true;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn(err);
+    if (!enc) return false;
     cuuint64_t dims[2] = {(cuuint64_t)kTcBK, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)kTcBK * 2};
     cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = cuTensorMapEncodeTiled(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
                                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
-        const char* s = nullptr;
-        cuGetErrorString(r, &s);
-        err = std::string("cuTensorMapEncodeTiled: ") + (s ? s : "error");
+        err = "cuTensorMapEncodeTiled failed with CUresult " + std::to_string((int)r);
         return false;
     }
     return true;

@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    cmd = [NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcuda"]
+    cmd = [NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

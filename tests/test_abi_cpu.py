@@ -48,3 +48,58 @@ def test_gemm_shape_mismatch_rejected(lib_built):
     b = _abi.tk_mat(buf.ctypes.data, 2, 2, 2, 1, 0)
     c = _abi.tk_mat_mut(buf.ctypes.data, 2, 2, 2, 1)
     assert lib.tk_gemm_f64(None, 1.0, C.byref(a), C.byref(b), 0.0, C.byref(c), None) == 1
+
+
+def _plan_status(prob, all_sectors=False):
+    """Runs tk_heff2_plan_create up to its first CUDA call with a fake context:
+    the host tables are built and self-checked; on a machine without a GPU the
+    call then stops at cudaSetDevice with TK_ERR_CUDA."""
+    from tk_gb300.heff import _Marshal
+
+    lib = _abi.load()
+    m = _Marshal()
+    el, er = m.env(prob.env_l), m.env(prob.env_r)
+    bi, bj = m.bst(prob.w_i), m.bst(prob.w_j)
+    fl = None
+    if not all_sectors:
+        farr = np.array(list(prob.flux) + [0], dtype=np.int32)
+        m.keep.append(farr)
+        fl = _abi.i32ptr(farr)
+    fake_ctx = np.zeros(4, dtype=np.int32)  # struct tk_ctx { int device = 0; }
+    h = C.c_void_p()
+    st = lib.tk_heff2_plan_create(fake_ctx.ctypes.data, C.byref(el), C.byref(er), C.byref(bi), C.byref(bj), fl, 0,
+                                  C.byref(h))
+    return st, lib.tk_last_error().decode()
+
+
+def test_host_tables_self_check_cpu(lib_built):
+    import torch
+    from helpers import small_problem
+
+    if torch.cuda.is_available():
+        import pytest
+
+        pytest.skip("CPU-only check (a GPU would create a real plan)")
+    for name, D in [("heisenberg", 40), ("hubbard", 48), ("cylinder", 96)]:
+        for all_sectors in (False, True):
+            st, msg = _plan_status(small_problem(name, D), all_sectors)
+            assert st == 4 and "cudaSetDevice" in msg, (name, st, msg)
+
+
+def test_sector_mismatch_cpu(lib_built):
+    import torch
+    from helpers import small_problem
+    from tk_gb300 import models
+
+    if torch.cuda.is_available():
+        import pytest
+
+        pytest.skip("CPU-only check")
+    p = small_problem("heisenberg", 12)
+    p.w_i = models.hubbard().bulk  # different quantum-number kind
+    st, msg = _plan_status(p)
+    assert st == 1 and "kinds" in msg
+    p = small_problem("heisenberg", 12)
+    p.w_j = models.cylinder_j1(4).bulk  # bond QIndex differs from the environment's
+    st, msg = _plan_status(p)
+    assert st == 2, (st, msg)
