@@ -2,11 +2,15 @@
 """Two-site DMRG H_eff matvec throughput on GB300.
 
 One step = one matvec y = H_eff x of the named two-site workload (synthetic,
-seeded; inputs resident in HBM for `value`).  `--impl reference` times the
-CPU restatement of the reference's matvec (the Rust reference cannot be
-built here) on the host cores instead.  With N ranks every rank runs an
-independent replica of the workload (the matvec does not shard across GPUs:
-replicas only); value = matvecs of all ranks / max-over-ranks time.
+seeded; inputs resident in HBM for `value`, L2 flushed between steps).
+`--impl reference` times the CPU restatement of the reference's matvec (the
+Rust reference cannot be built here) on the host cores instead.  With N ranks
+every rank runs an independent replica (the matvec does not shard across
+GPUs: replicas only); value = matvecs of all ranks / max-over-ranks time.
+
+Besides matvec/s the line reports the time to the lowest eigenpair of the same
+H_eff with the FP64 path and with the split-precision path + FP64 refinement,
+and |dE| between them (the metric's "at |dE| <= 1e-10").
 
 Prints one JSON line on rank 0.
 """
@@ -31,26 +35,25 @@ import numpy as np  # noqa: E402
 METRIC = "H_eff matvec/s (two-site, D=2048 Hubbard U(1)xU(1))"
 UNIT = "matvec/s"
 L2_BYTES = 129 * 1024 * 1024
+STAGES = ["stage1_L_psi", "stage2_wij_combine", "stage3_R"]
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hubbard_d2048")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16x3"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-lanczos", action="store_true")
     return ap.parse_args()
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
 def oracle_for(prob):
@@ -62,42 +65,43 @@ def oracle_for(prob):
                                     prob.env_l.data, prob.env_r.data)
 
 
-def time_cpu(orc, x, seconds: float, min_runs: int = 1):
-    """Runs whole matvecs until `seconds` elapse; returns (matvecs/s, runs, elapsed)."""
+def time_cpu(orc, x, seconds: float):
     y = np.empty_like(x)
-    orc.apply_into(x, y)  # warm
+    orc.apply_into(x, y)
     runs, t0 = 0, time.perf_counter()
     while True:
         orc.apply_into(x, y)
         runs += 1
         el = time.perf_counter() - t0
-        if el >= seconds and runs >= min_runs:
+        if el >= seconds:
             return runs / el, runs, el
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi SM clocks and throttle reasons, 100 ms period."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
-        self.device = device
-        self.proc = None
-        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"tk_clocks_{os.getpid()}.csv"
+        self.device, self.proc = device, None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"tk_clocks_{os.getpid()}_{device}.csv"
 
-    def __enter__(self):
+    def start(self):
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
-        except (OSError, FileNotFoundError):
+        except OSError:
             self.proc = None
+        t0 = time.time()
+        while self.proc and time.time() - t0 < 5.0 and self.path.stat().st_size == 0:
+            time.sleep(0.05)
         return self
 
-    def __exit__(self, *a):
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
@@ -106,18 +110,25 @@ class ClockSampler:
                 self.proc.kill()
             self.f.close()
 
-    def summary(self):
+    def summary(self, t_begin: float, t_end: float):
+        """Samples whose host timestamp falls in [t_begin, t_end] (loaded pre-phase + timed steps)."""
         if not self.proc or not self.path.exists():
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm, mx, reasons = [], None, set()
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        import datetime
+
+        sm, mx, reasons, power = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.path.read_text().splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
             try:
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                if ts < t_begin - 0.05 or ts > t_end + 0.05:
+                    continue
                 sm.append(float(f[1]))
                 mx = float(f[2])
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for n, v in zip(names, f[5:9]):
@@ -128,7 +139,8 @@ class ClockSampler:
         except OSError:
             pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(power) if power else None,
+                "window": "loaded pre-phase + timed steps"}
 
 
 def measured_peaks():
@@ -165,8 +177,7 @@ def traffic_for(workload: str, precision: str, kernel: str):
     if not p.exists():
         return None
     try:
-        d = json.loads(p.read_text())
-        return d.get(workload, {}).get(precision, {}).get(kernel)
+        return json.loads(p.read_text()).get(workload, {}).get(precision, {}).get(kernel)
     except ValueError:
         return None
 
@@ -185,23 +196,48 @@ def run_reference(args):
     cores = oracle.num_threads()
     for _ in range(args.warmup):
         orc.apply_into(x, y)
+    steps = max(1, min(args.steps, 60))  # bounded CPU sample
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         orc.apply_into(x, y)
     el = time.perf_counter() - t0
-    v = args.steps / el
+    v = steps / el
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) environments, Gaussian sector dims)",
-        "config": {"workload": args.workload, "block_dim": orc.total, "dense_dim": orc.dense_dim,
-                   "threads": cores},
+        "config": {"workload": args.workload, "block_dim": orc.total, "dense_dim": orc.dense_dim, "threads": cores},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full matvecs of {args.workload} (after {args.warmup} warm-up)"},
+                         "sample": f"{steps} full matvecs of {args.workload} (after {args.warmup} warm-up), "
+                                   "block-sparse FP64 restatement of build_heff_two_site, OpenMP over sector tasks"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gflops": orc.flops() * v / 1e9,
     }
     print(json.dumps(line), flush=True)
+
+
+def lanczos_compare(plan, torch, dev, prec_split: bool):
+    """Time to the lowest eigenpair: FP64 path vs split precision + FP64 refinement."""
+    from tk_gb300 import PREC_BF16X3, PREC_FP64
+
+    out = {}
+    cfg = dict(krylov_dim=30, max_restarts=40, tol=1e-9)
+    runs = [("fp64", PREC_FP64, 0)] + ([("bf16x3_refined", PREC_BF16X3, 4)] if prec_split else [])
+    for name, prec, refine in runs:
+        plan.set_precision(prec)
+        plan.lanczos(krylov_dim=cfg["krylov_dim"], max_restarts=0, tol=cfg["tol"], refine=0)  # graph capture, warm
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r = plan.lanczos(refine=refine, **cfg)
+        torch.cuda.synchronize(dev)
+        out[name] = {"E": r.eigenvalue, "residual": r.residual_norm, "converged": r.converged,
+                     "matvecs": r.matvec_count, "fp64_matvecs": r.fp64_matvec_count, "restarts": r.restarts,
+                     "seconds": time.perf_counter() - t0}
+    if prec_split:
+        out["dE"] = abs(out["fp64"]["E"] - out["bf16x3_refined"]["E"])
+        out["speedup"] = out["fp64"]["seconds"] / out["bf16x3_refined"]["seconds"]
+        plan.set_precision(PREC_BF16X3)
+    return out
 
 
 def run_ours(args):
@@ -222,13 +258,8 @@ def run_ours(args):
     plan = prob.plan(precision=PREC_FP64, device=local)
     prec_name = "fp64"
     if args.precision in ("auto", "bf16x3"):
-        try:
-            plan.set_precision(PREC_BF16X3)
-            prec_name = "bf16x3"
-        except Exception as e:  # noqa: BLE001
-            if args.precision == "bf16x3":
-                raise
-            print(f"# split precision unavailable: {e}", file=sys.stderr)
+        plan.set_precision(PREC_BF16X3)
+        prec_name = "bf16x3"
     n = plan.block_dim
     flops_total, alg_bytes = plan.cost()
     rng = np.random.default_rng(1 + rank)
@@ -238,8 +269,14 @@ def run_ours(args):
     y = torch.empty_like(x)
     flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
-    # warm-up
+    clk = ClockSampler(local).start()
     for _ in range(args.warmup):
+        flush.zero_()
+        plan.profile(x, y, reps=1, stream=stream)
+    torch.cuda.synchronize(dev)
+    # loaded pre-phase (untimed) so that the clock sampler sees the GPU under this load
+    t_load = time.time()
+    while time.time() - t_load < 0.4:
         flush.zero_()
         plan.profile(x, y, reps=1, stream=stream)
     torch.cuda.synchronize(dev)
@@ -247,14 +284,15 @@ def run_ours(args):
         dist.barrier()
     stage_ms = np.zeros(3)
     step_ms = []
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize(dev)
-        for _ in range(args.steps):
-            flush.zero_()  # L2 flushed between timed steps (outside the events)
-            ms, fl = plan.profile(x, y, reps=1, stream=stream)
-            stage_ms += np.array(ms)
-            step_ms.append(sum(ms))
-        torch.cuda.synchronize(dev)
+    torch.cuda.synchronize(dev)
+    for _ in range(args.steps):
+        flush.zero_()  # L2 flushed between timed steps (outside the events)
+        ms, fl, by = plan.profile(x, y, reps=1, stream=stream)
+        stage_ms += np.array(ms)
+        step_ms.append(sum(ms))
+    torch.cuda.synchronize(dev)
+    t_end = time.time()
+    clk.stop()
     if ws > 1:
         dist.barrier()
     total_s = sum(step_ms) / 1e3
@@ -264,8 +302,7 @@ def run_ours(args):
     max_s = float(t.item())
     value = args.steps * ws / max_s
     stage_ms /= args.steps
-    clocks = clk.summary()
-    # parity spot check of the timed matvec against the FP64 path (result read back, not timed)
+    clocks = clk.summary(t_load, t_end)
     y_fp = None
     if prec_name != "fp64":
         yb = y.clone()
@@ -290,35 +327,40 @@ def run_ours(args):
     if ws > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_value = args.steps * ws / float(te.item())
+    lz = None
+    if not args.no_lanczos and rank == 0:
+        lz = lanczos_compare(plan, torch, dev, prec_name != "fp64")
     if rank != 0:
         if ws > 1:
             dist.barrier()
             dist.destroy_process_group()
         return
-    # roofline of the dominant kernel (largest mean stage time)
+    # roofline of the dominant stage: tensor or HBM bound by arithmetic intensity
     peaks, peak_kind = measured_peaks()
-    names = ["stage1_L_psi_gemm", "stage2_wij_combine", "stage3_R_gemm"]
     dom = int(np.argmax(stage_ms))
-    if dom == 1:
-        bound, unit = "hbm", "GB/s"
-        comb_bytes = 8.0 * 2 * n * 4  # rough: the combine reads T1 and writes T2 (each ~ w x |psi|)
-        achieved = comb_bytes / (stage_ms[1] / 1e3) / 1e9
-        peak = peaks["hbm_gbs"]
-        peak_src = f"hbm_gbs ({peak_kind})"
-    elif prec_name == "fp64":
-        bound, unit = "tensor", "TFLOP/s"
-        achieved = fl[dom] / (stage_ms[dom] / 1e3) / 1e12
-        peak = dgemm_peak_tflops(torch, dev)
-        peak_src = "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"
+    sec = stage_ms[dom] / 1e3
+    products = 3.0 if prec_name != "fp64" else 1.0
+    if prec_name == "fp64":
+        tpeak = dgemm_peak_tflops(torch, dev)
+        tsrc = "cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has no FP64 entry)"
     else:
-        bound, unit = "tensor", "TFLOP/s"
-        achieved = fl[dom] / (stage_ms[dom] / 1e3) / 1e12
-        peak = peaks["bf16_tflops"]
-        peak_src = f"bf16_tflops ({peak_kind}); achieved counts FP64-equivalent flops, the pipe runs 3 bf16 products each"
-    roof = {"bound": bound, "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak if peak else None, "peak_source": peak_src,
-            "traffic": traffic_for(args.workload, prec_name, names[dom]),
-            "stage_ms": [float(v) for v in stage_ms]}
+        tpeak = peaks["bf16_tflops"]
+        tsrc = f"bf16_tflops ({peak_kind})"
+    hpeak = peaks["hbm_gbs"]
+    intensity = products * fl[dom] / max(by[dom], 1.0)  # pipe flops per compulsory byte
+    ridge = tpeak * 1e12 / (hpeak * 1e9)
+    t_ach = fl[dom] / sec / 1e12
+    h_ach = by[dom] / sec / 1e9
+    if dom == 1 or intensity < ridge:
+        roof = {"bound": "hbm", "achieved": h_ach, "peak": hpeak, "unit": "GB/s", "frac": h_ach / hpeak,
+                "peak_source": f"hbm_gbs ({peak_kind})"}
+    else:
+        roof = {"bound": "tensor", "achieved": t_ach, "peak": tpeak, "unit": "TFLOP/s", "frac": t_ach / tpeak,
+                "peak_source": tsrc}
+    roof.update({"kernel": STAGES[dom], "traffic": traffic_for(args.workload, prec_name, STAGES[dom]),
+                 "alg_bytes": by[dom], "alg_flops": fl[dom], "pipe_flops_per_byte": intensity, "ridge": ridge,
+                 "tensor_achieved_tflops": t_ach * products, "tensor_peak_tflops": tpeak,
+                 "stage_ms": [float(v) for v in stage_ms], "stage_bytes": by, "stage_flops": fl})
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         import oracle
@@ -331,7 +373,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": max_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if prec_name == "fp64" else "bf16x3(fp32 acc)",
+        "vs_baseline": None, "dtype": "f64" if prec_name == "fp64" else "bf16x3 (fp32 accumulate)",
         "data": "synthetic (seeded N(0,1) environments, Gaussian (N,2Sz) sector dims)",
         "config": {"workload": args.workload, "precision": prec_name, "block_dim": n, "dense_dim": plan.dense_dim,
                    "n_blocks": plan.n_blocks, "alg_gflop_per_matvec": flops_total / 1e9,
@@ -342,11 +384,13 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "api": "tk_heff2_apply_host_flat (pinned FlatBlockStorage host buffers)"},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": (4 if prec_name != "fp64" else 3) * args.steps,
         "clocks": clocks,
     }
     if y_fp is not None:
         line["split_vs_fp64_rel_err"] = y_fp
+    if lz is not None:
+        line["lanczos"] = lz
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()

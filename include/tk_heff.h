@@ -131,9 +131,11 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
  * as tk_heff2_apply -- with a CUDA event before, between and after the
  * three stages, waits for each, and writes the mean milliseconds of stage 1
  * (L x psi GEMMs), stage 2 (W_i W_j combine) and stage 3 (x R GEMMs) to
- * ms[0..2] and the algorithmic flops of each stage to flops[0..2]. */
+ * ms[0..2], the algorithmic flops of each stage to flops[0..2] and its
+ * compulsory global-memory bytes (operands read once, results written once,
+ * in the precision the plan runs) to bytes[0..2]; flops/bytes may be NULL. */
 tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream,
-                           int32_t reps, float* ms, double* flops);
+                           int32_t reps, float* ms, double* flops, double* bytes);
 
 /* y = H_eff x on device vectors in the block layout; stream-ordered. */
 tk_status tk_heff2_apply(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream);

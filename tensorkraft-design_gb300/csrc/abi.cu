@@ -312,7 +312,7 @@ tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {
 }  // extern "C"
 
 extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream,
-                                      int32_t reps, float* ms, double* flops) {
+                                      int32_t reps, float* ms, double* flops, double* bytes) {
     if (!plan || !x_dev || !y_dev || !ms || reps < 1) {
         set_error("tk_heff2_profile: invalid argument");
         return TK_ERR_INVALID_ARG;
@@ -325,6 +325,19 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
         flops[0] = H.g1.flops;
         flops[1] = H.comb_flops;
         flops[2] = H.g3.flops;
+    }
+    if (bytes) {
+        if (p->precision == TK_PREC_BF16X3) {
+            const TcTables& C = H.tc;
+            const double b16 = 2.0 * 2.0 * kTcBK;  // hi + lo bf16 per operand row element x 64
+            bytes[0] = 8.0 * H.total + b16 * (double)C.xq_rows + b16 * (double)C.lq_rows + 4.0 * C.t1_total;
+            bytes[1] = 4.0 * C.t1_total + b16 * (double)C.t2q_rows;
+            bytes[2] = b16 * (double)C.t2q_rows + b16 * (double)C.rq_rows + 8.0 * H.total;
+        } else {
+            bytes[0] = 8.0 * ((double)H.lbuf.size() + H.total + H.t1_total);
+            bytes[1] = 8.0 * ((double)H.t1_total + H.t2_total);
+            bytes[2] = 8.0 * ((double)H.t2_total + H.rbuf.size() + H.total);
+        }
     }
     cudaEvent_t ev[4];
     for (int i = 0; i < 4; ++i) TK_CUDA(cudaEventCreate(&ev[i]));

@@ -178,12 +178,14 @@ class Heff2Plan:
         check(self._lib.tk_heff2_apply(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), s))
 
     def profile(self, x, y, reps: int = 10, stream=None):
-        """Mean ms and algorithmic flops of each matvec stage (CUDA events per launch)."""
+        """Mean ms, algorithmic flops and bytes of each matvec stage (CUDA events per launch)."""
         ms = (C.c_float * 3)()
         fl = (C.c_double * 3)()
+        by = (C.c_double * 3)()
         s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
-        check(self._lib.tk_heff2_profile(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), s, reps, ms, fl))
-        return list(ms), list(fl)
+        check(self._lib.tk_heff2_profile(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), s, reps, ms, fl,
+                                         by))
+        return list(ms), list(fl), list(by)
 
     def apply_host(self, x: np.ndarray, y: np.ndarray):
         """The reference closure on host vectors in the dense layout."""
