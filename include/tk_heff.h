@@ -198,6 +198,21 @@ tk_status tk_gemm_f64(tk_ctx* ctx, double alpha, const tk_mat* a, const tk_mat* 
                       tk_mat_mut* c, void* stream);
 
 /*
+ * No counterpart in the reference.  tk_gemm_f64 for callers that cannot
+ * allocate device memory at call time (a sweep running out of a pre-sized
+ * arena, work recorded into a CUDA graph, latency-bound loops): same
+ * arguments and result, but the kernel's tile tables live in a fixed 1 MiB
+ * device array inside the library instead of per-call cudaMalloc'd buffers,
+ * so nothing is allocated or freed and the call does not synchronise
+ * (stream-ordered on `stream`).  At most 65 520 64x64 output tiles per call;
+ * larger calls return TK_ERR_INVALID_ARG.  The first call on a device looks up
+ * the array's address (make it before any stream capture).  Calls share the
+ * array: calls on different streams that overlap on the GPU race on it.
+ */
+tk_status tk_gemm_f64_noalloc(tk_ctx* ctx, double alpha, const tk_mat* a, const tk_mat* b,
+                              double beta, tk_mat_mut* c, void* stream);
+
+/*
  * SparseLinAlgBackend::block_gemm (tk-linalg/src/traits.rs:200-204,
  * tk-linalg/src/device/faer.rs:390-575) for rank-2 tensors: task per
  * compatible (key_a, key_b) pair, contributions to the same output key

@@ -91,6 +91,8 @@ SIGNATURES = [
                                       C.POINTER(tk_eigen_result), C.c_void_p]),
     ("tk_gemm_f64", C.c_int32, [C.c_void_p, C.c_double, C.POINTER(tk_mat), C.POINTER(tk_mat), C.c_double,
                                 C.POINTER(tk_mat_mut), C.c_void_p]),
+    ("tk_gemm_f64_noalloc", C.c_int32, [C.c_void_p, C.c_double, C.POINTER(tk_mat), C.POINTER(tk_mat), C.c_double,
+                                        C.POINTER(tk_mat_mut), C.c_void_p]),
     ("tk_block_gemm_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.POINTER(tk_bst_out)]),
     ("tk_bst_free", None, [C.POINTER(tk_bst_out)]),
     ("tk_spmv_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
