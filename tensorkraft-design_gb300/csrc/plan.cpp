@@ -335,6 +335,19 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
         if (j.rows <= 0 || j.cols <= 0 || j.src < 0 || j.src + (int64_t)j.rows * j.cols > T.total || j.xrow < 0 ||
             imax >= C.xq_rows * kTcBK) { err = "tensor-core split job"; return false; }
     }
+    auto flat_ok = [&](size_t njobs, const std::vector<int64_t>& start, const std::vector<int32_t>& first,
+                       int64_t total, const char* name) {
+        if (start.size() != njobs || first.size() != (size_t)((total + kTcChunk - 1) / kTcChunk)) {
+            err = std::string(name) + ": flat table size";
+            return false;
+        }
+        for (int32_t f : first)
+            if (f < 0 || (size_t)f >= njobs) { err = std::string(name) + ": flat table job"; return false; }
+        return true;
+    };
+    if (!flat_ok(C.split.size(), C.split_start, C.split_first, C.split_elems, "split") ||
+        !flat_ok(C.jobs.size(), C.comb_start, C.comb_first, C.comb_elems, "combine"))
+        return false;
     for (const TcCombJob& j : C.jobs) {
         int64_t kmax = (int64_t)j.k0 + j.cols - 1;
         int64_t imax = (((int64_t)j.t2row + (kmax >> 6) * j.cstride + j.rows - 1) << 6) + 63;
@@ -832,6 +845,25 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     C.mma_flops += 2.0 * kTcBM * kTcBN * (double)kch * BK;
                 }
         }
+        // flat launch tables of the split and combine kernels
+        auto flat = [](const auto& jobs, std::vector<int64_t>& start, std::vector<int32_t>& first, int64_t& total) {
+            start.clear();
+            first.clear();
+            total = 0;
+            for (const auto& j : jobs) {
+                start.push_back(total);
+                total += (int64_t)j.rows * j.cols;
+            }
+            size_t jj = 0;
+            for (int64_t e = 0; e < total; e += kTcChunk) {
+                while (jj + 1 < start.size() && start[jj + 1] <= e) ++jj;
+                first.push_back((int32_t)jj);
+            }
+        };
+        flat(C.split, C.split_start, C.split_first, C.split_elems);
+        flat(C.jobs, C.comb_start, C.comb_first, C.comb_elems);
+        for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
+        for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
         // split the constant operands into bf16 hi + lo
         auto split = [](const std::vector<double>& v, std::vector<uint16_t>& hi, std::vector<uint16_t>& lo) {
             hi.resize(v.size());

@@ -34,11 +34,13 @@ namespace tk {
 
 namespace {
 
-constexpr int NST = 2;                              // pipeline stages
 constexpr int A_BYTES = kTcBM * kTcBK * 2;          // 16 KB (one of hi / lo)
 constexpr int B_BYTES = kTcBN * kTcBK * 2;          // 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-constexpr int SMEM_BYTES = NST * STAGE_BYTES + 1024 + 256;
+// Shared memory of an NST-stage pipeline (+ alignment slack and barriers).
+// One stage (K <= 64, every stage-1 tile of the U(1)xU(1) workloads) fits
+// four CTAs per SM; two stages fit two.
+constexpr int smem_bytes(int nst) { return nst * STAGE_BYTES + 1024 + 256; }
 constexpr int TMEM_COLS = kTcBN;                    // fp32 accumulator 128 lanes x 64 columns
 constexpr long WAIT_LIMIT = 1L << 22;               // bounded mbarrier polls
 
@@ -140,6 +142,7 @@ __device__ __forceinline__ void store_out(const TcTile& t, int row, int col, flo
         out64[rowtab[t.out_off + row] + t.n0 + col] = (double)v;
 }
 
+template <int NST>
 __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restrict__ tiles,
                                                          const __grid_constant__ CUtensorMap mAh,
                                                          const __grid_constant__ CUtensorMap mAl,
@@ -249,66 +252,62 @@ __device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat1
     lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
 }
 
-// psi sub-block (D_A x D_B, row-major fp64) -> B operand rows (one per column b),
-// 64-wide K chunks over a; transposed through a 64 x 32 shared tile.
-__global__ void __launch_bounds__(256) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
-                                                        const double* __restrict__ x, __nv_bfloat16* __restrict__ xh,
-                                                        __nv_bfloat16* __restrict__ xl) {
-    const TcSplitJob j = jobs[blockIdx.x];
-    __shared__ double tile[64][33];
-    for (int a0 = 0; a0 < j.rows; a0 += 64)
-        for (int b0 = 0; b0 < j.cols; b0 += 32) {
-            __syncthreads();
-            for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
-                const int a = e >> 5, b = e & 31;
-                double v = 0.0;
-                if (a0 + a < j.rows && b0 + b < j.cols) v = x[j.src + (int64_t)(a0 + a) * j.cols + b0 + b];
-                tile[a][b] = v;
-            }
-            __syncthreads();
-            const int64_t rowbase = (int64_t)j.xrow + (int64_t)(a0 >> 6) * j.cstride;
-            for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
-                const int b = e >> 6, a = e & 63;
-                if (a0 + a < j.rows && b0 + b < j.cols) {
-                    __nv_bfloat16 h, l;
-                    split2(tile[a][b], h, l);
-                    const int64_t idx = ((rowbase + b0 + b) << 6) + a;
-                    xh[idx] = h;
-                    xl[idx] = l;
-                }
-            }
-        }
+// Job owning flat element e, searched forward from the chunk's first job.
+__device__ __forceinline__ int flat_job(const int64_t* __restrict__ start, int njobs, int first, int64_t e) {
+    int j = first;
+    while (j + 1 < njobs && start[j + 1] <= e) ++j;
+    return j;
 }
 
-__global__ void __launch_bounds__(256) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
-                                                         const TcCombTerm* __restrict__ terms,
-                                                         const float* __restrict__ t1, __nv_bfloat16* __restrict__ th,
-                                                         __nv_bfloat16* __restrict__ tl) {
-    const TcCombJob j = jobs[blockIdx.x];
-    __shared__ TcCombTerm st[32];
-    const int nterm = j.term_end - j.term_begin;
-    const int n = j.rows * j.cols;
-    // accumulate in registers over term chunks of 32; elements strided by block
-    for (int e0 = 0; e0 < n; e0 += blockDim.x) {
-        const int e = e0 + threadIdx.x;
-        const int r = e < n ? e / j.cols : 0, c = e < n ? e - r * j.cols : 0;
-        float acc = 0.f;
-        for (int t0 = 0; t0 < nterm; t0 += 32) {
-            const int tn = min(32, nterm - t0);
-            __syncthreads();
-            if (threadIdx.x < tn) st[threadIdx.x] = terms[j.term_begin + t0 + threadIdx.x];
-            __syncthreads();
-            if (e < n)
-                for (int t = 0; t < tn; ++t) acc = fmaf(st[t].coef, t1[st[t].in_off + (int64_t)r * st[t].in_rs + c], acc);
-        }
-        if (e < n) {
-            const int k = j.k0 + c;
-            const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
-            const __nv_bfloat16 h = __float2bfloat16_rn(acc);
-            th[idx] = h;
-            tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
-        }
+// psi sub-block (D_A x D_B, row-major fp64) -> stage-1 B operand rows (one per
+// column b, 64-wide K chunks over a), bf16 hi/lo.  One thread per element,
+// consecutive threads walk a (the operand's contiguous K direction); the
+// strided psi reads of one CTA share L1 lines.
+__global__ void __launch_bounds__(kTcChunk) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
+                                                             const int64_t* __restrict__ start,
+                                                             const int32_t* __restrict__ first, int njobs,
+                                                             int64_t total, const double* __restrict__ x,
+                                                             __nv_bfloat16* __restrict__ xh,
+                                                             __nv_bfloat16* __restrict__ xl) {
+    const int64_t e = (int64_t)blockIdx.x * kTcChunk + threadIdx.x;
+    if (e >= total) return;
+    const int jj = flat_job(start, njobs, first[blockIdx.x], e);
+    const TcSplitJob j = jobs[jj];
+    const int local = (int)(e - start[jj]);
+    const int b = local / j.rows, a = local - b * j.rows;
+    __nv_bfloat16 h, l;
+    split2(x[j.src + (int64_t)a * j.cols + b], h, l);
+    const int64_t idx = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b) << 6) + (a & 63);
+    xh[idx] = h;
+    xl[idx] = l;
+}
+
+// W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.  One
+// thread per output element; consecutive threads walk a slab row (contiguous
+// in T1 and in the operand chunk).
+__global__ void __launch_bounds__(kTcChunk) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+                                                              const int64_t* __restrict__ start,
+                                                              const int32_t* __restrict__ first, int njobs,
+                                                              int64_t total, const TcCombTerm* __restrict__ terms,
+                                                              const float* __restrict__ t1,
+                                                              __nv_bfloat16* __restrict__ th,
+                                                              __nv_bfloat16* __restrict__ tl) {
+    const int64_t e = (int64_t)blockIdx.x * kTcChunk + threadIdx.x;
+    if (e >= total) return;
+    const int jj = flat_job(start, njobs, first[blockIdx.x], e);
+    const TcCombJob j = jobs[jj];
+    const int local = (int)(e - start[jj]);
+    const int r = local / j.cols, c = local - r * j.cols;
+    float acc = 0.f;
+    for (int t = j.term_begin; t < j.term_end; ++t) {
+        const TcCombTerm tm = terms[t];
+        acc = fmaf(tm.coef, t1[tm.in_off + (int64_t)r * tm.in_rs + c], acc);
     }
+    const int k = j.k0 + c;
+    const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
+    const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+    th[idx] = h;
+    tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
 }
 
 template <class T>
@@ -366,11 +365,16 @@ struct TcPlan {
     TcCombJob* jobs = nullptr;
     TcCombTerm* terms = nullptr;
     int64_t* yrow = nullptr;
+    int64_t *split_start = nullptr, *comb_start = nullptr;
+    int32_t *split_first = nullptr, *comb_first = nullptr;
+    int64_t split_elems = 0, comb_elems = 0;
     int* err = nullptr;
     int n1 = 0, n3 = 0, nsplit = 0, njobs = 0;
+    int nst1 = 1, nst3 = 2;  // pipeline stages of the two GEMM launches
     CUtensorMap mLh, mLl, mXh, mXl, mTh, mTl, mRh, mRl;
     ~TcPlan() {
-        void* ps[] = {lh, ll, rh, rl, xh, xl, th, tl, t1, tiles1, tiles3, split, jobs, terms, yrow, err};
+        void* ps[] = {lh,    ll,    rh,   rl,   xh,          xl,         th,          tl,         t1,
+                      tiles1, tiles3, split, jobs, terms, yrow, split_start, comb_start, split_first, comb_first, err};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -400,7 +404,10 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = zeros(&p->th, C.t2q_rows)) != cudaSuccess || (e = zeros(&p->tl, C.t2q_rows)) != cudaSuccess ||
         (e = put(&p->tiles1, C.tiles1)) != cudaSuccess || (e = put(&p->tiles3, C.tiles3)) != cudaSuccess ||
         (e = put(&p->split, C.split)) != cudaSuccess || (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
-        (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess) {
+        (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess ||
+        (e = put(&p->split_start, C.split_start)) != cudaSuccess ||
+        (e = put(&p->split_first, C.split_first)) != cudaSuccess ||
+        (e = put(&p->comb_start, C.comb_start)) != cudaSuccess || (e = put(&p->comb_first, C.comb_first)) != cudaSuccess) {
         err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
@@ -413,13 +420,19 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n3 = (int)C.tiles3.size();
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
+    p->split_elems = C.split_elems;
+    p->comb_elems = C.comb_elems;
+    p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
+    p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
         !make_map(&p->mXh, p->xh, C.xq_rows, kTcBN, err) || !make_map(&p->mXl, p->xl, C.xq_rows, kTcBN, err) ||
         !make_map(&p->mTh, p->th, C.t2q_rows, kTcBM, err) || !make_map(&p->mTl, p->tl, C.t2q_rows, kTcBM, err) ||
         !make_map(&p->mRh, p->rh, C.rq_rows, kTcBN, err) || !make_map(&p->mRl, p->rl, C.rq_rows, kTcBN, err))
         return TK_ERR_CUDA;
-    if ((e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)) !=
-        cudaSuccess) {
+    if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
+            cudaSuccess) {
         err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return TK_ERR_CUDA;
     }
@@ -427,19 +440,33 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     return TK_OK;
 }
 
+namespace {
+
+void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, const CUtensorMap& al,
+                    const CUtensorMap& bh, const CUtensorMap& bl, float* o32, double* o64, const int64_t* rowtab,
+                    int* err, cudaStream_t s) {
+    if (n <= 0) return;
+    if (nst == 1)
+        tc_gemm_kernel<1><<<n, 128, smem_bytes(1), s>>>(tiles, ah, al, bh, bl, o32, o64, rowtab, err);
+    else
+        tc_gemm_kernel<2><<<n, 128, smem_bytes(2), s>>>(tiles, ah, al, bh, bl, o32, o64, rowtab, err);
+}
+
+}  // namespace
+
 cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double* x,
                            double* y, cudaStream_t s, int stage, std::string& err) {
     if (stage == 0) {
-        if (tc.nsplit > 0) split_psi_kernel<<<tc.nsplit, 256, 0, s>>>(tc.split, x, tc.xh, tc.xl);
-        if (tc.n1 > 0)
-            tc_gemm_kernel<<<tc.n1, 128, SMEM_BYTES, s>>>(tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl, tc.t1, nullptr,
-                                                          nullptr, tc.err);
+        if (tc.split_elems > 0)
+            split_psi_kernel<<<(unsigned)((tc.split_elems + kTcChunk - 1) / kTcChunk), kTcChunk, 0, s>>>(
+                tc.split, tc.split_start, tc.split_first, tc.nsplit, tc.split_elems, x, tc.xh, tc.xl);
+        launch_tc_gemm(tc.nst1, tc.n1, tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl, tc.t1, nullptr, nullptr, tc.err, s);
     } else if (stage == 1) {
-        if (tc.njobs > 0) combine_tc_kernel<<<tc.njobs, 256, 0, s>>>(tc.jobs, tc.terms, tc.t1, tc.th, tc.tl);
+        if (tc.comb_elems > 0)
+            combine_tc_kernel<<<(unsigned)((tc.comb_elems + kTcChunk - 1) / kTcChunk), kTcChunk, 0, s>>>(
+                tc.jobs, tc.comb_start, tc.comb_first, tc.njobs, tc.comb_elems, tc.terms, tc.t1, tc.th, tc.tl);
     } else {
-        if (tc.n3 > 0)
-            tc_gemm_kernel<<<tc.n3, 128, SMEM_BYTES, s>>>(tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl, nullptr, y,
-                                                          tc.yrow, tc.err);
+        launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl, nullptr, y, tc.yrow, tc.err, s);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) err = "tensor-core stage launch";

@@ -148,7 +148,16 @@ struct TcTables {
     std::vector<TcCombTerm> terms;
     std::vector<int64_t> yrow;  // y element offset of every stage-3 operand row
     double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
+    // Flat element-parallel launch of the split and combine kernels: element e
+    // of the concatenated job list belongs to the last job j with
+    // start[j] <= e; chunk c (kTcChunk elements, one CTA) starts its search at
+    // first[c].
+    std::vector<int64_t> split_start, comb_start;
+    std::vector<int32_t> split_first, comb_first;
+    int64_t split_elems = 0, comb_elems = 0;
+    int32_t max_kch1 = 0, max_kch3 = 0;
 };
+constexpr int kTcChunk = 256;
 
 // Everything the device needs for one two-site H_eff, built on the host.
 struct Heff2Tables {
