@@ -285,6 +285,7 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
     if (st != TK_OK) return st;
     TK_CUDA(cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     TK_CUDA(cudaStreamSynchronize(s));
+    if (plan->precision == TK_PREC_BF16X3) return tc_check_error(*plan->tc, s);
     return TK_OK;
 }
 
@@ -305,6 +306,7 @@ tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {
         if (st != TK_OK) return st;
         TK_CUDA(cudaMemcpyAsync(plan->pin_y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
         TK_CUDA(cudaStreamSynchronize(s));
+        if (plan->precision == TK_PREC_BF16X3 && (st = tc_check_error(*plan->tc, s)) != TK_OK) return st;
     }
     return tk_heff2_flat_to_dense(plan, plan->pin_y, y);
 }

@@ -456,6 +456,7 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
         if (rn <= cfg->tol || restarts >= cfg->max_restarts) break;
         ++restarts;
     }
+    if (p->tc && (st = tc_check_error(*p->tc, s)) != TK_OK) return st;
     out->eigenvalue = E;
     out->residual_norm = rn;
     out->converged = rn <= cfg->tol ? 1 : 0;

@@ -224,18 +224,31 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     const bool have = mbar_wait(done, 0, err, ERR_DONE_TIMEOUT);
     fence_after();
     // tcgen05.ld is warp-collective: decide per warp
-    const bool go = __all_sync(0xffffffffu, have && (*(volatile int*)err == 0));
+    const bool go = __all_sync(0xffffffffu, have);
     if (go) {
+        // Accumulator -> shared memory (the operand ring is free once `done`
+        // completed) -> coalesced row stores: thread r of warp w holds row
+        // 32w + r after tcgen05.ld; the warp then writes its 32 rows one at a
+        // time with consecutive lanes on consecutive columns.
+        float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
         const int row = threadIdx.x;
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
         for (int c0 = 0; c0 < kTcBN; c0 += 16) {
             float v[16];
             tmem_ld16(tbase + c0, v);
-            if (row < t.m_valid) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    if (c0 + j < t.n_valid) store_out(t, row, c0 + j, v[j], out32, out64, rowtab);
+            for (int j = 0; j < 16; ++j) stile[row][c0 + j] = v[j];
+        }
+        __syncwarp();
+        const int rend = min(t.m_valid, warp * 32 + 32);
+        for (int r = warp * 32; r < rend; ++r) {
+            if (t.mode == 0) {
+                float* o = out32 + t.out_off + (int64_t)r * t.ldc;
+                for (int col = lane; col < t.n_valid; col += 32) o[col] = stile[r][col];
+            } else {
+                double* o = out64 + rowtab[t.out_off + r] + t.n0;
+                for (int col = lane; col < t.n_valid; col += 32) o[col] = (double)stile[r][col];
             }
         }
     }
@@ -252,11 +265,31 @@ __device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat1
     lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
 }
 
-// Job owning flat element e, searched forward from the chunk's first job.
-__device__ __forceinline__ int flat_job(const int64_t* __restrict__ start, int njobs, int first, int64_t e) {
-    int j = first;
-    while (j + 1 < njobs && start[j + 1] <= e) ++j;
-    return j;
+// The jobs one chunk (CTA) touches -- first[c] .. first[c+1] -- and their
+// start offsets, staged in shared memory; returns the number staged.
+template <class Job>
+__device__ __forceinline__ int stage_jobs(const Job* __restrict__ jobs, const int64_t* __restrict__ start,
+                                          const int32_t* __restrict__ first, int njobs, int nchunks, Job* sj,
+                                          int64_t* ss) {
+    const int j0 = first[blockIdx.x];
+    const int j1 = (int)blockIdx.x + 1 < nchunks ? first[blockIdx.x + 1] : njobs - 1;
+    const int nj = j1 - j0 + 1;  // <= kTcChunk + 1
+    for (int i = threadIdx.x; i < nj; i += blockDim.x) {
+        sj[i] = jobs[j0 + i];
+        ss[i] = start[j0 + i];
+    }
+    __syncthreads();
+    return nj;
+}
+
+// Index of the staged job holding element e (binary search over starts).
+__device__ __forceinline__ int find_job(const int64_t* ss, int nj, int64_t e) {
+    int lo = 0, hi = nj - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ss[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 // psi sub-block (D_A x D_B, row-major fp64) -> stage-1 B operand rows (one per
@@ -269,11 +302,15 @@ __global__ void __launch_bounds__(kTcChunk) split_psi_kernel(const TcSplitJob* _
                                                              int64_t total, const double* __restrict__ x,
                                                              __nv_bfloat16* __restrict__ xh,
                                                              __nv_bfloat16* __restrict__ xl) {
+    __shared__ TcSplitJob sj[kTcChunk + 1];
+    __shared__ int64_t ss[kTcChunk + 1];
+    const int nchunks = (int)((total + kTcChunk - 1) / kTcChunk);
+    const int nj = stage_jobs(jobs, start, first, njobs, nchunks, sj, ss);
     const int64_t e = (int64_t)blockIdx.x * kTcChunk + threadIdx.x;
     if (e >= total) return;
-    const int jj = flat_job(start, njobs, first[blockIdx.x], e);
-    const TcSplitJob j = jobs[jj];
-    const int local = (int)(e - start[jj]);
+    const int jj = find_job(ss, nj, e);
+    const TcSplitJob j = sj[jj];
+    const int local = (int)(e - ss[jj]);
     const int b = local / j.rows, a = local - b * j.rows;
     __nv_bfloat16 h, l;
     split2(x[j.src + (int64_t)a * j.cols + b], h, l);
@@ -292,11 +329,15 @@ __global__ void __launch_bounds__(kTcChunk) combine_tc_kernel(const TcCombJob* _
                                                               const float* __restrict__ t1,
                                                               __nv_bfloat16* __restrict__ th,
                                                               __nv_bfloat16* __restrict__ tl) {
+    __shared__ TcCombJob sj[kTcChunk + 1];
+    __shared__ int64_t ss[kTcChunk + 1];
+    const int nchunks = (int)((total + kTcChunk - 1) / kTcChunk);
+    const int nj = stage_jobs(jobs, start, first, njobs, nchunks, sj, ss);
     const int64_t e = (int64_t)blockIdx.x * kTcChunk + threadIdx.x;
     if (e >= total) return;
-    const int jj = flat_job(start, njobs, first[blockIdx.x], e);
-    const TcCombJob j = jobs[jj];
-    const int local = (int)(e - start[jj]);
+    const int jj = find_job(ss, nj, e);
+    const TcCombJob j = sj[jj];
+    const int local = (int)(e - ss[jj]);
     const int r = local / j.cols, c = local - r * j.cols;
     float acc = 0.f;
     for (int t = j.term_begin; t < j.term_end; ++t) {
@@ -483,5 +524,20 @@ cudaError_t tc_apply(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs,
 }
 
 int* tc_error_word(TcPlan& tc) { return tc.err; }
+
+tk_status tc_check_error(TcPlan& tc, cudaStream_t s) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, tc.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail("tensor-core error word", e);
+    if (h != 0) {
+        cudaMemsetAsync(tc.err, 0, sizeof(int), s);
+        cudaStreamSynchronize(s);
+        set_error("tensor-core kernel: a bounded wait ran out (code " + std::to_string(h) +
+                  "); the affected output tiles were not written");
+        return TK_ERR_TIMEOUT;
+    }
+    return TK_OK;
+}
 
 }  // namespace tk

@@ -33,4 +33,6 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables& host, const CombJob* d
 namespace tk {
 // Device error word of the tensor-core kernels (0 = no bounded wait ran out).
 int* tc_error_word(TcPlan& tc);
+// Synchronises `s`, reads and clears the error word: TK_ERR_TIMEOUT if set.
+tk_status tc_check_error(TcPlan& tc, cudaStream_t s);
 }  // namespace tk
