@@ -265,15 +265,17 @@ __device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat1
     lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
 }
 
-// The jobs one chunk (CTA) touches -- first[c] .. first[c+1] -- and their
-// start offsets, staged in shared memory; returns the number staged.
+// The jobs chunk c (one CTA) touches, staged in shared memory with their
+// start offsets: jobs first[c] .. the job holding element cstart[c+1]-1, at
+// most kTcStageJobs (the plan guarantees it).  Returns the number staged.
 template <class Job>
 __device__ __forceinline__ int stage_jobs(const Job* __restrict__ jobs, const int64_t* __restrict__ start,
-                                          const int32_t* __restrict__ first, int njobs, int nchunks, Job* sj,
-                                          int64_t* ss) {
+                                          const int32_t* __restrict__ first, const int64_t* __restrict__ cstart,
+                                          int njobs, Job* sj, int64_t* ss, int64_t& e0, int64_t& e1) {
     const int j0 = first[blockIdx.x];
-    const int j1 = (int)blockIdx.x + 1 < nchunks ? first[blockIdx.x + 1] : njobs - 1;
-    const int nj = j1 - j0 + 1;  // <= kTcChunk + 1
+    e0 = cstart[blockIdx.x];
+    e1 = cstart[blockIdx.x + 1];
+    const int nj = min(kTcStageJobs, njobs - j0);
     for (int i = threadIdx.x; i < nj; i += blockDim.x) {
         sj[i] = jobs[j0 + i];
         ss[i] = start[j0 + i];
@@ -293,62 +295,87 @@ __device__ __forceinline__ int find_job(const int64_t* ss, int nj, int64_t e) {
 }
 
 // psi sub-block (D_A x D_B, row-major fp64) -> stage-1 B operand rows (one per
-// column b, 64-wide K chunks over a), bf16 hi/lo.  One thread per element,
-// consecutive threads walk a (the operand's contiguous K direction); the
-// strided psi reads of one CTA share L1 lines.
-__global__ void __launch_bounds__(kTcChunk) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
-                                                             const int64_t* __restrict__ start,
-                                                             const int32_t* __restrict__ first, int njobs,
-                                                             int64_t total, const double* __restrict__ x,
-                                                             __nv_bfloat16* __restrict__ xh,
-                                                             __nv_bfloat16* __restrict__ xl) {
-    __shared__ TcSplitJob sj[kTcChunk + 1];
-    __shared__ int64_t ss[kTcChunk + 1];
-    const int nchunks = (int)((total + kTcChunk - 1) / kTcChunk);
-    const int nj = stage_jobs(jobs, start, first, njobs, nchunks, sj, ss);
-    const int64_t e = (int64_t)blockIdx.x * kTcChunk + threadIdx.x;
-    if (e >= total) return;
-    const int jj = find_job(ss, nj, e);
-    const TcSplitJob j = sj[jj];
-    const int local = (int)(e - ss[jj]);
-    const int b = local / j.rows, a = local - b * j.rows;
-    __nv_bfloat16 h, l;
-    split2(x[j.src + (int64_t)a * j.cols + b], h, l);
-    const int64_t idx = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b) << 6) + (a & 63);
-    xh[idx] = h;
-    xl[idx] = l;
+// column b, 64-wide K chunks over a), bf16 hi/lo.  kTcPerThread elements per
+// thread, kTcThreads apart, so consecutive threads walk a (the operand's
+// contiguous K direction); the strided psi reads of one CTA share L1 lines.
+__global__ void __launch_bounds__(kTcThreads) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
+                                                               const int64_t* __restrict__ start,
+                                                               const int32_t* __restrict__ first,
+                                                               const int64_t* __restrict__ cstart, int njobs,
+                                                               const double* __restrict__ x,
+                                                               __nv_bfloat16* __restrict__ xh,
+                                                               __nv_bfloat16* __restrict__ xl) {
+    __shared__ TcSplitJob sj[kTcStageJobs];
+    __shared__ int64_t ss[kTcStageJobs];
+    int64_t e0, e1;
+    const int nj = stage_jobs(jobs, start, first, cstart, njobs, sj, ss, e0, e1);
+    double v[kTcPerThread];
+    int64_t idx[kTcPerThread];
+#pragma unroll
+    for (int k = 0; k < kTcPerThread; ++k) {
+        const int64_t e = e0 + threadIdx.x + k * kTcThreads;
+        idx[k] = -1;
+        if (e < e1) {
+            const int jj = find_job(ss, nj, e);
+            const TcSplitJob& j = sj[jj];
+            const int local = (int)(e - ss[jj]);
+            const int b = local / j.rows, a = local - b * j.rows;
+            v[k] = x[j.src + (int64_t)a * j.cols + b];
+            idx[k] = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b) << 6) + (a & 63);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kTcPerThread; ++k)
+        if (idx[k] >= 0) {
+            __nv_bfloat16 h, l;
+            split2(v[k], h, l);
+            xh[idx[k]] = h;
+            xl[idx[k]] = l;
+        }
 }
 
-// W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.  One
-// thread per output element; consecutive threads walk a slab row (contiguous
-// in T1 and in the operand chunk).
-__global__ void __launch_bounds__(kTcChunk) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
-                                                              const int64_t* __restrict__ start,
-                                                              const int32_t* __restrict__ first, int njobs,
-                                                              int64_t total, const TcCombTerm* __restrict__ terms,
-                                                              const float* __restrict__ t1,
-                                                              __nv_bfloat16* __restrict__ th,
-                                                              __nv_bfloat16* __restrict__ tl) {
-    __shared__ TcCombJob sj[kTcChunk + 1];
-    __shared__ int64_t ss[kTcChunk + 1];
-    const int nchunks = (int)((total + kTcChunk - 1) / kTcChunk);
-    const int nj = stage_jobs(jobs, start, first, njobs, nchunks, sj, ss);
-    const int64_t e = (int64_t)blockIdx.x * kTcChunk + threadIdx.x;
-    if (e >= total) return;
-    const int jj = find_job(ss, nj, e);
-    const TcCombJob j = sj[jj];
-    const int local = (int)(e - ss[jj]);
-    const int r = local / j.cols, c = local - r * j.cols;
-    float acc = 0.f;
-    for (int t = j.term_begin; t < j.term_end; ++t) {
-        const TcCombTerm tm = terms[t];
-        acc = fmaf(tm.coef, t1[tm.in_off + (int64_t)r * tm.in_rs + c], acc);
+// W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.
+// kTcPerThread output elements per thread, kTcThreads apart; consecutive
+// threads walk a slab row (contiguous in T1 and in the operand chunk).
+__global__ void __launch_bounds__(kTcThreads) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+                                                                const int64_t* __restrict__ start,
+                                                                const int32_t* __restrict__ first,
+                                                                const int64_t* __restrict__ cstart, int njobs,
+                                                                const TcCombTerm* __restrict__ terms,
+                                                                const float* __restrict__ t1,
+                                                                __nv_bfloat16* __restrict__ th,
+                                                                __nv_bfloat16* __restrict__ tl) {
+    __shared__ TcCombJob sj[kTcStageJobs];
+    __shared__ int64_t ss[kTcStageJobs];
+    int64_t e0, e1;
+    const int nj = stage_jobs(jobs, start, first, cstart, njobs, sj, ss, e0, e1);
+    float acc[kTcPerThread];
+    int64_t idx[kTcPerThread];
+#pragma unroll
+    for (int k = 0; k < kTcPerThread; ++k) {
+        const int64_t e = e0 + threadIdx.x + k * kTcThreads;
+        acc[k] = 0.f;
+        idx[k] = -1;
+        if (e < e1) {
+            const int jj = find_job(ss, nj, e);
+            const TcCombJob& j = sj[jj];
+            const int local = (int)(e - ss[jj]);
+            const int r = local / j.cols, c = local - r * j.cols;
+            for (int t = j.term_begin; t < j.term_end; ++t) {
+                const TcCombTerm tm = terms[t];
+                acc[k] = fmaf(tm.coef, __ldg(t1 + tm.in_off + (int64_t)r * tm.in_rs + c), acc[k]);
+            }
+            const int kk = j.k0 + c;
+            idx[k] = (((int64_t)j.t2row + (int64_t)(kk >> 6) * j.cstride + r) << 6) + (kk & 63);
+        }
     }
-    const int k = j.k0 + c;
-    const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
-    const __nv_bfloat16 h = __float2bfloat16_rn(acc);
-    th[idx] = h;
-    tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
+#pragma unroll
+    for (int k = 0; k < kTcPerThread; ++k)
+        if (idx[k] >= 0) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(acc[k]);
+            th[idx[k]] = h;
+            tl[idx[k]] = __float2bfloat16_rn(acc[k] - __bfloat162float(h));
+        }
 }
 
 template <class T>
@@ -406,16 +433,17 @@ struct TcPlan {
     TcCombJob* jobs = nullptr;
     TcCombTerm* terms = nullptr;
     int64_t* yrow = nullptr;
-    int64_t *split_start = nullptr, *comb_start = nullptr;
+    int64_t *split_start = nullptr, *comb_start = nullptr, *split_cstart = nullptr, *comb_cstart = nullptr;
     int32_t *split_first = nullptr, *comb_first = nullptr;
-    int64_t split_elems = 0, comb_elems = 0;
+    int split_chunks = 0, comb_chunks = 0;
     int* err = nullptr;
     int n1 = 0, n3 = 0, nsplit = 0, njobs = 0;
     int nst1 = 1, nst3 = 2;  // pipeline stages of the two GEMM launches
     CUtensorMap mLh, mLl, mXh, mXl, mTh, mTl, mRh, mRl;
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,   xh,          xl,         th,          tl,         t1,
-                      tiles1, tiles3, split, jobs, terms, yrow, split_start, comb_start, split_first, comb_first, err};
+                      tiles1, tiles3, split, jobs, terms, yrow, split_start, comb_start, split_first, comb_first, err,
+                      split_cstart, comb_cstart};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -448,7 +476,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess ||
         (e = put(&p->split_start, C.split_start)) != cudaSuccess ||
         (e = put(&p->split_first, C.split_first)) != cudaSuccess ||
-        (e = put(&p->comb_start, C.comb_start)) != cudaSuccess || (e = put(&p->comb_first, C.comb_first)) != cudaSuccess) {
+        (e = put(&p->comb_start, C.comb_start)) != cudaSuccess || (e = put(&p->comb_first, C.comb_first)) != cudaSuccess ||
+        (e = put(&p->split_cstart, C.split_cstart)) != cudaSuccess ||
+        (e = put(&p->comb_cstart, C.comb_cstart)) != cudaSuccess) {
         err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
@@ -461,8 +491,8 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n3 = (int)C.tiles3.size();
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
-    p->split_elems = C.split_elems;
-    p->comb_elems = C.comb_elems;
+    p->split_chunks = (int)C.split_first.size();
+    p->comb_chunks = (int)C.comb_first.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
@@ -498,14 +528,15 @@ void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, 
 cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double* x,
                            double* y, cudaStream_t s, int stage, std::string& err) {
     if (stage == 0) {
-        if (tc.split_elems > 0)
-            split_psi_kernel<<<(unsigned)((tc.split_elems + kTcChunk - 1) / kTcChunk), kTcChunk, 0, s>>>(
-                tc.split, tc.split_start, tc.split_first, tc.nsplit, tc.split_elems, x, tc.xh, tc.xl);
+        if (tc.split_chunks > 0)
+            split_psi_kernel<<<tc.split_chunks, kTcThreads, 0, s>>>(tc.split, tc.split_start, tc.split_first,
+                                                                     tc.split_cstart, tc.nsplit, x, tc.xh, tc.xl);
         launch_tc_gemm(tc.nst1, tc.n1, tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl, tc.t1, nullptr, nullptr, tc.err, s);
     } else if (stage == 1) {
-        if (tc.comb_elems > 0)
-            combine_tc_kernel<<<(unsigned)((tc.comb_elems + kTcChunk - 1) / kTcChunk), kTcChunk, 0, s>>>(
-                tc.jobs, tc.comb_start, tc.comb_first, tc.njobs, tc.comb_elems, tc.terms, tc.t1, tc.th, tc.tl);
+        if (tc.comb_chunks > 0)
+            combine_tc_kernel<<<tc.comb_chunks, kTcThreads, 0, s>>>(tc.jobs, tc.comb_start, tc.comb_first,
+                                                                     tc.comb_cstart, tc.njobs, tc.terms, tc.t1, tc.th,
+                                                                     tc.tl);
     } else {
         launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl, nullptr, y, tc.yrow, tc.err, s);
     }
