@@ -314,12 +314,24 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
         }
     }
     const TcTables& C = T.tc;
+    if (C.t1col_base.size() != C.t1col_stride.size()) { err = "T1 column tables"; return false; }
     for (const TcTile& t : C.tiles1) {
-        if (t.mode != 0 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
-            t.out_off < 0 || t.out_off + (int64_t)(t.m_valid - 1) * t.ldc + t.n_valid - 1 >= C.t1_total ||
-            t.a_row < 0 || t.b_row < 0) { err = "tensor-core stage 1 tile"; return false; }
+        if (t.mode != 2 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
+            t.n_mma < t.n_valid || t.n_mma > kTcBN || t.n_mma % 16 != 0 || t.out_off < 0 || t.ldc < 0 ||
+            t.out_off + t.n_valid > (int64_t)C.t1col_base.size() || t.a_row < 0 || t.b_row < 0) {
+            err = "tensor-core stage 1 tile";
+            return false;
+        }
+        for (int c = 0; c < t.n_valid; ++c) {
+            const int64_t base = C.t1col_base[t.out_off + c], st = C.t1col_stride[t.out_off + c];
+            if (base < 0 || st <= 0 || base + (int64_t)(t.ldc + t.m_valid - 1) * st >= C.t1_total) {
+                err = "tensor-core stage 1 output column";
+                return false;
+            }
+        }
     }
     for (const TcTile& t : C.tiles3) {
+        if (t.n_mma < t.n_valid || t.n_mma > kTcBN || t.n_mma % 16 != 0) { err = "tensor-core stage 3 tile N"; return false; }
         if (t.mode != 1 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
             t.out_off < 0 || t.out_off + t.m_valid - 1 >= (int64_t)C.yrow.size() || t.a_row < 0 || t.b_row < 0) {
             err = "tensor-core stage 3 tile";
@@ -747,6 +759,15 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                 j.cstride = (int32_t)cols;
                 C.split.push_back(j);
             }
+            // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B)
+            const int64_t colbase0 = (int64_t)C.t1col_base.size();
+            for (size_t jx = 0; jx < xp.size(); ++jx) {
+                const int64_t DB = QB.dim[xp[jx].second];
+                for (int64_t b = 0; b < DB; ++b) {
+                    C.t1col_base.push_back(t1off + xcol[jx] * rows + b);
+                    C.t1col_stride.push_back((int32_t)DB);
+                }
+            }
             for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
                 for (int64_t n0 = 0; n0 < cols; n0 += kTcBN) {
                     TcTile t{};
@@ -755,16 +776,20 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     t.kch = kch;
                     t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
                     t.n_valid = (int32_t)std::min<int64_t>(kTcBN, cols - n0);
-                    t.mode = 0;
-                    t.out_off = t1off + m0 * cols + n0;
-                    t.ldc = (int32_t)cols;
+                    t.n_mma = (t.n_valid + 15) / 16 * 16;
+                    t.mode = 2;
+                    t.out_off = colbase0 + n0;
+                    t.ldc = (int32_t)m0;
                     C.tiles1.push_back(t);
-                    C.mma_flops += 2.0 * kTcBM * kTcBN * (double)kch * BK;
+                    C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
             for (size_t i = 0; i < lp.size(); ++i)
-                for (size_t jx = 0; jx < xp.size(); ++jx)
+                for (size_t jx = 0; jx < xp.size(); ++jx) {
+                    const int64_t DB = QB.dim[xp[jx].second];
+                    // channel-0 row of the slab, row stride per a' = dws rows of D_B
                     pieces.push_back({pkey(xp[jx].first, lp[i].first, lp[i].second, xp[jx].second),
-                                      t1off + lrow[i] * cols + xcol[jx], (int32_t)(WL.dim[lp[i].second] * cols)});
+                                      t1off + xcol[jx] * rows + lrow[i] * DB, (int32_t)(WL.dim[lp[i].second] * DB)});
+                }
             t1off += rows * cols;
         }
         C.t1_total = t1off;
@@ -849,12 +874,13 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     t.kch = kch;
                     t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
                     t.n_valid = (int32_t)std::min<int64_t>(kTcBN, NB - n0);
+                    t.n_mma = (t.n_valid + 15) / 16 * 16;
                     t.mode = 1;
                     t.out_off = yb + m0;
                     t.ldc = 0;
                     t.n0 = (int32_t)n0;
                     C.tiles3.push_back(t);
-                    C.mma_flops += 2.0 * kTcBM * kTcBN * (double)kch * BK;
+                    C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
         }
         // flat launch tables of the split and combine kernels

@@ -101,16 +101,18 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 }
 
 // Instruction descriptor, kind::f16: fp32 accumulate, bf16 A and B, both
-// K-major, N>>3 at bit 17, M>>4 at bit 24.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcBN >> 3) << 17) |
-                            ((uint32_t)(kTcBM >> 4) << 24);
+// K-major, N>>3 at bit 17, M>>4 at bit 24.  N is chosen per tile.
+__device__ __forceinline__ uint32_t make_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
+}
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum)
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
         : "memory");
 }
 
@@ -134,12 +136,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ void store_out(const TcTile& t, int row, int col, float v, float* out32, double* out64,
-                                          const int64_t* rowtab) {
-    if (t.mode == 0)
-        out32[t.out_off + (int64_t)row * t.ldc + col] = v;
+// Output addressing of a tile element (row, col) relative to the tile origin.
+struct OutMap {
+    float* out32;
+    double* out64;
+    const int64_t* rowtab;
+    const int64_t* colbase;
+    const int32_t* colstride;
+};
+
+__device__ __forceinline__ void store_out(const TcTile& t, int row, int col, float v, const OutMap& o) {
+    if (t.mode == 2)
+        o.out32[o.colbase[t.out_off + col] + (int64_t)(t.ldc + row) * o.colstride[t.out_off + col]] = v;
     else
-        out64[rowtab[t.out_off + row] + t.n0 + col] = (double)v;
+        o.out64[o.rowtab[t.out_off + row] + t.n0 + col] = (double)v;
 }
 
 template <int NST>
@@ -147,9 +157,8 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
                                                          const __grid_constant__ CUtensorMap mAh,
                                                          const __grid_constant__ CUtensorMap mAl,
                                                          const __grid_constant__ CUtensorMap mBh,
-                                                         const __grid_constant__ CUtensorMap mBl,
-                                                         float* __restrict__ out32, double* __restrict__ out64,
-                                                         const int64_t* __restrict__ rowtab, int* err) {
+                                                         const __grid_constant__ CUtensorMap mBl, const OutMap om,
+                                                         int* err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
@@ -161,7 +170,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
 
     if (t.kch == 0) {  // no K: the tile is zero
         for (int e = threadIdx.x; e < t.m_valid * t.n_valid; e += blockDim.x)
-            store_out(t, e / t.n_valid, e % t.n_valid, 0.f, out32, out64, rowtab);
+            store_out(t, e / t.n_valid, e % t.n_valid, 0.f, om);
         return;
     }
     if (threadIdx.x == 0) {
@@ -183,23 +192,27 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     fence_after();
     const uint32_t tmem = *tslot;
     bool ok = true;
+    const int nb16 = t.n_mma >> 4;  // 16-row B boxes per operand and chunk
 
     if (warp == 0 && lane == 0) {
-        // producer: TMA loads of the K chunks
+        // producer: TMA loads of the K chunks (A: one 128-row box; B: n_mma/16 16-row boxes)
         for (int c = 0; c < t.kch && ok; ++c) {
             const int s = c % NST;
             if (c >= NST) ok = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
             if (!ok) break;
             uint8_t* st = smem + s * STAGE_BYTES;
-            mbar_expect_tx(&full[s], STAGE_BYTES);
+            mbar_expect_tx(&full[s], 2 * A_BYTES + 2 * t.n_mma * kTcBK * 2);
             const int ya = t.a_row + c * t.a_cs, yb = t.b_row + c * t.b_cs;
             tma_load_2d(st, &mAh, 0, ya, &full[s]);
             tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[s]);
-            tma_load_2d(st + 2 * A_BYTES, &mBh, 0, yb, &full[s]);
-            tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mBl, 0, yb, &full[s]);
+            for (int i = 0; i < nb16; ++i) {
+                tma_load_2d(st + 2 * A_BYTES + i * 16 * 128, &mBh, 0, yb + 16 * i, &full[s]);
+                tma_load_2d(st + 2 * A_BYTES + B_BYTES + i * 16 * 128, &mBl, 0, yb + 16 * i, &full[s]);
+            }
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer: three bf16 products per 16-wide K step
+        const uint32_t idesc = make_idesc(t.n_mma);
         for (int c = 0; c < t.kch && ok; ++c) {
             const int s = c % NST;
             ok = mbar_wait(&full[s], (c / NST) & 1, err, ERR_FULL_TIMEOUT);
@@ -211,9 +224,9 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
 #pragma unroll
             for (int kk = 0; kk < kTcBK / 16; ++kk) {
                 const uint64_t adv = (uint64_t)((kk * 32) >> 4);  // 16 bf16 = 32 bytes along K
-                mma_bf16(tmem, ah + adv, bh + adv, (c | kk) != 0);
-                mma_bf16(tmem, ah + adv, bl + adv, 1u);
-                mma_bf16(tmem, al + adv, bh + adv, 1u);
+                mma_bf16(tmem, ah + adv, bh + adv, idesc, (c | kk) != 0);
+                mma_bf16(tmem, ah + adv, bl + adv, idesc, 1u);
+                mma_bf16(tmem, al + adv, bh + adv, idesc, 1u);
             }
             mma_commit(&empty[s]);
         }
@@ -233,8 +246,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
         const int row = threadIdx.x;
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-        for (int c0 = 0; c0 < kTcBN; c0 += 16) {
+        for (int c0 = 0; c0 < t.n_mma; c0 += 16) {
             float v[16];
             tmem_ld16(tbase + c0, v);
 #pragma unroll
@@ -242,12 +254,23 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         }
         __syncwarp();
         const int rend = min(t.m_valid, warp * 32 + 32);
-        for (int r = warp * 32; r < rend; ++r) {
-            if (t.mode == 0) {
-                float* o = out32 + t.out_off + (int64_t)r * t.ldc;
-                for (int col = lane; col < t.n_valid; col += 32) o[col] = stile[r][col];
-            } else {
-                double* o = out64 + rowtab[t.out_off + r] + t.n0;
+        if (t.mode == 2) {
+            int64_t cb[2] = {0, 0};
+            int32_t cs[2] = {0, 0};
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (lane + 32 * h < t.n_valid) {
+                    cb[h] = om.colbase[t.out_off + lane + 32 * h];
+                    cs[h] = om.colstride[t.out_off + lane + 32 * h];
+                }
+            for (int r = warp * 32; r < rend; ++r)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    if (lane + 32 * h < t.n_valid)
+                        om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane + 32 * h];
+        } else {
+            for (int r = warp * 32; r < rend; ++r) {
+                double* o = om.out64 + om.rowtab[t.out_off + r] + t.n0;
                 for (int col = lane; col < t.n_valid; col += 32) o[col] = (double)stile[r][col];
             }
         }
@@ -433,6 +456,8 @@ struct TcPlan {
     TcCombJob* jobs = nullptr;
     TcCombTerm* terms = nullptr;
     int64_t* yrow = nullptr;
+    int64_t* t1col_base = nullptr;
+    int32_t* t1col_stride = nullptr;
     int64_t *split_start = nullptr, *comb_start = nullptr, *split_cstart = nullptr, *comb_cstart = nullptr;
     int32_t *split_first = nullptr, *comb_first = nullptr;
     int split_chunks = 0, comb_chunks = 0;
@@ -443,7 +468,7 @@ struct TcPlan {
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,   xh,          xl,         th,          tl,         t1,
                       tiles1, tiles3, split, jobs, terms, yrow, split_start, comb_start, split_first, comb_first, err,
-                      split_cstart, comb_cstart};
+                      split_cstart, comb_cstart, t1col_base, t1col_stride};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -478,7 +503,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = put(&p->split_first, C.split_first)) != cudaSuccess ||
         (e = put(&p->comb_start, C.comb_start)) != cudaSuccess || (e = put(&p->comb_first, C.comb_first)) != cudaSuccess ||
         (e = put(&p->split_cstart, C.split_cstart)) != cudaSuccess ||
-        (e = put(&p->comb_cstart, C.comb_cstart)) != cudaSuccess) {
+        (e = put(&p->comb_cstart, C.comb_cstart)) != cudaSuccess ||
+        (e = put(&p->t1col_base, C.t1col_base)) != cudaSuccess ||
+        (e = put(&p->t1col_stride, C.t1col_stride)) != cudaSuccess) {
         err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
@@ -496,9 +523,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
-        !make_map(&p->mXh, p->xh, C.xq_rows, kTcBN, err) || !make_map(&p->mXl, p->xl, C.xq_rows, kTcBN, err) ||
+        !make_map(&p->mXh, p->xh, C.xq_rows, 16, err) || !make_map(&p->mXl, p->xl, C.xq_rows, 16, err) ||
         !make_map(&p->mTh, p->th, C.t2q_rows, kTcBM, err) || !make_map(&p->mTl, p->tl, C.t2q_rows, kTcBM, err) ||
-        !make_map(&p->mRh, p->rh, C.rq_rows, kTcBN, err) || !make_map(&p->mRl, p->rl, C.rq_rows, kTcBN, err))
+        !make_map(&p->mRh, p->rh, C.rq_rows, 16, err) || !make_map(&p->mRl, p->rl, C.rq_rows, 16, err))
         return TK_ERR_CUDA;
     if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
             cudaSuccess ||
@@ -514,13 +541,12 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
 namespace {
 
 void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, const CUtensorMap& al,
-                    const CUtensorMap& bh, const CUtensorMap& bl, float* o32, double* o64, const int64_t* rowtab,
-                    int* err, cudaStream_t s) {
+                    const CUtensorMap& bh, const CUtensorMap& bl, const OutMap& om, int* err, cudaStream_t s) {
     if (n <= 0) return;
     if (nst == 1)
-        tc_gemm_kernel<1><<<n, 128, smem_bytes(1), s>>>(tiles, ah, al, bh, bl, o32, o64, rowtab, err);
+        tc_gemm_kernel<1><<<n, 128, smem_bytes(1), s>>>(tiles, ah, al, bh, bl, om, err);
     else
-        tc_gemm_kernel<2><<<n, 128, smem_bytes(2), s>>>(tiles, ah, al, bh, bl, o32, o64, rowtab, err);
+        tc_gemm_kernel<2><<<n, 128, smem_bytes(2), s>>>(tiles, ah, al, bh, bl, om, err);
 }
 
 }  // namespace
@@ -531,14 +557,16 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
         if (tc.split_chunks > 0)
             split_psi_kernel<<<tc.split_chunks, kTcThreads, 0, s>>>(tc.split, tc.split_start, tc.split_first,
                                                                      tc.split_cstart, tc.nsplit, x, tc.xh, tc.xl);
-        launch_tc_gemm(tc.nst1, tc.n1, tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl, tc.t1, nullptr, nullptr, tc.err, s);
+        launch_tc_gemm(tc.nst1, tc.n1, tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl,
+                       OutMap{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride}, tc.err, s);
     } else if (stage == 1) {
         if (tc.comb_chunks > 0)
             combine_tc_kernel<<<tc.comb_chunks, kTcThreads, 0, s>>>(tc.jobs, tc.comb_start, tc.comb_first,
                                                                      tc.comb_cstart, tc.njobs, tc.terms, tc.t1, tc.th,
                                                                      tc.tl);
     } else {
-        launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl, nullptr, y, tc.yrow, tc.err, s);
+        launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl,
+                       OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, tc.err, s);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) err = "tensor-core stage launch";

@@ -119,9 +119,10 @@ constexpr int kTcBK = 64;   // K chunk (128 bytes of bf16: one swizzle atom)
 struct TcTile {
     int32_t a_row, a_cs;     // A operand row of chunk 0 at this tile's m0; rows between chunks
     int32_t b_row, b_cs;     // B operand row of chunk 0 at this tile's n0; rows between chunks
-    int32_t kch, m_valid, n_valid, mode;  // mode 0: fp32 row-major out; 1: fp64 out through a row table
-    int64_t out_off;         // mode 0: element offset of (m0, n0); mode 1: row-table index of m0
-    int32_t ldc, n0;         // mode 0: row stride; mode 1: column offset added to the row table
+    int32_t kch, m_valid, n_valid, mode;  // mode 1: fp64 out through a row table; 2: fp32 out through column tables
+    int64_t out_off;         // mode 1: row-table index of m0; mode 2: column-table index of n0
+    int32_t ldc, n0;         // mode 1: n0 = column offset added to the row table; mode 2: ldc = m0
+    int32_t n_mma, pad;      // UMMA N of this tile: n_valid rounded up to 16 (<= kTcBN)
 };
 // psi sub-block -> stage-1 B operand (transposed into K-major chunks), hi/lo split.
 struct TcSplitJob {
@@ -147,6 +148,11 @@ struct TcTables {
     std::vector<TcCombJob> jobs;
     std::vector<TcCombTerm> terms;
     std::vector<int64_t> yrow;  // y element offset of every stage-3 operand row
+    // T1 is stored per (stack A, column block (p, B)) as a row-major
+    // [rows_A x D_B] matrix: element (r, c) of stack A sits at
+    // t1col_base[c] + r * t1col_stride[c] (c = global stage-1 column).
+    std::vector<int64_t> t1col_base;
+    std::vector<int32_t> t1col_stride;
     double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
     // Flat element-parallel launch of the split and combine kernels: element e
     // of the concatenated job list belongs to the last job j with
