@@ -347,31 +347,6 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
         if (j.rows <= 0 || j.cols <= 0 || j.src < 0 || j.src + (int64_t)j.rows * j.cols > T.total || j.xrow < 0 ||
             imax >= C.xq_rows * kTcBK) { err = "tensor-core split job"; return false; }
     }
-    auto flat_ok = [&](size_t njobs, const std::vector<int64_t>& start, const std::vector<int32_t>& first,
-                       const std::vector<int64_t>& cstart, int64_t total, const char* name) {
-        if (start.size() != njobs || cstart.size() != first.size() + 1 || (total > 0 && first.empty()) ||
-            cstart.front() != 0 || cstart.back() != total) {
-            err = std::string(name) + ": flat table size";
-            return false;
-        }
-        for (size_t c = 0; c < first.size(); ++c) {
-            const int32_t f = first[c];
-            const int64_t e0 = cstart[c], e1 = cstart[c + 1];
-            if (f < 0 || (size_t)f >= njobs || e1 <= e0 || e1 - e0 > kTcChunk || start[f] > e0 ||
-                ((size_t)f + 1 < njobs && start[f + 1] <= e0)) {
-                err = std::string(name) + ": flat chunk";
-                return false;
-            }
-            // the job holding e1 - 1 is within the staged window
-            size_t last = f;
-            while (last + 1 < njobs && start[last + 1] <= e1 - 1) ++last;
-            if (last - f + 1 > (size_t)kTcStageJobs) { err = std::string(name) + ": chunk spans too many jobs"; return false; }
-        }
-        return true;
-    };
-    if (!flat_ok(C.split.size(), C.split_start, C.split_first, C.split_cstart, C.split_elems, "split") ||
-        !flat_ok(C.jobs.size(), C.comb_start, C.comb_first, C.comb_cstart, C.comb_elems, "combine"))
-        return false;
     for (const TcCombJob& j : C.jobs) {
         int64_t kmax = (int64_t)j.k0 + j.cols - 1;
         int64_t imax = (((int64_t)j.t2row + (kmax >> 6) * j.cstride + j.rows - 1) << 6) + 63;
@@ -883,33 +858,6 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
         }
-        // flat launch tables of the split and combine kernels
-        auto flat = [](const auto& jobs, std::vector<int64_t>& start, std::vector<int32_t>& first,
-                       std::vector<int64_t>& cstart, int64_t& total) {
-            start.clear();
-            first.clear();
-            cstart.clear();
-            total = 0;
-            for (const auto& j : jobs) {
-                start.push_back(total);
-                total += (int64_t)j.rows * j.cols;
-            }
-            // greedy chunks: <= kTcChunk elements and <= kTcStageJobs jobs each
-            size_t jj = 0;
-            int64_t e = 0;
-            while (e < total) {
-                while (jj + 1 < start.size() && start[jj + 1] <= e) ++jj;
-                first.push_back((int32_t)jj);
-                cstart.push_back(e);
-                int64_t end = std::min<int64_t>(e + kTcChunk, total);
-                const size_t jlast = jj + kTcStageJobs - 1;  // last job this chunk may touch
-                if (jlast + 1 < start.size()) end = std::min<int64_t>(end, start[jlast + 1]);
-                e = end;
-            }
-            cstart.push_back(total);
-        };
-        flat(C.split, C.split_start, C.split_first, C.split_cstart, C.split_elems);
-        flat(C.jobs, C.comb_start, C.comb_first, C.comb_cstart, C.comb_elems);
         for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
         for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
         // split the constant operands into bf16 hi + lo

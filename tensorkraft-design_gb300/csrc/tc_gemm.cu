@@ -288,117 +288,87 @@ __device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat1
     lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
 }
 
-// The jobs chunk c (one CTA) touches, staged in shared memory with their
-// start offsets: jobs first[c] .. the job holding element cstart[c+1]-1, at
-// most kTcStageJobs (the plan guarantees it).  Returns the number staged.
-template <class Job>
-__device__ __forceinline__ int stage_jobs(const Job* __restrict__ jobs, const int64_t* __restrict__ start,
-                                          const int32_t* __restrict__ first, const int64_t* __restrict__ cstart,
-                                          int njobs, Job* sj, int64_t* ss, int64_t& e0, int64_t& e1) {
-    const int j0 = first[blockIdx.x];
-    e0 = cstart[blockIdx.x];
-    e1 = cstart[blockIdx.x + 1];
-    const int nj = min(kTcStageJobs, njobs - j0);
-    for (int i = threadIdx.x; i < nj; i += blockDim.x) {
-        sj[i] = jobs[j0 + i];
-        ss[i] = start[j0 + i];
-    }
-    __syncthreads();
-    return nj;
-}
-
-// Index of the staged job holding element e (binary search over starts).
-__device__ __forceinline__ int find_job(const int64_t* ss, int nj, int64_t e) {
-    int lo = 0, hi = nj - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (ss[mid] <= e) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
+constexpr int kWarpsPerCta = 8;       // combine
+constexpr int kSplitWarpsPerCta = 4;  // split: 4 x 8.4 KB transpose buffers
 
 // psi sub-block (D_A x D_B, row-major fp64) -> stage-1 B operand rows (one per
-// column b, 64-wide K chunks over a), bf16 hi/lo.  kTcPerThread elements per
-// thread, kTcThreads apart, so consecutive threads walk a (the operand's
-// contiguous K direction); the strided psi reads of one CTA share L1 lines.
-__global__ void __launch_bounds__(kTcThreads) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
-                                                               const int64_t* __restrict__ start,
-                                                               const int32_t* __restrict__ first,
-                                                               const int64_t* __restrict__ cstart, int njobs,
-                                                               const double* __restrict__ x,
-                                                               __nv_bfloat16* __restrict__ xh,
-                                                               __nv_bfloat16* __restrict__ xl) {
-    __shared__ TcSplitJob sj[kTcStageJobs];
-    __shared__ int64_t ss[kTcStageJobs];
-    int64_t e0, e1;
-    const int nj = stage_jobs(jobs, start, first, cstart, njobs, sj, ss, e0, e1);
-    double v[kTcPerThread];
-    int64_t idx[kTcPerThread];
-#pragma unroll
-    for (int k = 0; k < kTcPerThread; ++k) {
-        const int64_t e = e0 + threadIdx.x + k * kTcThreads;
-        idx[k] = -1;
-        if (e < e1) {
-            const int jj = find_job(ss, nj, e);
-            const TcSplitJob& j = sj[jj];
-            const int local = (int)(e - ss[jj]);
-            const int b = local / j.rows, a = local - b * j.rows;
-            v[k] = x[j.src + (int64_t)a * j.cols + b];
-            idx[k] = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b) << 6) + (a & 63);
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kTcPerThread; ++k)
-        if (idx[k] >= 0) {
-            __nv_bfloat16 h, l;
-            split2(v[k], h, l);
-            xh[idx[k]] = h;
-            xl[idx[k]] = l;
+// column b, 64-wide K chunks over a), bf16 hi/lo.  One warp per sub-block;
+// 32 x 32 tiles go through a per-warp shared-memory buffer so that the psi
+// reads run along b and the operand writes along a (both contiguous).
+__global__ void __launch_bounds__(32 * kSplitWarpsPerCta) split_psi_kernel(const TcSplitJob* __restrict__ jobs, int njobs,
+                                                                      const double* __restrict__ x,
+                                                                      __nv_bfloat16* __restrict__ xh,
+                                                                      __nv_bfloat16* __restrict__ xl) {
+    __shared__ double buf[kSplitWarpsPerCta][32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int jj = blockIdx.x * kSplitWarpsPerCta + warp;
+    if (jj >= njobs) return;
+    const TcSplitJob j = jobs[jj];
+    double (*t)[33] = buf[warp];
+    for (int a0 = 0; a0 < j.rows; a0 += 32)
+        for (int b0 = 0; b0 < j.cols; b0 += 32) {
+            const int na = min(32, j.rows - a0), nb = min(32, j.cols - b0);
+            for (int a = 0; a < na; ++a)
+                if (lane < nb) t[a][lane] = x[j.src + (int64_t)(a0 + a) * j.cols + b0 + lane];
+            __syncwarp();
+            for (int b = 0; b < nb; ++b)
+                if (lane < na) {
+                    __nv_bfloat16 h, l;
+                    split2(t[lane][b], h, l);
+                    const int a = a0 + lane;
+                    const int64_t idx = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b0 + b) << 6) + (a & 63);
+                    xh[idx] = h;
+                    xl[idx] = l;
+                }
+            __syncwarp();
         }
 }
 
-// W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.
-// kTcPerThread output elements per thread, kTcThreads apart; consecutive
-// threads walk a slab row (contiguous in T1 and in the operand chunk).
-__global__ void __launch_bounds__(kTcThreads) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
-                                                                const int64_t* __restrict__ start,
-                                                                const int32_t* __restrict__ first,
-                                                                const int64_t* __restrict__ cstart, int njobs,
-                                                                const TcCombTerm* __restrict__ terms,
-                                                                const float* __restrict__ t1,
-                                                                __nv_bfloat16* __restrict__ th,
-                                                                __nv_bfloat16* __restrict__ tl) {
-    __shared__ TcCombJob sj[kTcStageJobs];
-    __shared__ int64_t ss[kTcStageJobs];
-    int64_t e0, e1;
-    const int nj = stage_jobs(jobs, start, first, cstart, njobs, sj, ss, e0, e1);
-    float acc[kTcPerThread];
-    int64_t idx[kTcPerThread];
-#pragma unroll
-    for (int k = 0; k < kTcPerThread; ++k) {
-        const int64_t e = e0 + threadIdx.x + k * kTcThreads;
-        acc[k] = 0.f;
-        idx[k] = -1;
-        if (e < e1) {
-            const int jj = find_job(ss, nj, e);
-            const TcCombJob& j = sj[jj];
-            const int local = (int)(e - ss[jj]);
-            const int r = local / j.cols, c = local - r * j.cols;
-            for (int t = j.term_begin; t < j.term_end; ++t) {
-                const TcCombTerm tm = terms[t];
-                acc[k] = fmaf(tm.coef, __ldg(t1 + tm.in_off + (int64_t)r * tm.in_rs + c), acc[k]);
+// W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.  One
+// warp per output slab; its terms live in registers (lane t holds term t,
+// broadcast by shuffles), lanes walk the slab's elements in row-major order
+// (contiguous in T1 and in the operand chunk).
+__global__ void __launch_bounds__(32 * kWarpsPerCta) combine_tc_kernel(const TcCombJob* __restrict__ jobs, int njobs,
+                                                                       const TcCombTerm* __restrict__ terms,
+                                                                       const float* __restrict__ t1,
+                                                                       __nv_bfloat16* __restrict__ th,
+                                                                       __nv_bfloat16* __restrict__ tl) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int jj = blockIdx.x * kWarpsPerCta + warp;
+    if (jj >= njobs) return;
+    const TcCombJob j = jobs[jj];
+    const int n = j.rows * j.cols;
+    const int nterm = j.term_end - j.term_begin;
+    auto load_terms = [&](int t0) {
+        TcCombTerm m{};
+        if (lane < min(32, nterm - t0)) m = terms[j.term_begin + t0 + lane];
+        return m;
+    };
+    TcCombTerm mine = load_terms(0);
+    for (int e0 = 0; e0 < n; e0 += 32) {  // warp-uniform trip count (shuffles need every lane)
+        const int e = e0 + lane;
+        const bool valid = e < n;
+        const int r = valid ? e / j.cols : 0, c = valid ? e - r * j.cols : 0;
+        float acc = 0.f;
+        for (int t0 = 0; t0 < nterm; t0 += 32) {
+            if (t0 > 0) mine = load_terms(t0);
+            const int tn = min(32, nterm - t0);
+            for (int t = 0; t < tn; ++t) {
+                const int64_t off = __shfl_sync(0xffffffffu, mine.in_off, t);
+                const int rs = __shfl_sync(0xffffffffu, mine.in_rs, t);
+                const float cf = __shfl_sync(0xffffffffu, mine.coef, t);
+                if (valid) acc = fmaf(cf, __ldg(t1 + off + (int64_t)r * rs + c), acc);
             }
-            const int kk = j.k0 + c;
-            idx[k] = (((int64_t)j.t2row + (int64_t)(kk >> 6) * j.cstride + r) << 6) + (kk & 63);
+        }
+        if (nterm > 32) mine = load_terms(0);
+        if (valid) {
+            const int k = j.k0 + c;
+            const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
+            const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+            th[idx] = h;
+            tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
         }
     }
-#pragma unroll
-    for (int k = 0; k < kTcPerThread; ++k)
-        if (idx[k] >= 0) {
-            const __nv_bfloat16 h = __float2bfloat16_rn(acc[k]);
-            th[idx[k]] = h;
-            tl[idx[k]] = __float2bfloat16_rn(acc[k] - __bfloat162float(h));
-        }
 }
 
 template <class T>
@@ -458,17 +428,13 @@ struct TcPlan {
     int64_t* yrow = nullptr;
     int64_t* t1col_base = nullptr;
     int32_t* t1col_stride = nullptr;
-    int64_t *split_start = nullptr, *comb_start = nullptr, *split_cstart = nullptr, *comb_cstart = nullptr;
-    int32_t *split_first = nullptr, *comb_first = nullptr;
-    int split_chunks = 0, comb_chunks = 0;
     int* err = nullptr;
     int n1 = 0, n3 = 0, nsplit = 0, njobs = 0;
     int nst1 = 1, nst3 = 2;  // pipeline stages of the two GEMM launches
     CUtensorMap mLh, mLl, mXh, mXl, mTh, mTl, mRh, mRl;
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,   xh,          xl,         th,          tl,         t1,
-                      tiles1, tiles3, split, jobs, terms, yrow, split_start, comb_start, split_first, comb_first, err,
-                      split_cstart, comb_cstart, t1col_base, t1col_stride};
+                      tiles1, tiles3, split, jobs, terms, yrow, err, t1col_base, t1col_stride};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -499,11 +465,6 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = put(&p->tiles1, C.tiles1)) != cudaSuccess || (e = put(&p->tiles3, C.tiles3)) != cudaSuccess ||
         (e = put(&p->split, C.split)) != cudaSuccess || (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
         (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess ||
-        (e = put(&p->split_start, C.split_start)) != cudaSuccess ||
-        (e = put(&p->split_first, C.split_first)) != cudaSuccess ||
-        (e = put(&p->comb_start, C.comb_start)) != cudaSuccess || (e = put(&p->comb_first, C.comb_first)) != cudaSuccess ||
-        (e = put(&p->split_cstart, C.split_cstart)) != cudaSuccess ||
-        (e = put(&p->comb_cstart, C.comb_cstart)) != cudaSuccess ||
         (e = put(&p->t1col_base, C.t1col_base)) != cudaSuccess ||
         (e = put(&p->t1col_stride, C.t1col_stride)) != cudaSuccess) {
         err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
@@ -518,8 +479,6 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n3 = (int)C.tiles3.size();
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
-    p->split_chunks = (int)C.split_first.size();
-    p->comb_chunks = (int)C.comb_first.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
@@ -554,16 +513,15 @@ void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, 
 cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double* x,
                            double* y, cudaStream_t s, int stage, std::string& err) {
     if (stage == 0) {
-        if (tc.split_chunks > 0)
-            split_psi_kernel<<<tc.split_chunks, kTcThreads, 0, s>>>(tc.split, tc.split_start, tc.split_first,
-                                                                     tc.split_cstart, tc.nsplit, x, tc.xh, tc.xl);
+        if (tc.nsplit > 0)
+            split_psi_kernel<<<(tc.nsplit + kSplitWarpsPerCta - 1) / kSplitWarpsPerCta, 32 * kSplitWarpsPerCta, 0, s>>>(
+                tc.split, tc.nsplit, x, tc.xh, tc.xl);
         launch_tc_gemm(tc.nst1, tc.n1, tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl,
                        OutMap{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride}, tc.err, s);
     } else if (stage == 1) {
-        if (tc.comb_chunks > 0)
-            combine_tc_kernel<<<tc.comb_chunks, kTcThreads, 0, s>>>(tc.jobs, tc.comb_start, tc.comb_first,
-                                                                     tc.comb_cstart, tc.njobs, tc.terms, tc.t1, tc.th,
-                                                                     tc.tl);
+        if (tc.njobs > 0)
+            combine_tc_kernel<<<(tc.njobs + kWarpsPerCta - 1) / kWarpsPerCta, 32 * kWarpsPerCta, 0, s>>>(
+                tc.jobs, tc.njobs, tc.terms, tc.t1, tc.th, tc.tl);
     } else {
         launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl,
                        OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, tc.err, s);

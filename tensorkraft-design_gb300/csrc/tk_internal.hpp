@@ -154,20 +154,8 @@ struct TcTables {
     std::vector<int64_t> t1col_base;
     std::vector<int32_t> t1col_stride;
     double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
-    // Flat element-parallel launch of the split and combine kernels: element e
-    // of the concatenated job list belongs to the last job j with
-    // start[j] <= e.  Chunk c (one CTA) covers elements [cstart[c], cstart[c+1])
-    // -- at most kTcChunk elements touching at most kTcStageJobs jobs, the
-    // first of which is first[c].
-    std::vector<int64_t> split_start, comb_start, split_cstart, comb_cstart;
-    std::vector<int32_t> split_first, comb_first;
-    int64_t split_elems = 0, comb_elems = 0;
     int32_t max_kch1 = 0, max_kch3 = 0;
 };
-constexpr int kTcThreads = 256;                     // threads per split/combine CTA
-constexpr int kTcPerThread = 4;                     // elements per thread
-constexpr int kTcChunk = kTcThreads * kTcPerThread;  // max elements per CTA
-constexpr int kTcStageJobs = 128;                   // max jobs one CTA stages in shared memory
 
 // Everything the device needs for one two-site H_eff, built on the host.
 struct Heff2Tables {
