@@ -345,16 +345,23 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
     for (const TcSplitJob& j : C.split) {
         int64_t imax = (((int64_t)j.xrow + (int64_t)((j.rows - 1) >> 6) * j.cstride + j.cols - 1) << 6) + 63;
         if (j.rows <= 0 || j.cols <= 0 || j.src < 0 || j.src + (int64_t)j.rows * j.cols > T.total || j.xrow < 0 ||
-            imax >= C.xq_rows * kTcBK) { err = "tensor-core split job"; return false; }
+            j.a0 < 0 || j.a0 >= j.rows || j.b0 < 0 || j.b0 >= j.cols || imax >= C.xq_rows * kTcBK) {
+            err = "tensor-core split job";
+            return false;
+        }
     }
     for (const TcCombJob& j : C.jobs) {
         int64_t kmax = (int64_t)j.k0 + j.cols - 1;
-        int64_t imax = (((int64_t)j.t2row + (kmax >> 6) * j.cstride + j.rows - 1) << 6) + 63;
-        if (j.rows <= 0 || j.cols <= 0 || j.k0 < 0 || j.t2row < 0 || imax >= C.t2q_rows * kTcBK || j.term_begin < 0 ||
-            j.term_end < j.term_begin || (size_t)j.term_end > C.terms.size()) { err = "tensor-core combine job"; return false; }
+        int64_t imax = (((int64_t)j.t2row + (kmax >> 6) * j.cstride + j.r0 + j.rows - 1) << 6) + 63;
+        if (j.rows <= 0 || j.cols <= 0 || j.r0 < 0 || (int64_t)j.rows * j.cols > kTcCombMaxElems + j.cols || j.k0 < 0 ||
+            j.t2row < 0 || imax >= C.t2q_rows * kTcBK || j.term_begin < 0 || j.term_end < j.term_begin ||
+            (size_t)j.term_end > C.terms.size()) { err = "tensor-core combine job"; return false; }
         for (int t = j.term_begin; t < j.term_end; ++t) {
             const TcCombTerm& c = C.terms[t];
-            if (c.in_off < 0 || c.in_off + (int64_t)(j.rows - 1) * c.in_rs + j.cols - 1 >= C.t1_total) { err = "tensor-core combine term"; return false; }
+            if (c.in_off < 0 || c.in_off + (int64_t)(j.r0 + j.rows - 1) * c.in_rs + j.cols - 1 >= C.t1_total) {
+                err = "tensor-core combine term";
+                return false;
+            }
         }
     }
     return true;
@@ -732,7 +739,12 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                 j.cols = (int32_t)QB.dim[xp[i].second];
                 j.xrow = (int32_t)(xb + xcol[i]);
                 j.cstride = (int32_t)cols;
-                C.split.push_back(j);
+                for (int32_t a0 = 0; a0 < j.rows; a0 += 32)
+                    for (int32_t b0 = 0; b0 < j.cols; b0 += 32) {
+                        j.a0 = a0;
+                        j.b0 = b0;
+                        C.split.push_back(j);
+                    }
             }
             // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B)
             const int64_t colbase0 = (int64_t)C.t1col_base.size();
@@ -837,7 +849,16 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                             }
                         }
                         j.term_end = (int32_t)C.terms.size();
-                        if (j.term_end > j.term_begin) C.jobs.push_back(j);
+                        if (j.term_end > j.term_begin) {
+                            // row chunks of at most kTcCombMaxElems elements
+                            const int32_t all_rows = j.rows;
+                            const int32_t step = std::max<int32_t>(1, kTcCombMaxElems / std::max<int32_t>(1, j.cols));
+                            for (int32_t r0 = 0; r0 < all_rows; r0 += step) {
+                                j.r0 = r0;
+                                j.rows = std::min(step, all_rows - r0);
+                                C.jobs.push_back(j);
+                            }
+                        }
                     }
                 }
             }

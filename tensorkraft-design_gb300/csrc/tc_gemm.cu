@@ -305,22 +305,19 @@ __global__ void __launch_bounds__(32 * kSplitWarpsPerCta) split_psi_kernel(const
     if (jj >= njobs) return;
     const TcSplitJob j = jobs[jj];
     double (*t)[33] = buf[warp];
-    for (int a0 = 0; a0 < j.rows; a0 += 32)
-        for (int b0 = 0; b0 < j.cols; b0 += 32) {
-            const int na = min(32, j.rows - a0), nb = min(32, j.cols - b0);
-            for (int a = 0; a < na; ++a)
-                if (lane < nb) t[a][lane] = x[j.src + (int64_t)(a0 + a) * j.cols + b0 + lane];
-            __syncwarp();
-            for (int b = 0; b < nb; ++b)
-                if (lane < na) {
-                    __nv_bfloat16 h, l;
-                    split2(t[lane][b], h, l);
-                    const int a = a0 + lane;
-                    const int64_t idx = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b0 + b) << 6) + (a & 63);
-                    xh[idx] = h;
-                    xl[idx] = l;
-                }
-            __syncwarp();
+    const int a0 = j.a0, b0 = j.b0;
+    const int na = min(32, j.rows - a0), nb = min(32, j.cols - b0);
+    for (int a = 0; a < na; ++a)
+        if (lane < nb) t[a][lane] = x[j.src + (int64_t)(a0 + a) * j.cols + b0 + lane];
+    __syncwarp();
+    for (int b = 0; b < nb; ++b)
+        if (lane < na) {
+            __nv_bfloat16 h, l;
+            split2(t[lane][b], h, l);
+            const int a = a0 + lane;
+            const int64_t idx = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b0 + b) << 6) + (a & 63);
+            xh[idx] = h;
+            xl[idx] = l;
         }
 }
 
@@ -348,7 +345,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) combine_tc_kernel(const TcC
     for (int e0 = 0; e0 < n; e0 += 32) {  // warp-uniform trip count (shuffles need every lane)
         const int e = e0 + lane;
         const bool valid = e < n;
-        const int r = valid ? e / j.cols : 0, c = valid ? e - r * j.cols : 0;
+        const int rl = valid ? e / j.cols : 0, c = valid ? e - rl * j.cols : 0;
+        const int r = j.r0 + rl;  // row inside the slab
         float acc = 0.f;
         for (int t0 = 0; t0 < nterm; t0 += 32) {
             if (t0 > 0) mine = load_terms(t0);

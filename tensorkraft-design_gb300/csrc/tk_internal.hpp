@@ -125,16 +125,21 @@ struct TcTile {
     int32_t n_mma, pad;      // UMMA N of this tile: n_valid rounded up to 16 (<= kTcBN)
 };
 // psi sub-block -> stage-1 B operand (transposed into K-major chunks), hi/lo split.
+// One job = one 32 x 32 tile (a0, b0) of a sub-block (one warp each).
 struct TcSplitJob {
     int64_t src;             // flat offset of the (D_A x D_B) sub-block
     int32_t rows, cols;      // D_A (becomes K), D_B (becomes N)
     int32_t xrow, cstride;   // operand row of chunk 0 for column 0; rows between chunks
+    int32_t a0, b0;          // tile origin inside the sub-block
 };
-// T1 (fp32) -> stage-3 A operand (K-major chunks), hi/lo split.
+// T1 (fp32) -> stage-3 A operand (K-major chunks), hi/lo split.  One job =
+// rows [r0, r0 + rows) of one output slab, at most kTcCombMaxElems elements
+// (one warp each).
 struct TcCombJob {
     int32_t t2row, cstride;  // operand row of chunk 0 for slab row 0; rows between chunks
-    int32_t k0, rows, cols, term_begin, term_end, pad;
+    int32_t k0, rows, cols, term_begin, term_end, r0;
 };
+constexpr int kTcCombMaxElems = 512;
 struct TcCombTerm {
     int64_t in_off;
     int32_t in_rs;
