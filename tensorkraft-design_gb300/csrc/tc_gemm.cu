@@ -307,8 +307,16 @@ __global__ void __launch_bounds__(32 * kSplitWarpsPerCta) split_psi_kernel(const
     double (*t)[33] = buf[warp];
     const int a0 = j.a0, b0 = j.b0;
     const int na = min(32, j.rows - a0), nb = min(32, j.cols - b0);
-    for (int a = 0; a < na; ++a)
-        if (lane < nb) t[a][lane] = x[j.src + (int64_t)(a0 + a) * j.cols + b0 + lane];
+    // eight independent row loads in flight per batch
+    for (int a8 = 0; a8 < na; a8 += 8) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            v[u] = (a8 + u < na && lane < nb) ? x[j.src + (int64_t)(a0 + a8 + u) * j.cols + b0 + lane] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (a8 + u < na) t[a8 + u][lane] = v[u];
+    }
     __syncwarp();
     for (int b = 0; b < nb; ++b)
         if (lane < na) {
@@ -341,13 +349,21 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) combine_tc_kernel(const TcC
         if (lane < min(32, nterm - t0)) m = terms[j.term_begin + t0 + lane];
         return m;
     };
+    constexpr int U = 4;  // independent elements per lane (loads in flight per term)
     TcCombTerm mine = load_terms(0);
-    for (int e0 = 0; e0 < n; e0 += 32) {  // warp-uniform trip count (shuffles need every lane)
-        const int e = e0 + lane;
-        const bool valid = e < n;
-        const int rl = valid ? e / j.cols : 0, c = valid ? e - rl * j.cols : 0;
-        const int r = j.r0 + rl;  // row inside the slab
-        float acc = 0.f;
+    for (int e0 = 0; e0 < n; e0 += 32 * U) {  // warp-uniform trip count (shuffles need every lane)
+        bool valid[U];
+        int r[U], c[U];
+        float acc[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * 32 + lane;
+            valid[u] = e < n;
+            const int rl = valid[u] ? e / j.cols : 0;
+            c[u] = valid[u] ? e - rl * j.cols : 0;
+            r[u] = j.r0 + rl;  // row inside the slab
+            acc[u] = 0.f;
+        }
         for (int t0 = 0; t0 < nterm; t0 += 32) {
             if (t0 > 0) mine = load_terms(t0);
             const int tn = min(32, nterm - t0);
@@ -355,17 +371,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) combine_tc_kernel(const TcC
                 const int64_t off = __shfl_sync(0xffffffffu, mine.in_off, t);
                 const int rs = __shfl_sync(0xffffffffu, mine.in_rs, t);
                 const float cf = __shfl_sync(0xffffffffu, mine.coef, t);
-                if (valid) acc = fmaf(cf, __ldg(t1 + off + (int64_t)r * rs + c), acc);
+                float v[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) v[u] = valid[u] ? __ldg(t1 + off + (int64_t)r[u] * rs + c[u]) : 0.f;
+#pragma unroll
+                for (int u = 0; u < U; ++u) acc[u] = fmaf(cf, v[u], acc[u]);
             }
         }
         if (nterm > 32) mine = load_terms(0);
-        if (valid) {
-            const int k = j.k0 + c;
-            const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
-            const __nv_bfloat16 h = __float2bfloat16_rn(acc);
-            th[idx] = h;
-            tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
-        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (valid[u]) {
+                const int k = j.k0 + c[u];
+                const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r[u]) << 6) + (k & 63);
+                const __nv_bfloat16 h = __float2bfloat16_rn(acc[u]);
+                th[idx] = h;
+                tl[idx] = __float2bfloat16_rn(acc[u] - __bfloat162float(h));
+            }
     }
 }
 
