@@ -49,7 +49,40 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-lanczos", action="store_true")
+    ap.add_argument("--dmrg", action="store_true",
+                    help="also run the Heisenberg L=32, D=64, 4-sweep two-site DMRG (FP64 and split precision)")
+    ap.add_argument("--dmrg-cpu", action="store_true", help="with --dmrg: also run it on the CPU oracle solver")
     return ap.parse_args()
+
+
+def dmrg_cfg1(torch, with_cpu: bool):
+    """Heisenberg OBC L=32, J=1, U(1) 2Sz, MPO bond 5, D=64, random seeded MPS,
+    4 two-site sweeps, Lanczos krylov 20, tol 1e-12: energy per sweep and time."""
+    from tk_gb300 import PREC_BF16X3, PREC_FP64, dmrg, models
+
+    out = {"config": "heisenberg L=32 D=64 4 sweeps krylov=20 tol=1e-12 seed=2024"}
+    runs = [("gpu_fp64", lambda: dmrg.GpuSolver(PREC_FP64, krylov=20, restarts=4, tol=1e-12)),
+            ("gpu_bf16x3_refined", lambda: dmrg.GpuSolver(PREC_BF16X3, krylov=20, restarts=4, tol=1e-12, refine=4))]
+    if with_cpu:
+        sys.path.insert(0, str(ROOT / "tests"))
+        from helpers import CpuSolver
+
+        runs.append(("cpu_oracle_fp64", lambda: CpuSolver(krylov=20, restarts=4, tol=1e-12)))
+    m = models.heisenberg()
+    for name, mk in runs:
+        mps = dmrg.random_mps_u1(m, 32, 64, (0,), np.random.default_rng(2024))
+        solver = mk()
+        t0 = time.perf_counter()
+        st = dmrg.dmrg_two_site(m, mps, 64, 4, solver, (0,))
+        torch.cuda.synchronize()
+        out[name] = {"energies": st.energies, "seconds": time.perf_counter() - t0,
+                     "max_bond": st.max_bond[-1], "discarded_weight": st.trunc[-1],
+                     "matvecs": getattr(solver, "matvecs", None)}
+    e64 = out["gpu_fp64"]["energies"][-1]
+    out["dE_split_vs_fp64"] = abs(out["gpu_bf16x3_refined"]["energies"][-1] - e64)
+    if with_cpu:
+        out["dE_gpu_vs_cpu_oracle"] = abs(out["cpu_oracle_fp64"]["energies"][-1] - e64)
+    return out
 
 
 def dist_env():
@@ -391,6 +424,8 @@ def run_ours(args):
         line["split_vs_fp64_rel_err"] = y_fp
     if lz is not None:
         line["lanczos"] = lz
+    if args.dmrg:
+        line["dmrg_cfg1"] = dmrg_cfg1(torch, args.dmrg_cpu)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()

@@ -166,3 +166,26 @@ def ed_hubbard(n: int, t: float = 1.0, U: float = 4.0, N: int | None = None, sz2
     s2 = sum(c[(k, "u")].T @ c[(k, "u")] - c[(k, "d")].T @ c[(k, "d")] for k in range(n))
     sel = np.where((np.abs(np.diag(nt) - N) < 1e-9) & (np.abs(np.diag(s2) - sz2) < 1e-9))[0]
     return float(np.linalg.eigvalsh(H[np.ix_(sel, sel)])[0])
+
+
+class CpuSolver:
+    """DMRG eigen-solver on the CPU oracle: block-sparse FP64 matvec + numpy Lanczos."""
+
+    def __init__(self, krylov=20, restarts=3, tol=1e-12):
+        self.krylov, self.restarts, self.tol = krylov, restarts, tol
+
+    def solve(self, env_l, env_r, wi, wj, flux, theta_dense):
+        from oracle import lanczos
+
+        orc = oracle.BlockSparseOracle(wi.kind, qlegs(wi.indices[0]), qlegs(wj.indices[0]), qlegs(env_l.ket_idx),
+                                       qlegs(env_r.ket_idx), flux, wi.to_dense(), wj.to_dense(), env_l.data,
+                                       env_r.data)
+        x = orc.from_dense(theta_dense.reshape(-1))
+        if np.linalg.norm(x) == 0:
+            x = None
+        for _ in range(self.restarts + 1):
+            lam, x, _ = lanczos.lowest_eigenpair(orc.apply, orc.total, self.krylov, x0=x)
+            r = orc.apply(x) - lam * x
+            if np.linalg.norm(r) < self.tol:
+                break
+        return float(x @ orc.apply(x)), orc.to_dense(x)
