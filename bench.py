@@ -52,7 +52,37 @@ def parse():
     ap.add_argument("--dmrg", action="store_true",
                     help="also run the Heisenberg L=32, D=64, 4-sweep two-site DMRG (FP64 and split precision)")
     ap.add_argument("--dmrg-cpu", action="store_true", help="with --dmrg: also run it on the CPU oracle solver")
+    ap.add_argument("--compare-schedules", type=int, default=0, metavar="STEPS",
+                    help="also time STEPS FP64 matvecs with one grouped launch per stage and with one launch "
+                         "per sector block")
     return ap.parse_args()
+
+
+def compare_schedules(plan, x, y, torch, dev, steps: int, flush):
+    """FP64 matvec/s with the grouped launch and with one launch per output block."""
+    from tk_gb300 import PREC_BF16X3, PREC_FP64, _abi
+
+    prec = plan.precision
+    plan.set_precision(PREC_FP64)
+    out = {}
+    for name, sched in (("fp64_grouped", _abi.SCHED_GROUPED), ("fp64_per_block", _abi.SCHED_PER_BLOCK)):
+        plan.set_schedule(sched)
+        plan.apply(x, y)
+        torch.cuda.synchronize(dev)
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            plan.apply(x, y)
+            e.record()
+            e.synchronize()
+            tot += s.elapsed_time(e) / 1e3
+        out[name] = steps / tot
+    plan.set_schedule(_abi.SCHED_GROUPED)
+    plan.set_precision(prec)
+    out["grouped_speedup"] = out["fp64_grouped"] / out["fp64_per_block"]
+    return out
 
 
 def dmrg_cfg1(torch, with_cpu: bool):
@@ -424,6 +454,8 @@ def run_ours(args):
         line["split_vs_fp64_rel_err"] = y_fp
     if lz is not None:
         line["lanczos"] = lz
+    if args.compare_schedules > 0:
+        line["schedules"] = compare_schedules(plan, x, y, torch, dev, args.compare_schedules, flush)
     if args.dmrg:
         line["dmrg_cfg1"] = dmrg_cfg1(torch, args.dmrg_cpu)
     print(json.dumps(line), flush=True)

@@ -125,6 +125,15 @@ tk_status tk_heff2_blocks(const tk_heff2_plan* plan, uint64_t* keys, int64_t* of
 tk_status tk_heff2_cost(const tk_heff2_plan* plan, double* flops, double* bytes);
 tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
 
+/* Launch schedule of the FP64 sector GEMMs.  TK_SCHED_GROUPED (default): all
+ * sector GEMMs of a stage in one grouped launch.  TK_SCHED_PER_BLOCK: one
+ * launch per output block, the GPU analogue of the reference's one-task-at-a-
+ * time block_gemm loop (tk-linalg/src/device/faer.rs:439-512), kept as the
+ * baseline the grouped launch is measured against. */
+#define TK_SCHED_GROUPED   0
+#define TK_SCHED_PER_BLOCK 1
+tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule);
+
 /* Per-stage kernel timing for roofline reports (no reference counterpart;
  * observability in the spirit of DMRGStats, tk-dmrg/src/sweep/mod.rs:85-111):
  * runs `reps` complete matvecs y = H_eff x on `stream` -- the same launches

@@ -206,10 +206,36 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision) {
 }
 
 // The FP64 matvec: three stream-ordered launches.
+// One launch per output block (the per-block baseline schedule).
+static cudaError_t launch_per_block(const DevGemm& g, const double* A, const double* B, double* C, cudaStream_t s) {
+    for (size_t t = 0; t + 1 < g.task_tile_begin.size(); ++t) {
+        const int b = g.task_tile_begin[t], n = g.task_tile_begin[t + 1] - b;
+        cudaError_t e = launch_gemm_f64(g.tiles_by_task.p + b, n, g.tasks.p, g.segs.p, A, B, C, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// The FP64 matvec: three stream-ordered stages.
 static tk_status apply_fp64(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s) {
+    if (p->schedule == TK_SCHED_PER_BLOCK) {
+        TK_CUDA(launch_per_block(p->g1, p->lbuf.p, x, p->t1.p, s));
+        TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
+        TK_CUDA(launch_per_block(p->g3, p->t2.p, p->rbuf.p, y, s));
+        return TK_OK;
+    }
     TK_CUDA(launch_gemm_f64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p, x, p->t1.p, s));
     TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
     TK_CUDA(launch_gemm_f64(p->g3.tiles.p, p->g3.n_tiles, p->g3.tasks.p, p->g3.segs.p, p->t2.p, p->rbuf.p, y, s));
+    return TK_OK;
+}
+
+tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
+    if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK)) {
+        set_error("tk_heff2_set_schedule: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    plan->schedule = schedule;
     return TK_OK;
 }
 
@@ -359,13 +385,19 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
                                                stage, err);
                 if (e != cudaSuccess) return cuda_fail(err.c_str(), e);
             } else if (stage == 0) {
-                TK_CUDA(launch_gemm_f64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p, x_dev,
-                                        p->t1.p, s));
+                if (p->schedule == TK_SCHED_PER_BLOCK)
+                    TK_CUDA(launch_per_block(p->g1, p->lbuf.p, x_dev, p->t1.p, s));
+                else
+                    TK_CUDA(launch_gemm_f64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p,
+                                            x_dev, p->t1.p, s));
             } else if (stage == 1) {
                 TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
             } else {
-                TK_CUDA(launch_gemm_f64(p->g3.tiles.p, p->g3.n_tiles, p->g3.tasks.p, p->g3.segs.p, p->t2.p, p->rbuf.p,
-                                        y_dev, s));
+                if (p->schedule == TK_SCHED_PER_BLOCK)
+                    TK_CUDA(launch_per_block(p->g3, p->t2.p, p->rbuf.p, y_dev, s));
+                else
+                    TK_CUDA(launch_gemm_f64(p->g3.tiles.p, p->g3.n_tiles, p->g3.tasks.p, p->g3.segs.p, p->t2.p,
+                                            p->rbuf.p, y_dev, s));
             }
             TK_CUDA(cudaEventRecord(ev[stage + 1], s));
         }

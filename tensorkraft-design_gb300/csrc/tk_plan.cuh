@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <memory>
 #include <vector>
 
@@ -41,13 +42,21 @@ struct DevGemm {
     DevBuf<GemmSeg> segs;
     DevBuf<GemmTile> tiles;
     int n_tiles = 0;
+    // the same tiles grouped by task, for the one-launch-per-block schedule
+    DevBuf<GemmTile> tiles_by_task;
+    std::vector<int> task_tile_begin;  // n_tasks + 1 offsets into tiles_by_task
     cudaError_t upload(const GemmTable& g) {
         cudaError_t e;
         if ((e = tasks.upload(g.tasks)) != cudaSuccess) return e;
         if ((e = segs.upload(g.segs)) != cudaSuccess) return e;
         if ((e = tiles.upload(g.tiles)) != cudaSuccess) return e;
         n_tiles = (int)g.tiles.size();
-        return cudaSuccess;
+        std::vector<GemmTile> by(g.tiles);
+        std::stable_sort(by.begin(), by.end(), [](const GemmTile& a, const GemmTile& b) { return a.task < b.task; });
+        task_tile_begin.assign(g.tasks.size() + 1, 0);
+        for (const GemmTile& t : by) task_tile_begin[t.task + 1]++;
+        for (size_t i = 1; i < task_tile_begin.size(); ++i) task_tile_begin[i] += task_tile_begin[i - 1];
+        return tiles_by_task.upload(by);
     }
 };
 
@@ -62,6 +71,7 @@ struct LanczosGraphDeleter {
 struct tk_heff2_plan {
     int device = 0;
     int precision = TK_PREC_FP64;
+    int schedule = TK_SCHED_GROUPED;
     tk::Heff2Tables host;
     tk::DevBuf<double> lbuf, rbuf, t1, t2;
     tk::DevGemm g1, g3;

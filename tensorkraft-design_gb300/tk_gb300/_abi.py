@@ -16,6 +16,7 @@ TK_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "SECTOR_MISMATCH", 3: "OOM", 4: "CUDA", 5: "TIMEOUT",
                 6: "CANCELLED", 7: "UNSUPPORTED"}
 PREC_FP64, PREC_BF16X3 = 0, 1
+SCHED_GROUPED, SCHED_PER_BLOCK = 0, 1
 
 
 class TkError(RuntimeError):
@@ -80,6 +81,7 @@ SIGNATURES = [
     ("tk_heff2_blocks", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
     ("tk_heff2_cost", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("tk_heff2_set_precision", C.c_int32, [C.c_void_p, C.c_int32]),
+    ("tk_heff2_set_schedule", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_profile", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                      C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("tk_heff2_apply", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -168,6 +168,10 @@ class Heff2Plan:
         check(self._lib.tk_heff2_cost(self._h, C.byref(f), C.byref(b)))
         return f.value, b.value
 
+    def set_schedule(self, schedule: int):
+        """FP64 GEMM launch schedule: _abi.SCHED_GROUPED or _abi.SCHED_PER_BLOCK."""
+        check(self._lib.tk_heff2_set_schedule(self._h, schedule))
+
     def set_precision(self, precision: int):
         check(self._lib.tk_heff2_set_precision(self._h, precision))
         self.precision = precision

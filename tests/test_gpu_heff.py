@@ -142,3 +142,19 @@ def test_sector_mismatch_reported(lib_built):
     bad.bra_idx = q.env_l.bra_idx
     with pytest.raises(TkError):
         Heff2Plan(bad, env_r_bad, p.w_i, p.w_j)
+
+
+def test_per_block_schedule_matches_grouped(lib_built):
+    """One launch per output block gives the same numbers as the grouped launch."""
+    import torch
+    from tk_gb300 import _abi
+
+    p = small_problem("cylinder", 96)
+    plan = p.plan()
+    x = torch.from_numpy(np.random.default_rng(8).standard_normal(plan.block_dim)).cuda()
+    y1, y2 = torch.empty_like(x), torch.empty_like(x)
+    plan.apply(x, y1)
+    plan.set_schedule(_abi.SCHED_PER_BLOCK)
+    plan.apply(x, y2)
+    torch.cuda.synchronize()
+    assert torch.equal(y1, y2)
