@@ -92,7 +92,7 @@ def dmrg_cfg1(torch, with_cpu: bool):
 
     out = {"config": "heisenberg L=32 D=64 4 sweeps krylov=20 tol=1e-12 seed=2024"}
     runs = [("gpu_fp64", lambda: dmrg.GpuSolver(PREC_FP64, krylov=20, restarts=4, tol=1e-12)),
-            ("gpu_bf16x3_refined", lambda: dmrg.GpuSolver(PREC_BF16X3, krylov=20, restarts=4, tol=1e-12, refine=4))]
+            ("gpu_bf16x3_refined", lambda: dmrg.GpuSolver(PREC_BF16X3, krylov=20, restarts=4, tol=1e-12, refine=20))]
     if with_cpu:
         sys.path.insert(0, str(ROOT / "tests"))
         from helpers import CpuSolver
@@ -285,7 +285,7 @@ def lanczos_compare(plan, torch, dev, prec_split: bool):
 
     out = {}
     cfg = dict(krylov_dim=30, max_restarts=40, tol=1e-9)
-    runs = [("fp64", PREC_FP64, 0)] + ([("bf16x3_refined", PREC_BF16X3, 4)] if prec_split else [])
+    runs = [("fp64", PREC_FP64, 0)] + ([("bf16x3_refined", PREC_BF16X3, 30)] if prec_split else [])
     for name, prec, refine in runs:
         plan.set_precision(prec)
         plan.lanczos(krylov_dim=cfg["krylov_dim"], max_restarts=0, tol=cfg["tol"], refine=0)  # graph capture, warm

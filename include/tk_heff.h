@@ -165,8 +165,10 @@ tk_status tk_heff2_flat_to_dense(const tk_heff2_plan* plan, const double* flat, 
  * re-orthogonalisation, Sturm bisection for the eigenvalue; the Ritz vector
  * is solved for (the reference leaves it unsolved) and the residual
  * ||H x - E x|| is computed with an FP64 matvec.  With a split-precision
- * plan, `refine` FP64 correction steps follow.  Vectors are in the block
- * layout on the device.
+ * plan, up to `refine` Jacobi-Davidson steps follow each Lanczos run: one
+ * FP64 matvec each for an FP64 Rayleigh-Ritz step, with the correction
+ * equation solved by split-precision conjugate gradients.  Vectors are in the
+ * block layout on the device.
  */
 typedef struct {
     int32_t krylov_dim;

@@ -16,11 +16,12 @@
 // and captured once into a CUDA graph per (plan, k, precision); a Lanczos
 // call then costs one graph launch plus the Ritz/residual epilogue.
 //
-// Split-precision plans add `refine` FP64 correction steps after the
-// Lanczos run: r = H x - E x with an FP64 matvec, then the projected
-// correction equation (I-xx^T)(H-E)(I-xx^T) t = -r solved by conjugate
-// gradients with split-precision matvecs, x <- (x+t)/|x+t|.  The energy and
-// residual reported are those of FP64 matvecs.
+// Split-precision plans follow each Lanczos run with up to `refine`
+// Jacobi-Davidson steps in FP64 (one FP64 matvec each): Rayleigh-Ritz on an
+// FP64 search space, whose new directions solve the projected correction
+// equation (I-xx^T)(H-theta)(I-xx^T) t = -r by conjugate gradients with
+// split-precision matvecs.  The energy and residual reported are those of
+// FP64 matvecs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -131,8 +132,8 @@ __global__ void axpy2_kernel(double* __restrict__ w, const double* __restrict__ 
     }
 }
 
-// dst = src / *pnorm, or zeros when *pnorm < 1e-15 (breakdown).
-__global__ void normalize_kernel(double* __restrict__ dst, const double* __restrict__ src, const double* pnorm,
+// dst = src / *pnorm, or zeros when *pnorm < 1e-15 (breakdown); dst may be src.
+__global__ void normalize_kernel(double* dst, const double* src, const double* pnorm,
                                  int64_t n) {
     const double nv = *pnorm;
     const double inv = nv < 1e-15 ? 0.0 : 1.0 / nv;
@@ -271,55 +272,242 @@ tk_status fp64_residual(tk_heff2_plan* p, const Ws& ws, const double* x, double*
     return read_scalar(MISC(ws) + 1, rn, s);
 }
 
-tk_status dot_host(const Ws& ws, const double* a, const double* b, double* out, cudaStream_t s) {
-    cudaError_t e = multidot(ws, a, ws.n, 1, b, MISC(ws) + 2, 0, s);
-    if (e != cudaSuccess) return cuda_fail("multidot", e);
-    return read_scalar(MISC(ws) + 2, out, s);
+// ---- FP64 refinement of a split-precision eigenpair -------------------------
+//
+// Jacobi-Davidson with an FP64 search space: V holds up to RF_M orthonormal
+// directions and HV their FP64 images (one FP64 matvec per direction).  Each
+// outer step takes the Ritz pair (theta, x) of V^T H V, r = H x - theta x,
+// then solves the correction equation (I-xx^T)(H - theta)(I-xx^T) t = -r
+// approximately by `inner` conjugate-gradient steps whose matvecs run in the
+// split precision, and adds t (orthogonalised against V) to V.  The split
+// operator's error only slows the inner solve; theta and r always come from
+// FP64 matvecs, so the residual falls to FP64 rounding level.
+
+constexpr int RF_M = 8;       // refinement search-space size before a restart
+constexpr int kInnerCg = 12;  // split-precision CG steps per refinement step
+
+// CG scalars in device memory (RS = refinement scalar area):
+//   RS[0] shift theta, RS[2] x.q, RS[3] p.q, RS[8 + (j&1)] rr of step j
+inline double* RS(const Ws& s) { return s.scal + 4 * s.K + 16; }
+inline double* RC(const Ws& s) { return RS(s) + 16; }  // RF_M + 2 host-visible values
+
+__device__ __forceinline__ double cg_alpha(const double* rs, int j) {
+    const double rr = rs[8 + (j & 1)], pq = rs[3];
+    return (pq > 0.0 && rr > 0.0) ? rr / pq : 0.0;  // 0 freezes the iteration
 }
 
-// One correction step: CG on (I-xx^T)(H_lp - E)(I-xx^T) t = -r.
-tk_status correction_step(tk_heff2_plan* p, const Ws& ws, double* x, const double* r, double E, int iters,
-                          int precision, cudaStream_t s) {
+// q -= theta p; partial[b] = x.q, partial[RG + b] = p.q over this block's rows
+__global__ void __launch_bounds__(RT) cg_shift_dot2_kernel(double* __restrict__ q, const double* __restrict__ p,
+                                                           const double* __restrict__ x, const double* rs, int64_t n,
+                                                           double* __restrict__ partial) {
+    const double th = rs[0];
+    double a = 0.0, b = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)RT + threadIdx.x; i < n; i += (int64_t)RG * RT) {
+        const double pi = p[i];
+        const double qi = fma(-th, pi, q[i]);
+        q[i] = qi;
+        a = fma(x[i], qi, a);
+        b = fma(pi, qi, b);
+    }
+    __shared__ double red[2][RT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        red[0][warp] = a;
+        red[1][warp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double s = 0.0;
+        for (int wv = 0; wv < RT / 32; ++wv) s += red[threadIdx.x][wv];
+        partial[(int64_t)threadIdx.x * RG + blockIdx.x] = s;
+    }
+}
+
+// q -= (x.q) x; t += alpha p; res -= alpha q; partial[b] = res.res
+__global__ void __launch_bounds__(RT) cg_step_kernel(double* __restrict__ t, double* __restrict__ res,
+                                                     const double* __restrict__ p, const double* __restrict__ q,
+                                                     const double* __restrict__ x, const double* rs, int j, int64_t n,
+                                                     double* __restrict__ partial) {
+    const double alpha = cg_alpha(rs, j), xq = rs[2];
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)RT + threadIdx.x; i < n; i += (int64_t)RG * RT) {
+        double ri = res[i];
+        if (alpha != 0.0) {
+            t[i] = fma(alpha, p[i], t[i]);
+            ri = fma(-alpha, fma(-xq, x[i], q[i]), ri);
+            res[i] = ri;
+        }
+        acc = fma(ri, ri, acc);
+    }
+    __shared__ double red[RT / 32];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int wv = 0; wv < RT / 32; ++wv) s += red[wv];
+        partial[blockIdx.x] = s;
+    }
+}
+
+// p = res + (rr_{j+1} / rr_j) p, unless step j was frozen
+__global__ void cg_dir_kernel(double* __restrict__ p, const double* __restrict__ res, const double* rs, int j,
+                              int64_t n) {
+    if (cg_alpha(rs, j) == 0.0) return;
+    const double beta = rs[8 + ((j + 1) & 1)] / rs[8 + (j & 1)];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fma(beta, p[i], res[i]);
+}
+
+// Enqueues `iters` CG steps on (I-xx^T)(H_split - theta)(I-xx^T) t = -r with
+// theta at RS[0]; t, res, p, q are work vectors.  No host synchronisation.
+tk_status enqueue_correction(tk_heff2_plan* p, const Ws& ws, const double* x, const double* r, double* t,
+                             double* res, double* pv, double* q, int iters, int precision, cudaStream_t s) {
     const int64_t n = ws.n;
-    double* t = ws.vec + 2 * n;
-    double* res = ws.vec + 3 * n;
-    double* pv = ws.V;          // reuse the Krylov storage as CG work space
-    double* q = ws.V + n;
+    double* rs = RS(ws);
     cudaError_t e;
     if ((e = cudaMemsetAsync(t, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
-    // res = -r ; p = res
     if ((e = cudaMemsetAsync(res, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
     axpby_kernel<<<vgrid(n), 256, 0, s>>>(res, r, -1.0, 0.0, n);
     if ((e = cudaMemcpyAsync(pv, res, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
         return cuda_fail("cudaMemcpyAsync", e);
-    double rr = 0.0;
-    tk_status st = dot_host(ws, res, res, &rr, s);
-    if (st != TK_OK) return st;
-    const double rr0 = rr;
-    for (int it = 0; it < iters && rr > 1e-24 * rr0 && rr > 0.0; ++it) {
-        if ((st = tk_heff2_apply_prec(p, pv, q, s, precision)) != TK_OK) return st;
-        axpby_kernel<<<vgrid(n), 256, 0, s>>>(q, pv, -E, 1.0, n);
-        double xq = 0.0;
-        if ((st = dot_host(ws, x, q, &xq, s)) != TK_OK) return st;
-        axpby_kernel<<<vgrid(n), 256, 0, s>>>(q, x, -xq, 1.0, n);
-        double pq = 0.0;
-        if ((st = dot_host(ws, pv, q, &pq, s)) != TK_OK) return st;
-        if (!(pq > 0.0)) break;  // operator not positive on this direction: stop
-        const double alpha = rr / pq;
-        axpby_kernel<<<vgrid(n), 256, 0, s>>>(t, pv, alpha, 1.0, n);
-        axpby_kernel<<<vgrid(n), 256, 0, s>>>(res, q, -alpha, 1.0, n);
-        double rr_new = 0.0;
-        if ((st = dot_host(ws, res, res, &rr_new, s)) != TK_OK) return st;
-        const double beta = rr_new / rr;
-        axpby_kernel<<<vgrid(n), 256, 0, s>>>(pv, res, 1.0, beta, n);
-        rr = rr_new;
+    if ((e = multidot(ws, res, n, 1, res, rs + 8, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+    for (int j = 0; j < iters; ++j) {
+        tk_status st = tk_heff2_apply_prec(p, pv, q, s, precision);
+        if (st != TK_OK) return st;
+        cg_shift_dot2_kernel<<<RG, RT, 0, s>>>(q, pv, x, rs, n, ws.part);
+        reduce_partial_kernel<<<2, 128, 0, s>>>(ws.part, rs + 2, 0);
+        cg_step_kernel<<<RG, RT, 0, s>>>(t, res, pv, q, x, rs, j, n, ws.part);
+        reduce_partial_kernel<<<1, 128, 0, s>>>(ws.part, rs + 8 + ((j + 1) & 1), 0);
+        cg_dir_kernel<<<vgrid(n), 256, 0, s>>>(pv, res, rs, j, n);
     }
-    // x <- (x + t) / |x + t|
-    axpby_kernel<<<vgrid(n), 256, 0, s>>>(x, t, 1.0, 1.0, n);
-    if ((e = multidot(ws, x, n, 1, x, MISC(ws) + 3, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
-    normalize_kernel<<<vgrid(n), 256, 0, s>>>(x, x, MISC(ws) + 3, n);
     e = cudaGetLastError();
-    return e == cudaSuccess ? TK_OK : cuda_fail("correction step", e);
+    return e == cudaSuccess ? TK_OK : cuda_fail("correction solve", e);
+}
+
+// Lowest eigenpair of a symmetric m x m matrix (row-major, leading dim ld) by
+// cyclic Jacobi rotations; returns theta and writes the unit eigenvector.
+double small_sym_lowest(const std::vector<double>& g, int m, int ld, std::vector<double>& sv) {
+    std::vector<double> a((size_t)m * m), v((size_t)m * m, 0.0);
+    double frob = 0.0;
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) {
+            a[(size_t)i * m + j] = g[(size_t)i * ld + j];
+            frob += a[(size_t)i * m + j] * a[(size_t)i * m + j];
+        }
+    for (int i = 0; i < m; ++i) v[(size_t)i * m + i] = 1.0;
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0;
+        for (int i = 0; i < m; ++i)
+            for (int j = i + 1; j < m; ++j) off += a[(size_t)i * m + j] * a[(size_t)i * m + j];
+        if (off <= 1e-34 * frob || off == 0.0) break;
+        for (int pp = 0; pp < m; ++pp)
+            for (int qq = pp + 1; qq < m; ++qq) {
+                const double apq = a[(size_t)pp * m + qq];
+                if (apq == 0.0) continue;
+                const double th = (a[(size_t)qq * m + qq] - a[(size_t)pp * m + pp]) / (2.0 * apq);
+                const double tn = (th >= 0.0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double c = 1.0 / std::sqrt(tn * tn + 1.0), sn = tn * c;
+                for (int k = 0; k < m; ++k) {  // A <- A P
+                    const double akp = a[(size_t)k * m + pp], akq = a[(size_t)k * m + qq];
+                    a[(size_t)k * m + pp] = c * akp - sn * akq;
+                    a[(size_t)k * m + qq] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < m; ++k) {  // A <- P^T A
+                    const double apk = a[(size_t)pp * m + k], aqk = a[(size_t)qq * m + k];
+                    a[(size_t)pp * m + k] = c * apk - sn * aqk;
+                    a[(size_t)qq * m + k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < m; ++k) {  // V <- V P
+                    const double vkp = v[(size_t)k * m + pp], vkq = v[(size_t)k * m + qq];
+                    v[(size_t)k * m + pp] = c * vkp - sn * vkq;
+                    v[(size_t)k * m + qq] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    int lo = 0;
+    for (int i = 1; i < m; ++i)
+        if (a[(size_t)i * m + i] < a[(size_t)lo * m + lo]) lo = i;
+    sv.resize(m);
+    for (int k = 0; k < m; ++k) sv[k] = v[(size_t)k * m + lo];
+    return a[(size_t)lo * m + lo];
+}
+
+struct RefineState {
+    double* V;   // RF_M directions
+    double* HV;  // their FP64 images
+    int matvecs = 0, fp64_matvecs = 0;
+};
+
+// Jacobi-Davidson refinement (see above).  On entry x (unit), hx = H x,
+// r = hx - E x and rn = |r| come from an FP64 matvec; on exit they describe
+// the refined pair.  Work vectors: t at vec+2n, the Lanczos basis' first
+// three vectors for the CG (res, p, q).
+tk_status jd_refine(tk_heff2_plan* p, const Ws& ws, RefineState& rf, double* x, double* hx, double* r, double* E,
+                    double* rn, int outer, int inner, double tol, int precision, cudaStream_t s) {
+    const int64_t n = ws.n;
+    double* t = ws.vec + 2 * n;
+    double* rc = RC(ws);
+    cudaError_t e;
+    std::vector<double> G((size_t)RF_M * RF_M, 0.0), col(RF_M + 2), sv;
+    int m = 0;
+    auto restart = [&]() -> tk_status {
+        if ((e = cudaMemcpyAsync(rf.V, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+        if ((e = cudaMemcpyAsync(rf.HV, hx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+        G[0] = *E;
+        m = 1;
+        return TK_OK;
+    };
+    tk_status st = restart();
+    if (st != TK_OK) return st;
+    for (int it = 0; it < outer && *rn > tol; ++it) {
+        // correction t from the split-precision operator
+        if ((e = cudaMemcpyAsync(RS(ws), E, sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+        if ((st = enqueue_correction(p, ws, x, r, t, ws.V, ws.V + n, ws.V + 2 * n, inner, precision, s)) != TK_OK)
+            return st;
+        rf.matvecs += inner;
+        // t <- (I - V V^T)^2 t, normalised, as the next direction
+        double* vm = rf.V + (int64_t)m * n;
+        double* hvm = rf.HV + (int64_t)m * n;
+        for (int pass = 0; pass < 2; ++pass) {
+            if ((e = multidot(ws, rf.V, n, m, t, rc, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+            gemv_sub_kernel<<<vgrid(n), 256, 0, s>>>(rf.V, n, m, rc, t, n);
+        }
+        if ((e = multidot(ws, t, n, 1, t, rc + RF_M + 1, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+        normalize_kernel<<<vgrid(n), 256, 0, s>>>(vm, t, rc + RF_M + 1, n);
+        if ((st = tk_heff2_apply_prec(p, vm, hvm, s, TK_PREC_FP64)) != TK_OK) return st;
+        ++rf.matvecs;
+        ++rf.fp64_matvecs;
+        // new column of V^T H V and the direction's norm, in one read
+        if ((e = multidot(ws, rf.V, n, m + 1, hvm, rc, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+        if ((e = cudaMemcpyAsync(col.data(), rc, sizeof(double) * (RF_M + 2), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("refinement step", e);
+        if (!(col[RF_M + 1] >= 1e-15)) break;  // the correction lies in span(V): nothing new to add
+        for (int i = 0; i <= m; ++i) G[(size_t)i * RF_M + m] = G[(size_t)m * RF_M + i] = col[i];
+        ++m;
+        // Rayleigh-Ritz in FP64
+        const double theta = small_sym_lowest(G, m, RF_M, sv);
+        if ((e = cudaMemcpyAsync(rc, sv.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+        gemv_kernel<<<vgrid(n), 256, 0, s>>>(rf.V, n, m, rc, x, n);
+        gemv_kernel<<<vgrid(n), 256, 0, s>>>(rf.HV, n, m, rc, hx, n);
+        if ((e = cudaMemcpyAsync(r, hx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+        axpby_kernel<<<vgrid(n), 256, 0, s>>>(r, x, -theta, 1.0, n);
+        if ((e = multidot(ws, r, n, 1, r, MISC(ws) + 1, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+        if ((st = read_scalar(MISC(ws) + 1, rn, s)) != TK_OK) return st;
+        *E = theta;
+        if (m == RF_M && *rn > tol && (st = restart()) != TK_OK) return st;
+    }
+    return TK_OK;
 }
 
 }  // namespace
@@ -365,8 +553,9 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
         const int kk = std::max(k, 2);
         if ((e = p->lz_basis.alloc((size_t)(kk + 1) * n)) != cudaSuccess) return cuda_fail("alloc basis", e);
         if ((e = p->lz_w.alloc((size_t)n)) != cudaSuccess) return cuda_fail("alloc w", e);
-        if ((e = p->lz_scal.alloc((size_t)(4 * kk + 16))) != cudaSuccess) return cuda_fail("alloc scal", e);
-        if ((e = p->lz_part.alloc((size_t)RG * (kk + 1))) != cudaSuccess) return cuda_fail("alloc part", e);
+        if ((e = p->lz_scal.alloc((size_t)(4 * kk + 64))) != cudaSuccess) return cuda_fail("alloc scal", e);
+        if ((e = p->lz_part.alloc((size_t)RG * std::max(kk + 1, RF_M + 1))) != cudaSuccess)
+            return cuda_fail("alloc part", e);
         if ((e = p->lz_vec.alloc((size_t)4 * n)) != cudaSuccess) return cuda_fail("alloc vec", e);
         p->lz_cap_k = k;
     }
@@ -444,14 +633,17 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
         if ((st = fp64_residual(p, ws, x, hx, r, &E, &rn, s)) != TK_OK) return st;
         ++fp64_matvecs;
         ++matvecs;
-        // split precision: FP64 correction steps
-        for (int it = 0; it < cfg->refine && lz_prec != TK_PREC_FP64 && rn > cfg->tol; ++it) {
-            const int cg_iters = 16;
-            if ((st = correction_step(p, ws, x, r, E, cg_iters, lz_prec, s)) != TK_OK) return st;
-            matvecs += cg_iters;
-            if ((st = fp64_residual(p, ws, x, hx, r, &E, &rn, s)) != TK_OK) return st;
-            ++fp64_matvecs;
-            ++matvecs;
+        // split precision: FP64 Jacobi-Davidson refinement
+        if (lz_prec != TK_PREC_FP64 && cfg->refine > 0 && rn > cfg->tol) {
+            if (p->rf_v.n < (size_t)RF_M * n) {
+                if ((e = p->rf_v.alloc((size_t)RF_M * n)) != cudaSuccess) return cuda_fail("alloc refinement", e);
+                if ((e = p->rf_hv.alloc((size_t)RF_M * n)) != cudaSuccess) return cuda_fail("alloc refinement", e);
+            }
+            RefineState rf{p->rf_v.p, p->rf_hv.p};
+            if ((st = jd_refine(p, ws, rf, x, hx, r, &E, &rn, cfg->refine, kInnerCg, cfg->tol, lz_prec, s)) != TK_OK)
+                return st;
+            matvecs += rf.matvecs;
+            fp64_matvecs += rf.fp64_matvecs;
         }
         if (rn <= cfg->tol || restarts >= cfg->max_restarts) break;
         ++restarts;

@@ -157,7 +157,7 @@ def grow_right(R: np.ndarray, A: np.ndarray, W: np.ndarray) -> np.ndarray:
 class GpuSolver:
     """Device H_eff plan + device Lanczos (tk_heff2_plan_create + tk_lanczos_lowest)."""
 
-    def __init__(self, precision: int = 0, krylov: int = 20, tol: float = 1e-12, restarts: int = 3, refine: int = 3,
+    def __init__(self, precision: int = 0, krylov: int = 20, tol: float = 1e-12, restarts: int = 3, refine: int = 20,
                  device: int = 0):
         self.precision, self.krylov, self.tol, self.restarts, self.refine = precision, krylov, tol, restarts, refine
         self.device = device

@@ -251,7 +251,7 @@ class LanczosSolver:
     restart_vectors: int = 5
     max_iter: int = 0
     tol: float = 1e-10
-    refine: int = 2
+    refine: int = 20
 
     def lowest_eigenpair(self, plan: Heff2Plan, initial=None) -> EigenResult:
         return plan.lanczos(krylov_dim=self.max_krylov_dim, max_restarts=self.max_iter, tol=self.tol,

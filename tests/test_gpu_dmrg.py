@@ -29,5 +29,5 @@ def test_dmrg_fp64_matches_cpu_oracle(lib_built):
 
 def test_dmrg_split_refined_matches_fp64(lib_built):
     fp64 = _run(14, 24, 2, dmrg.GpuSolver(PREC_FP64, krylov=20, restarts=5, tol=1e-11))
-    split = _run(14, 24, 2, dmrg.GpuSolver(PREC_BF16X3, krylov=20, restarts=5, tol=1e-11, refine=4))
+    split = _run(14, 24, 2, dmrg.GpuSolver(PREC_BF16X3, krylov=20, restarts=5, tol=1e-11, refine=20))
     assert abs(split.energies[-1] - fp64.energies[-1]) < 1e-10

@@ -66,7 +66,7 @@ def test_refined_energy_matches_fp64(lib_built, name):
     r64 = plan64.lanczos(krylov_dim=40, max_restarts=30, tol=1e-10)
     assert r64.converged
     plan = p.plan(precision=PREC_BF16X3)
-    r = plan.lanczos(krylov_dim=40, max_restarts=30, tol=1e-10, refine=4)
+    r = plan.lanczos(krylov_dim=40, max_restarts=30, tol=1e-10, refine=20)
     assert abs(r.eigenvalue - r64.eigenvalue) < 1e-10, (r.eigenvalue, r64.eigenvalue, r.residual_norm)
     assert r.residual_norm < 1e-9
 
@@ -76,5 +76,5 @@ def test_refined_energy_exact_environment(lib_built):
 
     p = exact_problem(models.heisenberg(), 10, 4, (0,))
     plan = p.plan(precision=PREC_BF16X3)
-    r = plan.lanczos(krylov_dim=60, max_restarts=20, tol=1e-10, refine=4)
+    r = plan.lanczos(krylov_dim=60, max_restarts=20, tol=1e-10, refine=20)
     assert abs(r.eigenvalue - ed_heisenberg(10)) < 1e-10
