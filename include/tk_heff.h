@@ -190,6 +190,33 @@ tk_status tk_lanczos_lowest(tk_heff2_plan* plan, const tk_lanczos_cfg* cfg, cons
                             double* evec_dev, tk_eigen_result* out, void* stream);
 
 /*
+ * Davidson lowest eigenpair on the device: replaces
+ * DavidsonSolver::lowest_eigenpair (tk-dmrg/src/eigensolver/mod.rs:325-517),
+ * the sweep's default eigensolver (tk-dmrg/src/sweep/mod.rs:174-179).  Same
+ * start vector as Lanczos when x0 is NULL; Rayleigh-Ritz on V^T H V each
+ * iteration; stop when ||H y - theta y|| < tol; the correction is the
+ * residual, divided by (theta - H_ii) where |theta - H_ii| > 1e-14 when
+ * `diagonal` is given, orthogonalised against the search space, with the raw
+ * residual as fallback when it collapses below 1e-14; at `max_subspace`
+ * directions the space restarts from the Ritz vector (one matvec; the
+ * reference's `restart_vectors` is unused there too).  Every matvec of the
+ * search space is FP64.  With a split-precision plan and inner > 0 the
+ * correction instead solves (I-yy^T)(H-theta)(I-yy^T) t = -r by `inner`
+ * conjugate-gradient steps with split-precision matvecs (Jacobi-Davidson);
+ * inner = 0 keeps the reference's correction.  `restarts` is reported as 0.
+ */
+typedef struct {
+    int32_t max_subspace;    /* DavidsonSolver::max_subspace (reference default 60), <= 256 */
+    int32_t max_iter;        /* DavidsonSolver::max_iter (reference default 1000) */
+    double tol;              /* DavidsonSolver::tol (reference default 1e-10) */
+    const double* diagonal;  /* DavidsonSolver::diagonal: H_ii in the block layout (device) or NULL */
+    int32_t inner;           /* split-precision plans: CG steps per correction (0: the residual) */
+} tk_davidson_cfg;
+
+tk_status tk_davidson_lowest(tk_heff2_plan* plan, const tk_davidson_cfg* cfg, const double* x0_dev,
+                             double* evec_dev, tk_eigen_result* out, void* stream);
+
+/*
  * LinAlgBackend::gemm (tk-linalg/src/traits.rs:114-121) on device memory:
  * C = alpha*op(A)*op(B) + beta*C with element strides as in MatRef/MatMut
  * (tk-core/src/matview.rs:12-33).  `is_conjugated` is a no-op for f64.

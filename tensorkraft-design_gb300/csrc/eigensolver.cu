@@ -286,10 +286,8 @@ tk_status fp64_residual(tk_heff2_plan* p, const Ws& ws, const double* x, double*
 constexpr int RF_M = 8;       // refinement search-space size before a restart
 constexpr int kInnerCg = 12;  // split-precision CG steps per refinement step
 
-// CG scalars in device memory (RS = refinement scalar area):
-//   RS[0] shift theta, RS[2] x.q, RS[3] p.q, RS[8 + (j&1)] rr of step j
-inline double* RS(const Ws& s) { return s.scal + 4 * s.K + 16; }
-inline double* RC(const Ws& s) { return RS(s) + 16; }  // RF_M + 2 host-visible values
+// CG scalars in device memory (rs):
+//   rs[0] shift theta, rs[2] x.q, rs[3] p.q, rs[8 + (j&1)] rr of step j
 
 __device__ __forceinline__ double cg_alpha(const double* rs, int j) {
     const double rr = rs[8 + (j & 1)], pq = rs[3];
@@ -364,11 +362,10 @@ __global__ void cg_dir_kernel(double* __restrict__ p, const double* __restrict__
 }
 
 // Enqueues `iters` CG steps on (I-xx^T)(H_split - theta)(I-xx^T) t = -r with
-// theta at RS[0]; t, res, p, q are work vectors.  No host synchronisation.
-tk_status enqueue_correction(tk_heff2_plan* p, const Ws& ws, const double* x, const double* r, double* t,
+// theta at rs[0]; t, res, p, q are work vectors.  No host synchronisation.
+tk_status enqueue_correction(tk_heff2_plan* p, const Ws& ws, double* rs, const double* x, const double* r, double* t,
                              double* res, double* pv, double* q, int iters, int precision, cudaStream_t s) {
     const int64_t n = ws.n;
-    double* rs = RS(ws);
     cudaError_t e;
     if ((e = cudaMemsetAsync(t, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
     if ((e = cudaMemsetAsync(res, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
@@ -437,78 +434,204 @@ double small_sym_lowest(const std::vector<double>& g, int m, int ld, std::vector
     return a[(size_t)lo * m + lo];
 }
 
-struct RefineState {
-    double* V;   // RF_M directions
-    double* HV;  // their FP64 images
+// DavidsonSolver's diagonal preconditioner (eigensolver/mod.rs:427-437):
+// t_i = r_i / (theta - d_i) where |theta - d_i| > 1e-14, else t_i = r_i.
+__global__ void precondition_kernel(double* __restrict__ t, const double* __restrict__ r,
+                                    const double* __restrict__ d, double theta, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double den = theta - d[i];
+        t[i] = fabs(den) > 1e-14 ? r[i] / den : r[i];
+    }
+}
+
+// Search space of the FP64 subspace solver: V (orthonormal directions), HV
+// (their FP64 images), host-visible scalars sc and reduction partials.
+struct Subspace {
+    double* V;
+    double* HV;
+    double* sc;  // [0, M) coefficients, [M] a norm, [M+8, M+24) CG scalars
+    int M;
     int matvecs = 0, fp64_matvecs = 0;
 };
 
-// Jacobi-Davidson refinement (see above).  On entry x (unit), hx = H x,
-// r = hx - E x and rn = |r| come from an FP64 matvec; on exit they describe
-// the refined pair.  Work vectors: t at vec+2n, the Lanczos basis' first
-// three vectors for the CG (res, p, q).
-tk_status jd_refine(tk_heff2_plan* p, const Ws& ws, RefineState& rf, double* x, double* hx, double* r, double* E,
-                    double* rn, int outer, int inner, double tol, int precision, cudaStream_t s) {
+struct SubspaceCfg {
+    int max_iter;
+    double tol;
+    const double* diag;   // Davidson preconditioner (device, block layout) or null
+    int inner;            // > 0: correction by `inner` CG steps in `inner_prec`
+    int inner_prec;
+    bool restart_matvec;  // restart as DavidsonSolver: recompute H y, drop the correction
+    bool have_hx;         // hx = H x on entry (no first matvec)
+};
+
+// Davidson / Jacobi-Davidson on an FP64 search space (DavidsonSolver::
+// lowest_eigenpair, eigensolver/mod.rs:325-517):
+//   Rayleigh-Ritz on V^T H V (its upper triangle is V_i . HV_j, :368-376),
+//   y = V c, r = HV c - theta y (:389-411), stop when |r| < tol (:413-422);
+//   the correction is r (optionally diagonal-preconditioned) or, with
+//   inner > 0, an approximate solution of the projected correction equation;
+//   it is orthogonalised against V, falls back to the orthogonalised raw
+//   residual when it collapses below 1e-14 (:449-477), and is added with one
+//   FP64 matvec; at M directions the space restarts from y (:485-500).
+// Orthogonalisation is two passes of blocked classical Gram-Schmidt (the
+// reference uses one modified Gram-Schmidt pass), and the small eigenproblem
+// uses cyclic Jacobi with a relative stopping rule.
+// On exit x (unit), hx, r = hx - E x and rn describe the last Ritz pair.
+tk_status subspace_solve(tk_heff2_plan* p, const Ws& ws, Subspace& sp, const SubspaceCfg& cfg, double* x, double* hx,
+                         double* r, double* E, double* rn, bool* converged, cudaStream_t s) {
     const int64_t n = ws.n;
+    const int M = sp.M;
     double* t = ws.vec + 2 * n;
-    double* rc = RC(ws);
+    double* sc = sp.sc;
+    double* rs = sp.sc + M + 8;
     cudaError_t e;
-    std::vector<double> G((size_t)RF_M * RF_M, 0.0), col(RF_M + 2), sv;
-    int m = 0;
-    auto restart = [&]() -> tk_status {
-        if ((e = cudaMemcpyAsync(rf.V, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
-            return cuda_fail("cudaMemcpyAsync", e);
-        if ((e = cudaMemcpyAsync(rf.HV, hx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
-            return cuda_fail("cudaMemcpyAsync", e);
-        G[0] = *E;
-        m = 1;
+    tk_status st;
+    std::vector<double> G((size_t)M * M, 0.0), col(M + 1), cvec;
+    *converged = false;
+    // V_0 = x / |x|, HV_0 = H V_0
+    if ((e = multidot(ws, x, n, 1, x, sc + M, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+    normalize_kernel<<<vgrid(n), 256, 0, s>>>(sp.V, x, sc + M, n);
+    if (cfg.have_hx) {
+        normalize_kernel<<<vgrid(n), 256, 0, s>>>(sp.HV, hx, sc + M, n);
+    } else {
+        if ((st = tk_heff2_apply_prec(p, sp.V, sp.HV, s, TK_PREC_FP64)) != TK_OK) return st;
+        ++sp.matvecs;
+        ++sp.fp64_matvecs;
+    }
+    auto add_column = [&](int j) -> tk_status {  // G[i][j] = G[j][i] = V_i . HV_j, i <= j
+        cudaError_t e2 = multidot(ws, sp.V, n, j + 1, sp.HV + (int64_t)j * n, sc, 0, s);
+        if (e2 != cudaSuccess) return cuda_fail("multidot", e2);
+        if ((e2 = cudaMemcpyAsync(col.data(), sc, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e2);
+        if ((e2 = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("subspace step", e2);
+        for (int i = 0; i <= j; ++i) G[(size_t)i * M + j] = G[(size_t)j * M + i] = col[i];
         return TK_OK;
     };
-    tk_status st = restart();
-    if (st != TK_OK) return st;
-    for (int it = 0; it < outer && *rn > tol; ++it) {
-        // correction t from the split-precision operator
-        if ((e = cudaMemcpyAsync(RS(ws), E, sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    if ((st = add_column(0)) != TK_OK) return st;
+    int m = 1;
+    double theta = G[0];
+    for (int it = 0; it < cfg.max_iter; ++it) {
+        // Ritz pair and residual
+        theta = small_sym_lowest(G, m, M, cvec);
+        if ((e = cudaMemcpyAsync(sc, cvec.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
             return cuda_fail("cudaMemcpyAsync", e);
-        if ((st = enqueue_correction(p, ws, x, r, t, ws.V, ws.V + n, ws.V + 2 * n, inner, precision, s)) != TK_OK)
-            return st;
-        rf.matvecs += inner;
-        // t <- (I - V V^T)^2 t, normalised, as the next direction
-        double* vm = rf.V + (int64_t)m * n;
-        double* hvm = rf.HV + (int64_t)m * n;
-        for (int pass = 0; pass < 2; ++pass) {
-            if ((e = multidot(ws, rf.V, n, m, t, rc, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
-            gemv_sub_kernel<<<vgrid(n), 256, 0, s>>>(rf.V, n, m, rc, t, n);
-        }
-        if ((e = multidot(ws, t, n, 1, t, rc + RF_M + 1, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
-        normalize_kernel<<<vgrid(n), 256, 0, s>>>(vm, t, rc + RF_M + 1, n);
-        if ((st = tk_heff2_apply_prec(p, vm, hvm, s, TK_PREC_FP64)) != TK_OK) return st;
-        ++rf.matvecs;
-        ++rf.fp64_matvecs;
-        // new column of V^T H V and the direction's norm, in one read
-        if ((e = multidot(ws, rf.V, n, m + 1, hvm, rc, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
-        if ((e = cudaMemcpyAsync(col.data(), rc, sizeof(double) * (RF_M + 2), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-            return cuda_fail("cudaMemcpyAsync", e);
-        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("refinement step", e);
-        if (!(col[RF_M + 1] >= 1e-15)) break;  // the correction lies in span(V): nothing new to add
-        for (int i = 0; i <= m; ++i) G[(size_t)i * RF_M + m] = G[(size_t)m * RF_M + i] = col[i];
-        ++m;
-        // Rayleigh-Ritz in FP64
-        const double theta = small_sym_lowest(G, m, RF_M, sv);
-        if ((e = cudaMemcpyAsync(rc, sv.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-            return cuda_fail("cudaMemcpyAsync", e);
-        gemv_kernel<<<vgrid(n), 256, 0, s>>>(rf.V, n, m, rc, x, n);
-        gemv_kernel<<<vgrid(n), 256, 0, s>>>(rf.HV, n, m, rc, hx, n);
+        gemv_kernel<<<vgrid(n), 256, 0, s>>>(sp.V, n, m, sc, x, n);
+        gemv_kernel<<<vgrid(n), 256, 0, s>>>(sp.HV, n, m, sc, hx, n);
         if ((e = cudaMemcpyAsync(r, hx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
             return cuda_fail("cudaMemcpyAsync", e);
         axpby_kernel<<<vgrid(n), 256, 0, s>>>(r, x, -theta, 1.0, n);
-        if ((e = multidot(ws, r, n, 1, r, MISC(ws) + 1, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
-        if ((st = read_scalar(MISC(ws) + 1, rn, s)) != TK_OK) return st;
+        if ((e = multidot(ws, r, n, 1, r, sc + M, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+        if ((st = read_scalar(sc + M, rn, s)) != TK_OK) return st;
         *E = theta;
-        if (m == RF_M && *rn > tol && (st = restart()) != TK_OK) return st;
+        if (*rn < cfg.tol) {
+            *converged = true;
+            break;
+        }
+        // correction
+        if (cfg.inner > 0) {
+            if ((e = cudaMemcpyAsync(rs, &theta, sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                return cuda_fail("cudaMemcpyAsync", e);
+            if ((st = enqueue_correction(p, ws, rs, x, r, t, ws.V, ws.V + n, ws.V + 2 * n, cfg.inner, cfg.inner_prec,
+                                         s)) != TK_OK)
+                return st;
+            sp.matvecs += cfg.inner;
+        } else if (cfg.diag) {
+            precondition_kernel<<<vgrid(n), 256, 0, s>>>(t, r, cfg.diag, theta, n);
+        } else if ((e = cudaMemcpyAsync(t, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) {
+            return cuda_fail("cudaMemcpyAsync", e);
+        }
+        double cnorm = 0.0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            for (int pass = 0; pass < 2; ++pass) {
+                if ((e = multidot(ws, sp.V, n, m, t, sc, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+                gemv_sub_kernel<<<vgrid(n), 256, 0, s>>>(sp.V, n, m, sc, t, n);
+            }
+            if ((e = multidot(ws, t, n, 1, t, sc + M, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+            if ((st = read_scalar(sc + M, &cnorm, s)) != TK_OK) return st;
+            if (cnorm >= 1e-14 || attempt == 1) break;
+            // the correction collapsed into span(V): use the raw residual
+            if ((e = cudaMemcpyAsync(t, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+                return cuda_fail("cudaMemcpyAsync", e);
+        }
+        if (cnorm < 1e-14) break;  // converged or stagnated
+        if (m >= M) {
+            if (m >= n) break;  // the space is complete
+            if ((e = cudaMemcpyAsync(sp.V, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+                return cuda_fail("cudaMemcpyAsync", e);
+            if (cfg.restart_matvec) {
+                if ((st = tk_heff2_apply_prec(p, sp.V, sp.HV, s, TK_PREC_FP64)) != TK_OK) return st;
+                ++sp.matvecs;
+                ++sp.fp64_matvecs;
+                m = 1;
+                if ((st = add_column(0)) != TK_OK) return st;
+                continue;
+            }
+            if ((e = cudaMemcpyAsync(sp.HV, hx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+                return cuda_fail("cudaMemcpyAsync", e);
+            G[0] = theta;
+            m = 1;
+            // t is orthogonal to the old span, which contains y: append it below
+        }
+        double* vm = sp.V + (int64_t)m * n;
+        normalize_kernel<<<vgrid(n), 256, 0, s>>>(vm, t, sc + M, n);
+        if ((st = tk_heff2_apply_prec(p, vm, sp.HV + (int64_t)m * n, s, TK_PREC_FP64)) != TK_OK) return st;
+        ++sp.matvecs;
+        ++sp.fp64_matvecs;
+        if ((st = add_column(m)) != TK_OK) return st;
+        ++m;
     }
+    e = cudaGetLastError();
+    return e == cudaSuccess ? TK_OK : cuda_fail("subspace solve", e);
+}
+
+// Lanczos workspace for k steps (allocated on first use, grown on demand).
+tk_status ensure_lanczos_ws(tk_heff2_plan* p, int k, int64_t n, Ws* ws) {
+    cudaError_t e;
+    if (p->lz_cap_k < k) {
+        p->lz_basis.reset();
+        p->lz_w.reset();
+        p->lz_scal.reset();
+        p->lz_part.reset();
+        p->lz_vec.reset();
+        p->lz_graph.reset();
+        const int kk = std::max(k, 2);
+        if ((e = p->lz_basis.alloc((size_t)(kk + 1) * n)) != cudaSuccess) return cuda_fail("alloc basis", e);
+        if ((e = p->lz_w.alloc((size_t)n)) != cudaSuccess) return cuda_fail("alloc w", e);
+        if ((e = p->lz_scal.alloc((size_t)(4 * kk + 16))) != cudaSuccess) return cuda_fail("alloc scal", e);
+        if ((e = p->lz_part.alloc((size_t)RG * (kk + 1))) != cudaSuccess) return cuda_fail("alloc part", e);
+        if ((e = p->lz_vec.alloc((size_t)4 * n)) != cudaSuccess) return cuda_fail("alloc vec", e);
+        p->lz_cap_k = k;
+    }
+    *ws = Ws{p->lz_basis.p, p->lz_w.p, p->lz_scal.p, p->lz_part.p, p->lz_vec.p, n, std::max(p->lz_cap_k, 2)};
     return TK_OK;
 }
+
+// Search space of M directions; `ws` gets a partials buffer for M-wide multidots.
+tk_status ensure_subspace(tk_heff2_plan* p, int M, int64_t n, Ws* ws, Subspace* sp) {
+    cudaError_t e;
+    if (p->sub_cap < M) {
+        p->sub_cap = 0;
+        if ((e = p->sub_v.alloc((size_t)M * n)) != cudaSuccess) return cuda_fail("alloc search space", e);
+        if ((e = p->sub_hv.alloc((size_t)M * n)) != cudaSuccess) return cuda_fail("alloc search space", e);
+        if ((e = p->sub_sc.alloc((size_t)M + 32)) != cudaSuccess) return cuda_fail("alloc search space", e);
+        if ((e = p->sub_part.alloc((size_t)RG * (M + 1))) != cudaSuccess) return cuda_fail("alloc search space", e);
+        p->sub_cap = M;
+    }
+    ws->part = p->sub_part.p;
+    *sp = Subspace{p->sub_v.p, p->sub_hv.p, p->sub_sc.p, M};
+    return TK_OK;
+}
+
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        cudaGetDevice(&prev);
+        cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 }  // namespace tk
@@ -531,40 +654,17 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
         set_error("tk_lanczos_lowest: krylov_dim must be in [1, 512], restarts and refine >= 0");
         return TK_ERR_INVALID_ARG;
     }
-    int prev_dev = -1;
-    cudaGetDevice(&prev_dev);
-    cudaSetDevice(p->device);
-    struct Restore {
-        int d;
-        ~Restore() {
-            if (d >= 0) cudaSetDevice(d);
-        }
-    } restore{prev_dev};
+    DeviceScope scope(p->device);
     const int k = (int)std::min<int64_t>(cfg->krylov_dim, n);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
-    if (p->lz_cap_k < k) {
-        p->lz_basis.reset();
-        p->lz_w.reset();
-        p->lz_scal.reset();
-        p->lz_part.reset();
-        p->lz_vec.reset();
-        p->lz_graph.reset();
-        const int kk = std::max(k, 2);
-        if ((e = p->lz_basis.alloc((size_t)(kk + 1) * n)) != cudaSuccess) return cuda_fail("alloc basis", e);
-        if ((e = p->lz_w.alloc((size_t)n)) != cudaSuccess) return cuda_fail("alloc w", e);
-        if ((e = p->lz_scal.alloc((size_t)(4 * kk + 64))) != cudaSuccess) return cuda_fail("alloc scal", e);
-        if ((e = p->lz_part.alloc((size_t)RG * std::max(kk + 1, RF_M + 1))) != cudaSuccess)
-            return cuda_fail("alloc part", e);
-        if ((e = p->lz_vec.alloc((size_t)4 * n)) != cudaSuccess) return cuda_fail("alloc vec", e);
-        p->lz_cap_k = k;
-    }
-    Ws ws{p->lz_basis.p, p->lz_w.p, p->lz_scal.p, p->lz_part.p, p->lz_vec.p, n, std::max(p->lz_cap_k, 2)};
+    Ws ws;
+    tk_status st = ensure_lanczos_ws(p, k, n, &ws);
+    if (st != TK_OK) return st;
     double* x = evec_dev;
     double* hx = ws.vec;
     double* r = ws.vec + n;
     const int lz_prec = p->precision;
-    tk_status st;
     // start vector -> x
     if (x0_dev) {
         if (x0_dev != x && (e = cudaMemcpyAsync(x, x0_dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
@@ -635,15 +735,14 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
         ++matvecs;
         // split precision: FP64 Jacobi-Davidson refinement
         if (lz_prec != TK_PREC_FP64 && cfg->refine > 0 && rn > cfg->tol) {
-            if (p->rf_v.n < (size_t)RF_M * n) {
-                if ((e = p->rf_v.alloc((size_t)RF_M * n)) != cudaSuccess) return cuda_fail("alloc refinement", e);
-                if ((e = p->rf_hv.alloc((size_t)RF_M * n)) != cudaSuccess) return cuda_fail("alloc refinement", e);
-            }
-            RefineState rf{p->rf_v.p, p->rf_hv.p};
-            if ((st = jd_refine(p, ws, rf, x, hx, r, &E, &rn, cfg->refine, kInnerCg, cfg->tol, lz_prec, s)) != TK_OK)
-                return st;
-            matvecs += rf.matvecs;
-            fp64_matvecs += rf.fp64_matvecs;
+            Ws ws2 = ws;
+            Subspace sp;
+            if ((st = ensure_subspace(p, RF_M, n, &ws2, &sp)) != TK_OK) return st;
+            SubspaceCfg sc{cfg->refine, cfg->tol, nullptr, kInnerCg, lz_prec, false, true};
+            bool conv = false;
+            if ((st = subspace_solve(p, ws2, sp, sc, x, hx, r, &E, &rn, &conv, s)) != TK_OK) return st;
+            matvecs += sp.matvecs;
+            fp64_matvecs += sp.fp64_matvecs;
         }
         if (rn <= cfg->tol || restarts >= cfg->max_restarts) break;
         ++restarts;
@@ -655,5 +754,54 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
     out->matvec_count = matvecs;
     out->fp64_matvec_count = fp64_matvecs;
     out->restarts = restarts;
+    return TK_OK;
+}
+
+extern "C" tk_status tk_davidson_lowest(tk_heff2_plan* p, const tk_davidson_cfg* cfg, const double* x0_dev,
+                                        double* evec_dev, tk_eigen_result* out, void* stream) {
+    if (!p || !cfg || !out || !evec_dev) {
+        set_error("tk_davidson_lowest: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    *out = tk_eigen_result{};
+    const int64_t n = p->host.total;
+    if (n == 0) {
+        set_error("tk_davidson_lowest: empty two-site space");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (cfg->max_subspace < 1 || cfg->max_subspace > 256 || cfg->max_iter < 0 || cfg->inner < 0 ||
+        cfg->inner > 1000) {
+        set_error("tk_davidson_lowest: max_subspace must be in [1, 256], max_iter >= 0, inner in [0, 1000]");
+        return TK_ERR_INVALID_ARG;
+    }
+    DeviceScope scope(p->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    Ws ws;
+    tk_status st = ensure_lanczos_ws(p, 2, n, &ws);
+    if (st != TK_OK) return st;
+    const int M = (int)std::min<int64_t>(cfg->max_subspace, n);
+    Subspace sp;
+    if ((st = ensure_subspace(p, M, n, &ws, &sp)) != TK_OK) return st;
+    double* x = evec_dev;
+    if (x0_dev) {
+        if (x0_dev != x && (e = cudaMemcpyAsync(x, x0_dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
+    } else if ((e = launch_fill_start_vector(x, n, s)) != cudaSuccess) {
+        return cuda_fail("start vector", e);
+    }
+    const int inner = p->precision != TK_PREC_FP64 ? cfg->inner : 0;
+    SubspaceCfg sc{cfg->max_iter, cfg->tol, cfg->diagonal, inner, p->precision, true, false};
+    double E = 0.0, rn = INFINITY;
+    bool conv = false;
+    if ((st = subspace_solve(p, ws, sp, sc, x, ws.vec, ws.vec + n, &E, &rn, &conv, s)) != TK_OK) return st;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("davidson", e);
+    if (p->tc && (st = tc_check_error(*p->tc, s)) != TK_OK) return st;
+    out->eigenvalue = E;
+    out->residual_norm = rn;
+    out->converged = conv ? 1 : 0;
+    out->matvec_count = sp.matvecs;
+    out->fp64_matvec_count = sp.fp64_matvecs;
+    out->restarts = 0;
     return TK_OK;
 }

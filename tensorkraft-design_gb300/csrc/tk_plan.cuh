@@ -87,7 +87,9 @@ struct tk_heff2_plan {
     std::unique_ptr<tk::TcPlan, tk::TcPlanDeleter> tc;
     // Lanczos workspace (allocated on first use)
     tk::DevBuf<double> lz_basis, lz_w, lz_scal, lz_part, lz_vec;
-    tk::DevBuf<double> rf_v, rf_hv;  // FP64 refinement search space and its images
+    // FP64 search space of the Davidson / refinement solver (allocated on first use)
+    tk::DevBuf<double> sub_v, sub_hv, sub_sc, sub_part;
+    int sub_cap = 0;
     int lz_cap_k = 0;
     std::unique_ptr<tk::LanczosGraph, tk::LanczosGraphDeleter> lz_graph;
     ~tk_heff2_plan() {

@@ -47,6 +47,11 @@ class tk_lanczos_cfg(C.Structure):
                 ("refine", C.c_int32)]
 
 
+class tk_davidson_cfg(C.Structure):
+    _fields_ = [("max_subspace", C.c_int32), ("max_iter", C.c_int32), ("tol", C.c_double),
+                ("diagonal", C.c_void_p), ("inner", C.c_int32)]
+
+
 class tk_eigen_result(C.Structure):
     _fields_ = [("eigenvalue", C.c_double), ("residual_norm", C.c_double), ("converged", C.c_int32),
                 ("matvec_count", C.c_int32), ("fp64_matvec_count", C.c_int32), ("restarts", C.c_int32)]
@@ -91,6 +96,8 @@ SIGNATURES = [
     ("tk_heff2_flat_to_dense", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("tk_lanczos_lowest", C.c_int32, [C.c_void_p, C.POINTER(tk_lanczos_cfg), C.c_void_p, C.c_void_p,
                                       C.POINTER(tk_eigen_result), C.c_void_p]),
+    ("tk_davidson_lowest", C.c_int32, [C.c_void_p, C.POINTER(tk_davidson_cfg), C.c_void_p, C.c_void_p,
+                                       C.POINTER(tk_eigen_result), C.c_void_p]),
     ("tk_gemm_f64", C.c_int32, [C.c_void_p, C.c_double, C.POINTER(tk_mat), C.POINTER(tk_mat), C.c_double,
                                 C.POINTER(tk_mat_mut), C.c_void_p]),
     ("tk_gemm_f64_noalloc", C.c_int32, [C.c_void_p, C.c_double, C.POINTER(tk_mat), C.POINTER(tk_mat), C.c_double,

@@ -5,6 +5,7 @@ Python mirror of (kyungminlee/tensorkraft-design):
   MPO                      tk-dmrg/src/mpo/mod.rs:36-93             legs (s_in, s_out, w_L, w_R)
   build_heff_two_site      tk-dmrg/src/environments/mod.rs:491-602  -> (matvec closure, dim)
   LanczosSolver            tk-dmrg/src/eigensolver/mod.rs:58-164
+  DavidsonSolver           tk-dmrg/src/eigensolver/mod.rs:299-517
   EigenResult              tk-dmrg/src/eigensolver/mod.rs:22-33
 Every numeric call goes through libtk_heff.so (CUDA); nothing here computes.
 """
@@ -224,6 +225,21 @@ class Heff2Plan:
         return EigenResult(res.eigenvalue, evec, bool(res.converged), res.matvec_count, res.residual_norm,
                            res.fp64_matvec_count, res.restarts)
 
+    def davidson(self, max_subspace=60, max_iter=1000, tol=1e-10, diagonal=None, inner=0, x0=None,
+                 stream=None) -> EigenResult:
+        """tk_davidson_lowest; `diagonal` is a device tensor of H_ii in the block layout or None."""
+        import torch
+
+        evec = torch.empty(self.block_dim, dtype=torch.float64, device=f"cuda:{self.device}")
+        dp = C.c_void_p(diagonal.data_ptr()) if diagonal is not None else None
+        cfg = _abi.tk_davidson_cfg(max_subspace, max_iter, tol, dp, inner)
+        res = _abi.tk_eigen_result()
+        x0p = C.c_void_p(x0.data_ptr()) if x0 is not None else None
+        s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
+        check(self._lib.tk_davidson_lowest(self._h, C.byref(cfg), x0p, C.c_void_p(evec.data_ptr()), C.byref(res), s))
+        return EigenResult(res.eigenvalue, evec, bool(res.converged), res.matvec_count, res.residual_norm,
+                           res.fp64_matvec_count, res.restarts)
+
 
 def build_heff_two_site(env_l: Environment, env_r: Environment, mpo: MPO, sites: tuple, psi_flux=None,
                         precision: int = PREC_FP64, device: int = 0):
@@ -256,3 +272,21 @@ class LanczosSolver:
     def lowest_eigenpair(self, plan: Heff2Plan, initial=None) -> EigenResult:
         return plan.lanczos(krylov_dim=self.max_krylov_dim, max_restarts=self.max_iter, tol=self.tol,
                             refine=self.refine, x0=initial)
+
+
+@dataclass
+class DavidsonSolver:
+    """DavidsonSolver (eigensolver/mod.rs:299-323, defaults 60 / 5 / 1000 / 1e-10 / None) on
+    the device operator of a plan.  `inner` > 0 switches split-precision plans to
+    Jacobi-Davidson corrections; `restart_vectors` is unused, as in the reference."""
+
+    max_subspace: int = 60
+    restart_vectors: int = 5
+    max_iter: int = 1000
+    tol: float = 1e-10
+    diagonal: object = None
+    inner: int = 0
+
+    def lowest_eigenpair(self, plan: Heff2Plan, initial=None) -> EigenResult:
+        return plan.davidson(max_subspace=self.max_subspace, max_iter=self.max_iter, tol=self.tol,
+                             diagonal=self.diagonal, inner=self.inner, x0=initial)

@@ -109,6 +109,16 @@ def main():
              "dense": [[2, -1, 0], [-1, 2, -1], [0, -1, 2]], "krylov": 10, "eigenvalue": 2 - 2 ** 0.5,
              "tol": 1e-10},
         ],
+        "davidson": [
+            {"source": "tk-dmrg/src/eigensolver/mod.rs:702-707 (defaults)", "defaults": True,
+             "max_subspace": 60, "tol": 1e-10},
+            {"source": "tk-dmrg/src/eigensolver/mod.rs:709-732", "matrix": "diag", "diag": [3, 1, 4, 1, 5],
+             "diagonal": [3, 1, 4, 1, 5], "tol": 1e-10, "eigenvalue": 1.0, "atol": 1e-6, "converged": True},
+            {"source": "tk-dmrg/src/eigensolver/mod.rs:734-755", "matrix": "dense", "dense": [[2, -1], [-1, 2]],
+             "diagonal": [2, 2], "tol": 1e-8, "eigenvalue": 1.0, "atol": 1e-6, "converged": True},
+            {"source": "tk-dmrg/src/eigensolver/mod.rs:757-778", "matrix": "diag", "diag": [5, 2, 8, 1, 3],
+             "diagonal": None, "tol": 1e-8, "eigenvalue": 1.0, "atol": 1e-6, "converged": None},
+        ],
         "lanczos_random_diagonal": {
             "source": "tk-dmrg/tests/proptest_dmrg.rs:18-49 (+ regression seed dim=4, seed=0)",
             "cases": [{"dim": d, "seed": s, "diag": lcg_values(s + 42, d), "eigenvalue": min(lcg_values(s + 42, d))}

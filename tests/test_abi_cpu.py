@@ -39,6 +39,9 @@ def test_null_arguments_rejected(lib_built):
     cfg = _abi.tk_lanczos_cfg(20, 0, 1e-10, 0)
     assert lib.tk_lanczos_lowest(None, C.byref(cfg), None, None, None, None) == 1
     assert b"null" in lib.tk_last_error()
+    dcfg = _abi.tk_davidson_cfg(60, 1000, 1e-10, None, 0)
+    assert lib.tk_davidson_lowest(None, C.byref(dcfg), None, None, None, None) == 1
+    assert b"tk_davidson_lowest" in lib.tk_last_error()
 
 
 def test_gemm_shape_mismatch_rejected(lib_built):

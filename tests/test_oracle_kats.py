@@ -84,6 +84,37 @@ def test_lanczos_restatement_kats():
         assert abs(lam - case["eigenvalue"]) < rd["tol"]
 
 
+def test_davidson_restatement_kats():
+    """The numpy Davidson against the reference's Davidson tests (eigensolver/mod.rs:702-801)."""
+    from oracle import davidson
+
+    for case in KATS["davidson"]:
+        if case.get("defaults"):
+            continue
+        M = np.diag(case["diag"]) if case["matrix"] == "diag" else np.array(case["dense"], float)
+        lam, x, conv, count, rn = davidson.lowest_eigenpair(lambda v: M @ v, M.shape[0], tol=case["tol"],
+                                                            diagonal=case["diagonal"])
+        assert abs(lam - case["eigenvalue"]) < case["atol"]
+        if case["converged"]:
+            assert conv and rn < case["tol"]
+    ev, _ = davidson.symmetric_eigen_small(np.array([[2, -1, 0], [-1, 2, -1], [0, -1, 2]], float), 3)
+    assert abs(min(ev) - (2 - 2 ** 0.5)) < 1e-10  # symmetric_eigen_small_test (mod.rs:780-801)
+
+
+def test_davidson_restatement_restarts():
+    """Restarts (max_subspace < iterations needed) still converge."""
+    from oracle import davidson
+
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((30, 30))
+    M = A + A.T
+    lam0 = np.linalg.eigvalsh(M)[0]
+    lam, x, conv, count, rn = davidson.lowest_eigenpair(lambda v: M @ v, 30, max_subspace=5, tol=1e-9)
+    assert conv and abs(lam - lam0) < 1e-8
+    assert np.linalg.norm(M @ x - lam * x) < 1e-8
+    assert count == 93  # 5-vector spaces: 18 restarts, each one matvec
+
+
 def test_block_gemm_golden_is_consistent():
     """The regenerated LCG inputs reproduce the fixture's dense product."""
     g = KATS["block_gemm"]
