@@ -277,6 +277,48 @@ void tk_bst_free(tk_bst_out* t);
  * a rank-2 host tensor and host vectors (y fully overwritten). */
 tk_status tk_spmv_f64(tk_ctx* ctx, const tk_bst* a, const double* x, double* y);
 
+/*
+ * Device-resident environments for two-site sweeps.  The reference's
+ * Environment (tk-dmrg/src/environments/mod.rs:24-103) is a dense
+ * (bra, w, ket) array; a symmetric environment is non-zero only on sector
+ * triples with q(bra) = q(ket) + q(w), and these calls keep exactly those
+ * blocks: the canonical block layout lists every such triple, ascending by
+ * packed rank-3 key (bra leg in the low bits), blocks back to back, each
+ * row-major (a', w, a).  In the calls below a tk_env's `data` is a device
+ * pointer to that layout.
+ */
+/* Block count, keys, offsets (nullable: counts only; otherwise *n_blocks is
+ * the capacity on entry) and total length of the canonical layout. */
+tk_status tk_env_layout(int32_t qn_kind, const tk_qindex* bra, const tk_qindex* mpo, const tk_qindex* ket,
+                        int64_t* n_blocks, uint64_t* keys, int64_t* block_offsets, int64_t* total);
+/* build_heff_two_site (environments/mod.rs:491-602) over device environments
+ * in the canonical layout; otherwise as tk_heff2_plan_create.  The
+ * environments are read once during the call. */
+tk_status tk_heff2_plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                                   const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
+                                   tk_heff2_plan** out);
+/* contract_left_environment (environments/mod.rs:221-355):
+ *   L'[b', v, b] = sum conj(A[s', a', b']) L[a', w, a] W[s, s', w, v] A[s, a, b]
+ * A: rank-3 MPS site tensor (s, a_L, a_R), blocks with q(s) + q(a_L) = q(a_R),
+ * host keys/offsets and DEVICE data; W: rank-4 MPO site tensor, host data.
+ * L lies on (A's left bond, W's left bond); out_dev receives the canonical
+ * layout of (A's right bond, W's right bond, A's right bond), fully written.
+ * Stream-ordered; no host synchronisation. */
+tk_status tk_env_grow_left(tk_ctx* ctx, const tk_env* env_l, const tk_bst* a, const tk_bst* w, double* out_dev,
+                           void* stream);
+/* contract_right_environment (environments/mod.rs:357-483):
+ *   R'[a', w, a] = sum conj(A[s', a', b']) R[b', v, b] W[s, s', w, v] A[s, a, b]
+ * R lies on (A's right bond, W's right bond); out_dev receives the canonical
+ * layout of (A's left bond, W's left bond, A's left bond). */
+tk_status tk_env_grow_right(tk_ctx* ctx, const tk_env* env_r, const tk_bst* a, const tk_bst* w, double* out_dev,
+                            void* stream);
+/* Two-site start vector psi(s_i, s_j, a, b) = sum_c A_i(s_i, a, c) A_j(s_j, c, b)
+ * in the plan's block layout (device data in, device vector out).  The
+ * reference's sweep starts its eigensolver from no vector
+ * (sweep/mod.rs:390-396); this is the usual two-site guess instead. */
+tk_status tk_heff2_two_site_product(tk_heff2_plan* plan, const tk_bst* a_i, const tk_bst* a_j, double* psi_dev,
+                                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,23 @@
+"""Environment growth restatement (numpy) -- TEST INFRASTRUCTURE ONLY.
+
+contract_left_environment (tk-dmrg/src/environments/mod.rs:221-355) and
+contract_right_environment (:357-483) sum, over every (ket block, bra block,
+MPO block) triple of the site tensors, the products
+  L'[b', v, b] += conj(A[s', a', b']) L[a', w, a] W[s, s', w, v] A[s, a, b]
+  R'[a', w, a] += conj(A[s', a', b']) R[b', v, b] W[s, s', w, v] A[s, a, b]
+into a dense (bra, w, ket) array, with W's s_in pairing the ket and s_out the
+bra (:285-289).  On dense (zero-padded) site tensors that is one einsum each.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def grow_left(L, A, W):
+    """L: (Da, w, Da); A: (d, Da, Db); W: (d, d, w, v) -> (Db, v, Db)."""
+    return np.einsum("tpx,pwa,stwv,sab->xvb", A.conj(), L, W, A, optimize=True)
+
+
+def grow_right(R, A, W):
+    """R: (Db, v, Db); A: (d, Da, Db); W: (d, d, w, v) -> (Da, w, Da)."""
+    return np.einsum("txp,pvb,stwv,sab->xwa", A.conj(), R, W, A, optimize=True)

@@ -95,6 +95,16 @@ tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
         set_error("tk_heff2_plan_create: null argument");
         return TK_ERR_INVALID_ARG;
     }
+    return plan_create_impl(ctx, env_l, env_r, w_i, w_j, psi_flux, precision, nullptr, nullptr, out);
+}
+
+}  // extern "C"
+
+// Shared by tk_heff2_plan_create (dense host environments) and
+// tk_heff2_plan_create_dev (host copies of canonical block-layout ones).
+tk_status tk::plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                               const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, const double* l_blocks,
+                               const double* r_blocks, tk_heff2_plan** out) {
     *out = nullptr;
     if (precision != TK_PREC_FP64 && precision != TK_PREC_BF16X3) {
         set_error("tk_heff2_plan_create: unknown precision");
@@ -106,7 +116,8 @@ tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
         return TK_ERR_OOM;
     }
     std::string err;
-    tk_status st = build_heff2_tables(*env_l, *env_r, *w_i, *w_j, psi_flux, kF64TileM, kF64TileN, p->host, err);
+    tk_status st = build_heff2_tables(*env_l, *env_r, *w_i, *w_j, psi_flux, kF64TileM, kF64TileN, p->host, err,
+                                      l_blocks, r_blocks);
     if (st != TK_OK) {
         set_error("tk_heff2_plan_create: " + err);
         return st;
@@ -136,6 +147,8 @@ tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
     *out = p.release();
     return TK_OK;
 }
+
+extern "C" {
 
 void tk_heff2_plan_destroy(tk_heff2_plan* plan) {
     if (!plan) return;

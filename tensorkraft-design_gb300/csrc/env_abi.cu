@@ -1,0 +1,251 @@
+// env_abi.cu -- C ABI of the block-sparse environment operations: canonical
+// layout, H_eff plans over device environments, environment growth by one
+// site and the two-site start vector (tables in env.cpp).
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "tk_env.hpp"
+#include "tk_plan.cuh"
+
+static_assert(tk::kEnvTileM == tk::kF64TileM && tk::kEnvTileN == tk::kF64TileN,
+              "environment tables are cut for the grouped FP64 GEMM tile");
+
+using namespace tk;
+
+namespace {
+
+struct Guard {
+    int prev = -1;
+    bool ok = false;
+    explicit Guard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = (cudaSetDevice(dev) == cudaSuccess);
+    }
+    ~Guard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+// Stream-ordered scratch: allocated from the device's memory pool on the
+// call's stream and released on it, so nothing waits on the host.
+struct Scratch {
+    cudaStream_t s;
+    std::vector<void*> ptrs;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    ~Scratch() {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+    }
+    template <class T>
+    cudaError_t upload(const std::vector<T>& v, T** out) {
+        *out = nullptr;
+        if (v.empty()) return cudaSuccess;
+        cudaError_t e = alloc(v.size() * sizeof(T), (void**)out);
+        if (e != cudaSuccess) return e;
+        // pageable source: staged before the call returns
+        return cudaMemcpyAsync(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+    cudaError_t alloc(size_t bytes, void** out) {
+        cudaError_t e = cudaMallocAsync(out, std::max<size_t>(bytes, 16), s);
+        if (e == cudaSuccess) ptrs.push_back(*out);
+        return e;
+    }
+};
+
+tk_status launch_table(Scratch& sc, const GemmTable& g, const double* A, const double* B, double* C) {
+    GemmTask* t = nullptr;
+    GemmSeg* sg = nullptr;
+    GemmTile* tl = nullptr;
+    cudaError_t e;
+    if ((e = sc.upload(g.tasks, &t)) != cudaSuccess) return cuda_fail("upload tables", e);
+    if ((e = sc.upload(g.segs, &sg)) != cudaSuccess) return cuda_fail("upload tables", e);
+    if ((e = sc.upload(g.tiles, &tl)) != cudaSuccess) return cuda_fail("upload tables", e);
+    if ((e = launch_gemm_f64(tl, (int)g.tiles.size(), t, sg, A, B, C, sc.s)) != cudaSuccess)
+        return cuda_fail("grouped gemm", e);
+    return TK_OK;
+}
+
+bool env_legs(int kind, const tk_env& e, QIndex& bra, QIndex& mpo, QIndex& ket, std::string& err) {
+    return qindex_from_abi(kind, e.bra, bra, err) && qindex_from_abi(kind, e.mpo, mpo, err) &&
+           qindex_from_abi(kind, e.ket, ket, err);
+}
+
+tk_status grow(const char* name, bool left, tk_ctx* ctx, const tk_env* env, const tk_bst* a, const tk_bst* w,
+               double* out, void* stream) {
+    if (!ctx || !env || !a || !w || !out) {
+        set_error(std::string(name) + ": null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::string err;
+    Bst3 A;
+    Bst4 W;
+    QIndex eb, em, ek;
+    if (!bst3_from_abi(*a, A, "MPS site", err) || !bst4_from_abi(*w, W, "MPO site", err) ||
+        !env_legs(A.kind, *env, eb, em, ek, err)) {
+        set_error(std::string(name) + ": " + err);
+        return TK_ERR_INVALID_ARG;
+    }
+    if (W.kind != A.kind) {
+        set_error(std::string(name) + ": MPS and MPO quantum-number kinds differ");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (!env->data) {
+        set_error(std::string(name) + ": null environment data");
+        return TK_ERR_INVALID_ARG;
+    }
+    GrowTables G;
+    tk_status st = build_grow_tables(left, eb, em, ek, A, W, G, err);
+    if (st != TK_OK) {
+        set_error(std::string(name) + ": " + err);
+        return st;
+    }
+    Guard g(ctx->device);
+    if (!g.ok) {
+        set_error(std::string(name) + ": cudaSetDevice failed");
+        return TK_ERR_CUDA;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch sc(s);
+    cudaError_t e;
+    double *t1 = nullptr, *t2 = nullptr;
+    if ((e = sc.alloc(sizeof(double) * (size_t)G.t1_total, (void**)&t1)) != cudaSuccess) return cuda_fail("scratch", e);
+    if ((e = sc.alloc(sizeof(double) * (size_t)G.t2_total, (void**)&t2)) != cudaSuccess) return cuda_fail("scratch", e);
+    if ((e = cudaMemsetAsync(out, 0, sizeof(double) * (size_t)G.out_total, s)) != cudaSuccess)
+        return cuda_fail("cudaMemsetAsync", e);
+    if (left)
+        st = launch_table(sc, G.g1, env->data, A.data, t1);
+    else
+        st = launch_table(sc, G.g1, A.data, env->data, t1);
+    if (st != TK_OK) return st;
+    CombJob* jobs = nullptr;
+    CombTerm* terms = nullptr;
+    if ((e = sc.upload(G.jobs, &jobs)) != cudaSuccess) return cuda_fail("upload tables", e);
+    if ((e = sc.upload(G.terms, &terms)) != cudaSuccess) return cuda_fail("upload tables", e);
+    if ((e = launch_combine_f64(jobs, (int)G.jobs.size(), terms, t1, t2, s)) != cudaSuccess)
+        return cuda_fail("combine", e);
+    return launch_table(sc, G.g3, A.data, t2, out);
+}
+
+}  // namespace
+
+extern "C" {
+
+tk_status tk_env_layout(int32_t qn_kind, const tk_qindex* bra, const tk_qindex* mpo, const tk_qindex* ket,
+                        int64_t* n_blocks, uint64_t* keys, int64_t* block_offsets, int64_t* total) {
+    if (!bra || !mpo || !ket || !n_blocks) {
+        set_error("tk_env_layout: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (!qn_kind_valid(qn_kind)) {
+        set_error("tk_env_layout: unknown quantum-number kind");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::string err;
+    QIndex b, m, k;
+    if (!qindex_from_abi(qn_kind, *bra, b, err) || !qindex_from_abi(qn_kind, *mpo, m, err) ||
+        !qindex_from_abi(qn_kind, *ket, k, err)) {
+        set_error("tk_env_layout: " + err);
+        return TK_ERR_INVALID_ARG;
+    }
+    if (3 * qn_bits(qn_kind) > 64) {
+        set_error("tk_env_layout: rank-3 sector key exceeds 64 bits");
+        return TK_ERR_UNSUPPORTED;
+    }
+    EnvLayout lay;
+    env_layout(qn_kind, b, m, k, lay);
+    const int64_t n = (int64_t)lay.keys.size();
+    if (keys || block_offsets) {
+        if (*n_blocks < n) {
+            set_error("tk_env_layout: output arrays shorter than the block count");
+            *n_blocks = n;
+            return TK_ERR_INVALID_ARG;
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            if (keys) keys[i] = lay.keys[i];
+            if (block_offsets) block_offsets[i] = lay.off[i];
+        }
+    }
+    *n_blocks = n;
+    if (total) *total = lay.total;
+    return TK_OK;
+}
+
+tk_status tk_heff2_plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                                   const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
+                                   tk_heff2_plan** out) {
+    if (!ctx || !env_l || !env_r || !w_i || !w_j || !out || !env_l->data || !env_r->data) {
+        set_error("tk_heff2_plan_create_dev: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    std::string err;
+    QIndex lb, lm, lk, rb, rm, rk;
+    if (!env_legs(w_i->qn_kind, *env_l, lb, lm, lk, err) || !env_legs(w_i->qn_kind, *env_r, rb, rm, rk, err)) {
+        set_error("tk_heff2_plan_create_dev: environment: " + err);
+        return TK_ERR_INVALID_ARG;
+    }
+    EnvLayout ll, rl;
+    env_layout(w_i->qn_kind, lb, lm, lk, ll);
+    env_layout(w_i->qn_kind, rb, rm, rk, rl);
+    // the environments are small next to psi: read them once to the host to
+    // build the tables and the split-precision operand stacks
+    std::vector<double> lh((size_t)ll.total), rh((size_t)rl.total);
+    {
+        Guard g(ctx->device);
+        if (!g.ok) {
+            set_error("tk_heff2_plan_create_dev: cudaSetDevice failed");
+            return TK_ERR_CUDA;
+        }
+        cudaError_t e;
+        if (!lh.empty() && (e = cudaMemcpy(lh.data(), env_l->data, sizeof(double) * lh.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_fail("tk_heff2_plan_create_dev: read left environment", e);
+        if (!rh.empty() && (e = cudaMemcpy(rh.data(), env_r->data, sizeof(double) * rh.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_fail("tk_heff2_plan_create_dev: read right environment", e);
+    }
+    return plan_create_impl(ctx, env_l, env_r, w_i, w_j, psi_flux, precision, lh.data(), rh.data(), out);
+}
+
+tk_status tk_env_grow_left(tk_ctx* ctx, const tk_env* env_l, const tk_bst* a, const tk_bst* w, double* out_dev,
+                           void* stream) {
+    return grow("tk_env_grow_left", true, ctx, env_l, a, w, out_dev, stream);
+}
+
+tk_status tk_env_grow_right(tk_ctx* ctx, const tk_env* env_r, const tk_bst* a, const tk_bst* w, double* out_dev,
+                            void* stream) {
+    return grow("tk_env_grow_right", false, ctx, env_r, a, w, out_dev, stream);
+}
+
+tk_status tk_heff2_two_site_product(tk_heff2_plan* plan, const tk_bst* a_i, const tk_bst* a_j, double* psi_dev,
+                                    void* stream) {
+    if (!plan || !a_i || !a_j || !psi_dev) {
+        set_error("tk_heff2_two_site_product: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::string err;
+    Bst3 Ai, Aj;
+    if (!bst3_from_abi(*a_i, Ai, "A_i", err) || !bst3_from_abi(*a_j, Aj, "A_j", err)) {
+        set_error("tk_heff2_two_site_product: " + err);
+        return TK_ERR_INVALID_ARG;
+    }
+    GemmTable g;
+    tk_status st = build_product_tables(plan->host, Ai, Aj, g, err);
+    if (st != TK_OK) {
+        set_error("tk_heff2_two_site_product: " + err);
+        return st;
+    }
+    Guard gd(plan->device);
+    if (!gd.ok) {
+        set_error("tk_heff2_two_site_product: cudaSetDevice failed");
+        return TK_ERR_CUDA;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(psi_dev, 0, sizeof(double) * (size_t)plan->host.total, s)) != cudaSuccess)
+        return cuda_fail("cudaMemsetAsync", e);
+    Scratch sc(s);
+    return launch_table(sc, g, Ai.data, Aj.data, psi_dev);
+}
+
+}  // extern "C"

@@ -170,16 +170,6 @@ bool qindex_from_abi(int kind, const tk_qindex& in, QIndex& out, std::string& er
     return true;
 }
 
-namespace {
-
-struct Bst4 {
-    int kind = 0;
-    QIndex legs[4];
-    std::vector<uint64_t> keys;
-    std::vector<int64_t> offs;
-    const double* data = nullptr;
-};
-
 bool bst4_from_abi(const tk_bst& t, Bst4& o, const char* name, std::string& err) {
     if (t.rank != 4 || !t.legs) {
         err = std::string(name) + ": MPO site tensor must have rank 4 (s_in, s_out, w_L, w_R)";
@@ -241,6 +231,8 @@ bool mpo_dense(const Bst4& w, std::vector<double>& out, std::string& err) {
     return true;
 }
 
+namespace {
+
 // enumerate_valid_sectors (flux.rs:43-234) for the two-site tensor, directions
 // (In, In, In, Out): q(s_i) + q(s_j) + q(a_L) - q(a_R) == flux.
 void enumerate4(int kind, const QIndex* legs, const Qn& flux, std::vector<std::array<int, 4>>& out) {
@@ -257,16 +249,19 @@ void enumerate4(int kind, const QIndex* legs, const Qn& flux, std::vector<std::a
 
 }  // namespace
 
-static void add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n, const std::vector<int64_t>& kseg) {
-    const GemmTask& t = g.tasks[task_id];
-    int64_t ktot = 0;
-    for (int64_t k : kseg) ktot += k;
-    for (int m0 = 0; m0 < t.M; m0 += tile_m)
-        for (int n0 = 0; n0 < t.N; n0 += tile_n) g.tiles.push_back({task_id, m0, n0, 0});
-    (void)ktot;
+static void add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n, const std::vector<int64_t>&) {
+    gemm_add_tiles(g, task_id, tile_m, tile_n);
 }
 
-static void lpt_order(GemmTable& g, int tile_m, int tile_n) {
+void gemm_add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n) {
+    const GemmTask& t = g.tasks[task_id];
+    for (int m0 = 0; m0 < t.M; m0 += tile_m)
+        for (int n0 = 0; n0 < t.N; n0 += tile_n) g.tiles.push_back({task_id, m0, n0, 0});
+}
+
+static void lpt_order(GemmTable& g, int tile_m, int tile_n) { gemm_lpt_order(g, tile_m, tile_n); }
+
+void gemm_lpt_order(GemmTable& g, int tile_m, int tile_n) {
     // Cost of a tile = (rows) x (cols) x (total K); heaviest first.
     std::vector<double> ktot(g.tasks.size(), 0.0);
     for (size_t t = 0; t < g.tasks.size(); ++t)
@@ -282,8 +277,7 @@ static void lpt_order(GemmTable& g, int tile_m, int tile_n) {
 
 // Every device access the tables can produce, checked against its buffer on
 // the host: a table fault becomes an error code instead of a device fault.
-static bool validate_tables(const Heff2Tables& T, std::string& err) {
-    auto gemm_ok = [&](const GemmTable& g, int64_t na, int64_t nb, int64_t nc, const char* name) {
+bool gemm_table_ok(const GemmTable& g, int64_t na, int64_t nb, int64_t nc, const char* name, std::string& err) {
         for (const GemmTile& tl : g.tiles) {
             if (tl.task < 0 || (size_t)tl.task >= g.tasks.size()) { err = std::string(name) + ": tile task"; return false; }
             const GemmTask& t = g.tasks[tl.task];
@@ -302,17 +296,25 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
             }
         }
         return true;
-    };
-    if (!gemm_ok(T.g1, (int64_t)T.lbuf.size(), T.total, T.t1_total, "stage 1")) return false;
-    if (!gemm_ok(T.g3, T.t2_total, (int64_t)T.rbuf.size(), T.total, "stage 3")) return false;
-    for (const CombJob& j : T.jobs) {
-        if (j.rows <= 0 || j.cols <= 0 || j.out_off < 0 || j.out_off + (int64_t)(j.rows - 1) * j.out_rs + j.cols - 1 >= T.t2_total ||
-            j.term_begin < 0 || j.term_end < j.term_begin || (size_t)j.term_end > T.terms.size()) { err = "combine job range"; return false; }
+}
+
+bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>& terms, int64_t n_in, int64_t n_out,
+                   std::string& err) {
+    for (const CombJob& j : jobs) {
+        if (j.rows <= 0 || j.cols <= 0 || j.out_off < 0 || j.out_off + (int64_t)(j.rows - 1) * j.out_rs + j.cols - 1 >= n_out ||
+            j.term_begin < 0 || j.term_end < j.term_begin || (size_t)j.term_end > terms.size()) { err = "combine job range"; return false; }
         for (int t = j.term_begin; t < j.term_end; ++t) {
-            const CombTerm& c = T.terms[t];
-            if (c.in_off < 0 || c.in_off + (int64_t)(j.rows - 1) * c.in_rs + j.cols - 1 >= T.t1_total) { err = "combine term range"; return false; }
+            const CombTerm& c = terms[t];
+            if (c.in_off < 0 || c.in_off + (int64_t)(j.rows - 1) * c.in_rs + j.cols - 1 >= n_in) { err = "combine term range"; return false; }
         }
     }
+    return true;
+}
+
+static bool validate_tables(const Heff2Tables& T, std::string& err) {
+    if (!gemm_table_ok(T.g1, (int64_t)T.lbuf.size(), T.total, T.t1_total, "stage 1", err)) return false;
+    if (!gemm_table_ok(T.g3, T.t2_total, (int64_t)T.rbuf.size(), T.total, "stage 3", err)) return false;
+    if (!comb_table_ok(T.jobs, T.terms, T.t1_total, T.t2_total, err)) return false;
     const TcTables& C = T.tc;
     if (C.t1col_base.size() != C.t1col_stride.size()) { err = "T1 column tables"; return false; }
     for (const TcTile& t : C.tiles1) {
@@ -369,7 +371,7 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
 
 tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi,
                              const tk_bst& wj_abi, const int32_t* psi_flux, int tile_m, int tile_n,
-                             Heff2Tables& T, std::string& err) {
+                             Heff2Tables& T, std::string& err, const double* l_blocks, const double* r_blocks) {
     Bst4 wi, wj;
     if (!bst4_from_abi(wi_abi, wi, "W_i", err)) return TK_ERR_INVALID_ARG;
     if (!bst4_from_abi(wj_abi, wj, "W_j", err)) return TK_ERR_INVALID_ARG;
@@ -500,7 +502,22 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
     std::vector<int64_t> lblk((size_t)nA * nWL * nA, -1), rblk((size_t)nB * nWR * nB, -1);
     T.lbuf.clear();
     T.rbuf.clear();
-    for (int ap = 0; ap < nA; ++ap)
+    if (l_blocks) {
+        // canonical block layout: every charge-allowed block is a slab, in place
+        EnvLayout lay;
+        env_layout(kind, QA, WL, QA, lay);
+        for (size_t k = 0; k < lay.tri.size(); ++k)
+            lblk[((size_t)lay.tri[k][0] * nWL + lay.tri[k][1]) * nA + lay.tri[k][2]] = lay.off[k];
+        T.lbuf.assign(l_blocks, l_blocks + lay.total);
+    }
+    if (r_blocks) {
+        EnvLayout lay;
+        env_layout(kind, QB, WR, QB, lay);
+        for (size_t k = 0; k < lay.tri.size(); ++k)
+            rblk[((size_t)lay.tri[k][0] * nWR + lay.tri[k][1]) * nB + lay.tri[k][2]] = lay.off[k];
+        T.rbuf.assign(r_blocks, r_blocks + lay.total);
+    }
+    for (int ap = 0; ap < nA && !l_blocks; ++ap)
         for (int ws = 0; ws < nWL; ++ws)
             for (int a = 0; a < nA; ++a) {
                 bool nz = false;
@@ -518,7 +535,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                         T.lbuf.insert(T.lbuf.end(), row, row + QA.dim[a]);
                     }
             }
-    for (int bp = 0; bp < nB; ++bp)
+    for (int bp = 0; bp < nB && !r_blocks; ++bp)
         for (int ws = 0; ws < nWR; ++ws)
             for (int b = 0; b < nB; ++b) {
                 bool nz = false;
@@ -542,6 +559,13 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
     auto T1I = [&](int64_t p, int ap, int ws, int b) -> int64_t& {
         return t1[(((size_t)p * nA + ap) * nWL + ws) * nB + b];
     };
+    // ket sectors A of the L slabs (A', ws, A), ascending; charge conservation
+    // leaves at most a few per (A', ws), so the task scan below stays linear
+    std::vector<std::vector<int>> lslab_ket((size_t)nA * nWL);
+    for (int ap = 0; ap < nA; ++ap)
+        for (int ws = 0; ws < nWL; ++ws)
+            for (int a = 0; a < nA; ++a)
+                if (lblk[((size_t)ap * nWL + ws) * nA + a] >= 0) lslab_ket[(size_t)ap * nWL + ws].push_back(a);
     T.g1 = GemmTable();
     off = 0;
     for (int64_t p = 0; p < P; ++p)
@@ -550,10 +574,10 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                 for (int b = 0; b < nB; ++b) {
                     int seg0 = (int)T.g1.segs.size();
                     std::vector<int64_t> ks;
-                    for (int a = 0; a < nA; ++a) {
+                    for (int a : lslab_ket[(size_t)ap * nWL + ws]) {
                         int64_t lo = lblk[((size_t)ap * nWL + ws) * nA + a];
                         int64_t so = SUB(p, a, b);
-                        if (lo < 0 || so < 0) continue;
+                        if (so < 0) continue;
                         GemmSeg s{};
                         s.a_off = lo; s.a_rs = (int32_t)QA.dim[a]; s.a_cs = 1;
                         s.b_off = so; s.b_rs = (int32_t)QB.dim[b]; s.b_cs = 1;
@@ -599,6 +623,12 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
     auto T2I = [&](int64_t p, int ap, int ws, int b) -> int64_t& {
         return t2[(((size_t)p * nA + ap) * nWR + ws) * nB + b];
     };
+    // bra sectors B' of the R slabs (B', ws, B), ascending
+    std::vector<std::vector<int>> rslab_bra((size_t)nWR * nB);
+    for (int bp = 0; bp < nB; ++bp)
+        for (int ws = 0; ws < nWR; ++ws)
+            for (int b = 0; b < nB; ++b)
+                if (rblk[((size_t)bp * nWR + ws) * nB + b] >= 0) rslab_bra[(size_t)ws * nB + b].push_back(bp);
     T.jobs.clear();
     T.terms.clear();
     T.comb_flops = 0.0;
@@ -610,8 +640,11 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     // consumed by stage 3 only if some R slab (B', ws, B) exists and
                     // the output sub-block (p', A', B') exists
                     bool used = false;
-                    for (int bp = 0; bp < nB && !used; ++bp)
-                        if (rblk[((size_t)bp * nWR + ws) * nB + b] >= 0 && SUB(po, ap, bp) >= 0) used = true;
+                    for (int bp : rslab_bra[(size_t)ws * nB + b])
+                        if (SUB(po, ap, bp) >= 0) {
+                            used = true;
+                            break;
+                        }
                     if (!used) continue;
                     int64_t dws = WR.dim[ws];
                     size_t job0 = T.jobs.size();

@@ -1,6 +1,7 @@
 // tk_internal.hpp -- shared types of libtk_heff: quantum-number arithmetic,
 // flattened sector-GEMM task tables, and the host-side plan description.
 #pragma once
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -51,6 +52,18 @@ struct QIndex {
 // Copies a tk_qindex; checks sectors are strictly sorted with positive dims.
 bool qindex_from_abi(int kind, const tk_qindex& in, QIndex& out, std::string& err);
 
+// Rank-4 MPO site tensor (s_in, s_out, w_L, w_R) read from the ABI.
+struct Bst4 {
+    int kind = 0;
+    QIndex legs[4];
+    std::vector<uint64_t> keys;
+    std::vector<int64_t> offs;
+    const double* data = nullptr;
+};
+bool bst4_from_abi(const tk_bst& t, Bst4& o, const char* name, std::string& err);
+// Dense (d, d, wl, wr) copy in global indices (host data only).
+bool mpo_dense(const Bst4& w, std::vector<double>& out, std::string& err);
+
 // ---------------------------------------------------------------------------
 // Sector-GEMM tables.  One launch of the grouped GEMM kernel walks a tile
 // list; each tile belongs to a task (one output block) whose K dimension is a
@@ -98,6 +111,14 @@ struct GemmTable {
     std::vector<GemmTile> tiles;
     double flops = 0.0;
 };
+// Appends the (tile_m x tile_n) output tiles of task `task_id`.
+void gemm_add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n);
+// Orders tiles heaviest first (rows x cols x total K), stable.
+void gemm_lpt_order(GemmTable& g, int tile_m, int tile_n);
+// Every operand and output access of a table checked against buffer sizes.
+bool gemm_table_ok(const GemmTable& g, int64_t na, int64_t nb, int64_t nc, const char* name, std::string& err);
+bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>& terms, int64_t n_in, int64_t n_out,
+                   std::string& err);
 
 // ---------------------------------------------------------------------------
 // Split-precision (tensor-core) tables.  Both GEMM stages are regrouped into
@@ -189,10 +210,23 @@ struct Heff2Tables {
 uint16_t f32_to_bf16_bits(float f);
 float bf16_bits_to_f32(uint16_t b);
 
-// Builds the tables; returns TK_OK or an error code with `err` set.
+// Builds the tables; returns TK_OK or an error code with `err` set.  With
+// l_blocks / r_blocks (host copies of environments in the canonical block
+// layout of env_layout) the environments' dense data are not read.
 tk_status build_heff2_tables(const tk_env& L, const tk_env& R, const tk_bst& wi, const tk_bst& wj,
                              const int32_t* psi_flux, int tile_m, int tile_n, Heff2Tables& out,
-                             std::string& err);
+                             std::string& err, const double* l_blocks = nullptr, const double* r_blocks = nullptr);
+
+// Canonical block layout of a block-sparse environment (bra, mpo, ket): every
+// sector triple with q(bra) = q(ket) + q(mpo), ascending packed key (bra in
+// the low bits), blocks back to back, each row-major (a', w, a).
+struct EnvLayout {
+    std::vector<std::array<int, 3>> tri;  // (bra sector, mpo sector, ket sector)
+    std::vector<uint64_t> keys;
+    std::vector<int64_t> off;             // block offsets
+    int64_t total = 0;
+};
+void env_layout(int kind, const QIndex& bra, const QIndex& mpo, const QIndex& ket, EnvLayout& out);
 
 // Thread-local last-error message.
 void set_error(const std::string& msg);

@@ -104,4 +104,10 @@ extern "C" tk_status tk_heff2_apply_prec(tk_heff2_plan* p, const double* x, doub
 
 namespace tk {
 tk_status cuda_fail(const char* op, cudaError_t e);
+// Plan creation behind tk_heff2_plan_create / tk_heff2_plan_create_dev: with
+// l_blocks / r_blocks (host copies of canonical block-layout environments) the
+// environments' `data` pointers are not read.
+tk_status plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                           const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, const double* l_blocks,
+                           const double* r_blocks, tk_heff2_plan** out);
 }

@@ -105,6 +105,18 @@ SIGNATURES = [
     ("tk_block_gemm_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.POINTER(tk_bst_out)]),
     ("tk_bst_free", None, [C.POINTER(tk_bst_out)]),
     ("tk_spmv_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("tk_env_layout", C.c_int32, [C.c_int32, C.POINTER(tk_qindex), C.POINTER(tk_qindex), C.POINTER(tk_qindex),
+                                  C.POINTER(C.c_int64), C.POINTER(C.c_uint64), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int64)]),
+    ("tk_heff2_plan_create_dev", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.POINTER(tk_env), C.POINTER(tk_bst),
+                                             C.POINTER(tk_bst), C.POINTER(C.c_int32), C.c_int32,
+                                             C.POINTER(C.c_void_p)]),
+    ("tk_env_grow_left", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.POINTER(tk_bst), C.POINTER(tk_bst),
+                                     C.c_void_p, C.c_void_p]),
+    ("tk_env_grow_right", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.POINTER(tk_bst), C.POINTER(tk_bst),
+                                      C.c_void_p, C.c_void_p]),
+    ("tk_heff2_two_site_product", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.c_void_p,
+                                              C.c_void_p]),
 ]
 
 _lib = None

@@ -92,6 +92,65 @@ def random_mps_u1(model: ModelMPO, n: int, max_bond: int, total, rng: np.random.
     return mps
 
 
+def _charge_counts(pq, kind, n):
+    """Number of basis states of n sites per total charge (dict), by convolution."""
+    counts = [{identity(kind): 1}]
+    for _ in range(n):
+        nxt = {}
+        for q, c in counts[-1].items():
+            for qs in pq:
+                r = fuse(kind, q, qs)
+                nxt[r] = nxt.get(r, 0) + c
+        counts.append(nxt)
+    return counts
+
+
+def random_mps(model: ModelMPO, n: int, max_bond: int, total, rng: np.random.Generator, width: float = 0.35) -> DenseMPS:
+    """Random MPS for any abelian model: bond i gets every charge q reachable
+    from the left with total - q reachable from the right, weighted by a
+    Gaussian in q around the uniform filling i/n * total (width
+    width*sqrt(i(n-i)/n) per component), max_bond shared out by floor(weight
+    share) capped by the state count (sectors rounding to 0 dropped); blocks
+    N(0,1); then right-canonicalised and normalised."""
+    kind = model.kind
+    total = tuple(total)
+    pq = model.phys.state_charges()
+    cl = _charge_counts(pq, kind, n)
+    bonds = [QIndex(kind, [(identity(kind), 1)])]
+    for i in range(1, n):
+        sec = []
+        for q, c in cl[i].items():
+            rest = fuse(kind, total, dual(kind, q))
+            cr = cl[n - i].get(rest, 0)
+            if cr > 0:
+                sec.append((q, min(c, cr)))
+        sig = max(0.5, width * math.sqrt(i * (n - i) / n))
+        mean = [i / n * t for t in total]
+        w = np.array([math.exp(-sum((qc - m) ** 2 for qc, m in zip(q, mean)) / (2 * sig * sig)) for q, _ in sec])
+        share = np.floor(w / w.sum() * max_bond).astype(int)
+        if share.max() == 0:
+            share[int(np.argmax(w))] = 1
+        secs = sorted((q, int(min(a, cap))) for (q, cap), a in zip(sec, share) if min(a, cap) > 0)
+        bonds.append(QIndex(kind, secs))
+    bonds.append(QIndex(kind, [(total, 1)]))
+    tensors = []
+    for i in range(n):
+        bl, br = bonds[i], bonds[i + 1]
+        A = np.zeros((model.phys.total_dim, bl.total_dim, br.total_dim))
+        for s, qs in enumerate(pq):
+            ol = 0
+            for ql, dl in bl.sectors:
+                qr = fuse(kind, ql, qs)
+                orr = br.offset_of(qr)
+                if orr is not None:
+                    A[s, ol:ol + dl, orr:orr + br.dim_of(qr)] = rng.standard_normal((dl, br.dim_of(qr)))
+                ol += dl
+        tensors.append(A)
+    mps = DenseMPS(kind, model.phys, bonds, tensors)
+    right_canonicalize(mps)
+    return mps
+
+
 def _block_svd(M, row_q, col_q, kind):
     """SVD of M restricted to equal row/column charge; returns per-charge (q, U, S, Vt, rows, cols)."""
     out = []
@@ -209,7 +268,8 @@ def dmrg_two_site(model: ModelMPO, mps: DenseMPS, max_bond: int, sweeps: int, so
         theta = np.einsum("sab,tbc->stac", A, B)  # (s_i, s_j, aL, aR)
         bl, br = mps.bonds[i], mps.bonds[i + 2]
         wi, wj = mpo.tensors[i], mpo.tensors[i + 1]
-        E, vec = solver.solve(env(Ls[i], bl, wi.indices[2]), env(Rs[i + 2], br, wj.indices[3]), wi, wj, total,
+        # bond charges are cumulative from the left, so the two-site flux is zero
+        E, vec = solver.solve(env(Ls[i], bl, wi.indices[2]), env(Rs[i + 2], br, wj.indices[3]), wi, wj, zero,
                               theta)
         theta = vec.reshape(d, d, bl.total_dim, br.total_dim)
         # M[(s_i, aL), (s_j, aR)], row charge q(s_i)+q(aL), column charge q(aR)-q(s_j)

@@ -136,6 +136,25 @@ class Heff2Plan:
         h = C.c_void_p()
         check(self._lib.tk_heff2_plan_create(context(device), C.byref(el), C.byref(er), C.byref(bi), C.byref(bj),
                                              fl, precision, C.byref(h)))
+        self._finish(h, device, precision)
+
+    @classmethod
+    def from_device_envs(cls, env_l, env_r, w_i: BlockSparseTensor, w_j: BlockSparseTensor, psi_flux,
+                         precision: int = PREC_FP64, device: int = 0) -> "Heff2Plan":
+        """tk_heff2_plan_create_dev: environments are sweep.DeviceEnv (canonical block layout on the device)."""
+        self = cls.__new__(cls)
+        self._lib = _abi.load()
+        m = _Marshal()
+        el, er = env_l.marshal(m), env_r.marshal(m)
+        bi, bj = m.bst(w_i), m.bst(w_j)
+        farr = np.array(list(psi_flux) + [0], dtype=np.int32)
+        h = C.c_void_p()
+        check(self._lib.tk_heff2_plan_create_dev(context(device), C.byref(el), C.byref(er), C.byref(bi), C.byref(bj),
+                                                 _abi.i32ptr(farr), precision, C.byref(h)))
+        self._finish(h, device, precision)
+        return self
+
+    def _finish(self, h, device, precision):
         self._h = h
         self.device = device
         dd, bd, nb = C.c_int64(), C.c_int64(), C.c_int64()

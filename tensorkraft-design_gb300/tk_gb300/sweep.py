@@ -1,0 +1,444 @@
+"""Device-resident two-site DMRG sweeps.
+
+The reference's caller of the H_eff path is DMRGEngine::dmrg_step_two_site
+(tk-dmrg/src/sweep/mod.rs:348-448): build H_eff from the environments, solve
+for the lowest eigenpair (DavidsonSolver by default, :174-179), truncate the
+two-site vector by SVD, grow the environment.  Here every tensor of that loop
+stays on the GPU between steps:
+
+* MPS site tensors are block-sparse (s, a_L, a_R) with q(s) + q(a_L) = q(a_R)
+  (`SiteTensor`, FlatBlockStorage order, device data);
+* environments are block-sparse in the canonical layout of tk_env_layout
+  (`DeviceEnv`), grown by tk_env_grow_left / tk_env_grow_right
+  (contract_left/right_environment, environments/mod.rs:221-483);
+* each step builds its plan over the device environments
+  (tk_heff2_plan_create_dev), starts the eigensolver from the two-site
+  product A_i A_j (tk_heff2_two_site_product) and runs Davidson or Lanczos on
+  the device.
+
+Only the two-site vector goes to the host, for the block SVD: per bond charge
+q the matrix M_q[(s_i, a_L), (s_j, a_R)] is decomposed, the largest
+`max_bond` singular values over all charges are kept (ties broken by charge
+order, then position), and the new site tensors are written back
+(the reference reads only the truncation error, sweep/mod.rs:420-437).  The
+right environment of bond (i, i+1) covers sites i+2.. (the reference passes
+right(site+1), :374-375).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from ._abi import PREC_FP64, check
+from .heff import Heff2Plan, _Marshal, context
+from .symmetry import QIndex, dual, fuse, identity, key_pack, key_unpack
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _dptr(t):
+    return C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+
+
+def env_layout(kind: int, bra: QIndex, mpo: QIndex, ket: QIndex):
+    """Canonical block layout (keys, offsets, total) of tk_env_layout."""
+    lib = _abi.load()
+    m = _Marshal()
+    b, w, k = m.qindex(bra), m.qindex(mpo), m.qindex(ket)
+    n, tot = C.c_int64(0), C.c_int64(0)
+    check(lib.tk_env_layout(kind, C.byref(b), C.byref(w), C.byref(k), C.byref(n), None, None, C.byref(tot)))
+    keys = np.zeros(n.value, dtype=np.uint64)
+    offs = np.zeros(n.value, dtype=np.int64)
+    check(lib.tk_env_layout(kind, C.byref(b), C.byref(w), C.byref(k), C.byref(n), _abi.u64ptr(keys),
+                            _abi.i64ptr(offs), C.byref(tot)))
+    return keys, offs, tot.value
+
+
+class DeviceEnv:
+    """Block-sparse environment (bra, mpo, ket) in the canonical layout, device data."""
+
+    def __init__(self, kind: int, bra: QIndex, mpo: QIndex, ket: QIndex, data):
+        self.kind, self.bra, self.mpo, self.ket, self.data = kind, bra, mpo, ket, data
+
+    @classmethod
+    def from_dense(cls, kind, dense: np.ndarray, bra: QIndex, mpo: QIndex, ket: QIndex, device: int = 0):
+        keys, offs, total = env_layout(kind, bra, mpo, ket)
+        host = np.zeros(total)
+        for key, off in zip(keys, offs):
+            qb, qw, qk = key_unpack(kind, int(key), 3)
+            ob, ow, ok = bra.offset_of(qb), mpo.offset_of(qw), ket.offset_of(qk)
+            db, dw, dk = bra.dim_of(qb), mpo.dim_of(qw), ket.dim_of(qk)
+            host[off:off + db * dw * dk] = dense[ob:ob + db, ow:ow + dw, ok:ok + dk].reshape(-1)
+        return cls(kind, bra, mpo, ket, _torch().from_numpy(host).to(f"cuda:{device}"))
+
+    @classmethod
+    def boundary(cls, kind, bond: QIndex, mpo: QIndex, device: int = 0):
+        """left_boundary / right_boundary (environments/mod.rs:41-64): the 1x1x1 array [1]."""
+        if bond.total_dim != 1 or mpo.total_dim != 1:
+            raise ValueError("boundary environment needs one-dimensional bond and MPO legs")
+        return cls.from_dense(kind, np.ones((1, 1, 1)), bond, mpo, bond, device)
+
+    def to_dense(self) -> np.ndarray:
+        keys, offs, total = env_layout(self.kind, self.bra, self.mpo, self.ket)
+        host = self.data.cpu().numpy()
+        out = np.zeros((self.bra.total_dim, self.mpo.total_dim, self.ket.total_dim))
+        for key, off in zip(keys, offs):
+            qb, qw, qk = key_unpack(self.kind, int(key), 3)
+            ob, ow, ok = self.bra.offset_of(qb), self.mpo.offset_of(qw), self.ket.offset_of(qk)
+            db, dw, dk = self.bra.dim_of(qb), self.mpo.dim_of(qw), self.ket.dim_of(qk)
+            out[ob:ob + db, ow:ow + dw, ok:ok + dk] = host[off:off + db * dw * dk].reshape(db, dw, dk)
+        return out
+
+    def marshal(self, m: _Marshal) -> _abi.tk_env:
+        return _abi.tk_env(m.qindex(self.bra), m.qindex(self.mpo), m.qindex(self.ket), _dptr(self.data))
+
+
+class SiteTensor:
+    """Block-sparse MPS site tensor (s, a_L, a_R), q(s) + q(a_L) = q(a_R); blocks
+    in ascending packed-key order, each row-major (s, a, b); device data."""
+
+    def __init__(self, kind: int, legs: list, keys: np.ndarray, offs: np.ndarray, data):
+        self.kind, self.legs, self.keys, self.offs, self.data = kind, legs, keys, offs, data
+
+    @classmethod
+    def from_blocks(cls, kind, legs, blocks: dict, device: int = 0):
+        """blocks: {(q_s, q_L, q_R): array (d_s, D_L, D_R)}."""
+        items = sorted(((key_pack(kind, list(q)), a) for q, a in blocks.items()), key=lambda t: t[0])
+        keys = np.array([k for k, _ in items], dtype=np.uint64)
+        sizes = [a.size for _, a in items]
+        offs = np.zeros(len(items), dtype=np.int64)
+        if items:
+            offs[1:] = np.cumsum(sizes)[:-1]
+        host = np.concatenate([a.reshape(-1) for _, a in items]) if items else np.zeros(1)
+        return cls(kind, list(legs), keys, offs, _torch().from_numpy(np.ascontiguousarray(host)).to(f"cuda:{device}"))
+
+    @classmethod
+    def from_dense(cls, kind, legs, A: np.ndarray, device: int = 0):
+        P, QL, QR = legs
+        blocks = {}
+        for qs, ds in P.sectors:
+            os_ = P.offset_of(qs)
+            for ql, dl in QL.sectors:
+                qr = fuse(kind, qs, ql)
+                if QR.offset_of(qr) is None:
+                    continue
+                ol, orr, dr = QL.offset_of(ql), QR.offset_of(qr), QR.dim_of(qr)
+                blocks[(qs, ql, qr)] = np.ascontiguousarray(A[os_:os_ + ds, ol:ol + dl, orr:orr + dr])
+        return cls.from_blocks(kind, legs, blocks, device)
+
+    def blocks_host(self) -> dict:
+        host = self.data.cpu().numpy()
+        P, QL, QR = self.legs
+        out = {}
+        for key, off in zip(self.keys, self.offs):
+            qs, ql, qr = (tuple(q) for q in key_unpack(self.kind, int(key), 3))
+            shp = (P.dim_of(qs), QL.dim_of(ql), QR.dim_of(qr))
+            out[(qs, ql, qr)] = host[off:off + shp[0] * shp[1] * shp[2]].reshape(shp)
+        return out
+
+    def to_dense(self) -> np.ndarray:
+        P, QL, QR = self.legs
+        A = np.zeros((P.total_dim, QL.total_dim, QR.total_dim))
+        for (qs, ql, qr), b in self.blocks_host().items():
+            os_, ol, orr = P.offset_of(qs), QL.offset_of(ql), QR.offset_of(qr)
+            A[os_:os_ + b.shape[0], ol:ol + b.shape[1], orr:orr + b.shape[2]] = b
+        return A
+
+    def marshal(self, m: _Marshal) -> _abi.tk_bst:
+        legs = (_abi.tk_qindex * 3)(*[m.qindex(ix) for ix in self.legs])
+        dirs = np.array([0, 0, 1], dtype=np.int8)
+        flux = np.zeros(2, dtype=np.int32)
+        m.keep += [legs, dirs, flux, self.keys, self.offs]
+        return _abi.tk_bst(self.kind, 3, legs, _abi.i8ptr(dirs), _abi.i32ptr(flux), len(self.keys),
+                           _abi.u64ptr(self.keys), _abi.i64ptr(self.offs), _dptr(self.data))
+
+
+def _grow(fn_name: str, env: DeviceEnv, A: SiteTensor, W, left: bool, stream=None, device: int = 0) -> DeviceEnv:
+    lib = _abi.load()
+    m = _Marshal()
+    e, a, w = env.marshal(m), A.marshal(m), m.bst(W)
+    bond = A.legs[2] if left else A.legs[1]
+    wl = W.indices[3] if left else W.indices[2]
+    _, _, total = env_layout(A.kind, bond, wl, bond)
+    out = _torch().empty(max(total, 1), dtype=_torch().float64, device=f"cuda:{device}")
+    s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
+    check(getattr(lib, fn_name)(context(device), C.byref(e), C.byref(a), C.byref(w), C.c_void_p(out.data_ptr()), s))
+    return DeviceEnv(A.kind, bond, wl, bond, out[:total])
+
+
+def grow_left(env: DeviceEnv, A: SiteTensor, W, stream=None, device: int = 0) -> DeviceEnv:
+    """contract_left_environment on the device (tk_env_grow_left)."""
+    return _grow("tk_env_grow_left", env, A, W, True, stream, device)
+
+
+def grow_right(env: DeviceEnv, A: SiteTensor, W, stream=None, device: int = 0) -> DeviceEnv:
+    """contract_right_environment on the device (tk_env_grow_right)."""
+    return _grow("tk_env_grow_right", env, A, W, False, stream, device)
+
+
+def two_site_product(plan: Heff2Plan, Ai: SiteTensor, Aj: SiteTensor, stream=None):
+    """psi = A_i A_j in the plan's block layout (tk_heff2_two_site_product)."""
+    torch = _torch()
+    m = _Marshal()
+    a, b = Ai.marshal(m), Aj.marshal(m)
+    psi = torch.empty(plan.block_dim, dtype=torch.float64, device=f"cuda:{plan.device}")
+    s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
+    check(_abi.load().tk_heff2_two_site_product(plan.handle, C.byref(a), C.byref(b), C.c_void_p(psi.data_ptr()), s))
+    return psi
+
+
+def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool):
+    """Block SVD of the two-site vector (plan block layout) per bond charge.
+
+    Rows of M_q are (s_i, a_L) in global (state, index) order, columns (s_j,
+    a_R) likewise; the kept set is the `max_bond` largest singular values above
+    `cutoff` over all charges, ties broken by charge order then position.
+    Returns (A_i blocks, A_j blocks, new bond QIndex, discarded weight);
+    to_right puts S into A_j (A_i left-canonical), else into A_i; the kept
+    part is normalised."""
+    PI, PJ, QA, QB = legs
+    pqi, pqj = PI.state_charges(), PJ.state_charges()
+    rows, cols = {}, {}      # q -> list of (state, sector charge, offset)
+    nrow, ncol = {}, {}
+    for s, qs in enumerate(pqi):
+        for qa, da in QA.sectors:
+            q = fuse(kind, qs, qa)
+            rows.setdefault(q, {})[(s, qa)] = nrow.get(q, 0)
+            nrow[q] = nrow.get(q, 0) + da
+    for t, qt in enumerate(pqj):
+        for qb, db in QB.sectors:
+            q = fuse(kind, qb, dual(kind, qt))
+            cols.setdefault(q, {})[(t, qb)] = ncol.get(q, 0)
+            ncol[q] = ncol.get(q, 0) + db
+    charges = sorted(set(rows) & set(cols))
+    M = {q: np.zeros((nrow[q], ncol[q])) for q in charges}
+    for key, off in zip(keys, offs):
+        qsi, qsj, qa, qb = (tuple(x) for x in key_unpack(kind, int(key), 4))
+        ni, nj, da, db = PI.dim_of(qsi), PJ.dim_of(qsj), QA.dim_of(qa), QB.dim_of(qb)
+        blk = psi[off:off + ni * nj * da * db].reshape(ni, nj, da, db)
+        for li in range(ni):
+            s = PI.offset_of(qsi) + li
+            q = fuse(kind, qsi, qa)
+            for lj in range(nj):
+                t = PJ.offset_of(qsj) + lj
+                r0, c0 = rows[q][(s, qa)], cols[q][(t, qb)]
+                M[q][r0:r0 + da, c0:c0 + db] = blk[li, lj]
+    svd = {}
+    allsv = []
+    for bi, q in enumerate(charges):
+        U, S, Vt = np.linalg.svd(M[q], full_matrices=False)
+        svd[q] = (U, S, Vt)
+        allsv += [(float(x), bi, j) for j, x in enumerate(S)]
+    allsv.sort(key=lambda t: (-t[0], t[1], t[2]))
+    keep = [t for t in allsv[:max_bond] if t[0] > cutoff]
+    kept = {}
+    for _, bi, _ in keep:
+        kept[charges[bi]] = kept.get(charges[bi], 0) + 1
+    disc = sum(x * x for x, _, _ in allsv[len(keep):])
+    nb = QIndex(kind, [(q, kept[q]) for q in charges if q in kept])
+    norm = math.sqrt(sum(x * x for x, _, _ in keep)) or 1.0
+    Ai, Aj = {}, {}
+    for q, k in kept.items():
+        U, S, Vt = svd[q]
+        Uk, Vk = U[:, :k], Vt[:k]
+        if to_right:
+            Vk = (S[:k, None] * Vk) / norm
+        else:
+            Uk = (Uk * S[None, :k]) / norm
+        for (s, qa), r0 in rows[q].items():
+            qs = pqi[s]
+            da = QA.dim_of(qa)
+            li = s - PI.offset_of(qs)
+            blk = Ai.setdefault((qs, qa, q), np.zeros((PI.dim_of(qs), da, k)))
+            blk[li] = Uk[r0:r0 + da]
+        for (t, qb), c0 in cols[q].items():
+            qt = pqj[t]
+            db = QB.dim_of(qb)
+            lj = t - PJ.offset_of(qt)
+            blk = Aj.setdefault((qt, q, qb), np.zeros((PJ.dim_of(qt), k, db)))
+            blk[lj] = Vk[:, c0:c0 + db]
+    return Ai, Aj, nb, disc
+
+
+def random_site_tensors(model, n: int, max_bond: int, total, rng: np.random.Generator, width: float = 0.35,
+                        device: int = 0):
+    """Random right-canonical block-sparse MPS (no dense tensors): bond charges
+    as in dmrg.random_mps (Gaussian weights around uniform filling, capped by
+    the state counts), then from the right each site's rows per left charge
+    are orthonormalised (QR of random N(0,1) blocks), capping a left sector at
+    its column count; site 0 is random and normalised."""
+    from .dmrg import _charge_counts
+
+    kind = model.kind
+    total = tuple(total)
+    pq = model.phys.state_charges()
+    P = model.phys
+    cl = _charge_counts(pq, kind, n)
+    dims = [{identity(kind): 1}]
+    for i in range(1, n):
+        sec = []
+        for q, c in cl[i].items():
+            cr = cl[n - i].get(fuse(kind, total, dual(kind, q)), 0)
+            if cr > 0:
+                sec.append((q, min(c, cr)))
+        sig = max(0.5, width * math.sqrt(i * (n - i) / n))
+        mean = [i / n * t for t in total]
+        w = np.array([math.exp(-sum((qc - mm) ** 2 for qc, mm in zip(q, mean)) / (2 * sig * sig)) for q, _ in sec])
+        share = np.floor(w / w.sum() * max_bond).astype(int)
+        if share.max() == 0:
+            share[int(np.argmax(w))] = 1
+        dims.append({q: int(min(a, cap)) for (q, cap), a in zip(sec, share) if min(a, cap) > 0})
+    dims.append({total: 1})
+    # right to left: cap each left sector by its column count, orthonormalise rows
+    blocks = [None] * n
+    for i in range(n - 1, 0, -1):
+        right = dims[i + 1]
+        newd = {}
+        site = {}
+        for ql, dl in sorted(dims[i].items()):
+            colsec = [(qs, fuse(kind, qs, ql)) for qs in sorted(set(pq))]
+            colsec = [(qs, qr) for qs, qr in colsec if qr in right]
+            ncols = sum(P.dim_of(qs) * right[qr] for qs, qr in colsec)
+            k = min(dl, ncols)
+            if k == 0:
+                continue
+            G = rng.standard_normal((ncols, k))
+            Q, _ = np.linalg.qr(G)
+            rowsM = Q.T  # k x ncols, orthonormal rows
+            c0 = 0
+            for qs, qr in colsec:
+                ds, dr = P.dim_of(qs), right[qr]
+                site[(qs, ql, qr)] = rowsM[:, c0:c0 + ds * dr].reshape(k, ds, dr).transpose(1, 0, 2).copy()
+                c0 += ds * dr
+            newd[ql] = k
+        dims[i] = newd
+        blocks[i] = site
+    site0 = {}
+    for qs in sorted(set(pq)):
+        qr = fuse(kind, qs, identity(kind))
+        if qr in dims[1]:
+            site0[(qs, identity(kind), qr)] = rng.standard_normal((P.dim_of(qs), 1, dims[1][qr]))
+    nrm = math.sqrt(sum(float(np.sum(b * b)) for b in site0.values()))
+    blocks[0] = {k: v / nrm for k, v in site0.items()}
+    bonds = [QIndex(kind, sorted(d.items())) for d in dims]
+    # drop blocks whose sectors were removed on the right
+    sites = []
+    for i in range(n):
+        legs = [P, bonds[i], bonds[i + 1]]
+        bl = {k: v for k, v in blocks[i].items() if bonds[i].offset_of(k[1]) is not None
+              and bonds[i + 1].offset_of(k[2]) is not None}
+        sites.append(SiteTensor.from_blocks(kind, legs, bl, device))
+    return sites, bonds
+
+
+@dataclass
+class SweepRecord:
+    energies: list = field(default_factory=list)   # energy after each half sweep
+    trunc: list = field(default_factory=list)      # max discarded weight per half sweep
+    max_bond: list = field(default_factory=list)
+    seconds: list = field(default_factory=list)    # wall time per half sweep
+    matvecs: int = 0
+    fp64_matvecs: int = 0
+    phase_seconds: dict = field(default_factory=lambda: {"plan": 0.0, "solve": 0.0, "svd": 0.0, "grow": 0.0})
+
+
+class DeviceDMRG:
+    """Two-site DMRG with device-resident MPS and environments.
+
+    solver: "davidson" (the reference sweep's default; split-precision plans
+    use Jacobi-Davidson corrections with `inner` split-precision CG steps) or
+    "lanczos" (split-precision plans refined by FP64 Jacobi-Davidson)."""
+
+    def __init__(self, model, sites: list, bonds: list, precision: int = PREC_FP64, solver: str = "davidson",
+                 tol: float = 1e-10, max_subspace: int = 60, max_iter: int = 1000, inner: int = 12,
+                 krylov: int = 20, restarts: int = 10, refine: int = 20, device: int = 0):
+        self.model, self.kind = model, model.kind
+        self.n = len(sites)
+        self.sites, self.bonds = list(sites), list(bonds)
+        self.W = model.chain(self.n).tensors
+        self.precision, self.solver, self.tol = precision, solver, tol
+        self.max_subspace, self.max_iter, self.inner = max_subspace, max_iter, inner
+        self.krylov, self.restarts, self.refine = krylov, restarts, refine
+        self.device = device
+        self.zero = identity(self.kind)
+        n = self.n
+        self.L = [None] * (n + 1)
+        self.R = [None] * (n + 1)
+        self.L[0] = DeviceEnv.boundary(self.kind, self.bonds[0], self.W[0].indices[2], device)
+        self.R[n] = DeviceEnv.boundary(self.kind, self.bonds[n], self.W[n - 1].indices[3], device)
+        for i in range(n - 1, 0, -1):
+            self.R[i] = grow_right(self.R[i + 1], self.sites[i], self.W[i], device=device)
+
+    @classmethod
+    def from_dense_mps(cls, model, mps, **kw):
+        dev = kw.get("device", 0)
+        sites = [SiteTensor.from_dense(model.kind, [mps.phys, mps.bonds[i], mps.bonds[i + 1]], mps.tensors[i], dev)
+                 for i in range(mps.n)]
+        return cls(model, sites, list(mps.bonds), **kw)
+
+    def _solve(self, plan, x0):
+        if self.solver == "lanczos":
+            return plan.lanczos(krylov_dim=self.krylov, max_restarts=self.restarts, tol=self.tol, refine=self.refine,
+                                x0=x0)
+        inner = self.inner if plan.precision != PREC_FP64 else 0
+        return plan.davidson(max_subspace=self.max_subspace, max_iter=self.max_iter, tol=self.tol, inner=inner, x0=x0)
+
+    def step(self, i: int, to_right: bool, max_bond: int, cutoff: float, rec: SweepRecord):
+        torch = _torch()
+        t0 = time.perf_counter()
+        plan = Heff2Plan.from_device_envs(self.L[i], self.R[i + 2], self.W[i], self.W[i + 1], self.zero,
+                                          precision=self.precision, device=self.device)
+        x0 = two_site_product(plan, self.sites[i], self.sites[i + 1])
+        if float(torch.linalg.norm(x0)) == 0.0:
+            x0 = None
+        t1 = time.perf_counter()
+        r = self._solve(plan, x0)
+        rec.matvecs += r.matvec_count
+        rec.fp64_matvecs += r.fp64_matvec_count
+        psi = r.eigenvector.cpu().numpy()
+        t2 = time.perf_counter()
+        keys, offs = plan.blocks()
+        legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
+        Ai, Aj, nb, disc = split_two_site(self.kind, psi, keys, offs, legs, max_bond, cutoff, to_right)
+        P = self.model.phys
+        self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
+        self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
+        self.bonds[i + 1] = nb
+        t3 = time.perf_counter()
+        if to_right:
+            self.L[i + 1] = grow_left(self.L[i], self.sites[i], self.W[i], device=self.device)
+        else:
+            self.R[i + 1] = grow_right(self.R[i + 2], self.sites[i + 1], self.W[i + 1], device=self.device)
+        plan.close()
+        torch.cuda.synchronize(self.device)
+        t4 = time.perf_counter()
+        ph = rec.phase_seconds
+        ph["plan"] += t1 - t0
+        ph["solve"] += t2 - t1
+        ph["svd"] += t3 - t2
+        ph["grow"] += t4 - t3
+        return r.eigenvalue, disc
+
+    def run(self, max_bond: int, sweeps: int, cutoff: float = 1e-14) -> SweepRecord:
+        rec = SweepRecord()
+        for _ in range(sweeps):
+            for to_right, rng_ in ((True, range(0, self.n - 1)), (False, range(self.n - 2, -1, -1))):
+                t0 = time.perf_counter()
+                e, tmax = None, 0.0
+                for i in rng_:
+                    e, disc = self.step(i, to_right, max_bond, cutoff, rec)
+                    tmax = max(tmax, disc)
+                rec.seconds.append(time.perf_counter() - t0)
+                rec.energies.append(e)
+                rec.trunc.append(tmax)
+                rec.max_bond.append(max(b.total_dim for b in self.bonds))
+        return rec
