@@ -52,6 +52,12 @@ def parse():
     ap.add_argument("--dmrg", action="store_true",
                     help="also run the Heisenberg L=32, D=64, 4-sweep two-site DMRG (FP64 and split precision)")
     ap.add_argument("--dmrg-cpu", action="store_true", help="with --dmrg: also run it on the CPU oracle solver")
+    ap.add_argument("--sweeps", type=int, default=0, metavar="K",
+                    help="also time K device-resident two-site sweeps of the Hubbard chain (FP64 Davidson and "
+                         "split-precision Jacobi-Davidson from the same MPS, after --sweep-warmup split sweeps)")
+    ap.add_argument("--sweep-sites", type=int, default=64)
+    ap.add_argument("--sweep-bond", type=int, default=2048)
+    ap.add_argument("--sweep-warmup", type=int, default=2)
     ap.add_argument("--compare-schedules", type=int, default=0, metavar="STEPS",
                     help="also time STEPS FP64 matvecs with one grouped launch per stage and with one launch "
                          "per sector block")
@@ -112,6 +118,40 @@ def dmrg_cfg1(torch, with_cpu: bool):
     out["dE_split_vs_fp64"] = abs(out["gpu_bf16x3_refined"]["energies"][-1] - e64)
     if with_cpu:
         out["dE_gpu_vs_cpu_oracle"] = abs(out["cpu_oracle_fp64"]["energies"][-1] - e64)
+    return out
+
+
+def sweep_hubbard(torch, n: int, D: int, warm: int, timed: int):
+    """Hubbard chain t=1, U=4, half filling, (N, 2Sz), JW MPO w=6, bond D:
+    random right-canonical block MPS (seed 2024), `warm` split-precision
+    sweeps, then `timed` sweeps from that same MPS with FP64 Davidson (the
+    reference sweep's solver) and with split-precision Jacobi-Davidson."""
+    from tk_gb300 import PREC_BF16X3, PREC_FP64, models, sweep
+
+    m = models.hubbard()
+    t0 = time.perf_counter()
+    sites, bonds = sweep.random_site_tensors(m, n, D, (n, 0), np.random.default_rng(2024), width=0.75)
+    out = {"config": f"hubbard L={n} t=1 U=4 N={n} 2Sz=0 D={D} davidson tol=1e-10 seed=2024",
+           "init_seconds": time.perf_counter() - t0}
+    warm_dmrg = sweep.DeviceDMRG(m, sites, bonds, precision=PREC_BF16X3, solver="davidson", tol=1e-10)
+    rec = warm_dmrg.run(D, warm)
+    torch.cuda.synchronize()
+    out["warmup"] = {"sweeps": warm, "energies": rec.energies, "seconds": rec.seconds}
+    snap = [sweep.SiteTensor(t.kind, t.legs, t.keys, t.offs, t.data.clone()) for t in warm_dmrg.sites]
+    snap_bonds = list(warm_dmrg.bonds)
+    del warm_dmrg
+    for name, prec in (("fp64", PREC_FP64), ("bf16x3", PREC_BF16X3)):
+        sites2 = [sweep.SiteTensor(t.kind, t.legs, t.keys, t.offs, t.data.clone()) for t in snap]
+        dm = sweep.DeviceDMRG(m, sites2, list(snap_bonds), precision=prec, solver="davidson", tol=1e-10)
+        torch.cuda.synchronize()
+        rec = dm.run(D, timed)
+        out[name] = {"seconds_per_sweep": sum(rec.seconds) / timed, "energies": rec.energies,
+                     "max_trunc": max(rec.trunc), "max_bond": rec.max_bond[-1], "matvecs": rec.matvecs,
+                     "fp64_matvecs": rec.fp64_matvecs,
+                     "phase_seconds": {k: round(v, 3) for k, v in rec.phase_seconds.items()}}
+        del dm
+    out["sweep_speedup"] = out["fp64"]["seconds_per_sweep"] / out["bf16x3"]["seconds_per_sweep"]
+    out["dE"] = abs(out["fp64"]["energies"][-1] - out["bf16x3"]["energies"][-1])
     return out
 
 
@@ -458,6 +498,9 @@ def run_ours(args):
         line["schedules"] = compare_schedules(plan, x, y, torch, dev, args.compare_schedules, flush)
     if args.dmrg:
         line["dmrg_cfg1"] = dmrg_cfg1(torch, args.dmrg_cpu)
+    if args.sweeps > 0:
+        line["sweeps_hubbard"] = sweep_hubbard(torch, args.sweep_sites, args.sweep_bond, args.sweep_warmup,
+                                               args.sweeps)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()

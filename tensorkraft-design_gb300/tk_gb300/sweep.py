@@ -16,10 +16,11 @@ stays on the GPU between steps:
   product A_i A_j (tk_heff2_two_site_product) and runs Davidson or Lanczos on
   the device.
 
-Only the two-site vector goes to the host, for the block SVD: per bond charge
-q the matrix M_q[(s_i, a_L), (s_j, a_R)] is decomposed, the largest
-`max_bond` singular values over all charges are kept (ties broken by charge
-order, then position), and the new site tensors are written back
+Only the two-site vector goes to the host, for the truncation: per bond
+charge q the matrix M_q[(s_i, a_L), (s_j, a_R)] is decomposed through its
+density matrix, the largest `max_bond` singular values over all charges are
+kept (ties broken by charge order, then position), and the new site tensors
+are written back
 (the reference reads only the truncation error, sweep/mod.rs:420-437).  The
 right environment of bond (i, i+1) covers sites i+2.. (the reference passes
 right(site+1), :374-375).
@@ -197,17 +198,22 @@ def two_site_product(plan: Heff2Plan, Ai: SiteTensor, Aj: SiteTensor, stream=Non
 
 
 def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool):
-    """Block SVD of the two-site vector (plan block layout) per bond charge.
+    """Truncated decomposition of the two-site vector (plan block layout) per bond charge.
 
     Rows of M_q are (s_i, a_L) in global (state, index) order, columns (s_j,
-    a_R) likewise; the kept set is the `max_bond` largest singular values above
-    `cutoff` over all charges, ties broken by charge order then position.
-    Returns (A_i blocks, A_j blocks, new bond QIndex, discarded weight);
-    to_right puts S into A_j (A_i left-canonical), else into A_i; the kept
-    part is normalised."""
+    a_R) likewise.  The kept basis comes from the density matrix of the side
+    that becomes isometric (White's density-matrix truncation): moving right,
+    rho = M_q M_q^T, A_i = its leading eigenvectors and A_j = A_i^T M_q;
+    moving left, rho = M_q^T M_q, A_j = eigenvectors^T and A_i = M_q A_j^T.
+    Its eigenvalues are the squared singular values of M_q; the kept set is
+    the `max_bond` largest singular values above `cutoff` over all charges,
+    ties broken by charge order then position.  The isometric factor is
+    orthonormal to rounding and the other factor is the exact projection of
+    M_q (no division by small singular values).  Returns (A_i blocks, A_j
+    blocks, new bond QIndex, discarded weight), the kept part normalised."""
     PI, PJ, QA, QB = legs
     pqi, pqj = PI.state_charges(), PJ.state_charges()
-    rows, cols = {}, {}      # q -> list of (state, sector charge, offset)
+    rows, cols = {}, {}      # q -> {(state, sector charge): offset}
     nrow, ncol = {}, {}
     for s, qs in enumerate(pqi):
         for qa, da in QA.sectors:
@@ -225,19 +231,21 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
         qsi, qsj, qa, qb = (tuple(x) for x in key_unpack(kind, int(key), 4))
         ni, nj, da, db = PI.dim_of(qsi), PJ.dim_of(qsj), QA.dim_of(qa), QB.dim_of(qb)
         blk = psi[off:off + ni * nj * da * db].reshape(ni, nj, da, db)
+        q = fuse(kind, qsi, qa)
         for li in range(ni):
             s = PI.offset_of(qsi) + li
-            q = fuse(kind, qsi, qa)
             for lj in range(nj):
                 t = PJ.offset_of(qsj) + lj
                 r0, c0 = rows[q][(s, qa)], cols[q][(t, qb)]
                 M[q][r0:r0 + da, c0:c0 + db] = blk[li, lj]
-    svd = {}
+    eig = {}
     allsv = []
     for bi, q in enumerate(charges):
-        U, S, Vt = np.linalg.svd(M[q], full_matrices=False)
-        svd[q] = (U, S, Vt)
-        allsv += [(float(x), bi, j) for j, x in enumerate(S)]
+        G = M[q] @ M[q].T if to_right else M[q].T @ M[q]
+        w, Z = np.linalg.eigh(G)
+        w, Z = w[::-1], Z[:, ::-1]
+        eig[q] = Z
+        allsv += [(math.sqrt(max(float(x), 0.0)), bi, j) for j, x in enumerate(w)]
     allsv.sort(key=lambda t: (-t[0], t[1], t[2]))
     keep = [t for t in allsv[:max_bond] if t[0] > cutoff]
     kept = {}
@@ -248,12 +256,11 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     norm = math.sqrt(sum(x * x for x, _, _ in keep)) or 1.0
     Ai, Aj = {}, {}
     for q, k in kept.items():
-        U, S, Vt = svd[q]
-        Uk, Vk = U[:, :k], Vt[:k]
+        Z = eig[q][:, :k]
         if to_right:
-            Vk = (S[:k, None] * Vk) / norm
+            Uk, Vk = Z, (Z.T @ M[q]) / norm
         else:
-            Uk = (Uk * S[None, :k]) / norm
+            Uk, Vk = (M[q] @ Z) / norm, Z.T
         for (s, qa), r0 in rows[q].items():
             qs = pqi[s]
             da = QA.dim_of(qa)

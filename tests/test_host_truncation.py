@@ -1,0 +1,87 @@
+"""Host side of the device sweeps: the two-site truncation (density-matrix
+eigendecomposition per bond charge) against a dense SVD."""
+import numpy as np
+
+from tk_gb300 import models
+from tk_gb300.sweep import split_two_site
+from tk_gb300.symmetry import QIndex, fuse, key_pack
+
+
+def _layout(kind, P, QA, QB):
+    items = []
+    for qi, di in P.sectors:
+        for qj, dj in P.sectors:
+            for qa, da in QA.sectors:
+                qb = fuse(kind, fuse(kind, qi, qj), qa)
+                if QB.offset_of(qb) is None:
+                    continue
+                items.append((key_pack(kind, [qi, qj, qa, qb]), (qi, qj, qa, qb), di * dj * da * QB.dim_of(qb)))
+    items.sort()
+    keys = np.array([k for k, _, _ in items], dtype=np.uint64)
+    offs = np.zeros(len(items), dtype=np.int64)
+    offs[1:] = np.cumsum([s for _, _, s in items])[:-1]
+    return keys, offs, [q for _, q, _ in items], sum(s for _, _, s in items)
+
+
+def _dense(kind, psi, keys, offs, qs, P, QA, QB):
+    d = P.total_dim
+    T = np.zeros((d, d, QA.total_dim, QB.total_dim))
+    for off, (qi, qj, qa, qb) in zip(offs, qs):
+        ni, nj, da, db = P.dim_of(qi), P.dim_of(qj), QA.dim_of(qa), QB.dim_of(qb)
+        oi, oj, oa, ob = P.offset_of(qi), P.offset_of(qj), QA.offset_of(qa), QB.offset_of(qb)
+        T[oi:oi + ni, oj:oj + nj, oa:oa + da, ob:ob + db] = psi[off:off + ni * nj * da * db].reshape(ni, nj, da, db)
+    return T
+
+
+def _rebuild(Ai, Aj, nb, P, QA, QB):
+    d = P.total_dim
+    A = np.zeros((d, QA.total_dim, nb.total_dim))
+    B = np.zeros((d, nb.total_dim, QB.total_dim))
+    for (qs, ql, qr), b in Ai.items():
+        A[P.offset_of(qs):P.offset_of(qs) + b.shape[0], QA.offset_of(ql):QA.offset_of(ql) + b.shape[1],
+          nb.offset_of(qr):nb.offset_of(qr) + b.shape[2]] = b
+    for (qs, ql, qr), b in Aj.items():
+        B[P.offset_of(qs):P.offset_of(qs) + b.shape[0], nb.offset_of(ql):nb.offset_of(ql) + b.shape[1],
+          QB.offset_of(qr):QB.offset_of(qr) + b.shape[2]] = b
+    return A, B
+
+
+def _case():
+    m = models.hubbard()
+    kind, P = m.kind, m.phys
+    QA = QIndex(kind, [((2, 0), 3), ((3, -1), 4), ((3, 1), 4), ((4, 0), 5)])
+    QB = QIndex(kind, [((4, 0), 3), ((5, -1), 5), ((5, 1), 5), ((6, 0), 6), ((6, 2), 2), ((6, -2), 2)])
+    keys, offs, qs, total = _layout(kind, P, QA, QB)
+    psi = np.random.default_rng(0).standard_normal(total)
+    psi /= np.linalg.norm(psi)
+    return kind, P, QA, QB, keys, offs, qs, psi
+
+
+def test_full_rank_reconstructs_and_is_isometric():
+    kind, P, QA, QB, keys, offs, qs, psi = _case()
+    T = _dense(kind, psi, keys, offs, qs, P, QA, QB)
+    for to_right in (True, False):
+        Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], 10_000, 0.0, to_right)
+        A, B = _rebuild(Ai, Aj, nb, P, QA, QB)
+        assert disc < 1e-24
+        assert np.allclose(np.einsum("sab,tbc->stac", A, B), T, atol=1e-12)
+        if to_right:
+            assert np.allclose(np.einsum("sab,sac->bc", A, A), np.eye(nb.total_dim), atol=1e-12)
+        else:
+            assert np.allclose(np.einsum("sab,scb->ac", B, B), np.eye(nb.total_dim), atol=1e-12)
+
+
+def test_truncation_keeps_the_largest_singular_values():
+    kind, P, QA, QB, keys, offs, qs, psi = _case()
+    T = _dense(kind, psi, keys, offs, qs, P, QA, QB)
+    d = P.total_dim
+    M = T.transpose(0, 2, 1, 3).reshape(d * QA.total_dim, d * QB.total_dim)
+    sv = np.sort(np.linalg.svd(M, compute_uv=False))[::-1]  # block structure: same singular values
+    D = 9
+    Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], D, 0.0, True)
+    assert nb.total_dim == D
+    assert abs(disc - np.sum(sv[D:] ** 2)) < 1e-12
+    A, B = _rebuild(Ai, Aj, nb, P, QA, QB)
+    kept = np.einsum("sab,tbc->stac", A, B) * np.sqrt(np.sum(sv[:D] ** 2))  # undo the normalisation
+    # the kept state is the best rank-D approximation: its overlap with T is the kept weight
+    assert abs(np.sum(kept * T) - np.sum(sv[:D] ** 2)) < 1e-12
