@@ -487,7 +487,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "api": "tk_heff2_apply_host_flat (pinned FlatBlockStorage host buffers)"},
-        "gpu_launches": (4 if prec_name != "fp64" else 3) * args.steps,
+        "gpu_launches": 3 * args.steps,
         "clocks": clocks,
     }
     if y_fp is not None:

@@ -278,6 +278,16 @@ void tk_bst_free(tk_bst_out* t);
 tk_status tk_spmv_f64(tk_ctx* ctx, const tk_bst* a, const double* x, double* y);
 
 /*
+ * Self-check, no reference counterpart: the split-precision kernels convert
+ * fp64 <-> fp32 from the IEEE 754 bit layouts on the integer pipes (the FP64
+ * pipe of this GPU is narrow).  Compares those conversions with the hardware
+ * ones on n device doubles (fp64 -> fp32 where the result is a normal fp32;
+ * fp32 -> fp64 on the fp32 bit patterns taken from the doubles' bits) and
+ * writes the number of mismatches to *mismatches.  Synchronous.
+ */
+tk_status tk_check_split_conversions(tk_ctx* ctx, const double* x_dev, int64_t n, uint64_t* mismatches);
+
+/*
  * Device-resident environments for two-site sweeps.  The reference's
  * Environment (tk-dmrg/src/environments/mod.rs:24-103) is a dense
  * (bra, w, ket) array; a symmetric environment is non-zero only on sector

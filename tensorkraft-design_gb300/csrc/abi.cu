@@ -352,6 +352,28 @@ tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {
 
 }  // extern "C"
 
+extern "C" tk_status tk_check_split_conversions(tk_ctx* ctx, const double* x_dev, int64_t n, uint64_t* mismatches) {
+    if (!ctx || !mismatches || (n > 0 && !x_dev) || n < 0) {
+        set_error("tk_check_split_conversions: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    if (!g.ok) {
+        set_error("tk_check_split_conversions: cudaSetDevice failed");
+        return TK_ERR_CUDA;
+    }
+    unsigned long long* d = nullptr;
+    TK_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemset(d, 0, sizeof(h));
+    if (e == cudaSuccess) e = tc_conversion_check(x_dev, n, d, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail("tk_check_split_conversions", e);
+    *mismatches = h;
+    return TK_OK;
+}
+
 extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream,
                                       int32_t reps, float* ms, double* flops, double* bytes) {
     if (!plan || !x_dev || !y_dev || !ms || reps < 1) {
@@ -371,7 +393,7 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
         if (p->precision == TK_PREC_BF16X3) {
             const TcTables& C = H.tc;
             const double b16 = 2.0 * 2.0 * kTcBK;  // hi + lo bf16 per operand row element x 64
-            bytes[0] = 8.0 * H.total + b16 * (double)C.xq_rows + b16 * (double)C.lq_rows + 4.0 * C.t1_total;
+            bytes[0] = 8.0 * H.total + b16 * (double)C.lq_rows + 4.0 * C.t1_total;
             bytes[1] = 4.0 * C.t1_total + b16 * (double)C.t2q_rows;
             bytes[2] = b16 * (double)C.t2q_rows + b16 * (double)C.rq_rows + 8.0 * H.total;
         } else {

@@ -316,7 +316,11 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
     if (!gemm_table_ok(T.g3, T.t2_total, (int64_t)T.rbuf.size(), T.total, "stage 3", err)) return false;
     if (!comb_table_ok(T.jobs, T.terms, T.t1_total, T.t2_total, err)) return false;
     const TcTables& C = T.tc;
-    if (C.t1col_base.size() != C.t1col_stride.size()) { err = "T1 column tables"; return false; }
+    if (C.t1col_base.size() != C.t1col_stride.size() || C.xsrc.size() != C.t1col_base.size() ||
+        C.xstride.size() != C.t1col_base.size()) {
+        err = "T1 column tables";
+        return false;
+    }
     for (const TcTile& t : C.tiles1) {
         if (t.mode != 2 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
             t.n_mma < t.n_valid || t.n_mma > kTcBN || t.n_mma % 16 != 0 || t.out_off < 0 || t.ldc < 0 ||
@@ -324,10 +328,19 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
             err = "tensor-core stage 1 tile";
             return false;
         }
+        if (t.k_valid <= 0 || t.k_valid > t.kch * kTcBK || t.k_valid <= (t.kch - 1) * kTcBK) {
+            err = "tensor-core stage 1 K";
+            return false;
+        }
         for (int c = 0; c < t.n_valid; ++c) {
             const int64_t base = C.t1col_base[t.out_off + c], st = C.t1col_stride[t.out_off + c];
             if (base < 0 || st <= 0 || base + (int64_t)(t.ldc + t.m_valid - 1) * st >= C.t1_total) {
                 err = "tensor-core stage 1 output column";
+                return false;
+            }
+            const int64_t xs = C.xsrc[t.out_off + c], xst = C.xstride[t.out_off + c];
+            if (xs < 0 || xst <= 0 || xs + (int64_t)(t.k_valid - 1) * xst >= T.total) {
+                err = "tensor-core stage 1 psi column";
                 return false;
             }
         }
@@ -342,14 +355,6 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
         for (int r = 0; r < t.m_valid; ++r) {
             int64_t y0 = C.yrow[t.out_off + r];
             if (y0 < 0 || y0 + t.n0 + t.n_valid - 1 >= T.total) { err = "tensor-core stage 3 output row"; return false; }
-        }
-    }
-    for (const TcSplitJob& j : C.split) {
-        int64_t imax = (((int64_t)j.xrow + (int64_t)((j.rows - 1) >> 6) * j.cstride + j.cols - 1) << 6) + 63;
-        if (j.rows <= 0 || j.cols <= 0 || j.src < 0 || j.src + (int64_t)j.rows * j.cols > T.total || j.xrow < 0 ||
-            j.a0 < 0 || j.a0 >= j.rows || j.b0 < 0 || j.b0 >= j.cols || imax >= C.xq_rows * kTcBK) {
-            err = "tensor-core split job";
-            return false;
         }
     }
     for (const TcCombJob& j : C.jobs) {
@@ -753,9 +758,8 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
             if (rows == 0 || cols == 0) continue;
             const int64_t K = QA.dim[a];
             const int32_t kch = kchunks(K);
-            const int64_t lb = C.lq_rows, xb = C.xq_rows;
+            const int64_t lb = C.lq_rows;
             C.lq_rows += kch * rows;
-            C.xq_rows += kch * cols;
             lq64.resize((size_t)C.lq_rows * BK, 0.0);
             for (size_t i = 0; i < lp.size(); ++i) {
                 int ap = lp[i].first, ws = lp[i].second;
@@ -765,34 +769,25 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     for (int64_t k = 0; k < K; ++k)
                         lq64[(size_t)(lb + (k / BK) * rows + lrow[i] + r) * BK + (k % BK)] = src[r * K + k];
             }
-            for (size_t i = 0; i < xp.size(); ++i) {
-                TcSplitJob j{};
-                j.src = SUB(xp[i].first, a, xp[i].second);
-                j.rows = (int32_t)K;
-                j.cols = (int32_t)QB.dim[xp[i].second];
-                j.xrow = (int32_t)(xb + xcol[i]);
-                j.cstride = (int32_t)cols;
-                for (int32_t a0 = 0; a0 < j.rows; a0 += 32)
-                    for (int32_t b0 = 0; b0 < j.cols; b0 += 32) {
-                        j.a0 = a0;
-                        j.b0 = b0;
-                        C.split.push_back(j);
-                    }
-            }
-            // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B)
+            // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B);
+            // the B operand column b of block (p, B) is column b of the psi sub-block (D_A x D_B)
             const int64_t colbase0 = (int64_t)C.t1col_base.size();
             for (size_t jx = 0; jx < xp.size(); ++jx) {
                 const int64_t DB = QB.dim[xp[jx].second];
+                const int64_t src = SUB(xp[jx].first, a, xp[jx].second);
                 for (int64_t b = 0; b < DB; ++b) {
                     C.t1col_base.push_back(t1off + xcol[jx] * rows + b);
                     C.t1col_stride.push_back((int32_t)DB);
+                    C.xsrc.push_back(src + b);
+                    C.xstride.push_back((int32_t)DB);
                 }
             }
             for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
                 for (int64_t n0 = 0; n0 < cols; n0 += kTcBN) {
                     TcTile t{};
                     t.a_row = (int32_t)(lb + m0); t.a_cs = (int32_t)rows;
-                    t.b_row = (int32_t)(xb + n0); t.b_cs = (int32_t)cols;
+                    t.b_row = 0; t.b_cs = 0;
+                    t.k_valid = (int32_t)K;
                     t.kch = kch;
                     t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
                     t.n_valid = (int32_t)std::min<int64_t>(kTcBN, cols - n0);
@@ -926,7 +921,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
         };
         split(lq64, C.lq_hi, C.lq_lo);
         split(rq64, C.rq_hi, C.rq_lo);
-        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
+        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
             err = "tensor-core operand rows exceed 32 bits";
             return TK_ERR_UNSUPPORTED;
         }

@@ -4,10 +4,10 @@
 // a product a*b is evaluated as hi_a*hi_b + hi_a*lo_b + lo_a*hi_b with fp32
 // accumulation in tensor memory (the lo*lo term, ~2^-16 relative, is dropped).
 //
-// One matvec = four launches on one stream:
-//   split_psi_kernel   psi (fp64, FlatBlockStorage) -> stage-1 B operand, hi/lo,
-//                      transposed through shared memory into K-major chunks
-//   tc_gemm_kernel     stage 1, T1 = L_stack(A) * psi_A        (fp32 out)
+// One matvec = three launches on one stream:
+//   tc_gemm1_kernel    stage 1, T1 = L_stack(A) * psi_A        (fp32 out); the
+//                      psi operand is read from the fp64 vector and split into
+//                      bf16 hi/lo in shared memory by the kernel itself
 //   combine_tc_kernel  W_i*W_j channel combine, T1 -> stage-3 A operand hi/lo
 //   tc_gemm_kernel     stage 3, y = T2_stack(B') * R_stack(B')^T (fp64 out via a row table)
 //
@@ -124,6 +124,15 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// Programmatic dependent launch: the four kernels of a matvec are launched
+// with programmatic stream serialisation, so a kernel's prologue (tables,
+// barriers, TMEM) overlaps the previous kernel's tail.  Every kernel calls
+// grid_dep_wait() before it reads or writes any buffer another kernel of the
+// stream touches; the wait returns once the previous grid has completed and
+// its memory is visible, which orders the whole stream transitively.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
     asm volatile(
@@ -134,6 +143,61 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Conversions between fp64 and fp32 on the integer pipes.  This GPU's FP64
+// pipe is narrow (a few operations per SM and clock) and the hardware
+// conversions issue to it, so the per-element conversions of the split
+// kernels are done from the IEEE 754 bit layouts instead.
+//
+// fp64 -> fp32, round to nearest even (IEEE 754-2008 default rounding): equal
+// to __double2float_rn for every finite input whose result is a normal fp32;
+// results below the normal fp32 range (|x| < 2^-126) flush to a signed zero,
+// results above it become +-inf; inf and NaN map to inf and a quiet NaN.
+__device__ __forceinline__ float d2f_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FF);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (m ? 0x400000u : 0u));
+    int fe = e - 1023 + 127;
+    if (fe <= 0) return __uint_as_float(sign);
+    uint32_t mant = (uint32_t)(m >> 29);
+    const unsigned long long rem = m & ((1ull << 29) - 1), half = 1ull << 28;
+    if (rem > half || (rem == half && (mant & 1u))) {
+        if (++mant == (1u << 23)) {
+            mant = 0;
+            ++fe;
+        }
+    }
+    if (fe >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((uint32_t)fe << 23) | mant);
+}
+
+// fp32 -> fp64, exact for every input (subnormal fp32 values are normalised).
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const int e = (int)((u >> 23) & 0xFF);
+    uint32_t m = u & 0x7FFFFFu;
+    if (e == 0xFF) return __longlong_as_double((long long)(sign | (0x7FFull << 52) | ((unsigned long long)m << 29)));
+    if (e == 0) {
+        if (m == 0) return __longlong_as_double((long long)sign);
+        const int sh = __clz(m) - 8;  // bring the leading one to bit 23
+        m = (m << sh) & 0x7FFFFFu;
+        const unsigned long long de = (unsigned long long)(1 - 127 + 1023 - sh);
+        return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)m << 29)));
+    }
+    const unsigned long long de = (unsigned long long)(e - 127 + 1023);
+    return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)m << 29)));
+}
+
+// x ~ hi + lo with hi = bf16(x32), lo = bf16(x32 - hi), x32 = fp32(x); the
+// difference is exact in fp32.
+__device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+    const float f = d2f_bits(x);
+    hi = __float2bfloat16_rn(f);
+    lo = __float2bfloat16_rn(f - __bfloat162float(hi));
 }
 
 // Output addressing of a tile element (row, col) relative to the tile origin.
@@ -167,8 +231,10 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     uint32_t* tslot = (uint32_t*)(done + 1);
     const TcTile t = tiles[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    grid_dep_launch();
 
     if (t.kch == 0) {  // no K: the tile is zero
+        grid_dep_wait();
         for (int e = threadIdx.x; e < t.m_valid * t.n_valid; e += blockDim.x)
             store_out(t, e / t.n_valid, e % t.n_valid, 0.f, om);
         return;
@@ -191,6 +257,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
+    grid_dep_wait();
     bool ok = true;
     const int nb16 = t.n_mma >> 4;  // 16-row B boxes per operand and chunk
 
@@ -271,7 +338,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         } else {
             for (int r = warp * 32; r < rend; ++r) {
                 double* o = om.out64 + om.rowtab[t.out_off + r] + t.n0;
-                for (int col = lane; col < t.n_valid; col += 32) o[col] = (double)stile[r][col];
+                for (int col = lane; col < t.n_valid; col += 32) o[col] = f2d_bits(stile[r][col]);
             }
         }
     }
@@ -283,102 +350,228 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     }
 }
 
-__device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-    hi = __float2bfloat16_rn((float)x);
-    lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
-constexpr int kWarpsPerCta = 8;       // combine
-constexpr int kSplitWarpsPerCta = 4;  // split: 4 x 8.4 KB transpose buffers
-
-// psi sub-block (D_A x D_B, row-major fp64) -> stage-1 B operand rows (one per
-// column b, 64-wide K chunks over a), bf16 hi/lo.  One warp per sub-block;
-// 32 x 32 tiles go through a per-warp shared-memory buffer so that the psi
-// reads run along b and the operand writes along a (both contiguous).
-__global__ void __launch_bounds__(32 * kSplitWarpsPerCta) split_psi_kernel(const TcSplitJob* __restrict__ jobs, int njobs,
-                                                                      const double* __restrict__ x,
-                                                                      __nv_bfloat16* __restrict__ xh,
-                                                                      __nv_bfloat16* __restrict__ xl) {
-    __shared__ double buf[kSplitWarpsPerCta][32][33];
+// Stage 1 with the psi operand built in shared memory.  The L stack (A) comes
+// in by TMA as in tc_gemm_kernel; the B tile (n_mma columns x 64 K) is read
+// from the fp64 vector by all 128 threads (column n of the tile is
+// psi[xsrc[n] + k * xstride[n]], zero past the stack's K), split into bf16
+// hi / lo and written in the layout a 128-byte-swizzled TMA load would give:
+// row n at n * 128 bytes, its 16-byte chunk j at position j ^ (n % 8).  A
+// proxy fence and a block barrier hand the tile to the MMA thread.  Loop trip
+// counts stay block-uniform (bounded waits are combined with
+// __syncthreads_and) so no thread can be left at a barrier.
+template <int NST>
+__global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restrict__ tiles,
+                                                          const __grid_constant__ CUtensorMap mAh,
+                                                          const __grid_constant__ CUtensorMap mAl,
+                                                          const double* __restrict__ x,
+                                                          const int64_t* __restrict__ xsrc,
+                                                          const int32_t* __restrict__ xstride, const OutMap om,
+                                                          int* err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
+    uint64_t* empty = full + NST;
+    uint64_t* done = empty + NST;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    const TcTile t = tiles[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int jj = blockIdx.x * kSplitWarpsPerCta + warp;
-    if (jj >= njobs) return;
-    const TcSplitJob j = jobs[jj];
-    double (*t)[33] = buf[warp];
-    const int a0 = j.a0, b0 = j.b0;
-    const int na = min(32, j.rows - a0), nb = min(32, j.cols - b0);
-    // eight independent row loads in flight per batch
-    for (int a8 = 0; a8 < na; a8 += 8) {
-        double v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-            v[u] = (a8 + u < na && lane < nb) ? x[j.src + (int64_t)(a0 + a8 + u) * j.cols + b0 + lane] : 0.0;
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-            if (a8 + u < na) t[a8 + u][lane] = v[u];
+    grid_dep_launch();
+
+    if (t.kch == 0) {
+        grid_dep_wait();
+        for (int e = threadIdx.x; e < t.m_valid * t.n_valid; e += blockDim.x)
+            store_out(t, e / t.n_valid, e % t.n_valid, 0.f, om);
+        return;
     }
-    __syncwarp();
-    for (int b = 0; b < nb; ++b)
-        if (lane < na) {
-            __nv_bfloat16 h, l;
-            split2(t[lane][b], h, l);
-            const int a = a0 + lane;
-            const int64_t idx = (((int64_t)j.xrow + (int64_t)(a >> 6) * j.cstride + b0 + b) << 6) + (a & 63);
-            xh[idx] = h;
-            xl[idx] = l;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
         }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    grid_dep_wait();
+    const uint32_t idesc = make_idesc(t.n_mma);
+    for (int c = 0; c < t.kch; ++c) {
+        const int s = c % NST;
+        bool good = true;
+        if (c >= NST) good = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
+        if (!__syncthreads_and(good)) break;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&full[s], 2 * A_BYTES);
+            const int ya = t.a_row + c * t.a_cs;
+            tma_load_2d(st, &mAh, 0, ya, &full[s]);
+            tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[s]);
+        }
+        uint8_t* bh = st + 2 * A_BYTES;
+        uint8_t* bl = bh + B_BYTES;
+        const int kbase = c * kTcBK;
+        // 16-wide K steps that hold data: only those are filled and multiplied
+        const int ksteps = min(kTcBK / 16, (t.k_valid - kbase + 15) / 16);
+        const int npair = t.n_mma * 8 * ksteps;  // (column, k pair) elements
+        for (int e0 = threadIdx.x; e0 < npair; e0 += 128 * 4) {
+            double v[4][2];
+            int nn[4], kk[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * 128;
+                nn[u] = e % t.n_mma;
+                kk[u] = 2 * (e / t.n_mma);
+                const bool col = e < npair && nn[u] < t.n_valid;
+                const int64_t src = col ? xsrc[t.out_off + nn[u]] : 0;
+                const int64_t stp = col ? xstride[t.out_off + nn[u]] : 0;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int k = kbase + kk[u] + h;
+                    v[u][h] = (col && k < t.k_valid) ? x[src + (int64_t)k * stp] : 0.0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (e0 + u * 128 >= npair) continue;
+                __nv_bfloat16 h0, l0, h1, l1;
+                split2(v[u][0], h0, l0);
+                split2(v[u][1], h1, l1);
+                const int n = nn[u], k = kk[u];
+                const uint32_t off = (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
+                *reinterpret_cast<uint32_t*>(bh + off) = pack2(h0, h1);
+                *reinterpret_cast<uint32_t*>(bl + off) = pack2(l0, l1);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (warp == 1 && lane == 0) {
+            if (mbar_wait(&full[s], (c / NST) & 1, err, ERR_FULL_TIMEOUT)) {
+                fence_after();
+                const uint32_t sa = smem_u32(st);
+                const uint64_t ah = sw128_desc(sa), al = sw128_desc(sa + A_BYTES);
+                const uint64_t bhd = sw128_desc(sa + 2 * A_BYTES), bld = sw128_desc(sa + 2 * A_BYTES + B_BYTES);
+                for (int q = 0; q < ksteps; ++q) {
+                    const uint64_t adv = (uint64_t)((q * 32) >> 4);
+                    mma_bf16(tmem, ah + adv, bhd + adv, idesc, (c | q) != 0);
+                    mma_bf16(tmem, ah + adv, bld + adv, idesc, 1u);
+                    mma_bf16(tmem, al + adv, bhd + adv, idesc, 1u);
+                }
+            }
+            mma_commit(&empty[s]);
+        }
+    }
+    if (warp == 1 && lane == 0) mma_commit(done);
+    __syncwarp();
+    const bool have = mbar_wait(done, 0, err, ERR_DONE_TIMEOUT);
+    fence_after();
+    const bool go = __all_sync(0xffffffffu, have);
+    if (go) {
+        float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
+        const int row = threadIdx.x;
+        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < t.n_mma; c0 += 16) {
+            float v[16];
+            tmem_ld16(tbase + c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) stile[row][c0 + j] = v[j];
+        }
+        __syncwarp();
+        const int rend = min(t.m_valid, warp * 32 + 32);
+        int64_t cb[2] = {0, 0};
+        int32_t cs[2] = {0, 0};
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (lane + 32 * h < t.n_valid) {
+                cb[h] = om.colbase[t.out_off + lane + 32 * h];
+                cs[h] = om.colstride[t.out_off + lane + 32 * h];
+            }
+        for (int r = warp * 32; r < rend; ++r)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (lane + 32 * h < t.n_valid) om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane + 32 * h];
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
 }
+
+constexpr int kCombThreads = 128;  // combine: threads per job
 
 // W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.  One
-// warp per output slab; its terms live in registers (lane t holds term t,
-// broadcast by shuffles), lanes walk the slab's elements in row-major order
-// (contiguous in T1 and in the operand chunk).
-__global__ void __launch_bounds__(32 * kWarpsPerCta) combine_tc_kernel(const TcCombJob* __restrict__ jobs, int njobs,
-                                                                       const TcCombTerm* __restrict__ terms,
-                                                                       const float* __restrict__ t1,
-                                                                       __nv_bfloat16* __restrict__ th,
-                                                                       __nv_bfloat16* __restrict__ tl) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int jj = blockIdx.x * kWarpsPerCta + warp;
-    if (jj >= njobs) return;
-    const TcCombJob j = jobs[jj];
+// CTA per job (rows [r0, r0 + rows) of one output slab, at most
+// kTcCombMaxElems elements unless a single row is longer); its terms are
+// staged in shared memory and each thread owns U elements, so a thread has
+// TU x U independent T1 loads in flight before the first use.  Elements run
+// in row-major order, contiguous in T1 and in the operand chunk.
+__global__ void __launch_bounds__(kCombThreads) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+                                                                  const TcCombTerm* __restrict__ terms,
+                                                                  const float* __restrict__ t1,
+                                                                  __nv_bfloat16* __restrict__ th,
+                                                                  __nv_bfloat16* __restrict__ tl) {
+    constexpr int U = 4, TU = 4, TCH = 64;
+    __shared__ TcCombTerm st[TCH];
+    const TcCombJob j = jobs[blockIdx.x];
+    grid_dep_launch();
     const int n = j.rows * j.cols;
     const int nterm = j.term_end - j.term_begin;
-    auto load_terms = [&](int t0) {
-        TcCombTerm m{};
-        if (lane < min(32, nterm - t0)) m = terms[j.term_begin + t0 + lane];
-        return m;
-    };
-    constexpr int U = 4;  // independent elements per lane (loads in flight per term)
-    TcCombTerm mine = load_terms(0);
-    for (int e0 = 0; e0 < n; e0 += 32 * U) {  // warp-uniform trip count (shuffles need every lane)
+    grid_dep_wait();
+    for (int e0 = 0; e0 < n; e0 += U * kCombThreads) {  // block-uniform trip count
         bool valid[U];
         int r[U], c[U];
         float acc[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int e = e0 + u * 32 + lane;
+            const int e = e0 + u * kCombThreads + threadIdx.x;
             valid[u] = e < n;
             const int rl = valid[u] ? e / j.cols : 0;
             c[u] = valid[u] ? e - rl * j.cols : 0;
             r[u] = j.r0 + rl;  // row inside the slab
             acc[u] = 0.f;
         }
-        for (int t0 = 0; t0 < nterm; t0 += 32) {
-            if (t0 > 0) mine = load_terms(t0);
-            const int tn = min(32, nterm - t0);
-            for (int t = 0; t < tn; ++t) {
-                const int64_t off = __shfl_sync(0xffffffffu, mine.in_off, t);
-                const int rs = __shfl_sync(0xffffffffu, mine.in_rs, t);
-                const float cf = __shfl_sync(0xffffffffu, mine.coef, t);
-                float v[U];
+        for (int t0 = 0; t0 < nterm; t0 += TCH) {
+            const int tn = min(TCH, nterm - t0);
+            __syncthreads();
+            if (threadIdx.x < tn) st[threadIdx.x] = terms[j.term_begin + t0 + threadIdx.x];
+            __syncthreads();
+            int t = 0;
+            for (; t + TU <= tn; t += TU) {
+                float v[TU][U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) v[u] = valid[u] ? __ldg(t1 + off + (int64_t)r[u] * rs + c[u]) : 0.f;
+                for (int q = 0; q < TU; ++q) {
+                    const int64_t off = st[t + q].in_off;
+                    const int rs = st[t + q].in_rs;
 #pragma unroll
-                for (int u = 0; u < U; ++u) acc[u] = fmaf(cf, v[u], acc[u]);
+                    for (int u = 0; u < U; ++u)
+                        v[q][u] = valid[u] ? __ldg(t1 + off + (int64_t)r[u] * rs + c[u]) : 0.f;
+                }
+#pragma unroll
+                for (int q = 0; q < TU; ++q)
+#pragma unroll
+                    for (int u = 0; u < U; ++u) acc[u] = fmaf(st[t + q].coef, v[q][u], acc[u]);
+            }
+            for (; t < tn; ++t) {
+                const int64_t off = st[t].in_off;
+                const int rs = st[t].in_rs;
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (valid[u]) acc[u] = fmaf(st[t].coef, __ldg(t1 + off + (int64_t)r[u] * rs + c[u]), acc[u]);
             }
         }
-        if (nterm > 32) mine = load_terms(0);
 #pragma unroll
         for (int u = 0; u < U; ++u)
             if (valid[u]) {
@@ -439,22 +632,23 @@ bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string
 
 struct TcPlan {
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
-    __nv_bfloat16 *xh = nullptr, *xl = nullptr, *th = nullptr, *tl = nullptr;
+    __nv_bfloat16 *th = nullptr, *tl = nullptr;
     float* t1 = nullptr;
     TcTile *tiles1 = nullptr, *tiles3 = nullptr;
-    TcSplitJob* split = nullptr;
     TcCombJob* jobs = nullptr;
     TcCombTerm* terms = nullptr;
     int64_t* yrow = nullptr;
     int64_t* t1col_base = nullptr;
     int32_t* t1col_stride = nullptr;
+    int64_t* xsrc = nullptr;
+    int32_t* xstride = nullptr;
     int* err = nullptr;
-    int n1 = 0, n3 = 0, nsplit = 0, njobs = 0;
+    int n1 = 0, n3 = 0, njobs = 0;
     int nst1 = 1, nst3 = 2;  // pipeline stages of the two GEMM launches
-    CUtensorMap mLh, mLl, mXh, mXl, mTh, mTl, mRh, mRl;
+    CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl;
     ~TcPlan() {
-        void* ps[] = {lh,    ll,    rh,   rl,   xh,          xl,         th,          tl,         t1,
-                      tiles1, tiles3, split, jobs, terms, yrow, err, t1col_base, t1col_stride};
+        void* ps[] = {lh,   ll,    rh,   rl,         th,           tl,   t1,      tiles1, tiles3,
+                      jobs, terms, yrow, t1col_base, t1col_stride, xsrc, xstride, err};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -480,10 +674,10 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     };
     if ((e = put(&p->lh, bf(C.lq_hi))) != cudaSuccess || (e = put(&p->ll, bf(C.lq_lo))) != cudaSuccess ||
         (e = put(&p->rh, bf(C.rq_hi))) != cudaSuccess || (e = put(&p->rl, bf(C.rq_lo))) != cudaSuccess ||
-        (e = zeros(&p->xh, C.xq_rows)) != cudaSuccess || (e = zeros(&p->xl, C.xq_rows)) != cudaSuccess ||
         (e = zeros(&p->th, C.t2q_rows)) != cudaSuccess || (e = zeros(&p->tl, C.t2q_rows)) != cudaSuccess ||
         (e = put(&p->tiles1, C.tiles1)) != cudaSuccess || (e = put(&p->tiles3, C.tiles3)) != cudaSuccess ||
-        (e = put(&p->split, C.split)) != cudaSuccess || (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
+        (e = put(&p->xsrc, C.xsrc)) != cudaSuccess || (e = put(&p->xstride, C.xstride)) != cudaSuccess ||
+        (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
         (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess ||
         (e = put(&p->t1col_base, C.t1col_base)) != cudaSuccess ||
         (e = put(&p->t1col_stride, C.t1col_stride)) != cudaSuccess) {
@@ -497,18 +691,20 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     }
     p->n1 = (int)C.tiles1.size();
     p->n3 = (int)C.tiles3.size();
-    p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
-        !make_map(&p->mXh, p->xh, C.xq_rows, 16, err) || !make_map(&p->mXl, p->xl, C.xq_rows, 16, err) ||
         !make_map(&p->mTh, p->th, C.t2q_rows, kTcBM, err) || !make_map(&p->mTl, p->tl, C.t2q_rows, kTcBM, err) ||
         !make_map(&p->mRh, p->rh, C.rq_rows, 16, err) || !make_map(&p->mRl, p->rl, C.rq_rows, 16, err))
         return TK_ERR_CUDA;
     if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
             cudaSuccess ||
         (e = cudaFuncSetAttribute(tc_gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
             cudaSuccess) {
         err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return TK_ERR_CUDA;
@@ -519,13 +715,29 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
 
 namespace {
 
+// Launch with programmatic stream serialisation (see grid_dep_wait).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, const CUtensorMap& al,
                     const CUtensorMap& bh, const CUtensorMap& bl, const OutMap& om, int* err, cudaStream_t s) {
     if (n <= 0) return;
     if (nst == 1)
-        tc_gemm_kernel<1><<<n, 128, smem_bytes(1), s>>>(tiles, ah, al, bh, bl, om, err);
+        launch_pdl(tc_gemm_kernel<1>, n, 128, smem_bytes(1), s, tiles, ah, al, bh, bl, om, err);
     else
-        tc_gemm_kernel<2><<<n, 128, smem_bytes(2), s>>>(tiles, ah, al, bh, bl, om, err);
+        launch_pdl(tc_gemm_kernel<2>, n, 128, smem_bytes(2), s, tiles, ah, al, bh, bl, om, err);
 }
 
 }  // namespace
@@ -533,15 +745,19 @@ void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, 
 cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double* x,
                            double* y, cudaStream_t s, int stage, std::string& err) {
     if (stage == 0) {
-        if (tc.nsplit > 0)
-            split_psi_kernel<<<(tc.nsplit + kSplitWarpsPerCta - 1) / kSplitWarpsPerCta, 32 * kSplitWarpsPerCta, 0, s>>>(
-                tc.split, tc.nsplit, x, tc.xh, tc.xl);
-        launch_tc_gemm(tc.nst1, tc.n1, tc.tiles1, tc.mLh, tc.mLl, tc.mXh, tc.mXl,
-                       OutMap{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride}, tc.err, s);
+        const OutMap om{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride};
+        if (tc.n1 > 0) {
+            if (tc.nst1 == 1)
+                launch_pdl(tc_gemm1_kernel<1>, tc.n1, 128, smem_bytes(1), s, (const TcTile*)tc.tiles1, tc.mLh, tc.mLl,
+                           x, (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+            else
+                launch_pdl(tc_gemm1_kernel<2>, tc.n1, 128, smem_bytes(2), s, (const TcTile*)tc.tiles1, tc.mLh, tc.mLl,
+                           x, (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+        }
     } else if (stage == 1) {
         if (tc.njobs > 0)
-            combine_tc_kernel<<<(tc.njobs + kWarpsPerCta - 1) / kWarpsPerCta, 32 * kWarpsPerCta, 0, s>>>(
-                tc.jobs, tc.njobs, tc.terms, tc.t1, tc.th, tc.tl);
+            launch_pdl(combine_tc_kernel, tc.njobs, kCombThreads, 0, s, (const TcCombJob*)tc.jobs,
+                       (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
     } else {
         launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl,
                        OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, tc.err, s);
@@ -558,6 +774,36 @@ cudaError_t tc_apply(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs,
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+namespace {
+
+// Counts inputs where the integer-pipe conversions differ from the hardware
+// ones: d2f_bits vs __double2float_rn (inputs with a normal fp32 result) and
+// f2d_bits vs the fp32 -> fp64 conversion (every fp32 value).
+__global__ void conversion_check_kernel(const double* __restrict__ x, int64_t n, unsigned long long* bad) {
+    unsigned long long cnt = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        const float ref = __double2float_rn(v);
+        const float got = d2f_bits(v);
+        const bool normal = fabsf(ref) >= 1.17549435e-38f && fabsf(ref) <= 3.40282347e38f;
+        if (normal && __float_as_uint(ref) != __float_as_uint(got)) ++cnt;
+        const float f = __uint_as_float((uint32_t)(__double_as_longlong(v) >> 16));  // any fp32 bit pattern
+        if (f == f) {
+            const double dr = (double)f, dg = f2d_bits(f);
+            if (__double_as_longlong(dr) != __double_as_longlong(dg)) ++cnt;
+        }
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+}  // namespace
+
+cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* bad, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    conversion_check_kernel<<<152 * 4, 256, 0, s>>>(x, n, bad);
+    return cudaGetLastError();
 }
 
 int* tc_error_word(TcPlan& tc) { return tc.err; }

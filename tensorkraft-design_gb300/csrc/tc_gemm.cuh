@@ -31,6 +31,9 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables& host, const CombJob* d
 }  // namespace tk
 
 namespace tk {
+// Adds to *bad (device) the number of inputs where the split kernels' integer
+// fp64 <-> fp32 conversions differ from the hardware conversions.
+cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* bad, cudaStream_t s);
 // Device error word of the tensor-core kernels (0 = no bounded wait ran out).
 int* tc_error_word(TcPlan& tc);
 // Synchronises `s`, reads and clears the error word: TK_ERR_TIMEOUT if set.

@@ -124,7 +124,9 @@ bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>
 // Split-precision (tensor-core) tables.  Both GEMM stages are regrouped into
 // "stacks" that share one operand:
 //   stage 1, one stack per ket sector A of L: rows = every L slab (A', ws, A)
-//     stacked, columns = every psi sub-block (p, A, B) side by side, K = D_A;
+//     stacked, columns = every psi sub-block (p, A, B) side by side, K = D_A
+//     (the psi operand is read and split straight from the fp64 vector by
+//     the stage-1 kernel, through the per-column tables xsrc / xstride);
 //   stage 3, one stack per bra sector B' of R: rows = every y sub-block
 //     (p', A', B') stacked, columns = D_B', K = every R slab (B', ws, B)
 //     concatenated.
@@ -143,15 +145,7 @@ struct TcTile {
     int32_t kch, m_valid, n_valid, mode;  // mode 1: fp64 out through a row table; 2: fp32 out through column tables
     int64_t out_off;         // mode 1: row-table index of m0; mode 2: column-table index of n0
     int32_t ldc, n0;         // mode 1: n0 = column offset added to the row table; mode 2: ldc = m0
-    int32_t n_mma, pad;      // UMMA N of this tile: n_valid rounded up to 16 (<= kTcBN)
-};
-// psi sub-block -> stage-1 B operand (transposed into K-major chunks), hi/lo split.
-// One job = one 32 x 32 tile (a0, b0) of a sub-block (one warp each).
-struct TcSplitJob {
-    int64_t src;             // flat offset of the (D_A x D_B) sub-block
-    int32_t rows, cols;      // D_A (becomes K), D_B (becomes N)
-    int32_t xrow, cstride;   // operand row of chunk 0 for column 0; rows between chunks
-    int32_t a0, b0;          // tile origin inside the sub-block
+    int32_t n_mma, k_valid;  // UMMA N (n_valid rounded up to 16, <= kTcBN); stage 1: K of the stack (D_A)
 };
 // T1 (fp32) -> stage-3 A operand (K-major chunks), hi/lo split.  One job =
 // rows [r0, r0 + rows) of one output slab, at most kTcCombMaxElems elements
@@ -167,10 +161,9 @@ struct TcCombTerm {
     float coef;
 };
 struct TcTables {
-    int64_t lq_rows = 0, rq_rows = 0, xq_rows = 0, t2q_rows = 0, t1_total = 0;
+    int64_t lq_rows = 0, rq_rows = 0, t2q_rows = 0, t1_total = 0;
     std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
     std::vector<TcTile> tiles1, tiles3;
-    std::vector<TcSplitJob> split;
     std::vector<TcCombJob> jobs;
     std::vector<TcCombTerm> terms;
     std::vector<int64_t> yrow;  // y element offset of every stage-3 operand row
@@ -179,6 +172,9 @@ struct TcTables {
     // t1col_base[c] + r * t1col_stride[c] (c = global stage-1 column).
     std::vector<int64_t> t1col_base;
     std::vector<int32_t> t1col_stride;
+    // stage-1 B operand: column c is psi[xsrc[c] + k * xstride[c]], k < K of its stack
+    std::vector<int64_t> xsrc;
+    std::vector<int32_t> xstride;
     double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
     int32_t max_kch1 = 0, max_kch3 = 0;
 };

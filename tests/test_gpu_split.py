@@ -78,3 +78,28 @@ def test_refined_energy_exact_environment(lib_built):
     plan = p.plan(precision=PREC_BF16X3)
     r = plan.lanczos(krylov_dim=60, max_restarts=20, tol=1e-10, refine=20)
     assert abs(r.eigenvalue - ed_heisenberg(10)) < 1e-10
+
+
+def test_integer_pipe_conversions_match_hardware(lib_built):
+    """The split kernels' fp64 <-> fp32 conversions (integer pipes) equal the
+    hardware conversions: random doubles over many magnitudes, ties, and edge
+    patterns."""
+    import ctypes as C
+
+    import torch
+    from tk_gb300 import _abi
+    from tk_gb300.heff import context
+
+    rng = np.random.default_rng(12)
+    vals = [rng.standard_normal(200_000) * 10.0 ** rng.uniform(-30, 30, 200_000),
+            rng.uniform(-1, 1, 100_000),
+            # exact round-to-nearest-even ties and their neighbours at the fp32 boundary
+            np.frombuffer((np.arange(50_000, dtype=np.uint64) * np.uint64(1 << 29)
+                           | np.uint64(0x3FF0000010000000)).tobytes(), dtype=np.float64),
+            np.array([0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 1.1754943508222875e-38, 2.0 ** -149,
+                      np.inf, -np.inf, 1e-300, 1e300, 65504.0, np.pi])]
+    x = torch.from_numpy(np.concatenate(vals)).cuda()
+    bad = C.c_uint64(99)
+    _abi.check(_abi.load().tk_check_split_conversions(context(0), C.c_void_p(x.data_ptr()), x.numel(),
+                                                      C.byref(bad)))
+    assert bad.value == 0
