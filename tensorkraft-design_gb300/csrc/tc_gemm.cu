@@ -407,6 +407,14 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
     const uint32_t tmem = *tslot;
     grid_dep_wait();
     const uint32_t idesc = make_idesc(t.n_mma);
+    // B fill assignment: thread -> one tile column and every fill_step-th k pair
+    const int tid = (int)threadIdx.x;
+    const int fill_step = 128 / t.n_mma;
+    const int fill_col = tid < fill_step * t.n_mma ? tid % t.n_mma : -1;
+    const int fill_kq0 = tid / t.n_mma;
+    const bool fill_valid = fill_col >= 0 && fill_col < t.n_valid;
+    const int64_t fill_src = fill_valid ? xsrc[t.out_off + fill_col] : 0;
+    const int64_t fill_stp = fill_valid ? xstride[t.out_off + fill_col] : 0;
     for (int c = 0; c < t.kch; ++c) {
         const int s = c % NST;
         bool good = true;
@@ -424,34 +432,32 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
         const int kbase = c * kTcBK;
         // 16-wide K steps that hold data: only those are filled and multiplied
         const int ksteps = min(kTcBK / 16, (t.k_valid - kbase + 15) / 16);
-        const int npair = t.n_mma * 8 * ksteps;  // (column, k pair) elements
-        for (int e0 = threadIdx.x; e0 < npair; e0 += 128 * 4) {
-            double v[4][2];
-            int nn[4], kk[4];
+        const int nkp = 8 * ksteps;  // k pairs holding data in this chunk
+        if (fill_col >= 0) {
+            for (int kq0 = fill_kq0; kq0 < nkp; kq0 += 4 * fill_step) {
+                double v[4][2];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int e = e0 + u * 128;
-                nn[u] = e % t.n_mma;
-                kk[u] = 2 * (e / t.n_mma);
-                const bool col = e < npair && nn[u] < t.n_valid;
-                const int64_t src = col ? xsrc[t.out_off + nn[u]] : 0;
-                const int64_t stp = col ? xstride[t.out_off + nn[u]] : 0;
+                for (int u = 0; u < 4; ++u) {
+                    const int kq = kq0 + u * fill_step;
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int k = kbase + kk[u] + h;
-                    v[u][h] = (col && k < t.k_valid) ? x[src + (int64_t)k * stp] : 0.0;
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = kbase + 2 * kq + h;
+                        v[u][h] = (kq < nkp && fill_valid && k < t.k_valid) ? x[fill_src + (int64_t)k * fill_stp] : 0.0;
+                    }
                 }
-            }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (e0 + u * 128 >= npair) continue;
-                __nv_bfloat16 h0, l0, h1, l1;
-                split2(v[u][0], h0, l0);
-                split2(v[u][1], h1, l1);
-                const int n = nn[u], k = kk[u];
-                const uint32_t off = (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
-                *reinterpret_cast<uint32_t*>(bh + off) = pack2(h0, h1);
-                *reinterpret_cast<uint32_t*>(bl + off) = pack2(l0, l1);
+                for (int u = 0; u < 4; ++u) {
+                    const int kq = kq0 + u * fill_step;
+                    if (kq >= nkp) continue;
+                    __nv_bfloat16 h0, l0, h1, l1;
+                    split2(v[u][0], h0, l0);
+                    split2(v[u][1], h1, l1);
+                    const int n = fill_col, k = 2 * kq;
+                    const uint32_t off =
+                        (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
+                    *reinterpret_cast<uint32_t*>(bh + off) = pack2(h0, h1);
+                    *reinterpret_cast<uint32_t*>(bl + off) = pack2(l0, l1);
+                }
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
