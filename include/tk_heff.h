@@ -217,6 +217,34 @@ tk_status tk_davidson_lowest(tk_heff2_plan* plan, const tk_davidson_cfg* cfg, co
                              double* evec_dev, tk_eigen_result* out, void* stream);
 
 /*
+ * Krylov matrix exponential out = exp(alpha H_eff) v on the device: replaces
+ * exp_krylov_f64 (tk-dmrg/src/tdvp/mod.rs:197-270) and fills in the complex
+ * case the reference leaves as a stub (exp_krylov<T>, :386-396) for the real
+ * symmetric H_eff of a plan.  m = min(krylov_dim, dim) steps; a zero input
+ * (norm < 1e-30) gives zeros; the Krylov space is cut at the first step whose
+ * new norm is below `tol` (happy breakdown); exp(alpha T_m) e_1 comes from the
+ * eigendecomposition of the projected tridiagonal matrix, exact for any
+ * complex alpha (alpha = -dt for imaginary time, -i dt for real time).
+ * v_im == NULL means a real input; out_im may be NULL only for a real input
+ * and a real alpha.  Vectors are in the block layout on the device; a
+ * complex input costs two matvecs per Krylov step.  Synchronous.
+ */
+typedef struct {
+    int32_t krylov_dim;
+    double tol;
+} tk_expm_cfg;
+
+typedef struct {
+    int32_t krylov_used;    /* Krylov dimension after a breakdown cut */
+    int32_t matvec_count;
+    double input_norm;      /* ||v|| */
+} tk_expm_result;
+
+tk_status tk_expm_krylov(tk_heff2_plan* plan, const tk_expm_cfg* cfg, double alpha_re, double alpha_im,
+                         const double* v_re, const double* v_im, double* out_re, double* out_im,
+                         tk_expm_result* result, void* stream);
+
+/*
  * LinAlgBackend::gemm (tk-linalg/src/traits.rs:114-121) on device memory:
  * C = alpha*op(A)*op(B) + beta*C with element strides as in MatRef/MatMut
  * (tk-core/src/matview.rs:12-33).  `is_conjugated` is a no-op for f64.

@@ -386,17 +386,18 @@ tk_status enqueue_correction(tk_heff2_plan* p, const Ws& ws, double* rs, const d
     return e == cudaSuccess ? TK_OK : cuda_fail("correction solve", e);
 }
 
-// Lowest eigenpair of a symmetric m x m matrix (row-major, leading dim ld) by
-// cyclic Jacobi rotations; returns theta and writes the unit eigenvector.
-double small_sym_lowest(const std::vector<double>& g, int m, int ld, std::vector<double>& sv) {
-    std::vector<double> a((size_t)m * m), v((size_t)m * m, 0.0);
+// All eigenpairs of a symmetric m x m matrix (row-major, leading dim ld) by
+// cyclic Jacobi rotations: w[i] and column i of z (row-major m x m).
+void small_sym_eig(const std::vector<double>& g, int m, int ld, std::vector<double>& w, std::vector<double>& z) {
+    std::vector<double> a((size_t)m * m);
+    z.assign((size_t)m * m, 0.0);
     double frob = 0.0;
     for (int i = 0; i < m; ++i)
         for (int j = 0; j < m; ++j) {
             a[(size_t)i * m + j] = g[(size_t)i * ld + j];
             frob += a[(size_t)i * m + j] * a[(size_t)i * m + j];
         }
-    for (int i = 0; i < m; ++i) v[(size_t)i * m + i] = 1.0;
+    for (int i = 0; i < m; ++i) z[(size_t)i * m + i] = 1.0;
     for (int sweep = 0; sweep < 64; ++sweep) {
         double off = 0.0;
         for (int i = 0; i < m; ++i)
@@ -419,19 +420,27 @@ double small_sym_lowest(const std::vector<double>& g, int m, int ld, std::vector
                     a[(size_t)pp * m + k] = c * apk - sn * aqk;
                     a[(size_t)qq * m + k] = sn * apk + c * aqk;
                 }
-                for (int k = 0; k < m; ++k) {  // V <- V P
-                    const double vkp = v[(size_t)k * m + pp], vkq = v[(size_t)k * m + qq];
-                    v[(size_t)k * m + pp] = c * vkp - sn * vkq;
-                    v[(size_t)k * m + qq] = sn * vkp + c * vkq;
+                for (int k = 0; k < m; ++k) {  // Z <- Z P
+                    const double zkp = z[(size_t)k * m + pp], zkq = z[(size_t)k * m + qq];
+                    z[(size_t)k * m + pp] = c * zkp - sn * zkq;
+                    z[(size_t)k * m + qq] = sn * zkp + c * zkq;
                 }
             }
     }
+    w.resize(m);
+    for (int i = 0; i < m; ++i) w[i] = a[(size_t)i * m + i];
+}
+
+// Lowest eigenpair (theta and the unit eigenvector) of the same kind of matrix.
+double small_sym_lowest(const std::vector<double>& g, int m, int ld, std::vector<double>& sv) {
+    std::vector<double> w, z;
+    small_sym_eig(g, m, ld, w, z);
     int lo = 0;
     for (int i = 1; i < m; ++i)
-        if (a[(size_t)i * m + i] < a[(size_t)lo * m + lo]) lo = i;
+        if (w[i] < w[lo]) lo = i;
     sv.resize(m);
-    for (int k = 0; k < m; ++k) sv[k] = v[(size_t)k * m + lo];
-    return a[(size_t)lo * m + lo];
+    for (int k = 0; k < m; ++k) sv[k] = z[(size_t)k * m + lo];
+    return w[lo];
 }
 
 // DavidsonSolver's diagonal preconditioner (eigensolver/mod.rs:427-437):
@@ -633,10 +642,153 @@ struct DeviceScope {
     }
 };
 
+// out = X1 + i X2 in the vector's own complex form: with nc = 2 the length-2n
+// vectors hold (re; im) halves and multiplication by i maps (x; y) to (-y; x).
+__global__ void expm_assemble_kernel(double* __restrict__ out_re, double* __restrict__ out_im,
+                                     const double* __restrict__ x1, const double* __restrict__ x2, int64_t n, int nc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (nc == 2) {
+            out_re[i] = x1[i] - x2[n + i];
+            if (out_im) out_im[i] = x1[n + i] + x2[i];
+        } else {
+            out_re[i] = x1[i];
+            if (out_im) out_im[i] = x2[i];
+        }
+    }
+}
+
+// exp(alpha H) v for the plan's (real symmetric) H and a real or complex v:
+// Lanczos with full re-orthogonalisation on the real vector v~ = v (nc = 1)
+// or (Re v; Im v) (nc = 2, H applied to each half), whose recurrence
+// coefficients are those of the complex Lanczos process; exp(alpha T_m) e_1
+// from the eigendecomposition of the tridiagonal T_m (any complex alpha);
+// result = sum_k c_k V_k with complex c_k.
+tk_status expm_run(tk_heff2_plan* p, const Ws& ws, int nc, int64_t n, int m, double tol, double are, double aim,
+                   const double* vre, const double* vim, double* ore, double* oim, double* x2, tk_expm_result* res,
+                   cudaStream_t s) {
+    const int64_t nn = ws.n;  // nc * n
+    cudaError_t e;
+    tk_status st;
+    if ((e = cudaMemcpyAsync(ws.V, vre, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return cuda_fail("cudaMemcpyAsync", e);
+    if (nc == 2 && (e = cudaMemcpyAsync(ws.V + n, vim, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return cuda_fail("cudaMemcpyAsync", e);
+    if ((e = multidot(ws, ws.V, nn, 1, ws.V, MISC(ws), 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+    double beta0 = 0.0;
+    if ((st = read_scalar(MISC(ws), &beta0, s)) != TK_OK) return st;
+    res->input_norm = beta0;
+    if (beta0 < 1e-30) {  // exp_krylov_f64 returns zeros (tdvp/mod.rs:214-217)
+        if ((e = cudaMemsetAsync(ore, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
+        if (oim && (e = cudaMemsetAsync(oim, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
+        return TK_OK;
+    }
+    normalize_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V, ws.V, MISC(ws), nn);
+    for (int j = 0; j < m; ++j) {
+        double* vj = ws.V + (int64_t)j * nn;
+        for (int h = 0; h < nc; ++h)
+            if ((st = tk_heff2_apply_prec(p, vj + h * n, ws.w + h * n, s, p->precision)) != TK_OK) return st;
+        res->matvec_count += nc;
+        if ((e = multidot(ws, vj, nn, 1, ws.w, ALPHA(ws) + j, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+        axpy2_kernel<<<vgrid(nn), 256, 0, s>>>(ws.w, vj, ALPHA(ws) + j, j > 0 ? ws.V + (int64_t)(j - 1) * nn : nullptr,
+                                                j > 0 ? BETA(ws) + (j - 1) : nullptr, nn);
+        for (int pass = 0; pass < 2; ++pass) {
+            if ((e = multidot(ws, ws.V, nn, j + 1, ws.w, COEF(ws), 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+            gemv_sub_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V, nn, j + 1, COEF(ws), ws.w, nn);
+        }
+        if ((e = multidot(ws, ws.w, nn, 1, ws.w, BETA(ws) + j, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
+        if (j + 1 < m) normalize_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V + (int64_t)(j + 1) * nn, ws.w, BETA(ws) + j, nn);
+    }
+    std::vector<double> ab(2 * (size_t)ws.K);
+    if ((e = cudaMemcpyAsync(ab.data(), ws.scal, sizeof(double) * 2 * ws.K, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_fail("cudaMemcpyAsync", e);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("krylov exponential", e);
+    // happy breakdown (tdvp/mod.rs:250-254): the space is invariant after step j
+    int am = m;
+    for (int j = 0; j < m; ++j)
+        if (ab[ws.K + j] < tol) {
+            am = j + 1;
+            break;
+        }
+    res->krylov_used = am;
+    std::vector<double> T((size_t)am * am, 0.0), w, z;
+    for (int j = 0; j < am; ++j) {
+        T[(size_t)j * am + j] = ab[j];
+        if (j + 1 < am) T[(size_t)j * am + j + 1] = T[(size_t)(j + 1) * am + j] = ab[ws.K + j];
+    }
+    small_sym_eig(T, am, am, w, z);
+    // c_k = beta0 * sum_l z[k][l] exp(alpha w_l) z[0][l]
+    std::vector<double> c(2 * (size_t)am, 0.0);
+    for (int l = 0; l < am; ++l) {
+        const double mag = std::exp(are * w[l]), ph = aim * w[l];
+        const double er = mag * std::cos(ph), ei = mag * std::sin(ph);
+        for (int k = 0; k < am; ++k) {
+            const double f = beta0 * z[(size_t)k * am + l] * z[l];
+            c[k] += f * er;
+            c[am + k] += f * ei;
+        }
+    }
+    if ((e = cudaMemcpyAsync(COEF(ws), c.data(), sizeof(double) * 2 * am, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail("cudaMemcpyAsync", e);
+    gemv_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V, nn, am, COEF(ws), ws.w, nn);
+    gemv_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V, nn, am, COEF(ws) + am, x2, nn);
+    expm_assemble_kernel<<<vgrid(n), 256, 0, s>>>(ore, oim, ws.w, x2, n, nc);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? TK_OK : cuda_fail("krylov exponential", e);
+}
+
 }  // namespace
 }  // namespace tk
 
 using namespace tk;
+
+extern "C" tk_status tk_expm_krylov(tk_heff2_plan* p, const tk_expm_cfg* cfg, double alpha_re, double alpha_im,
+                                    const double* v_re, const double* v_im, double* out_re, double* out_im,
+                                    tk_expm_result* res, void* stream) {
+    if (!p || !cfg || !res || !v_re || !out_re) {
+        set_error("tk_expm_krylov: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    *res = tk_expm_result{};
+    const bool cplx = v_im != nullptr;
+    if (!out_im && (cplx || alpha_im != 0.0)) {
+        set_error("tk_expm_krylov: a complex result needs out_im");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (cfg->krylov_dim < 1 || cfg->krylov_dim > 256 || !(cfg->tol >= 0.0)) {
+        set_error("tk_expm_krylov: krylov_dim must be in [1, 256] and tol >= 0");
+        return TK_ERR_INVALID_ARG;
+    }
+    const int64_t n = p->host.total;
+    if (n == 0) {
+        set_error("tk_expm_krylov: empty two-site space");
+        return TK_ERR_INVALID_ARG;
+    }
+    DeviceScope scope(p->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    const int nc = cplx ? 2 : 1;
+    const int m = (int)std::min<int64_t>(cfg->krylov_dim, nc * n);  // min(krylov_dim, dim) (tdvp/mod.rs:207)
+    const int64_t nn = nc * n;
+    if (p->ex_cap_m < m || p->ex_cap_n < nn) {
+        const int mm = std::max(m, p->ex_cap_m);
+        const int64_t nmax = std::max(nn, p->ex_cap_n);
+        p->ex_cap_m = 0;
+        if ((e = p->ex_basis.alloc((size_t)(mm + 1) * nmax)) != cudaSuccess) return cuda_fail("alloc krylov basis", e);
+        if ((e = p->ex_w.alloc((size_t)nmax)) != cudaSuccess) return cuda_fail("alloc krylov", e);
+        if ((e = p->ex_x2.alloc((size_t)nmax)) != cudaSuccess) return cuda_fail("alloc krylov", e);
+        if ((e = p->ex_scal.alloc((size_t)(4 * (mm + 2) + 16))) != cudaSuccess) return cuda_fail("alloc krylov", e);
+        if ((e = p->ex_part.alloc((size_t)RG * (mm + 1))) != cudaSuccess) return cuda_fail("alloc krylov", e);
+        p->ex_cap_m = mm;
+        p->ex_cap_n = nmax;
+    }
+    Ws ws{p->ex_basis.p, p->ex_w.p, p->ex_scal.p, p->ex_part.p, nullptr, nn, std::max(p->ex_cap_m, 2)};
+    tk_status st = expm_run(p, ws, nc, n, m, cfg->tol, alpha_re, alpha_im, v_re, v_im, out_re, out_im, p->ex_x2.p,
+                            res, s);
+    if (st != TK_OK) return st;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("krylov exponential", e);
+    if (p->tc && (st = tc_check_error(*p->tc, s)) != TK_OK) return st;
+    return TK_OK;
+}
 
 extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* cfg, const double* x0_dev,
                                        double* evec_dev, tk_eigen_result* out, void* stream) {

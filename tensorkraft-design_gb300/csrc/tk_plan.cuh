@@ -90,6 +90,10 @@ struct tk_heff2_plan {
     // FP64 search space of the Davidson / refinement solver (allocated on first use)
     tk::DevBuf<double> sub_v, sub_hv, sub_sc, sub_part;
     int sub_cap = 0;
+    // Krylov-exponential workspace (allocated on first use)
+    tk::DevBuf<double> ex_basis, ex_w, ex_x2, ex_scal, ex_part;
+    int ex_cap_m = 0;
+    int64_t ex_cap_n = 0;
     int lz_cap_k = 0;
     std::unique_ptr<tk::LanczosGraph, tk::LanczosGraphDeleter> lz_graph;
     ~tk_heff2_plan() {

@@ -52,6 +52,14 @@ class tk_davidson_cfg(C.Structure):
                 ("diagonal", C.c_void_p), ("inner", C.c_int32)]
 
 
+class tk_expm_cfg(C.Structure):
+    _fields_ = [("krylov_dim", C.c_int32), ("tol", C.c_double)]
+
+
+class tk_expm_result(C.Structure):
+    _fields_ = [("krylov_used", C.c_int32), ("matvec_count", C.c_int32), ("input_norm", C.c_double)]
+
+
 class tk_eigen_result(C.Structure):
     _fields_ = [("eigenvalue", C.c_double), ("residual_norm", C.c_double), ("converged", C.c_int32),
                 ("matvec_count", C.c_int32), ("fp64_matvec_count", C.c_int32), ("restarts", C.c_int32)]
@@ -98,6 +106,8 @@ SIGNATURES = [
                                       C.POINTER(tk_eigen_result), C.c_void_p]),
     ("tk_davidson_lowest", C.c_int32, [C.c_void_p, C.POINTER(tk_davidson_cfg), C.c_void_p, C.c_void_p,
                                        C.POINTER(tk_eigen_result), C.c_void_p]),
+    ("tk_expm_krylov", C.c_int32, [C.c_void_p, C.POINTER(tk_expm_cfg), C.c_double, C.c_double, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(tk_expm_result), C.c_void_p]),
     ("tk_gemm_f64", C.c_int32, [C.c_void_p, C.c_double, C.POINTER(tk_mat), C.POINTER(tk_mat), C.c_double,
                                 C.POINTER(tk_mat_mut), C.c_void_p]),
     ("tk_gemm_f64_noalloc", C.c_int32, [C.c_void_p, C.c_double, C.POINTER(tk_mat), C.POINTER(tk_mat), C.c_double,

@@ -244,6 +244,24 @@ class Heff2Plan:
         return EigenResult(res.eigenvalue, evec, bool(res.converged), res.matvec_count, res.residual_norm,
                            res.fp64_matvec_count, res.restarts)
 
+    def expm(self, alpha, v_re, v_im=None, krylov_dim=30, tol=1e-12, stream=None):
+        """exp(alpha H) v (tk_expm_krylov); alpha real or complex, v device tensors.
+        Returns (out_re, out_im or None, krylov_used, matvec_count)."""
+        import torch
+
+        alpha = complex(alpha)
+        out_re = torch.empty(self.block_dim, dtype=torch.float64, device=f"cuda:{self.device}")
+        cplx = v_im is not None or alpha.imag != 0.0
+        out_im = torch.empty_like(out_re) if cplx else None
+        cfg = _abi.tk_expm_cfg(krylov_dim, tol)
+        res = _abi.tk_expm_result()
+        s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
+        check(self._lib.tk_expm_krylov(self._h, C.byref(cfg), alpha.real, alpha.imag, C.c_void_p(v_re.data_ptr()),
+                                       C.c_void_p(v_im.data_ptr()) if v_im is not None else None,
+                                       C.c_void_p(out_re.data_ptr()),
+                                       C.c_void_p(out_im.data_ptr()) if out_im is not None else None, C.byref(res), s))
+        return out_re, out_im, res.krylov_used, res.matvec_count
+
     def davidson(self, max_subspace=60, max_iter=1000, tol=1e-10, diagonal=None, inner=0, x0=None,
                  stream=None) -> EigenResult:
         """tk_davidson_lowest; `diagonal` is a device tensor of H_ii in the block layout or None."""

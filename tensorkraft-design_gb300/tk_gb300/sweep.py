@@ -347,6 +347,31 @@ def random_site_tensors(model, n: int, max_bond: int, total, rng: np.random.Gene
     return sites, bonds
 
 
+def _identity_mpo(kind, wq: QIndex):
+    """MPO tensor of a dummy site: physical dimension 1 (zero charge), W = identity on the channel."""
+    from .models import INCOMING, OUTGOING, dense_to_bst
+
+    p1 = QIndex(kind, [(identity(kind), 1)])
+    W = np.eye(wq.total_dim).reshape(1, 1, wq.total_dim, wq.total_dim)
+    return dense_to_bst(kind, W, [p1, p1, wq, wq], [INCOMING, OUTGOING, OUTGOING, INCOMING], identity(kind)), p1
+
+
+def _identity_site(kind, p1: QIndex, bond: QIndex, device: int):
+    blocks = {(identity(kind), q, q): np.eye(d).reshape(1, d, d) for q, d in bond.sectors}
+    return SiteTensor.from_blocks(kind, [p1, bond, bond], blocks, device)
+
+
+def _plan_to_site(kind, psi: np.ndarray, keys, offs, legs) -> dict:
+    """Plan block layout (s, 1, a, b) of a one-site plan -> site blocks (s, a, b)."""
+    P, QA, QB = legs
+    out = {}
+    for key, off in zip(keys, offs):
+        qs, _, qa, qb = (tuple(x) for x in key_unpack(kind, int(key), 4))
+        ds, da, db = P.dim_of(qs), QA.dim_of(qa), QB.dim_of(qb)
+        out[(qs, qa, qb)] = psi[off:off + ds * da * db].reshape(ds, da, db).copy()
+    return out
+
+
 @dataclass
 class SweepRecord:
     energies: list = field(default_factory=list)   # energy after each half sweep
@@ -434,6 +459,71 @@ class DeviceDMRG:
         ph["svd"] += t3 - t2
         ph["grow"] += t4 - t3
         return r.eigenvalue, disc
+
+    # ---- imaginary-time two-site TDVP ---------------------------------------------
+    def _one_site_plan(self, k: int):
+        """H_eff of site k (L_k, W_k, R_{k+1}) as a two-site plan with a dummy second site."""
+        Wd, p1 = _identity_mpo(self.kind, self.W[k].indices[3])
+        plan = Heff2Plan.from_device_envs(self.L[k], self.R[k + 1], self.W[k], Wd, self.zero,
+                                          precision=self.precision, device=self.device)
+        return plan, p1
+
+    def _evolve_center(self, k: int, tau: float, rec: "SweepRecord"):
+        """C_k <- exp(tau H1(k)) C_k, normalised (the backward step of the projector splitting)."""
+        torch = _torch()
+        plan, p1 = self._one_site_plan(k)
+        dummy = _identity_site(self.kind, p1, self.bonds[k + 1], self.device)
+        c = two_site_product(plan, self.sites[k], dummy)
+        out, _, _, mv = plan.expm(tau, c, krylov_dim=self.krylov, tol=1e-12)
+        rec.matvecs += mv
+        out = out / torch.linalg.norm(out)
+        keys, offs = plan.blocks()
+        blocks = _plan_to_site(self.kind, out.cpu().numpy(), keys, offs,
+                               [self.model.phys, self.bonds[k], self.bonds[k + 1]])
+        self.sites[k] = SiteTensor.from_blocks(self.kind, [self.model.phys, self.bonds[k], self.bonds[k + 1]],
+                                               blocks, self.device)
+        plan.close()
+
+    def tdvp_step(self, dtau: float, max_bond: int, rec: "SweepRecord", cutoff: float = 1e-14):
+        """One imaginary-time step exp(-dtau H) by two-site TDVP: a left-to-right and a
+        right-to-left half sweep of dtau/2 each; every two-site update evolves forward by
+        exp(-dtau/2 H2), the new single-site center backward by exp(+dtau/2 H1)
+        (projector splitting).  The state is kept normalised; returns the energy
+        <psi|H|psi> of the last two-site update."""
+        torch = _torch()
+        half = 0.5 * dtau
+        n = self.n
+        energy = None
+        for to_right, bonds in ((True, range(0, n - 1)), (False, range(n - 2, -1, -1))):
+            for i in bonds:
+                plan = Heff2Plan.from_device_envs(self.L[i], self.R[i + 2], self.W[i], self.W[i + 1], self.zero,
+                                                  precision=self.precision, device=self.device)
+                x = two_site_product(plan, self.sites[i], self.sites[i + 1])
+                y, _, _, mv = plan.expm(-half, x, krylov_dim=self.krylov, tol=1e-12)
+                rec.matvecs += mv
+                y = y / torch.linalg.norm(y)
+                hy = torch.empty_like(y)
+                plan.apply(y, hy)
+                energy = float(torch.dot(y, hy))
+                keys, offs = plan.blocks()
+                legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
+                Ai, Aj, nb, disc = split_two_site(self.kind, y.cpu().numpy(), keys, offs, legs, max_bond, cutoff,
+                                                  to_right)
+                P = self.model.phys
+                self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
+                self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
+                self.bonds[i + 1] = nb
+                plan.close()
+                if to_right:
+                    self.L[i + 1] = grow_left(self.L[i], self.sites[i], self.W[i], device=self.device)
+                    if i + 1 < n - 1:
+                        self._evolve_center(i + 1, half, rec)
+                else:
+                    self.R[i + 1] = grow_right(self.R[i + 2], self.sites[i + 1], self.W[i + 1], device=self.device)
+                    if i > 0:
+                        self._evolve_center(i, half, rec)
+        torch.cuda.synchronize(self.device)
+        return energy
 
     def run(self, max_bond: int, sweeps: int, cutoff: float = 1e-14) -> SweepRecord:
         rec = SweepRecord()

@@ -119,6 +119,15 @@ def main():
             {"source": "tk-dmrg/src/eigensolver/mod.rs:757-778", "matrix": "diag", "diag": [5, 2, 8, 1, 3],
              "diagonal": None, "tol": 1e-8, "eigenvalue": 1.0, "atol": 1e-6, "converged": None},
         ],
+        "exp_krylov": [
+            {"source": "tk-dmrg/src/tdvp/mod.rs:411-433 (identity)", "matrix": "diag", "diag": [1, 1, 1, 1, 1],
+             "v": [1, 0, 0, 0, 0], "alpha": 0.5, "krylov": 10, "tol": 1e-12, "atol": 1e-8},
+            {"source": "tk-dmrg/src/tdvp/mod.rs:435-460 (diagonal)", "matrix": "diag", "diag": [1, 2, 3],
+             "v": [1, 1, 1], "alpha": -0.1, "krylov": 10, "tol": 1e-12, "atol": 1e-6},
+            {"source": "tk-dmrg/src/tdvp/mod.rs:462-484 (zero time)", "matrix": "dense",
+             "dense": [[2, -1, 0, 0], [-1, 2, -1, 0], [0, -1, 2, -1], [0, 0, -1, 2]],
+             "v": [1, 2, 3, 4], "alpha": 0.0, "krylov": 10, "tol": 1e-12, "atol": 1e-10},
+        ],
         "lanczos_random_diagonal": {
             "source": "tk-dmrg/tests/proptest_dmrg.rs:18-49 (+ regression seed dim=4, seed=0)",
             "cases": [{"dim": d, "seed": s, "diag": lcg_values(s + 42, d), "eigenvalue": min(lcg_values(s + 42, d))}

@@ -120,3 +120,23 @@ def test_block_gemm_golden_is_consistent():
     g = KATS["block_gemm"]
     assert len(g["dense_product"]) == g["shape"][0] * g["shape"][1]
     assert np.isfinite(g["dense_product"]).all()
+
+
+def test_exp_krylov_restatement_kats():
+    """The numpy exp_krylov_f64 against the reference's tests (tdvp/mod.rs:411-484) and scipy."""
+    from scipy.linalg import expm
+
+    from oracle import krylov_exp
+
+    for case in KATS["exp_krylov"]:
+        M = np.diag(case["diag"]).astype(float) if case["matrix"] == "diag" else np.array(case["dense"], float)
+        v = np.array(case["v"], float)
+        out = krylov_exp.exp_krylov(lambda x: M @ x, v, case["alpha"], len(v), case["krylov"], case["tol"])
+        assert np.allclose(out, expm(case["alpha"] * M) @ v, atol=case["atol"], rtol=0)
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((30, 30))
+    M = (A + A.T) / 2
+    v = rng.standard_normal(30)
+    for alpha in (-0.05, -0.3j, 0.2 - 0.1j):
+        out = krylov_exp.exp_krylov(lambda x: M @ x, v.astype(complex), alpha, 30, 30, 1e-12)
+        assert np.allclose(out, expm(alpha * M) @ v, atol=1e-10, rtol=0)
