@@ -201,8 +201,9 @@ tk_status tk_lanczos_lowest(tk_heff2_plan* plan, const tk_lanczos_cfg* cfg, cons
  * directions the space restarts from the Ritz vector (one matvec; the
  * reference's `restart_vectors` is unused there too).  Every matvec of the
  * search space is FP64.  With a split-precision plan and inner > 0 the
- * correction instead solves (I-yy^T)(H-theta)(I-yy^T) t = -r by `inner`
- * conjugate-gradient steps with split-precision matvecs (Jacobi-Davidson);
+ * correction instead solves (I-yy^T)(H-theta)(I-yy^T) t = -r by at most
+ * `inner` conjugate-gradient steps with split-precision matvecs
+ * (Jacobi-Davidson), stopping once the CG residual has fallen by 1e-4;
  * inner = 0 keeps the reference's correction.  `restarts` is reported as 0.
  */
 typedef struct {

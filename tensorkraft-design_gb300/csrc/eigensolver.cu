@@ -283,8 +283,10 @@ tk_status fp64_residual(tk_heff2_plan* p, const Ws& ws, const double* x, double*
 // operator's error only slows the inner solve; theta and r always come from
 // FP64 matvecs, so the residual falls to FP64 rounding level.
 
-constexpr int RF_M = 8;       // refinement search-space size before a restart
-constexpr int kInnerCg = 12;  // split-precision CG steps per refinement step
+constexpr int RF_M = 8;         // refinement search-space size before a restart
+constexpr int kInnerCg = 40;    // split-precision CG steps per refinement step, at most
+constexpr int kCgCheck = 4;     // CG steps between convergence checks (one host read each)
+constexpr double kCgRel = 1e-4; // CG stops once its residual fell by this factor
 
 // CG scalars in device memory (rs):
 //   rs[0] shift theta, rs[2] x.q, rs[3] p.q, rs[8 + (j&1)] rr of step j
@@ -364,23 +366,33 @@ __global__ void cg_dir_kernel(double* __restrict__ p, const double* __restrict__
 // Enqueues `iters` CG steps on (I-xx^T)(H_split - theta)(I-xx^T) t = -r with
 // theta at rs[0]; t, res, p, q are work vectors.  No host synchronisation.
 tk_status enqueue_correction(tk_heff2_plan* p, const Ws& ws, double* rs, const double* x, const double* r, double* t,
-                             double* res, double* pv, double* q, int iters, int precision, cudaStream_t s) {
+                             double* res, double* pv, double* q, int iters, int precision, cudaStream_t s, int* used) {
     const int64_t n = ws.n;
     cudaError_t e;
+    *used = 0;
     if ((e = cudaMemsetAsync(t, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
     if ((e = cudaMemsetAsync(res, 0, sizeof(double) * n, s)) != cudaSuccess) return cuda_fail("memset", e);
     axpby_kernel<<<vgrid(n), 256, 0, s>>>(res, r, -1.0, 0.0, n);
     if ((e = cudaMemcpyAsync(pv, res, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
         return cuda_fail("cudaMemcpyAsync", e);
     if ((e = multidot(ws, res, n, 1, res, rs + 8, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
+    double rr0 = 0.0;
+    tk_status st = read_scalar(rs + 8, &rr0, s);
+    if (st != TK_OK) return st;
     for (int j = 0; j < iters; ++j) {
-        tk_status st = tk_heff2_apply_prec(p, pv, q, s, precision);
-        if (st != TK_OK) return st;
+        if ((st = tk_heff2_apply_prec(p, pv, q, s, precision)) != TK_OK) return st;
         cg_shift_dot2_kernel<<<RG, RT, 0, s>>>(q, pv, x, rs, n, ws.part);
         reduce_partial_kernel<<<2, 128, 0, s>>>(ws.part, rs + 2, 0);
         cg_step_kernel<<<RG, RT, 0, s>>>(t, res, pv, q, x, rs, j, n, ws.part);
         reduce_partial_kernel<<<1, 128, 0, s>>>(ws.part, rs + 8 + ((j + 1) & 1), 0);
         cg_dir_kernel<<<vgrid(n), 256, 0, s>>>(pv, res, rs, j, n);
+        *used = j + 1;
+        // every kCgCheck steps: stop once the residual fell by kCgRel
+        if ((j + 1) % kCgCheck == 0 && j + 1 < iters) {
+            double rr = 0.0;
+            if ((st = read_scalar(rs + 8 + ((j + 1) & 1), &rr, s)) != TK_OK) return st;
+            if (!(rr > kCgRel * kCgRel * rr0)) break;
+        }
     }
     e = cudaGetLastError();
     return e == cudaSuccess ? TK_OK : cuda_fail("correction solve", e);
@@ -540,10 +552,11 @@ tk_status subspace_solve(tk_heff2_plan* p, const Ws& ws, Subspace& sp, const Sub
         if (cfg.inner > 0) {
             if ((e = cudaMemcpyAsync(rs, &theta, sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
                 return cuda_fail("cudaMemcpyAsync", e);
+            int used = 0;
             if ((st = enqueue_correction(p, ws, rs, x, r, t, ws.V, ws.V + n, ws.V + 2 * n, cfg.inner, cfg.inner_prec,
-                                         s)) != TK_OK)
+                                         s, &used)) != TK_OK)
                 return st;
-            sp.matvecs += cfg.inner;
+            sp.matvecs += used;
         } else if (cfg.diag) {
             precondition_kernel<<<vgrid(n), 256, 0, s>>>(t, r, cfg.diag, theta, n);
         } else if ((e = cudaMemcpyAsync(t, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) {

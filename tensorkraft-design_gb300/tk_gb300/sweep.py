@@ -391,7 +391,7 @@ class DeviceDMRG:
     "lanczos" (split-precision plans refined by FP64 Jacobi-Davidson)."""
 
     def __init__(self, model, sites: list, bonds: list, precision: int = PREC_FP64, solver: str = "davidson",
-                 tol: float = 1e-10, max_subspace: int = 60, max_iter: int = 1000, inner: int = 12,
+                 tol: float = 1e-10, max_subspace: int = 60, max_iter: int = 1000, inner: int = 40,
                  krylov: int = 20, restarts: int = 10, refine: int = 20, device: int = 0):
         self.model, self.kind = model, model.kind
         self.n = len(sites)
