@@ -18,6 +18,9 @@
  *   SparseLinAlgBackend        tk-linalg/src/traits.rs:190-205
  *   IterativeEigensolver       tk-dmrg/src/eigensolver/mod.rs:22-55
  *   LanczosSolver              tk-dmrg/src/eigensolver/mod.rs:58-164
+ *   DavidsonSolver             tk-dmrg/src/eigensolver/mod.rs:299-601
+ *   exp_krylov_f64             tk-dmrg/src/tdvp/mod.rs:197-396
+ *   contract_left/right_environment  tk-dmrg/src/environments/mod.rs:221-483
  *   LinAlgError / DmrgError    tk-linalg/src/error.rs:5-39, tk-dmrg/src/error.rs:9-59
  */
 #ifndef TK_HEFF_H
