@@ -1,6 +1,7 @@
 // gemm_fp64.cu -- FP64 sector-GEMM path of the two-site H_eff.
 //
-// grouped_gemm_f64: one CTA per 64x64 output tile.  A tile's task is one
+// grouped_gemm_f64: one CTA per output tile (64, 32 or 16 square, chosen per
+// task by the host so small sector blocks are not padded).  A tile's task is one
 // output block; its K dimension is a list of segments (one per contributing
 // sector pair), accumulated in registers, so every output element is written
 // exactly once and no atomics are needed.  Operand tiles are staged through
@@ -20,51 +21,46 @@ namespace tk {
 
 namespace {
 
-constexpr int BM = kF64TileM;
-constexpr int BN = kF64TileN;
 constexpr int BK = 16;
-constexpr int NT = 256;  // 16 x 16 threads, 4 x 4 outputs each
+constexpr int NT = 256;  // 16 x 16 threads
 
-__global__ void __launch_bounds__(NT) grouped_gemm_f64_kernel(const GemmTile* __restrict__ tiles, int n_tiles,
-                                                              const GemmTask* __restrict__ tasks,
-                                                              const GemmSeg* __restrict__ segs,
-                                                              const double* __restrict__ A,
-                                                              const double* __restrict__ B,
-                                                              double* __restrict__ C) {
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
-    const int tile_id = blockIdx.x;
-    if (tile_id >= n_tiles) return;
-    const GemmTile tile = tiles[tile_id];
-    const GemmTask task = tasks[tile.task];
+// One E x E output tile (E = 64, 32 or 16): thread (tx, ty) owns the
+// (E/16) x (E/16) outputs (ty + 16 i, tx + 16 j).  Every output sums its
+// segments in order and k ascending inside each, whatever E is, so the tile
+// edge does not change the result.
+template <int E>
+__device__ __forceinline__ void gemm_tile(const GemmTile& tile, const GemmTask& task, const GemmSeg* __restrict__ segs,
+                                          const double* __restrict__ A, const double* __restrict__ B,
+                                          double* __restrict__ C, double (*As)[65], double (*Bs)[65]) {
+    constexpr int R = E / 16;
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    double acc[4][4];
+    double acc[R][R];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < R; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < R; ++j) acc[i][j] = 0.0;
 
     for (int s = task.seg_begin; s < task.seg_end; ++s) {
         const GemmSeg sg = segs[s];
         for (int k0 = 0; k0 < sg.K; k0 += BK) {
-            // A tile: BM x BK
+            // A tile: E x BK
 #pragma unroll
-            for (int r = 0; r < (BM * BK) / NT; ++r) {
+            for (int r = 0; r < (E * BK) / NT; ++r) {
                 int e = tid + r * NT;
                 int m, k;
-                if (sg.a_cs == 1) { k = e % BK; m = e / BK; } else { m = e % BM; k = e / BM; }
+                if (sg.a_cs == 1) { k = e % BK; m = e / BK; } else { m = e % E; k = e / E; }
                 int gm = tile.m0 + m, gk = k0 + k;
                 double v = 0.0;
                 if (gm < task.M && gk < sg.K) v = A[sg.a_off + (int64_t)gm * sg.a_rs + (int64_t)gk * sg.a_cs];
                 As[k][m] = v;
             }
-            // B tile: BK x BN
+            // B tile: BK x E
 #pragma unroll
-            for (int r = 0; r < (BK * BN) / NT; ++r) {
+            for (int r = 0; r < (BK * E) / NT; ++r) {
                 int e = tid + r * NT;
                 int k, n;
-                if (sg.b_cs == 1) { n = e % BN; k = e / BN; } else { k = e % BK; n = e / BK; }
+                if (sg.b_cs == 1) { n = e % E; k = e / E; } else { k = e % BK; n = e / BK; }
                 int gn = tile.n0 + n, gk = k0 + k;
                 double v = 0.0;
                 if (gn < task.N && gk < sg.K) v = B[sg.b_off + (int64_t)gk * sg.b_rs + (int64_t)gn * sg.b_cs];
@@ -73,25 +69,25 @@ __global__ void __launch_bounds__(NT) grouped_gemm_f64_kernel(const GemmTile* __
             __syncthreads();
 #pragma unroll
             for (int k = 0; k < BK; ++k) {
-                double a[4], b[4];
+                double a[R], b[R];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) a[i] = As[k][ty + 16 * i];
+                for (int i = 0; i < R; ++i) a[i] = As[k][ty + 16 * i];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) b[j] = Bs[k][tx + 16 * j];
+                for (int j = 0; j < R; ++j) b[j] = Bs[k][tx + 16 * j];
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
+                for (int i = 0; i < R; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                    for (int j = 0; j < R; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
             }
             __syncthreads();
         }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < R; ++i) {
         int gm = tile.m0 + ty + 16 * i;
         if (gm >= task.M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < R; ++j) {
             int gn = tile.n0 + tx + 16 * j;
             if (gn >= task.N) continue;
             double* c = C + task.c_off + (int64_t)gm * task.c_rs + (int64_t)gn * task.c_cs;
@@ -99,6 +95,25 @@ __global__ void __launch_bounds__(NT) grouped_gemm_f64_kernel(const GemmTile* __
             if (task.beta != 0.0) v += task.beta * *c;
             *c = v;
         }
+    }
+}
+
+__global__ void __launch_bounds__(NT) grouped_gemm_f64_kernel(const GemmTile* __restrict__ tiles, int n_tiles,
+                                                              const GemmTask* __restrict__ tasks,
+                                                              const GemmSeg* __restrict__ segs,
+                                                              const double* __restrict__ A,
+                                                              const double* __restrict__ B,
+                                                              double* __restrict__ C) {
+    __shared__ double As[BK][65];
+    __shared__ double Bs[BK][65];
+    const int tile_id = blockIdx.x;
+    if (tile_id >= n_tiles) return;
+    const GemmTile tile = tiles[tile_id];
+    const GemmTask task = tasks[tile.task];
+    switch (tile.cls) {  // block-uniform
+    case 1: gemm_tile<32>(tile, task, segs, A, B, C, As, Bs); break;
+    case 2: gemm_tile<16>(tile, task, segs, A, B, C, As, Bs); break;
+    default: gemm_tile<64>(tile, task, segs, A, B, C, As, Bs); break;
     }
 }
 

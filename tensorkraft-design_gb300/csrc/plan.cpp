@@ -253,10 +253,27 @@ static void add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n, const s
     gemm_add_tiles(g, task_id, tile_m, tile_n);
 }
 
+int gemm_tile_class(int M, int N) {
+    // square tiles of edge 64 >> cls; cost = tiles x (area + a fixed per-tile share)
+    int best = 0;
+    double best_cost = 0.0;
+    for (int cls = 0; cls < kGemmTileClasses; ++cls) {
+        const int e = 64 >> cls;
+        const double cost = (double)((M + e - 1) / e) * ((N + e - 1) / e) * ((double)e * e + 256.0);
+        if (cls == 0 || cost < best_cost) {
+            best = cls;
+            best_cost = cost;
+        }
+    }
+    return best;
+}
+
 void gemm_add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n) {
     const GemmTask& t = g.tasks[task_id];
-    for (int m0 = 0; m0 < t.M; m0 += tile_m)
-        for (int n0 = 0; n0 < t.N; n0 += tile_n) g.tiles.push_back({task_id, m0, n0, 0});
+    const int cls = (tile_m == 64 && tile_n == 64) ? gemm_tile_class(t.M, t.N) : 0;
+    const int e = 64 >> cls;
+    for (int m0 = 0; m0 < t.M; m0 += e)
+        for (int n0 = 0; n0 < t.N; n0 += e) g.tiles.push_back({task_id, m0, n0, cls});
 }
 
 static void lpt_order(GemmTable& g, int tile_m, int tile_n) { gemm_lpt_order(g, tile_m, tile_n); }
@@ -268,7 +285,8 @@ void gemm_lpt_order(GemmTable& g, int tile_m, int tile_n) {
         for (int s = g.tasks[t].seg_begin; s < g.tasks[t].seg_end; ++s) ktot[t] += g.segs[s].K;
     auto cost = [&](const GemmTile& x) {
         const GemmTask& t = g.tasks[x.task];
-        double rm = std::min(tile_m, t.M - x.m0), rn = std::min(tile_n, t.N - x.n0);
+        const int e = std::min(tile_m, 64 >> x.cls);
+        double rm = std::min(e, t.M - x.m0), rn = std::min(std::min(tile_n, 64 >> x.cls), t.N - x.n0);
         return (ktot[x.task] + 1.0) * rm * rn;
     };
     std::stable_sort(g.tiles.begin(), g.tiles.end(),
@@ -280,6 +298,7 @@ void gemm_lpt_order(GemmTable& g, int tile_m, int tile_n) {
 bool gemm_table_ok(const GemmTable& g, int64_t na, int64_t nb, int64_t nc, const char* name, std::string& err) {
         for (const GemmTile& tl : g.tiles) {
             if (tl.task < 0 || (size_t)tl.task >= g.tasks.size()) { err = std::string(name) + ": tile task"; return false; }
+            if (tl.cls < 0 || tl.cls >= kGemmTileClasses) { err = std::string(name) + ": tile class"; return false; }
             const GemmTask& t = g.tasks[tl.task];
             if (tl.m0 < 0 || tl.m0 >= t.M || tl.n0 < 0 || tl.n0 >= t.N) { err = std::string(name) + ": tile origin"; return false; }
         }

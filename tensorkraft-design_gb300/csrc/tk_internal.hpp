@@ -84,9 +84,12 @@ struct GemmTask {
     int32_t seg_begin, seg_end;
     double alpha, beta;
 };
+// A tile is a square of edge 64 >> cls (cls 0: 64, 1: 32, 2: 16), chosen per
+// task so small sector blocks are not padded to 64 x 64.
 struct GemmTile {
-    int32_t task, m0, n0, pad;
+    int32_t task, m0, n0, cls;
 };
+constexpr int kGemmTileClasses = 3;
 // Channel combine (W_i*W_j applied between the two GEMM stages):
 //   out[out_off + r*out_rs + c] = sum_t coef_t * in[in_off_t + r*in_rs_t + c]
 struct CombJob {
@@ -111,7 +114,11 @@ struct GemmTable {
     std::vector<GemmTile> tiles;
     double flops = 0.0;
 };
-// Appends the (tile_m x tile_n) output tiles of task `task_id`.
+// Tile class of an M x N task: the edge (64, 32 or 16) with the least
+// padded area plus a fixed per-tile share.
+int gemm_tile_class(int M, int N);
+// Appends the output tiles of task `task_id`; with tile_m = tile_n = 64 the
+// edge comes from gemm_tile_class, otherwise 64 x 64 tiles.
 void gemm_add_tiles(GemmTable& g, int task_id, int tile_m, int tile_n);
 // Orders tiles heaviest first (rows x cols x total K), stable.
 void gemm_lpt_order(GemmTable& g, int tile_m, int tile_n);
