@@ -310,6 +310,34 @@ void tk_bst_free(tk_bst_out* t);
 tk_status tk_spmv_f64(tk_ctx* ctx, const tk_bst* a, const double* x, double* y);
 
 /*
+ * Complex (planar) variants for real-time evolution: build_heff_two_site and
+ * the environment contractions are generic over the scalar type in the
+ * reference (T = C64 included); here complex environments and vectors are
+ * stored as separate real and imaginary arrays in the same layouts, and each
+ * complex sector GEMM runs as four real grouped GEMMs over the same tables.
+ * FP64 only.  The MPO stays real.
+ *   tk_heff2_plan_create_dev_complex: as tk_heff2_plan_create_dev with the
+ *     imaginary parts of both environments (device, canonical layout).
+ *   tk_heff2_apply_complex: y = H_eff x on planar device vectors.
+ *   tk_env_grow_left/right_complex: the contractions with conj(A) on the bra.
+ *   tk_heff2_two_site_product_complex: psi = A_i A_j.
+ * tk_expm_krylov on a complex plan treats its input as complex (v_im may be
+ * NULL for a zero imaginary part) and needs out_im.
+ */
+tk_status tk_heff2_plan_create_dev_complex(tk_ctx* ctx, const tk_env* env_l, const double* env_l_im,
+                                           const tk_env* env_r, const double* env_r_im, const tk_bst* w_i,
+                                           const tk_bst* w_j, const int32_t* psi_flux, tk_heff2_plan** out);
+tk_status tk_heff2_apply_complex(tk_heff2_plan* plan, const double* x_re, const double* x_im, double* y_re,
+                                 double* y_im, void* stream);
+tk_status tk_env_grow_left_complex(tk_ctx* ctx, const tk_env* env_l, const double* env_l_im, const tk_bst* a,
+                                   const double* a_im, const tk_bst* w, double* out_re, double* out_im, void* stream);
+tk_status tk_env_grow_right_complex(tk_ctx* ctx, const tk_env* env_r, const double* env_r_im, const tk_bst* a,
+                                    const double* a_im, const tk_bst* w, double* out_re, double* out_im, void* stream);
+tk_status tk_heff2_two_site_product_complex(tk_heff2_plan* plan, const tk_bst* a_i, const double* a_i_im,
+                                            const tk_bst* a_j, const double* a_j_im, double* psi_re, double* psi_im,
+                                            void* stream);
+
+/*
  * Self-check, no reference counterpart: the split-precision kernels convert
  * fp64 <-> fp32 from the IEEE 754 bit layouts on the integer pipes (the FP64
  * pipe of this GPU is narrow).  Compares those conversions with the hardware

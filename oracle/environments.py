@@ -21,3 +21,12 @@ def grow_left(L, A, W):
 def grow_right(R, A, W):
     """R: (Db, v, Db); A: (d, Da, Db); W: (d, d, w, v) -> (Da, w, Da)."""
     return np.einsum("txp,pvb,stwv,sab->xwa", A.conj(), R, W, A, optimize=True)
+
+
+def heff_single_site_dense(L, W, R):
+    """Dense single-site H_eff of build_heff_single_site (environments/mod.rs:603-678):
+    H[(s', a', b'), (s, a, b)] = sum L[a', w, a] W[s, s', w, v] R[b', v, b],
+    rows and columns in the (s, a_L, a_R) row-major layout."""
+    d, Da, Db = W.shape[0], L.shape[0], R.shape[0]
+    H = np.einsum("pwa,stwv,qvb->tpqsab", L, W, R, optimize=True)
+    return H.reshape(d * Da * Db, d * Da * Db)

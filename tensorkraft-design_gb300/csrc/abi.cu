@@ -203,6 +203,10 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision) {
         set_error("tk_heff2_set_precision: unknown precision");
         return TK_ERR_INVALID_ARG;
     }
+    if (plan->is_complex) {
+        set_error("tk_heff2_set_precision: complex plans run in FP64 only");
+        return TK_ERR_UNSUPPORTED;
+    }
     DeviceGuard g(plan->device);
     if (!plan->tc) {
         std::string err;
@@ -243,6 +247,34 @@ static tk_status apply_fp64(tk_heff2_plan* p, const double* x, double* y, cudaSt
     return TK_OK;
 }
 
+// The complex FP64 matvec: each stage's GEMM as four real launches over the
+// same tables (planar operands); the channel combine (real MPO) on each part.
+tk_status tk_heff2_apply_complex_s(tk_heff2_plan* p, const double* xr, const double* xi, double* yr, double* yi,
+                                   cudaStream_t s) {
+    if (!p->is_complex) {
+        set_error("complex matvec on a real plan");
+        return TK_ERR_INVALID_ARG;
+    }
+    TK_CUDA(launch_gemm_c64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p, p->lbuf_im.p, xr, xi,
+                            p->t1.p, p->t1_im.p, false, s));
+    TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
+    TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1_im.p, p->t2_im.p, s));
+    TK_CUDA(launch_gemm_c64(p->g3.tiles.p, p->g3.n_tiles, p->g3.tasks.p, p->g3.segs.p, p->t2.p, p->t2_im.p, p->rbuf.p,
+                            p->rbuf_im.p, yr, yi, false, s));
+    return TK_OK;
+}
+
+tk_status tk_heff2_apply_complex(tk_heff2_plan* plan, const double* xr, const double* xi, double* yr, double* yi,
+                                 void* stream) {
+    if (!plan || ((!xr || !xi || !yr || !yi) && plan->host.total > 0)) {
+        set_error("tk_heff2_apply_complex: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (plan->host.total == 0) return TK_OK;
+    DeviceGuard g(plan->device);
+    return tk_heff2_apply_complex_s(plan, xr, xi, yr, yi, (cudaStream_t)stream);
+}
+
 tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
     if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK)) {
         set_error("tk_heff2_set_schedule: invalid argument");
@@ -253,6 +285,10 @@ tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
 }
 
 tk_status tk_heff2_apply_prec(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s, int precision) {
+    if (p->is_complex) {
+        set_error("real matvec on a complex plan (use tk_heff2_apply_complex)");
+        return TK_ERR_INVALID_ARG;
+    }
     if (precision == TK_PREC_BF16X3) {
         std::string err;
         cudaError_t e = tc_apply(*p->tc, p->host, p->jobs.p, p->n_jobs, p->terms.p, x, y, s, err);

@@ -670,10 +670,11 @@ __global__ void expm_assemble_kernel(double* __restrict__ out_re, double* __rest
     }
 }
 
-// exp(alpha H) v for the plan's (real symmetric) H and a real or complex v:
-// Lanczos with full re-orthogonalisation on the real vector v~ = v (nc = 1)
-// or (Re v; Im v) (nc = 2, H applied to each half), whose recurrence
-// coefficients are those of the complex Lanczos process; exp(alpha T_m) e_1
+// exp(alpha H) v for the plan's H and a real or complex v: Lanczos with full
+// re-orthogonalisation on the real vector v~ = v (nc = 1) or (Re v; Im v)
+// (nc = 2; a real H acts on each half, a complex Hermitian H as the real
+// symmetric [[Re H, -Im H], [Im H, Re H]]), whose recurrence coefficients are
+// those of the complex Lanczos process; exp(alpha T_m) e_1
 // from the eigendecomposition of the tridiagonal T_m (any complex alpha);
 // result = sum_k c_k V_k with complex c_k.
 tk_status expm_run(tk_heff2_plan* p, const Ws& ws, int nc, int64_t n, int m, double tol, double are, double aim,
@@ -684,8 +685,11 @@ tk_status expm_run(tk_heff2_plan* p, const Ws& ws, int nc, int64_t n, int m, dou
     tk_status st;
     if ((e = cudaMemcpyAsync(ws.V, vre, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
         return cuda_fail("cudaMemcpyAsync", e);
-    if (nc == 2 && (e = cudaMemcpyAsync(ws.V + n, vim, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
-        return cuda_fail("cudaMemcpyAsync", e);
+    if (nc == 2) {
+        e = vim ? cudaMemcpyAsync(ws.V + n, vim, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)
+                : cudaMemsetAsync(ws.V + n, 0, sizeof(double) * n, s);
+        if (e != cudaSuccess) return cuda_fail("cudaMemcpyAsync", e);
+    }
     if ((e = multidot(ws, ws.V, nn, 1, ws.V, MISC(ws), 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
     double beta0 = 0.0;
     if ((st = read_scalar(MISC(ws), &beta0, s)) != TK_OK) return st;
@@ -698,9 +702,14 @@ tk_status expm_run(tk_heff2_plan* p, const Ws& ws, int nc, int64_t n, int m, dou
     normalize_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V, ws.V, MISC(ws), nn);
     for (int j = 0; j < m; ++j) {
         double* vj = ws.V + (int64_t)j * nn;
-        for (int h = 0; h < nc; ++h)
-            if ((st = tk_heff2_apply_prec(p, vj + h * n, ws.w + h * n, s, p->precision)) != TK_OK) return st;
-        res->matvec_count += nc;
+        if (p->is_complex) {  // complex Hermitian H on (re; im): one complex matvec
+            if ((st = tk_heff2_apply_complex_s(p, vj, vj + n, ws.w, ws.w + n, s)) != TK_OK) return st;
+            res->matvec_count += 1;
+        } else {  // real H: each half on its own
+            for (int h = 0; h < nc; ++h)
+                if ((st = tk_heff2_apply_prec(p, vj + h * n, ws.w + h * n, s, p->precision)) != TK_OK) return st;
+            res->matvec_count += nc;
+        }
         if ((e = multidot(ws, vj, nn, 1, ws.w, ALPHA(ws) + j, 0, s)) != cudaSuccess) return cuda_fail("multidot", e);
         axpy2_kernel<<<vgrid(nn), 256, 0, s>>>(ws.w, vj, ALPHA(ws) + j, j > 0 ? ws.V + (int64_t)(j - 1) * nn : nullptr,
                                                 j > 0 ? BETA(ws) + (j - 1) : nullptr, nn);
@@ -762,7 +771,7 @@ extern "C" tk_status tk_expm_krylov(tk_heff2_plan* p, const tk_expm_cfg* cfg, do
         return TK_ERR_INVALID_ARG;
     }
     *res = tk_expm_result{};
-    const bool cplx = v_im != nullptr;
+    const bool cplx = v_im != nullptr || p->is_complex;
     if (!out_im && (cplx || alpha_im != 0.0)) {
         set_error("tk_expm_krylov: a complex result needs out_im");
         return TK_ERR_INVALID_ARG;

@@ -67,13 +67,36 @@ tk_status launch_table(Scratch& sc, const GemmTable& g, const double* A, const d
     return TK_OK;
 }
 
+// A GEMM table uploaded to stream-ordered scratch.
+struct DevTable {
+    GemmTask* t = nullptr;
+    GemmSeg* sg = nullptr;
+    GemmTile* tl = nullptr;
+    int n = 0;
+    tk_status upload(Scratch& sc, const GemmTable& g) {
+        cudaError_t e;
+        if ((e = sc.upload(g.tasks, &t)) != cudaSuccess || (e = sc.upload(g.segs, &sg)) != cudaSuccess ||
+            (e = sc.upload(g.tiles, &tl)) != cudaSuccess)
+            return cuda_fail("upload tables", e);
+        n = (int)g.tiles.size();
+        return TK_OK;
+    }
+};
+
 bool env_legs(int kind, const tk_env& e, QIndex& bra, QIndex& mpo, QIndex& ket, std::string& err) {
     return qindex_from_abi(kind, e.bra, bra, err) && qindex_from_abi(kind, e.mpo, mpo, err) &&
            qindex_from_abi(kind, e.ket, ket, err);
 }
 
+// env_im / a_im / out_im non-null: complex (planar) environment growth.
 tk_status grow(const char* name, bool left, tk_ctx* ctx, const tk_env* env, const tk_bst* a, const tk_bst* w,
-               double* out, void* stream) {
+               double* out, void* stream, const double* env_im = nullptr, const double* a_im = nullptr,
+               double* out_im = nullptr) {
+    const bool cplx = env_im || a_im || out_im;
+    if (cplx && !(env_im && a_im && out_im)) {
+        set_error(std::string(name) + ": complex growth needs every imaginary part");
+        return TK_ERR_INVALID_ARG;
+    }
     if (!ctx || !env || !a || !w || !out) {
         set_error(std::string(name) + ": null argument");
         return TK_ERR_INVALID_ARG;
@@ -109,23 +132,46 @@ tk_status grow(const char* name, bool left, tk_ctx* ctx, const tk_env* env, cons
     cudaStream_t s = (cudaStream_t)stream;
     Scratch sc(s);
     cudaError_t e;
+    const size_t parts = cplx ? 2 : 1;
     double *t1 = nullptr, *t2 = nullptr;
-    if ((e = sc.alloc(sizeof(double) * (size_t)G.t1_total, (void**)&t1)) != cudaSuccess) return cuda_fail("scratch", e);
-    if ((e = sc.alloc(sizeof(double) * (size_t)G.t2_total, (void**)&t2)) != cudaSuccess) return cuda_fail("scratch", e);
+    if ((e = sc.alloc(sizeof(double) * parts * (size_t)G.t1_total, (void**)&t1)) != cudaSuccess)
+        return cuda_fail("scratch", e);
+    if ((e = sc.alloc(sizeof(double) * parts * (size_t)G.t2_total, (void**)&t2)) != cudaSuccess)
+        return cuda_fail("scratch", e);
     if ((e = cudaMemsetAsync(out, 0, sizeof(double) * (size_t)G.out_total, s)) != cudaSuccess)
         return cuda_fail("cudaMemsetAsync", e);
-    if (left)
-        st = launch_table(sc, G.g1, env->data, A.data, t1);
-    else
-        st = launch_table(sc, G.g1, A.data, env->data, t1);
-    if (st != TK_OK) return st;
+    if (cplx && (e = cudaMemsetAsync(out_im, 0, sizeof(double) * (size_t)G.out_total, s)) != cudaSuccess)
+        return cuda_fail("cudaMemsetAsync", e);
     CombJob* jobs = nullptr;
     CombTerm* terms = nullptr;
     if ((e = sc.upload(G.jobs, &jobs)) != cudaSuccess) return cuda_fail("upload tables", e);
     if ((e = sc.upload(G.terms, &terms)) != cudaSuccess) return cuda_fail("upload tables", e);
-    if ((e = launch_combine_f64(jobs, (int)G.jobs.size(), terms, t1, t2, s)) != cudaSuccess)
+    if (!cplx) {
+        if (left)
+            st = launch_table(sc, G.g1, env->data, A.data, t1);
+        else
+            st = launch_table(sc, G.g1, A.data, env->data, t1);
+        if (st != TK_OK) return st;
+        if ((e = launch_combine_f64(jobs, (int)G.jobs.size(), terms, t1, t2, s)) != cudaSuccess)
+            return cuda_fail("combine", e);
+        return launch_table(sc, G.g3, A.data, t2, out);
+    }
+    // complex: stage 1 without conjugation, stage 3 with the bra (site operand) conjugated
+    double* t1i = t1 + G.t1_total;
+    double* t2i = t2 + G.t2_total;
+    DevTable g1, g3;
+    if ((st = g1.upload(sc, G.g1)) != TK_OK || (st = g3.upload(sc, G.g3)) != TK_OK) return st;
+    if (left)
+        e = launch_gemm_c64(g1.tl, g1.n, g1.t, g1.sg, env->data, env_im, A.data, a_im, t1, t1i, false, s);
+    else
+        e = launch_gemm_c64(g1.tl, g1.n, g1.t, g1.sg, A.data, a_im, env->data, env_im, t1, t1i, false, s);
+    if (e != cudaSuccess) return cuda_fail("grouped gemm", e);
+    if ((e = launch_combine_f64(jobs, (int)G.jobs.size(), terms, t1, t2, s)) != cudaSuccess ||
+        (e = launch_combine_f64(jobs, (int)G.jobs.size(), terms, t1i, t2i, s)) != cudaSuccess)
         return cuda_fail("combine", e);
-    return launch_table(sc, G.g3, A.data, t2, out);
+    if ((e = launch_gemm_c64(g3.tl, g3.n, g3.t, g3.sg, A.data, a_im, t2, t2i, out, out_im, true, s)) != cudaSuccess)
+        return cuda_fail("grouped gemm", e);
+    return TK_OK;
 }
 
 }  // namespace
@@ -215,6 +261,77 @@ tk_status tk_env_grow_left(tk_ctx* ctx, const tk_env* env_l, const tk_bst* a, co
 tk_status tk_env_grow_right(tk_ctx* ctx, const tk_env* env_r, const tk_bst* a, const tk_bst* w, double* out_dev,
                             void* stream) {
     return grow("tk_env_grow_right", false, ctx, env_r, a, w, out_dev, stream);
+}
+
+tk_status tk_env_grow_left_complex(tk_ctx* ctx, const tk_env* env_l, const double* env_l_im, const tk_bst* a,
+                                   const double* a_im, const tk_bst* w, double* out_re, double* out_im, void* stream) {
+    return grow("tk_env_grow_left_complex", true, ctx, env_l, a, w, out_re, stream, env_l_im, a_im, out_im);
+}
+
+tk_status tk_env_grow_right_complex(tk_ctx* ctx, const tk_env* env_r, const double* env_r_im, const tk_bst* a,
+                                    const double* a_im, const tk_bst* w, double* out_re, double* out_im, void* stream) {
+    return grow("tk_env_grow_right_complex", false, ctx, env_r, a, w, out_re, stream, env_r_im, a_im, out_im);
+}
+
+tk_status tk_heff2_plan_create_dev_complex(tk_ctx* ctx, const tk_env* env_l, const double* env_l_im,
+                                           const tk_env* env_r, const double* env_r_im, const tk_bst* w_i,
+                                           const tk_bst* w_j, const int32_t* psi_flux, tk_heff2_plan** out) {
+    if (!env_l_im || !env_r_im) {
+        set_error("tk_heff2_plan_create_dev_complex: null imaginary part");
+        return TK_ERR_INVALID_ARG;
+    }
+    tk_status st = tk_heff2_plan_create_dev(ctx, env_l, env_r, w_i, w_j, psi_flux, TK_PREC_FP64, out);
+    if (st != TK_OK) return st;
+    tk_heff2_plan* p = *out;
+    Guard g(p->device);
+    cudaError_t e;
+    const size_t nl = p->lbuf.n, nr = p->rbuf.n;
+    if ((e = p->lbuf_im.alloc(nl)) != cudaSuccess || (e = p->rbuf_im.alloc(nr)) != cudaSuccess ||
+        (e = p->t1_im.alloc(std::max<size_t>(p->t1.n, 1))) != cudaSuccess ||
+        (e = p->t2_im.alloc(std::max<size_t>(p->t2.n, 1))) != cudaSuccess ||
+        (nl && (e = cudaMemcpy(p->lbuf_im.p, env_l_im, sizeof(double) * nl, cudaMemcpyDeviceToDevice)) != cudaSuccess) ||
+        (nr && (e = cudaMemcpy(p->rbuf_im.p, env_r_im, sizeof(double) * nr, cudaMemcpyDeviceToDevice)) != cudaSuccess)) {
+        tk_heff2_plan_destroy(p);
+        *out = nullptr;
+        return cuda_fail("tk_heff2_plan_create_dev_complex", e);
+    }
+    p->is_complex = true;
+    return TK_OK;
+}
+
+tk_status tk_heff2_two_site_product_complex(tk_heff2_plan* plan, const tk_bst* a_i, const double* a_i_im,
+                                            const tk_bst* a_j, const double* a_j_im, double* psi_re, double* psi_im,
+                                            void* stream) {
+    if (!plan || !a_i || !a_j || !a_i_im || !a_j_im || !psi_re || !psi_im) {
+        set_error("tk_heff2_two_site_product_complex: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::string err;
+    Bst3 Ai, Aj;
+    if (!bst3_from_abi(*a_i, Ai, "A_i", err) || !bst3_from_abi(*a_j, Aj, "A_j", err)) {
+        set_error("tk_heff2_two_site_product_complex: " + err);
+        return TK_ERR_INVALID_ARG;
+    }
+    GemmTable gt;
+    tk_status st = build_product_tables(plan->host, Ai, Aj, gt, err);
+    if (st != TK_OK) {
+        set_error("tk_heff2_two_site_product_complex: " + err);
+        return st;
+    }
+    Guard gd(plan->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    const size_t n = (size_t)plan->host.total;
+    if ((e = cudaMemsetAsync(psi_re, 0, sizeof(double) * n, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(psi_im, 0, sizeof(double) * n, s)) != cudaSuccess)
+        return cuda_fail("cudaMemsetAsync", e);
+    Scratch sc(s);
+    DevTable g;
+    if ((st = g.upload(sc, gt)) != TK_OK) return st;
+    if ((e = launch_gemm_c64(g.tl, g.n, g.t, g.sg, Ai.data, a_i_im, Aj.data, a_j_im, psi_re, psi_im, false, s)) !=
+        cudaSuccess)
+        return cuda_fail("grouped gemm", e);
+    return TK_OK;
 }
 
 tk_status tk_heff2_two_site_product(tk_heff2_plan* plan, const tk_bst* a_i, const tk_bst* a_j, double* psi_dev,

@@ -31,7 +31,8 @@ constexpr int NT = 256;  // 16 x 16 threads
 template <int E>
 __device__ __forceinline__ void gemm_tile(const GemmTile& tile, const GemmTask& task, const GemmSeg* __restrict__ segs,
                                           const double* __restrict__ A, const double* __restrict__ B,
-                                          double* __restrict__ C, double (*As)[65], double (*Bs)[65]) {
+                                          double* __restrict__ C, double (*As)[65], double (*Bs)[65], double amul,
+                                          int accumulate) {
     constexpr int R = E / 16;
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
@@ -91,8 +92,11 @@ __device__ __forceinline__ void gemm_tile(const GemmTile& tile, const GemmTask& 
             int gn = tile.n0 + tx + 16 * j;
             if (gn >= task.N) continue;
             double* c = C + task.c_off + (int64_t)gm * task.c_rs + (int64_t)gn * task.c_cs;
-            double v = task.alpha * acc[i][j];
-            if (task.beta != 0.0) v += task.beta * *c;
+            double v = amul * task.alpha * acc[i][j];
+            if (accumulate)
+                v += *c;
+            else if (task.beta != 0.0)
+                v += task.beta * *c;
             *c = v;
         }
     }
@@ -103,7 +107,7 @@ __global__ void __launch_bounds__(NT) grouped_gemm_f64_kernel(const GemmTile* __
                                                               const GemmSeg* __restrict__ segs,
                                                               const double* __restrict__ A,
                                                               const double* __restrict__ B,
-                                                              double* __restrict__ C) {
+                                                              double* __restrict__ C, double amul, int accumulate) {
     __shared__ double As[BK][65];
     __shared__ double Bs[BK][65];
     const int tile_id = blockIdx.x;
@@ -111,9 +115,9 @@ __global__ void __launch_bounds__(NT) grouped_gemm_f64_kernel(const GemmTile* __
     const GemmTile tile = tiles[tile_id];
     const GemmTask task = tasks[tile.task];
     switch (tile.cls) {  // block-uniform
-    case 1: gemm_tile<32>(tile, task, segs, A, B, C, As, Bs); break;
-    case 2: gemm_tile<16>(tile, task, segs, A, B, C, As, Bs); break;
-    default: gemm_tile<64>(tile, task, segs, A, B, C, As, Bs); break;
+    case 1: gemm_tile<32>(tile, task, segs, A, B, C, As, Bs, amul, accumulate); break;
+    case 2: gemm_tile<16>(tile, task, segs, A, B, C, As, Bs, amul, accumulate); break;
+    default: gemm_tile<64>(tile, task, segs, A, B, C, As, Bs, amul, accumulate); break;
     }
 }
 
@@ -148,10 +152,23 @@ __global__ void start_vector_kernel(double* v, int64_t n) {
 }  // namespace
 
 cudaError_t launch_gemm_f64(const GemmTile* tiles, int n_tiles, const GemmTask* tasks, const GemmSeg* segs,
-                            const double* A, const double* B, double* C, cudaStream_t s) {
+                            const double* A, const double* B, double* C, cudaStream_t s, double amul,
+                            bool accumulate) {
     if (n_tiles <= 0) return cudaSuccess;
-    grouped_gemm_f64_kernel<<<n_tiles, NT, 0, s>>>(tiles, n_tiles, tasks, segs, A, B, C);
+    grouped_gemm_f64_kernel<<<n_tiles, NT, 0, s>>>(tiles, n_tiles, tasks, segs, A, B, C, amul, accumulate ? 1 : 0);
     return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_c64(const GemmTile* tiles, int n_tiles, const GemmTask* tasks, const GemmSeg* segs,
+                            const double* Ar, const double* Ai, const double* Br, const double* Bi, double* Cr,
+                            double* Ci, bool conj_a, cudaStream_t s) {
+    // (Ar + i Ai)^(*) (Br + i Bi): re = Ar Br -+ Ai Bi, im = Ar Bi +- Ai Br
+    const double si = conj_a ? 1.0 : -1.0;
+    cudaError_t e;
+    if ((e = launch_gemm_f64(tiles, n_tiles, tasks, segs, Ar, Br, Cr, s, 1.0, false)) != cudaSuccess) return e;
+    if ((e = launch_gemm_f64(tiles, n_tiles, tasks, segs, Ai, Bi, Cr, s, si, true)) != cudaSuccess) return e;
+    if ((e = launch_gemm_f64(tiles, n_tiles, tasks, segs, Ar, Bi, Ci, s, 1.0, false)) != cudaSuccess) return e;
+    return launch_gemm_f64(tiles, n_tiles, tasks, segs, Ai, Br, Ci, s, -si, true);
 }
 
 cudaError_t launch_combine_f64(const CombJob* jobs, int n_jobs, const CombTerm* terms, const double* in,

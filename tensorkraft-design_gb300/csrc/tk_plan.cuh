@@ -74,6 +74,9 @@ struct tk_heff2_plan {
     int schedule = TK_SCHED_GROUPED;
     tk::Heff2Tables host;
     tk::DevBuf<double> lbuf, rbuf, t1, t2;
+    // complex environments (planar): imaginary parts of the slabs and intermediates
+    bool is_complex = false;
+    tk::DevBuf<double> lbuf_im, rbuf_im, t1_im, t2_im;
     tk::DevGemm g1, g3;
     tk::DevBuf<tk::CombJob> jobs;
     tk::DevBuf<tk::CombTerm> terms;
@@ -105,6 +108,9 @@ struct tk_heff2_plan {
 
 // Dispatches one matvec in the requested precision (stream-ordered).
 extern "C" tk_status tk_heff2_apply_prec(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s, int precision);
+// The complex FP64 matvec of a complex plan on planar vectors (stream-ordered).
+extern "C" tk_status tk_heff2_apply_complex_s(tk_heff2_plan* p, const double* xr, const double* xi, double* yr,
+                                              double* yi, cudaStream_t s);
 
 namespace tk {
 tk_status cuda_fail(const char* op, cudaError_t e);

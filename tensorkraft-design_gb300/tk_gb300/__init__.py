@@ -5,9 +5,9 @@ the host-side mirror of the reference's types and the ctypes binding.
 """
 from . import _abi, symmetry
 from ._abi import PREC_BF16X3, PREC_FP64, TkError
-from .heff import (DavidsonSolver, EigenResult, Environment, Heff2Plan, LanczosSolver, MPO, build_heff_two_site,
-                   context)
+from .heff import (DavidsonSolver, EigenResult, Environment, Heff2Plan, LanczosSolver, MPO, build_heff_single_site,
+                   build_heff_two_site, context)
 from .symmetry import QIndex, BlockSparseTensor
 
 __all__ = ["PREC_FP64", "PREC_BF16X3", "TkError", "Environment", "MPO", "Heff2Plan", "LanczosSolver", "DavidsonSolver",
-           "EigenResult", "build_heff_two_site", "QIndex", "BlockSparseTensor", "context", "symmetry", "_abi"]
+           "EigenResult", "build_heff_two_site", "build_heff_single_site", "QIndex", "BlockSparseTensor", "context", "symmetry", "_abi"]

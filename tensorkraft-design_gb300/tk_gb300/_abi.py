@@ -115,6 +115,16 @@ SIGNATURES = [
     ("tk_block_gemm_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.POINTER(tk_bst_out)]),
     ("tk_bst_free", None, [C.POINTER(tk_bst_out)]),
     ("tk_spmv_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("tk_heff2_plan_create_dev_complex", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.c_void_p, C.POINTER(tk_env),
+                                                     C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst),
+                                                     C.POINTER(C.c_int32), C.POINTER(C.c_void_p)]),
+    ("tk_heff2_apply_complex", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("tk_env_grow_left_complex", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.c_void_p, C.POINTER(tk_bst),
+                                             C.c_void_p, C.POINTER(tk_bst), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("tk_env_grow_right_complex", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.c_void_p, C.POINTER(tk_bst),
+                                              C.c_void_p, C.POINTER(tk_bst), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("tk_heff2_two_site_product_complex", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.c_void_p, C.POINTER(tk_bst),
+                                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("tk_check_split_conversions", C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_uint64)]),
     ("tk_env_layout", C.c_int32, [C.c_int32, C.POINTER(tk_qindex), C.POINTER(tk_qindex), C.POINTER(tk_qindex),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_uint64), C.POINTER(C.c_int64),

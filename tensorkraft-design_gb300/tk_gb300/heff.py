@@ -4,6 +4,7 @@ Python mirror of (kyungminlee/tensorkraft-design):
   Environment              tk-dmrg/src/environments/mod.rs:24-103  dense (bra, w, ket)
   MPO                      tk-dmrg/src/mpo/mod.rs:36-93             legs (s_in, s_out, w_L, w_R)
   build_heff_two_site      tk-dmrg/src/environments/mod.rs:491-602  -> (matvec closure, dim)
+  build_heff_single_site   tk-dmrg/src/environments/mod.rs:603-678  -> (matvec closure, dim)
   LanczosSolver            tk-dmrg/src/eigensolver/mod.rs:58-164
   DavidsonSolver           tk-dmrg/src/eigensolver/mod.rs:299-517
   EigenResult              tk-dmrg/src/eigensolver/mod.rs:22-33
@@ -154,8 +155,35 @@ class Heff2Plan:
         self._finish(h, device, precision)
         return self
 
+    @classmethod
+    def from_device_envs_complex(cls, env_l, env_r, w_i: BlockSparseTensor, w_j: BlockSparseTensor, psi_flux,
+                                 device: int = 0) -> "Heff2Plan":
+        """tk_heff2_plan_create_dev_complex: complex (planar) device environments, FP64."""
+        env_l, env_r = env_l.complexified(), env_r.complexified()
+        self = cls.__new__(cls)
+        self._lib = _abi.load()
+        m = _Marshal()
+        el, er = env_l.marshal(m), env_r.marshal(m)
+        bi, bj = m.bst(w_i), m.bst(w_j)
+        farr = np.array(list(psi_flux) + [0], dtype=np.int32)
+        h = C.c_void_p()
+        check(self._lib.tk_heff2_plan_create_dev_complex(context(device), C.byref(el),
+                                                         C.c_void_p(env_l.data_im.data_ptr()), C.byref(er),
+                                                         C.c_void_p(env_r.data_im.data_ptr()), C.byref(bi),
+                                                         C.byref(bj), _abi.i32ptr(farr), C.byref(h)))
+        self._finish(h, device, PREC_FP64)
+        self.is_complex = True
+        return self
+
+    def apply_complex(self, x_re, x_im, y_re, y_im, stream=None):
+        """y = H x on planar complex device vectors (complex plans)."""
+        s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
+        check(self._lib.tk_heff2_apply_complex(self._h, C.c_void_p(x_re.data_ptr()), C.c_void_p(x_im.data_ptr()),
+                                               C.c_void_p(y_re.data_ptr()), C.c_void_p(y_im.data_ptr()), s))
+
     def _finish(self, h, device, precision):
         self._h = h
+        self.is_complex = False
         self.device = device
         dd, bd, nb = C.c_int64(), C.c_int64(), C.c_int64()
         check(self._lib.tk_heff2_dims(h, C.byref(dd), C.byref(bd), C.byref(nb)))
@@ -251,7 +279,7 @@ class Heff2Plan:
 
         alpha = complex(alpha)
         out_re = torch.empty(self.block_dim, dtype=torch.float64, device=f"cuda:{self.device}")
-        cplx = v_im is not None or alpha.imag != 0.0
+        cplx = v_im is not None or alpha.imag != 0.0 or self.is_complex
         out_im = torch.empty_like(out_re) if cplx else None
         cfg = _abi.tk_expm_cfg(krylov_dim, tol)
         res = _abi.tk_expm_result()
@@ -288,6 +316,37 @@ def build_heff_two_site(env_l: Environment, env_r: Environment, mpo: MPO, sites:
     i, j = sites
     plan = Heff2Plan(env_l, env_r, mpo.site_tensor(i), mpo.site_tensor(j), psi_flux=psi_flux,
                      precision=precision, device=device)
+
+    def matvec(x, y):
+        plan.apply_host(x, y)
+
+    matvec.plan = plan
+    return matvec, plan.dense_dim
+
+
+def identity_mpo_site(wq: QIndex) -> BlockSparseTensor:
+    """MPO tensor of a dummy site of physical dimension 1 (zero charge) that passes
+    the channel through: W[0, 0, w, w'] = delta(w, w')."""
+    from .models import INCOMING, OUTGOING, dense_to_bst
+    from .symmetry import identity
+
+    zero = identity(wq.kind)
+    p1 = QIndex(wq.kind, [(zero, 1)])
+    W = np.eye(wq.total_dim).reshape(1, 1, wq.total_dim, wq.total_dim)
+    return dense_to_bst(wq.kind, W, [p1, p1, wq, wq], [INCOMING, OUTGOING, OUTGOING, INCOMING], zero)
+
+
+def build_heff_single_site(env_l: Environment, env_r: Environment, mpo: MPO, site: int, psi_flux=None,
+                           precision: int = PREC_FP64, device: int = 0):
+    """build_heff_single_site (environments/mod.rs:603-678): (matvec, dim) on dense host
+    vectors in the (s, a_L, a_R) layout, dim = d * D_L * D_R.
+
+    Runs as a two-site plan whose second site is a dummy of physical dimension 1
+    that passes the MPO channel through, so the two-site layout (s, 1, a_L, a_R)
+    is the single-site one."""
+    w = mpo.site_tensor(site)
+    plan = Heff2Plan(env_l, env_r, w, identity_mpo_site(w.indices[3]), psi_flux=psi_flux, precision=precision,
+                     device=device)
 
     def matvec(x, y):
         plan.apply_host(x, y)

@@ -36,7 +36,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import PREC_FP64, check
-from .heff import Heff2Plan, _Marshal, context
+from .heff import Heff2Plan, _Marshal, context, identity_mpo_site
 from .symmetry import QIndex, dual, fuse, identity, key_pack, key_unpack
 
 
@@ -67,19 +67,28 @@ def env_layout(kind: int, bra: QIndex, mpo: QIndex, ket: QIndex):
 class DeviceEnv:
     """Block-sparse environment (bra, mpo, ket) in the canonical layout, device data."""
 
-    def __init__(self, kind: int, bra: QIndex, mpo: QIndex, ket: QIndex, data):
+    def __init__(self, kind: int, bra: QIndex, mpo: QIndex, ket: QIndex, data, data_im=None):
         self.kind, self.bra, self.mpo, self.ket, self.data = kind, bra, mpo, ket, data
+        self.data_im = data_im  # imaginary part (same layout) of a complex environment, or None
+
+    @property
+    def is_complex(self):
+        return self.data_im is not None
 
     @classmethod
     def from_dense(cls, kind, dense: np.ndarray, bra: QIndex, mpo: QIndex, ket: QIndex, device: int = 0):
         keys, offs, total = env_layout(kind, bra, mpo, ket)
-        host = np.zeros(total)
+        host = np.zeros(total, dtype=np.complex128 if np.iscomplexobj(dense) else np.float64)
         for key, off in zip(keys, offs):
             qb, qw, qk = key_unpack(kind, int(key), 3)
             ob, ow, ok = bra.offset_of(qb), mpo.offset_of(qw), ket.offset_of(qk)
             db, dw, dk = bra.dim_of(qb), mpo.dim_of(qw), ket.dim_of(qk)
             host[off:off + db * dw * dk] = dense[ob:ob + db, ow:ow + dw, ok:ok + dk].reshape(-1)
-        return cls(kind, bra, mpo, ket, _torch().from_numpy(host).to(f"cuda:{device}"))
+        dev = f"cuda:{device}"
+        if np.iscomplexobj(host):
+            return cls(kind, bra, mpo, ket, _torch().from_numpy(host.real.copy()).to(dev),
+                       _torch().from_numpy(host.imag.copy()).to(dev))
+        return cls(kind, bra, mpo, ket, _torch().from_numpy(host).to(dev))
 
     @classmethod
     def boundary(cls, kind, bond: QIndex, mpo: QIndex, device: int = 0):
@@ -88,10 +97,17 @@ class DeviceEnv:
             raise ValueError("boundary environment needs one-dimensional bond and MPO legs")
         return cls.from_dense(kind, np.ones((1, 1, 1)), bond, mpo, bond, device)
 
+    def complexified(self) -> "DeviceEnv":
+        if self.is_complex:
+            return self
+        return DeviceEnv(self.kind, self.bra, self.mpo, self.ket, self.data, _torch().zeros_like(self.data))
+
     def to_dense(self) -> np.ndarray:
         keys, offs, total = env_layout(self.kind, self.bra, self.mpo, self.ket)
         host = self.data.cpu().numpy()
-        out = np.zeros((self.bra.total_dim, self.mpo.total_dim, self.ket.total_dim))
+        if self.is_complex:
+            host = host + 1j * self.data_im.cpu().numpy()
+        out = np.zeros((self.bra.total_dim, self.mpo.total_dim, self.ket.total_dim), dtype=host.dtype)
         for key, off in zip(keys, offs):
             qb, qw, qk = key_unpack(self.kind, int(key), 3)
             ob, ow, ok = self.bra.offset_of(qb), self.mpo.offset_of(qw), self.ket.offset_of(qk)
@@ -107,12 +123,26 @@ class SiteTensor:
     """Block-sparse MPS site tensor (s, a_L, a_R), q(s) + q(a_L) = q(a_R); blocks
     in ascending packed-key order, each row-major (s, a, b); device data."""
 
-    def __init__(self, kind: int, legs: list, keys: np.ndarray, offs: np.ndarray, data):
+    def __init__(self, kind: int, legs: list, keys: np.ndarray, offs: np.ndarray, data, data_im=None):
         self.kind, self.legs, self.keys, self.offs, self.data = kind, legs, keys, offs, data
+        self.data_im = data_im  # imaginary part of a complex tensor, or None
+
+    @property
+    def is_complex(self):
+        return self.data_im is not None
+
+    def complexified(self) -> "SiteTensor":
+        if self.is_complex:
+            return self
+        return SiteTensor(self.kind, self.legs, self.keys, self.offs, self.data, _torch().zeros_like(self.data))
+
+    def clone(self) -> "SiteTensor":
+        return SiteTensor(self.kind, self.legs, self.keys, self.offs, self.data.clone(),
+                          self.data_im.clone() if self.is_complex else None)
 
     @classmethod
     def from_blocks(cls, kind, legs, blocks: dict, device: int = 0):
-        """blocks: {(q_s, q_L, q_R): array (d_s, D_L, D_R)}."""
+        """blocks: {(q_s, q_L, q_R): array (d_s, D_L, D_R)}, real or complex."""
         items = sorted(((key_pack(kind, list(q)), a) for q, a in blocks.items()), key=lambda t: t[0])
         keys = np.array([k for k, _ in items], dtype=np.uint64)
         sizes = [a.size for _, a in items]
@@ -120,7 +150,11 @@ class SiteTensor:
         if items:
             offs[1:] = np.cumsum(sizes)[:-1]
         host = np.concatenate([a.reshape(-1) for _, a in items]) if items else np.zeros(1)
-        return cls(kind, list(legs), keys, offs, _torch().from_numpy(np.ascontiguousarray(host)).to(f"cuda:{device}"))
+        dev = f"cuda:{device}"
+        if np.iscomplexobj(host):
+            return cls(kind, list(legs), keys, offs, _torch().from_numpy(np.ascontiguousarray(host.real)).to(dev),
+                       _torch().from_numpy(np.ascontiguousarray(host.imag)).to(dev))
+        return cls(kind, list(legs), keys, offs, _torch().from_numpy(np.ascontiguousarray(host)).to(dev))
 
     @classmethod
     def from_dense(cls, kind, legs, A: np.ndarray, device: int = 0):
@@ -138,6 +172,8 @@ class SiteTensor:
 
     def blocks_host(self) -> dict:
         host = self.data.cpu().numpy()
+        if self.is_complex:
+            host = host + 1j * self.data_im.cpu().numpy()
         P, QL, QR = self.legs
         out = {}
         for key, off in zip(self.keys, self.offs):
@@ -148,7 +184,7 @@ class SiteTensor:
 
     def to_dense(self) -> np.ndarray:
         P, QL, QR = self.legs
-        A = np.zeros((P.total_dim, QL.total_dim, QR.total_dim))
+        A = np.zeros((P.total_dim, QL.total_dim, QR.total_dim), dtype=np.complex128 if self.is_complex else np.float64)
         for (qs, ql, qr), b in self.blocks_host().items():
             os_, ol, orr = P.offset_of(qs), QL.offset_of(ql), QR.offset_of(qr)
             A[os_:os_ + b.shape[0], ol:ol + b.shape[1], orr:orr + b.shape[2]] = b
@@ -163,38 +199,59 @@ class SiteTensor:
                            _abi.u64ptr(self.keys), _abi.i64ptr(self.offs), _dptr(self.data))
 
 
-def _grow(fn_name: str, env: DeviceEnv, A: SiteTensor, W, left: bool, stream=None, device: int = 0) -> DeviceEnv:
+def _grow(left: bool, env: DeviceEnv, A: SiteTensor, W, stream=None, device: int = 0) -> DeviceEnv:
+    torch = _torch()
     lib = _abi.load()
+    cplx = env.is_complex or A.is_complex
+    if cplx:
+        env, A = env.complexified(), A.complexified()
     m = _Marshal()
     e, a, w = env.marshal(m), A.marshal(m), m.bst(W)
     bond = A.legs[2] if left else A.legs[1]
     wl = W.indices[3] if left else W.indices[2]
     _, _, total = env_layout(A.kind, bond, wl, bond)
-    out = _torch().empty(max(total, 1), dtype=_torch().float64, device=f"cuda:{device}")
+    out = torch.empty(max(total, 1), dtype=torch.float64, device=f"cuda:{device}")
     s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
-    check(getattr(lib, fn_name)(context(device), C.byref(e), C.byref(a), C.byref(w), C.c_void_p(out.data_ptr()), s))
-    return DeviceEnv(A.kind, bond, wl, bond, out[:total])
+    if not cplx:
+        fn = lib.tk_env_grow_left if left else lib.tk_env_grow_right
+        check(fn(context(device), C.byref(e), C.byref(a), C.byref(w), C.c_void_p(out.data_ptr()), s))
+        return DeviceEnv(A.kind, bond, wl, bond, out[:total])
+    out_im = torch.empty_like(out)
+    fn = lib.tk_env_grow_left_complex if left else lib.tk_env_grow_right_complex
+    check(fn(context(device), C.byref(e), C.c_void_p(env.data_im.data_ptr()), C.byref(a),
+             C.c_void_p(A.data_im.data_ptr()), C.byref(w), C.c_void_p(out.data_ptr()), C.c_void_p(out_im.data_ptr()),
+             s))
+    return DeviceEnv(A.kind, bond, wl, bond, out[:total], out_im[:total])
 
 
 def grow_left(env: DeviceEnv, A: SiteTensor, W, stream=None, device: int = 0) -> DeviceEnv:
-    """contract_left_environment on the device (tk_env_grow_left)."""
-    return _grow("tk_env_grow_left", env, A, W, True, stream, device)
+    """contract_left_environment on the device (tk_env_grow_left[_complex])."""
+    return _grow(True, env, A, W, stream, device)
 
 
 def grow_right(env: DeviceEnv, A: SiteTensor, W, stream=None, device: int = 0) -> DeviceEnv:
-    """contract_right_environment on the device (tk_env_grow_right)."""
-    return _grow("tk_env_grow_right", env, A, W, False, stream, device)
+    """contract_right_environment on the device (tk_env_grow_right[_complex])."""
+    return _grow(False, env, A, W, stream, device)
 
 
 def two_site_product(plan: Heff2Plan, Ai: SiteTensor, Aj: SiteTensor, stream=None):
-    """psi = A_i A_j in the plan's block layout (tk_heff2_two_site_product)."""
+    """psi = A_i A_j in the plan's block layout; (re, im) for a complex plan, else re."""
     torch = _torch()
     m = _Marshal()
-    a, b = Ai.marshal(m), Aj.marshal(m)
-    psi = torch.empty(plan.block_dim, dtype=torch.float64, device=f"cuda:{plan.device}")
     s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
-    check(_abi.load().tk_heff2_two_site_product(plan.handle, C.byref(a), C.byref(b), C.c_void_p(psi.data_ptr()), s))
-    return psi
+    psi = torch.empty(plan.block_dim, dtype=torch.float64, device=f"cuda:{plan.device}")
+    if not plan.is_complex:
+        a, b = Ai.marshal(m), Aj.marshal(m)
+        check(_abi.load().tk_heff2_two_site_product(plan.handle, C.byref(a), C.byref(b), C.c_void_p(psi.data_ptr()),
+                                                      s))
+        return psi
+    Ai, Aj = Ai.complexified(), Aj.complexified()
+    a, b = Ai.marshal(m), Aj.marshal(m)
+    psi_im = torch.empty_like(psi)
+    check(_abi.load().tk_heff2_two_site_product_complex(plan.handle, C.byref(a), C.c_void_p(Ai.data_im.data_ptr()),
+                                                        C.byref(b), C.c_void_p(Aj.data_im.data_ptr()),
+                                                        C.c_void_p(psi.data_ptr()), C.c_void_p(psi_im.data_ptr()), s))
+    return psi, psi_im
 
 
 def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool):
@@ -226,7 +283,7 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
             cols.setdefault(q, {})[(t, qb)] = ncol.get(q, 0)
             ncol[q] = ncol.get(q, 0) + db
     charges = sorted(set(rows) & set(cols))
-    M = {q: np.zeros((nrow[q], ncol[q])) for q in charges}
+    M = {q: np.zeros((nrow[q], ncol[q]), dtype=psi.dtype) for q in charges}
     for key, off in zip(keys, offs):
         qsi, qsj, qa, qb = (tuple(x) for x in key_unpack(kind, int(key), 4))
         ni, nj, da, db = PI.dim_of(qsi), PJ.dim_of(qsj), QA.dim_of(qa), QB.dim_of(qb)
@@ -241,7 +298,7 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     eig = {}
     allsv = []
     for bi, q in enumerate(charges):
-        G = M[q] @ M[q].T if to_right else M[q].T @ M[q]
+        G = M[q] @ M[q].conj().T if to_right else M[q].conj().T @ M[q]
         w, Z = np.linalg.eigh(G)
         w, Z = w[::-1], Z[:, ::-1]
         eig[q] = Z
@@ -258,20 +315,20 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     for q, k in kept.items():
         Z = eig[q][:, :k]
         if to_right:
-            Uk, Vk = Z, (Z.T @ M[q]) / norm
+            Uk, Vk = Z, (Z.conj().T @ M[q]) / norm
         else:
-            Uk, Vk = (M[q] @ Z) / norm, Z.T
+            Uk, Vk = (M[q] @ Z) / norm, Z.conj().T
         for (s, qa), r0 in rows[q].items():
             qs = pqi[s]
             da = QA.dim_of(qa)
             li = s - PI.offset_of(qs)
-            blk = Ai.setdefault((qs, qa, q), np.zeros((PI.dim_of(qs), da, k)))
+            blk = Ai.setdefault((qs, qa, q), np.zeros((PI.dim_of(qs), da, k), dtype=Uk.dtype))
             blk[li] = Uk[r0:r0 + da]
         for (t, qb), c0 in cols[q].items():
             qt = pqj[t]
             db = QB.dim_of(qb)
             lj = t - PJ.offset_of(qt)
-            blk = Aj.setdefault((qt, q, qb), np.zeros((PJ.dim_of(qt), k, db)))
+            blk = Aj.setdefault((qt, q, qb), np.zeros((PJ.dim_of(qt), k, db), dtype=Vk.dtype))
             blk[lj] = Vk[:, c0:c0 + db]
     return Ai, Aj, nb, disc
 
@@ -345,15 +402,6 @@ def random_site_tensors(model, n: int, max_bond: int, total, rng: np.random.Gene
               and bonds[i + 1].offset_of(k[2]) is not None}
         sites.append(SiteTensor.from_blocks(kind, legs, bl, device))
     return sites, bonds
-
-
-def _identity_mpo(kind, wq: QIndex):
-    """MPO tensor of a dummy site: physical dimension 1 (zero charge), W = identity on the channel."""
-    from .models import INCOMING, OUTGOING, dense_to_bst
-
-    p1 = QIndex(kind, [(identity(kind), 1)])
-    W = np.eye(wq.total_dim).reshape(1, 1, wq.total_dim, wq.total_dim)
-    return dense_to_bst(kind, W, [p1, p1, wq, wq], [INCOMING, OUTGOING, OUTGOING, INCOMING], identity(kind)), p1
 
 
 def _identity_site(kind, p1: QIndex, bond: QIndex, device: int):
@@ -461,53 +509,75 @@ class DeviceDMRG:
         return r.eigenvalue, disc
 
     # ---- imaginary-time two-site TDVP ---------------------------------------------
-    def _one_site_plan(self, k: int):
-        """H_eff of site k (L_k, W_k, R_{k+1}) as a two-site plan with a dummy second site."""
-        Wd, p1 = _identity_mpo(self.kind, self.W[k].indices[3])
-        plan = Heff2Plan.from_device_envs(self.L[k], self.R[k + 1], self.W[k], Wd, self.zero,
-                                          precision=self.precision, device=self.device)
-        return plan, p1
+    def _plan(self, L, R, Wi, Wj, cplx: bool):
+        if cplx:
+            return Heff2Plan.from_device_envs_complex(L, R, Wi, Wj, self.zero, device=self.device)
+        return Heff2Plan.from_device_envs(L, R, Wi, Wj, self.zero, precision=self.precision, device=self.device)
 
-    def _evolve_center(self, k: int, tau: float, rec: "SweepRecord"):
-        """C_k <- exp(tau H1(k)) C_k, normalised (the backward step of the projector splitting)."""
+    def _one_site_plan(self, k: int, cplx: bool):
+        """H_eff of site k (L_k, W_k, R_{k+1}) as a two-site plan with a dummy second site."""
+        Wd = identity_mpo_site(self.W[k].indices[3])
+        return self._plan(self.L[k], self.R[k + 1], self.W[k], Wd, cplx), Wd.indices[0]
+
+    @staticmethod
+    def _expm(plan, alpha, x, krylov):
+        """exp(alpha H) x, normalised; x and the result are re or (re, im)."""
         torch = _torch()
-        plan, p1 = self._one_site_plan(k)
+        xr, xi = (x, None) if not isinstance(x, tuple) else x
+        yr, yi, _, mv = plan.expm(alpha, xr, xi, krylov_dim=krylov, tol=1e-12)
+        nrm = torch.sqrt(torch.dot(yr, yr) + (torch.dot(yi, yi) if yi is not None else 0.0))
+        yr = yr / nrm
+        yi = yi / nrm if yi is not None else None
+        return (yr, yi) if yi is not None else yr, mv
+
+    @staticmethod
+    def _host(y):
+        return (y[0].cpu().numpy() + 1j * y[1].cpu().numpy()) if isinstance(y, tuple) else y.cpu().numpy()
+
+    def _evolve_center(self, k: int, alpha, rec: "SweepRecord", cplx: bool):
+        """C_k <- exp(alpha H1(k)) C_k, normalised (the backward step of the projector splitting)."""
+        plan, p1 = self._one_site_plan(k, cplx)
         dummy = _identity_site(self.kind, p1, self.bonds[k + 1], self.device)
         c = two_site_product(plan, self.sites[k], dummy)
-        out, _, _, mv = plan.expm(tau, c, krylov_dim=self.krylov, tol=1e-12)
+        out, mv = self._expm(plan, alpha, c, self.krylov)
         rec.matvecs += mv
-        out = out / torch.linalg.norm(out)
         keys, offs = plan.blocks()
-        blocks = _plan_to_site(self.kind, out.cpu().numpy(), keys, offs,
-                               [self.model.phys, self.bonds[k], self.bonds[k + 1]])
-        self.sites[k] = SiteTensor.from_blocks(self.kind, [self.model.phys, self.bonds[k], self.bonds[k + 1]],
-                                               blocks, self.device)
+        legs = [self.model.phys, self.bonds[k], self.bonds[k + 1]]
+        blocks = _plan_to_site(self.kind, self._host(out), keys, offs, legs)
+        self.sites[k] = SiteTensor.from_blocks(self.kind, legs, blocks, self.device)
         plan.close()
 
-    def tdvp_step(self, dtau: float, max_bond: int, rec: "SweepRecord", cutoff: float = 1e-14):
-        """One imaginary-time step exp(-dtau H) by two-site TDVP: a left-to-right and a
-        right-to-left half sweep of dtau/2 each; every two-site update evolves forward by
-        exp(-dtau/2 H2), the new single-site center backward by exp(+dtau/2 H1)
-        (projector splitting).  The state is kept normalised; returns the energy
-        <psi|H|psi> of the last two-site update."""
+    def tdvp_step(self, dt: float, max_bond: int, rec: "SweepRecord", cutoff: float = 1e-14,
+                  real_time: bool = False):
+        """One TDVP step by two-site projector splitting: a left-to-right and a
+        right-to-left half sweep of dt/2 each; every two-site update evolves forward
+        by exp(-(dt/2) H2) (imaginary time) or exp(-i (dt/2) H2) (real time, complex
+        MPS and environments), the new single-site center backward by the inverse
+        one-site step.  The state is kept normalised (truncation loses norm); returns
+        the energy <psi|H|psi> of the last two-site update."""
         torch = _torch()
-        half = 0.5 * dtau
+        half = 0.5 * dt
+        fwd, bwd = (-1j * half, 1j * half) if real_time else (-half, half)
+        cplx = real_time or any(t.is_complex for t in self.sites)
         n = self.n
         energy = None
         for to_right, bonds in ((True, range(0, n - 1)), (False, range(n - 2, -1, -1))):
             for i in bonds:
-                plan = Heff2Plan.from_device_envs(self.L[i], self.R[i + 2], self.W[i], self.W[i + 1], self.zero,
-                                                  precision=self.precision, device=self.device)
+                plan = self._plan(self.L[i], self.R[i + 2], self.W[i], self.W[i + 1], cplx)
                 x = two_site_product(plan, self.sites[i], self.sites[i + 1])
-                y, _, _, mv = plan.expm(-half, x, krylov_dim=self.krylov, tol=1e-12)
+                y, mv = self._expm(plan, fwd, x, self.krylov)
                 rec.matvecs += mv
-                y = y / torch.linalg.norm(y)
-                hy = torch.empty_like(y)
-                plan.apply(y, hy)
-                energy = float(torch.dot(y, hy))
+                if cplx:
+                    hr, hi = torch.empty_like(y[0]), torch.empty_like(y[1])
+                    plan.apply_complex(y[0], y[1], hr, hi)
+                    energy = float(torch.dot(y[0], hr) + torch.dot(y[1], hi))
+                else:
+                    hy = torch.empty_like(y)
+                    plan.apply(y, hy)
+                    energy = float(torch.dot(y, hy))
                 keys, offs = plan.blocks()
                 legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
-                Ai, Aj, nb, disc = split_two_site(self.kind, y.cpu().numpy(), keys, offs, legs, max_bond, cutoff,
+                Ai, Aj, nb, disc = split_two_site(self.kind, self._host(y), keys, offs, legs, max_bond, cutoff,
                                                   to_right)
                 P = self.model.phys
                 self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
@@ -517,13 +587,54 @@ class DeviceDMRG:
                 if to_right:
                     self.L[i + 1] = grow_left(self.L[i], self.sites[i], self.W[i], device=self.device)
                     if i + 1 < n - 1:
-                        self._evolve_center(i + 1, half, rec)
+                        self._evolve_center(i + 1, bwd, rec, cplx)
                 else:
                     self.R[i + 1] = grow_right(self.R[i + 2], self.sites[i + 1], self.W[i + 1], device=self.device)
                     if i > 0:
-                        self._evolve_center(i, half, rec)
+                        self._evolve_center(i, bwd, rec, cplx)
         torch.cuda.synchronize(self.device)
         return energy
+
+    def apply_site_operator(self, site: int, op: np.ndarray, q_op):
+        """|psi> <- O_site |psi> for a one-site operator O (d x d, O[s', s]) that changes
+        the charge by q_op: the site's blocks move from s to s', and every bond right of
+        the site (charges are cumulative from the left) shifts by q_op.  The right
+        environments are rebuilt.  Fermionic operators need their Jordan-Wigner string
+        on the sites left of `site` (none for site 0)."""
+        kind, P = self.kind, self.model.phys
+        pq = P.state_charges()
+
+        def shift(ix: QIndex):
+            return QIndex(kind, [(fuse(kind, q, tuple(q_op)), d) for q, d in ix.sectors])
+
+        new_bonds = list(self.bonds[:site + 1]) + [shift(b) for b in self.bonds[site + 1:]]
+        new_sites = []
+        for k, t in enumerate(self.sites):
+            blocks = t.blocks_host()
+            if k < site:
+                new_sites.append(t)
+                continue
+            out = {}
+            for (qs, ql, qr), b in blocks.items():
+                if k > site:
+                    out[(qs, fuse(kind, ql, tuple(q_op)), fuse(kind, qr, tuple(q_op)))] = b
+                    continue
+                for sp in range(P.total_dim):
+                    for sl in range(P.dim_of(qs)):
+                        s0 = P.offset_of(qs) + sl
+                        c = op[sp, s0]
+                        if c == 0:
+                            continue
+                        qsp = pq[sp]
+                        key = (qsp, ql, fuse(kind, qr, tuple(q_op)))
+                        blk = out.setdefault(key, np.zeros((P.dim_of(qsp),) + b.shape[1:], dtype=np.result_type(b, op)))
+                        blk[sp - P.offset_of(qsp)] += c * b[sl]
+            new_sites.append(SiteTensor.from_blocks(kind, [P, new_bonds[k], new_bonds[k + 1]], out, self.device))
+        self.sites, self.bonds = new_sites, new_bonds
+        n = self.n
+        self.R[n] = DeviceEnv.boundary(kind, self.bonds[n], self.W[n - 1].indices[3], self.device)
+        for i in range(n - 1, site, -1):
+            self.R[i] = grow_right(self.R[i + 1], self.sites[i], self.W[i], device=self.device)
 
     def run(self, max_bond: int, sweeps: int, cutoff: float = 1e-14) -> SweepRecord:
         rec = SweepRecord()

@@ -81,3 +81,108 @@ def test_imaginary_time_tdvp_reaches_ground_state(lib_built):
     energies = [d.tdvp_step(1.5, 32, rec) for _ in range(30)]
     assert all(b <= a + 1e-9 for a, b in zip(energies[5:], energies[6:]))
     assert abs(energies[-1] - ed_heisenberg(10)) < 1e-8
+
+
+@pytest.mark.parametrize("name,D", [("heisenberg", 12), ("hubbard", 10)])
+def test_single_site_closure_matches_dense(lib_built, name, D):
+    """build_heff_single_site (a two-site plan with a dummy second site) == the reference's dense H."""
+    from oracle import environments as oe
+    from tk_gb300.heff import MPO, build_heff_single_site
+
+    p = small_problem(name, D)
+    mpo = MPO([p.w_i], [p.w_i.indices[0].total_dim], p.flux)
+    matvec, dim = build_heff_single_site(p.env_l, p.env_r, mpo, 0)
+    H = oe.heff_single_site_dense(p.env_l.data, p.w_i.to_dense(), p.env_r.data)
+    assert dim == H.shape[0]
+    rng = np.random.default_rng(2)
+    for _ in range(2):
+        x = rng.standard_normal(dim)
+        y = np.zeros(dim)
+        matvec(x, y)
+        assert np.linalg.norm(y - H @ x) < 1e-12 * np.linalg.norm(H @ x)
+
+
+def _dense_state(sites):
+    v = np.ones((1,), dtype=complex)
+    for t in sites:
+        A = t.to_dense()
+        v = np.einsum("xa,sab->xsb", v.reshape(-1, A.shape[1]), A).reshape(-1, A.shape[2])
+    return v.reshape(-1)
+
+
+def _heisenberg_dense(n):
+    sz = np.diag([-0.5, 0.5])
+    sp = np.array([[0.0, 0.0], [1.0, 0.0]])
+    eye = np.eye(2)
+
+    def site(o, k):
+        out = np.ones((1, 1))
+        for j in range(n):
+            out = np.kron(out, o if j == k else eye)
+        return out
+
+    H = np.zeros((2 ** n, 2 ** n))
+    for k in range(n - 1):
+        H += site(sz, k) @ site(sz, k + 1)
+        H += 0.5 * (site(sp, k) @ site(sp.T, k + 1) + site(sp.T, k) @ site(sp, k + 1))
+    return H
+
+
+def test_complex_plan_matches_dense(lib_built):
+    """Complex environments: tk_heff2_apply_complex against the dense complex H_eff."""
+    import torch
+
+    p = small_problem("heisenberg", 10)
+    rng = np.random.default_rng(8)
+    # Hermitian complex environments: real part from the problem, imaginary part antisymmetric in (bra, ket)
+    def cplx_env(e):
+        im = rng.standard_normal(e.data.shape)
+        im = im - np.transpose(im, (2, 1, 0))
+        return e.data + 0.3j * im
+
+    Lc, Rc = cplx_env(p.env_l), cplx_env(p.env_r)
+    # keep only the charge-allowed blocks (the canonical layout's support)
+    dl = sweep.DeviceEnv.from_dense(p.kind, Lc, p.env_l.bra_idx, p.env_l.mpo_idx, p.env_l.ket_idx)
+    dr = sweep.DeviceEnv.from_dense(p.kind, Rc, p.env_r.bra_idx, p.env_r.mpo_idx, p.env_r.ket_idx)
+    plan = __import__("tk_gb300").Heff2Plan.from_device_envs_complex(dl, dr, p.w_i, p.w_j, p.flux)
+    Lm, Rm = dl.to_dense(), dr.to_dense()
+    Wi, Wj = p.w_i.to_dense(), p.w_j.to_dense()
+    x = rng.standard_normal(plan.block_dim) + 1j * rng.standard_normal(plan.block_dim)
+    xd = plan.flat_to_dense(x.real) + 1j * plan.flat_to_dense(x.imag)
+    d = Wi.shape[0]
+    X = xd.reshape(d, d, Lm.shape[0], Rm.shape[0])
+    Y = np.einsum("pwa,stwv,uxvz,qzb,suab->txpq", Lm, Wi, Wj, Rm, X, optimize=True)
+    yr, yi = torch.empty(plan.block_dim, dtype=torch.float64).cuda(), torch.empty(plan.block_dim,
+                                                                                 dtype=torch.float64).cuda()
+    plan.apply_complex(_dev(x.real), _dev(x.imag), yr, yi)
+    got = yr.cpu().numpy() + 1j * yi.cpu().numpy()
+    want = plan.dense_to_flat(Y.reshape(-1).real) + 1j * plan.dense_to_flat(Y.reshape(-1).imag)
+    assert np.linalg.norm(got - want) < 1e-12 * np.linalg.norm(want)
+
+
+def test_real_time_tdvp_matches_exact_evolution(lib_built):
+    """G(t) = <phi| exp(-i H t) |phi>, phi = S+_0 |ground state>, by real-time two-site
+    TDVP with complex environments, against dense evolution (Heisenberg chain, 8 sites,
+    exact bond dimension)."""
+    from scipy.linalg import expm
+
+    from tk_gb300 import dmrg
+
+    m = models.heisenberg()
+    n, D = 8, 16
+    mps = dmrg.random_mps_u1(m, n, D, (0,), np.random.default_rng(4))
+    dev = sweep.DeviceDMRG.from_dense_mps(m, mps, precision=PREC_FP64, solver="davidson", tol=1e-11)
+    rec = dev.run(D, 3)
+    H = _heisenberg_dense(n)
+    assert abs(rec.energies[-1] - np.linalg.eigvalsh(H)[0]) < 1e-9
+    dev.apply_site_operator(0, np.array([[0.0, 0.0], [1.0, 0.0]]), (2,))
+    phi = _dense_state(dev.sites)
+    phi /= np.linalg.norm(phi)
+    rec2 = sweep.SweepRecord()
+    dt = 0.1
+    for step in range(1, 9):
+        dev.tdvp_step(dt, D, rec2, real_time=True)
+        phit = _dense_state(dev.sites)
+        g = np.vdot(phi, phit)
+        g_ref = np.vdot(phi, expm(-1j * H * dt * step) @ phi)
+        assert abs(g - g_ref) < 1e-8, (step, g, g_ref)

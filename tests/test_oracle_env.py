@@ -45,3 +45,26 @@ def test_growth_restatement_matches_literal_sums():
     R = rng.standard_normal((4, 3, 4))
     assert np.allclose(oe.grow_left(L, A, W), _literal_left(L, A, W), rtol=0, atol=1e-12)
     assert np.allclose(oe.grow_right(R, A, W), _literal_right(R, A, W), rtol=0, atol=1e-12)
+
+
+def test_single_site_restatement_matches_literal_loops():
+    """heff_single_site_dense against the reference's element loops (environments/mod.rs:619-664)."""
+    rng = np.random.default_rng(5)
+    d, Da, Db, w, v = 2, 3, 4, 2, 3
+    L = rng.standard_normal((Da, w, Da))
+    R = rng.standard_normal((Db, v, Db))
+    W = rng.standard_normal((d, d, w, v))
+    dim = d * Da * Db
+    H = np.zeros((dim, dim))
+    for s_in in range(d):
+        for s_out in range(d):
+            for wl in range(w):
+                for wr in range(v):
+                    for a_l in range(Da):
+                        for ap_l in range(Da):
+                            lw = L[ap_l, wl, a_l] * W[s_in, s_out, wl, wr]
+                            for a_r in range(Db):
+                                for ap_r in range(Db):
+                                    H[(s_out * Da + ap_l) * Db + ap_r, (s_in * Da + a_l) * Db + a_r] += \
+                                        lw * R[ap_r, wr, a_r]
+    assert np.allclose(oe.heff_single_site_dense(L, W, R), H, atol=1e-12, rtol=0)
