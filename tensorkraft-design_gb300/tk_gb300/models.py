@@ -156,6 +156,65 @@ def hubbard(t: float = 1.0, U: float = 4.0) -> ModelMPO:
 
 
 # ----------------------------------------------------------------------------
+# Fermion chains with site-dependent couplings (Anderson impurity, chain geometry)
+# ----------------------------------------------------------------------------
+
+
+@dataclass
+class ChainModel:
+    """A chain MPO with its own tensor on every site (same interface as ModelMPO.chain)."""
+
+    kind: int
+    phys: QIndex
+    tensors: list
+
+    def chain(self, n_sites: int) -> MPO:
+        if n_sites != len(self.tensors):
+            raise ValueError("ChainModel has a fixed length")
+        return MPO(list(self.tensors), [self.phys.total_dim] * n_sites, (0,) * (2 if self.kind == U1U1 else 1))
+
+
+def fermion_chain(hop, U, eps) -> ChainModel:
+    """H = sum_i hop[i] sum_s (c+_{i s} c_{i+1 s} + h.c.) + sum_i U[i] n_{i up} n_{i dn}
+    + sum_i eps[i] (n_{i up} + n_{i dn}); (N, 2Sz) charges, Jordan-Wigner strings as in
+    `hubbard` (which is the uniform case hop = -t)."""
+    n = len(U)
+    if len(eps) != n or len(hop) != n - 1:
+        raise ValueError("need n on-site terms and n-1 hoppings")
+    phys = QIndex(U1U1, [((0, 0), 1), ((1, -1), 1), ((1, 1), 1), ((2, 0), 1)])
+    o = hubbard_local()
+    cdu, cdd, F, I = o["cdu"], o["cdd"], o["F"], o["I"]
+    cu, cd = cdu.T, cdd.T
+    charges = [(0, 0), (1, 1), (-1, -1), (1, -1), (-1, 1), (0, 0)]
+    tensors = []
+    for i in range(n):
+        onsite = U[i] * (o["nu"] @ o["nd"]) + eps[i] * (o["nu"] + o["nd"])
+        t = hop[i] if i < n - 1 else 0.0
+        entries = [(0, 0, I), (0, 1, t * (cdu @ F)), (0, 2, t * (F @ cu)), (0, 3, t * (cdd @ F)),
+                   (0, 4, t * (F @ cd)), (1, 5, cu), (2, 5, cdu), (3, 5, cd), (4, 5, cdd), (0, 5, onsite),
+                   (5, 5, I)]
+        if i == 0:
+            w, _, _ = site_tensor(U1U1, phys, [charges[0]], charges, [(0, wr, m) for (wl, wr, m) in entries if wl == 0])
+        elif i == n - 1:
+            w, _, _ = site_tensor(U1U1, phys, charges, [charges[5]], [(wl, 0, m) for (wl, wr, m) in entries if wr == 5])
+        else:
+            w, _, _ = site_tensor(U1U1, phys, charges, charges, entries)
+        tensors.append(w)
+    return ChainModel(U1U1, phys, tensors)
+
+
+def anderson_chain(n: int, U: float = 3.0, seed: int = 5, v: float = 0.5) -> ChainModel:
+    """Single-impurity Anderson model in chain geometry (impurity = site 0, n-1 bath
+    sites): U on the impurity at half filling (eps_d = -U/2), impurity-bath hopping v,
+    seeded bath on-site energies eps_k ~ 0.1 N(0,1) and chain hoppings 0.5 (1 + 0.1 N(0,1))."""
+    rng = np.random.default_rng(seed)
+    hop = [v] + list(0.5 * (1.0 + 0.1 * rng.standard_normal(n - 2)))
+    eps = [-0.5 * U] + list(0.1 * rng.standard_normal(n - 1))
+    Us = [U] + [0.0] * (n - 1)
+    return fermion_chain(hop, Us, eps)
+
+
+# ----------------------------------------------------------------------------
 # J1 Heisenberg on a width-W cylinder, column-major (snake) ordering, bond 2+3W
 # ----------------------------------------------------------------------------
 

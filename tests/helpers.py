@@ -168,6 +168,36 @@ def ed_hubbard(n: int, t: float = 1.0, U: float = 4.0, N: int | None = None, sz2
     return float(np.linalg.eigvalsh(H[np.ix_(sel, sel)])[0])
 
 
+def fermion_ops(n: int):
+    """Jordan-Wigner annihilators c[(site, 'u'|'d')] on the 4^n Fock space (site 0 the
+    most significant factor), in the sorted local basis of models.hubbard_local."""
+    o = models.hubbard_local()
+    a_up, a_dn, F = o["cdu"].T, o["cdd"].T, o["F"]
+
+    def site_op(m, k):
+        out = np.array([[1.0]])
+        for s in range(n):
+            out = np.kron(out, m if s == k else (F if s < k else np.eye(4)))
+        return out
+
+    return {(k, sg): site_op(a, k) for k in range(n) for sg, a in (("u", a_up), ("d", a_dn))}
+
+
+def fermion_chain_dense(hop, U, eps):
+    """Dense H of models.fermion_chain, built from fermion_ops (independently of the MPO)."""
+    n = len(U)
+    c = fermion_ops(n)
+    H = np.zeros((4 ** n, 4 ** n))
+    for k in range(n - 1):
+        for sg in "ud":
+            h = c[(k, sg)].T @ c[(k + 1, sg)]
+            H += hop[k] * (h + h.T)
+    for k in range(n):
+        nu, nd = c[(k, "u")].T @ c[(k, "u")], c[(k, "d")].T @ c[(k, "d")]
+        H += U[k] * nu @ nd + eps[k] * (nu + nd)
+    return H, c
+
+
 class CpuSolver:
     """DMRG eigen-solver on the CPU oracle: block-sparse FP64 matvec + numpy Lanczos."""
 

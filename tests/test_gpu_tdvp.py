@@ -186,3 +186,41 @@ def test_real_time_tdvp_matches_exact_evolution(lib_built):
         g = np.vdot(phi, phit)
         g_ref = np.vdot(phi, expm(-1j * H * dt * step) @ phi)
         assert abs(g - g_ref) < 1e-8, (step, g, g_ref)
+
+
+def test_anderson_impurity_greens_function(lib_built):
+    """Impurity G(t) ~ <phi| exp(-i H t) |phi>, phi = c+_{0 up} |ground state>, of the
+    Anderson chain (4 sites, exact bond dimension) by real-time TDVP, against the dense
+    Jordan-Wigner evolution."""
+    from scipy.linalg import expm
+
+    from helpers import fermion_chain_dense
+    from tk_gb300 import dmrg
+
+    n, D = 4, 16
+    U = 3.0
+    rng = np.random.default_rng(5)
+    hop = [0.5] + list(0.5 * (1.0 + 0.1 * rng.standard_normal(n - 2)))
+    eps = [-0.5 * U] + list(0.1 * rng.standard_normal(n - 1))
+    Us = [U] + [0.0] * (n - 1)
+    m = models.fermion_chain(hop, Us, eps)
+    H, c = fermion_chain_dense(hop, Us, eps)
+    mps = dmrg.random_mps(m, n, D, (n, 0), np.random.default_rng(3))
+    dev = sweep.DeviceDMRG.from_dense_mps(m, mps, precision=PREC_FP64, solver="davidson", tol=1e-11)
+    rec = dev.run(D, 3)
+    nt = sum(c[(k, s)].T @ c[(k, s)] for k in range(n) for s in "ud")
+    s2 = sum(c[(k, "u")].T @ c[(k, "u")] - c[(k, "d")].T @ c[(k, "d")] for k in range(n))
+    sel = np.where((np.abs(np.diag(nt) - n) < 1e-9) & (np.abs(np.diag(s2)) < 1e-9))[0]
+    w, V = np.linalg.eigh(H[np.ix_(sel, sel)])
+    assert abs(rec.energies[-1] - w[0]) < 1e-9
+    cdu = models.hubbard_local()["cdu"]
+    dev.apply_site_operator(0, cdu, (1, 1))
+    phi = _dense_state(dev.sites)
+    phi /= np.linalg.norm(phi)
+    rec2 = sweep.SweepRecord()
+    dt = 0.1
+    for step in range(1, 7):
+        dev.tdvp_step(dt, D, rec2, real_time=True)
+        g = np.vdot(phi, _dense_state(dev.sites))
+        g_ref = np.vdot(phi, expm(-1j * H * dt * step) @ phi)
+        assert abs(g - g_ref) < 1e-8, (step, g, g_ref)

@@ -48,3 +48,26 @@ def test_flatten_layout_is_key_sorted():
     keys, offs, data = t.flatten()
     assert np.all(np.diff(keys.astype(np.float64)) > 0)
     assert offs[0] == 0 and data.size == sum(b.size for b in t.blocks.values())
+
+
+def _mpo_dense(mpo):
+    """Contract an open-boundary MPO into its dense operator (site 0 most significant)."""
+    Ws = [t.to_dense() for t in mpo.tensors]
+    M = Ws[0][:, :, 0, :]  # (s_in, s_out, w)
+    for W in Ws[1:]:
+        M = np.einsum("abw,cdwv->acbdv", M, W).reshape(M.shape[0] * W.shape[0], M.shape[1] * W.shape[1], -1)
+    return M[:, :, 0].T  # H[out, in]
+
+
+def test_fermion_chain_mpo_matches_jordan_wigner():
+    """models.fermion_chain contracted to a dense operator == the Jordan-Wigner H of the
+    same couplings, and the uniform case is models.hubbard."""
+    from helpers import fermion_chain_dense
+    from tk_gb300 import models
+
+    hop, U, eps = [0.4, -0.7], [3.0, 0.5, 0.0], [-1.5, 0.2, -0.1]
+    H, _ = fermion_chain_dense(hop, U, eps)
+    assert np.allclose(_mpo_dense(models.fermion_chain(hop, U, eps).chain(3)), H, atol=1e-12)
+    uni = models.fermion_chain([-1.0, -1.0, -1.0], [4.0] * 4, [0.0] * 4).chain(4)
+    ref = models.hubbard(1.0, 4.0).chain(4)
+    assert np.allclose(_mpo_dense(uni), _mpo_dense(ref), atol=1e-12)
