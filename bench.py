@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -58,6 +59,9 @@ def parse():
     ap.add_argument("--sweep-sites", type=int, default=64)
     ap.add_argument("--sweep-bond", type=int, default=2048)
     ap.add_argument("--sweep-warmup", type=int, default=2)
+    ap.add_argument("--tdvp-steps", type=int, default=0, metavar="K",
+                    help="also time K real-time TDVP steps of the impurity Green's function (Anderson chain, "
+                         "16 sites, D=1024, dt=0.05, Krylov 16) after a split-precision DMRG ground state")
     ap.add_argument("--compare-schedules", type=int, default=0, metavar="STEPS",
                     help="also time STEPS FP64 matvecs with one grouped launch per stage and with one launch "
                          "per sector block")
@@ -152,6 +156,41 @@ def sweep_hubbard(torch, n: int, D: int, warm: int, timed: int):
         del dm
     out["sweep_speedup"] = out["fp64"]["seconds_per_sweep"] / out["bf16x3"]["seconds_per_sweep"]
     out["dE"] = abs(out["fp64"]["energies"][-1] - out["bf16x3"]["energies"][-1])
+    return out
+
+
+def tdvp_anderson(torch, steps: int, n: int = 16, D: int = 1024, dt: float = 0.05):
+    """Anderson impurity (U=3, half filling, seeded bath, chain geometry) with n sites:
+    ground state by two split-precision Davidson sweeps at bond D, phi = c+_{0 up}|gs>,
+    then `steps` real-time two-site TDVP steps of dt (complex FP64 environments,
+    Krylov 16); G(t) = <phi(0)|phi(t)> from the impurity site, time per step."""
+    from tk_gb300 import PREC_BF16X3, models, sweep
+
+    m = models.anderson_chain(n, U=3.0, seed=5)
+    sites, bonds = sweep.random_site_tensors(m, n, D, (n, 0), np.random.default_rng(2024), width=0.75)
+    dm = sweep.DeviceDMRG(m, sites, bonds, precision=PREC_BF16X3, solver="davidson", tol=1e-10, krylov=16)
+    t0 = time.perf_counter()
+    rec = dm.run(D, 2)
+    out = {"config": f"anderson chain n={n} U=3 D={D} dt={dt} krylov=16 seed=5", "ground_energies": rec.energies,
+           "ground_seconds": time.perf_counter() - t0}
+    e0 = rec.energies[-1]
+    dm.apply_site_operator(0, models.hubbard_local()["cdu"], (1, 1))
+    phi0 = [t.clone() for t in dm.sites]
+    norm = math.sqrt(sweep.mps_overlap(phi0, phi0).real)
+    rec2 = sweep.SweepRecord()
+    g, secs = [], []
+    for k in range(steps):
+        ts = time.perf_counter()
+        dm.tdvp_step(dt, D, rec2, real_time=True)
+        secs.append(time.perf_counter() - ts)
+        # G>(t) = <gs| c exp(-i (H - E0) t) c+ |gs>; the evolved state is kept normalised
+        t = dt * (k + 1)
+        g.append(complex(np.exp(1j * e0 * t)) * norm * sweep.mps_overlap(phi0, dm.sites))
+    out["seconds_per_step"] = sum(secs) / max(1, len(secs))
+    out["g_greater"] = [[round(dt * (k + 1), 6), v.real, v.imag] for k, v in enumerate(g)]
+    out["g_greater_0"] = norm * norm
+    out["matvecs"] = rec2.matvecs
+    out["max_bond"] = max(b.total_dim for b in dm.bonds)
     return out
 
 
@@ -501,6 +540,8 @@ def run_ours(args):
     if args.sweeps > 0:
         line["sweeps_hubbard"] = sweep_hubbard(torch, args.sweep_sites, args.sweep_bond, args.sweep_warmup,
                                                args.sweeps)
+    if args.tdvp_steps > 0:
+        line["tdvp_anderson"] = tdvp_anderson(torch, args.tdvp_steps)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()

@@ -420,6 +420,26 @@ def _plan_to_site(kind, psi: np.ndarray, keys, offs, legs) -> dict:
     return out
 
 
+def mps_overlap(bra: list, ket: list) -> complex:
+    """<bra|ket> of two block-sparse MPS on the same sites (bond bases may differ):
+    the left transfer matrix is kept per bond charge, E_q (D_q^bra x D_q^ket), and
+    E'_{q'} = sum_s A_s^H E_q B_s over matching (s, q) blocks."""
+    E = None
+    for a, b in zip(bra, ket):
+        Ab, Bb = a.blocks_host(), b.blocks_host()
+        if E is None:
+            E = {ql: np.ones((1, 1), dtype=complex) for (_, ql, _) in Ab}
+        nxt = {}
+        for (qs, ql, qr), blk_a in Ab.items():
+            blk_b = Bb.get((qs, ql, qr))
+            if blk_b is None or ql not in E:
+                continue
+            t = np.einsum("sxa,xy,syb->ab", blk_a.conj(), E[ql], blk_b, optimize=True)
+            nxt[qr] = nxt[qr] + t if qr in nxt else t
+        E = nxt
+    return complex(sum(v[0, 0] for v in E.values())) if E else 0j
+
+
 @dataclass
 class SweepRecord:
     energies: list = field(default_factory=list)   # energy after each half sweep

@@ -215,7 +215,10 @@ def test_anderson_impurity_greens_function(lib_built):
     assert abs(rec.energies[-1] - w[0]) < 1e-9
     cdu = models.hubbard_local()["cdu"]
     dev.apply_site_operator(0, cdu, (1, 1))
+    phi_sites = [t.clone() for t in dev.sites]
+    phi_norm2 = sweep.mps_overlap(phi_sites, phi_sites).real
     phi = _dense_state(dev.sites)
+    assert abs(np.vdot(phi, phi).real - phi_norm2) < 1e-12
     phi /= np.linalg.norm(phi)
     rec2 = sweep.SweepRecord()
     dt = 0.1
@@ -224,3 +227,5 @@ def test_anderson_impurity_greens_function(lib_built):
         g = np.vdot(phi, _dense_state(dev.sites))
         g_ref = np.vdot(phi, expm(-1j * H * dt * step) @ phi)
         assert abs(g - g_ref) < 1e-8, (step, g, g_ref)
+        # the block-sparse overlap gives the same amplitude
+        assert abs(sweep.mps_overlap(phi_sites, dev.sites) / np.sqrt(phi_norm2) - g) < 1e-10
