@@ -10,10 +10,11 @@ vector is solved for, and the truncated SVD is written back into the MPS
 
 Environment growth follows contract_left/right_environment
 (tk-dmrg/src/environments/mod.rs:225-483) on dense (bra, w, ket) blocks.
-Truncation: block SVD per bond charge, the largest `max_bond` singular
-values kept over all sectors, ties broken by the sector's charge order so
-the kept set is deterministic (the reference does one dense SVD, truncation/
-mod.rs:56-127, and assigns no sectors).
+Truncation: block SVD per bond charge, ranked over all sectors (ties broken
+by the sector's charge order so the kept set is deterministic) and cut by the
+rule of truncate_svd (truncation/mod.rs:56-127: sigma >= cutoff * sigma_max,
+at most max_bond, at least one), which does one dense SVD and assigns no
+sectors.
 
 The eigen-solver is pluggable: anything with
 `solve(env_l, env_r, w_i, w_j, flux, theta_dense) -> (energy, vector)`;
@@ -279,11 +280,18 @@ def dmrg_two_site(model: ModelMPO, mps: DenseMPS, max_bond: int, sweeps: int, so
         blocks = _block_svd(M, row_q, col_q, kind)
         allsv = [(s, bi) for bi, b in enumerate(blocks) for s in b[2]]
         allsv.sort(key=lambda t: (-t[0], t[1]))
-        keep = [t for t in allsv[:max_bond] if t[0] > cutoff]
+        # truncate_svd (truncation/mod.rs:71-99): sigma >= cutoff * sigma_max, at most
+        # max_bond, at least one; error = discarded share of sum sigma^2
+        thr = cutoff * (allsv[0][0] if allsv else 0.0)
+        nkeep = 0
+        while nkeep < min(max_bond, len(allsv)) and not allsv[nkeep][0] < thr:
+            nkeep += 1
+        keep = allsv[:max(nkeep, min(1, len(allsv)))]
         kept = {}
         for s, bi in keep:
             kept[bi] = kept.get(bi, 0) + 1
-        disc = sum(s * s for s, _ in allsv[len(keep):])
+        total_sq = sum(s * s for s, _ in allsv)
+        disc = (sum(s * s for s, _ in allsv[len(keep):]) / total_sq) if total_sq > 0 else 0.0
         new_sec = [(blocks[bi][0], k) for bi, k in sorted(kept.items(), key=lambda t: blocks[t[0]][0])]
         nb = QIndex(kind, new_sec)
         Dn = nb.total_dim

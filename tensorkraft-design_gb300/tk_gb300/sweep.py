@@ -262,9 +262,11 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     that becomes isometric (White's density-matrix truncation): moving right,
     rho = M_q M_q^T, A_i = its leading eigenvectors and A_j = A_i^T M_q;
     moving left, rho = M_q^T M_q, A_j = eigenvectors^T and A_i = M_q A_j^T.
-    Its eigenvalues are the squared singular values of M_q; the kept set is
-    the `max_bond` largest singular values above `cutoff` over all charges,
-    ties broken by charge order then position.  The isometric factor is
+    Its eigenvalues are the squared singular values of M_q; the kept set
+    follows truncate_svd (truncation/mod.rs:71-99) on the singular values of
+    all charges (ties broken by charge order then position): sigma >=
+    cutoff * sigma_max, at most `max_bond`, at least one; the returned error is
+    the discarded share of sum sigma^2.  The isometric factor is
     orthonormal to rounding and the other factor is the exact projection of
     M_q (no division by small singular values).  Returns (A_i blocks, A_j
     blocks, new bond QIndex, discarded weight), the kept part normalised."""
@@ -304,11 +306,18 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
         eig[q] = Z
         allsv += [(math.sqrt(max(float(x), 0.0)), bi, j) for j, x in enumerate(w)]
     allsv.sort(key=lambda t: (-t[0], t[1], t[2]))
-    keep = [t for t in allsv[:max_bond] if t[0] > cutoff]
+    # truncate_svd (truncation/mod.rs:71-99): keep sigma >= cutoff * sigma_max, at most
+    # max_bond, at least one; the error is the discarded share of sum sigma^2
+    thr = cutoff * (allsv[0][0] if allsv else 0.0)
+    nkeep = 0
+    while nkeep < min(max_bond, len(allsv)) and not allsv[nkeep][0] < thr:
+        nkeep += 1
+    keep = allsv[:max(nkeep, min(1, len(allsv)))]
     kept = {}
     for _, bi, _ in keep:
         kept[charges[bi]] = kept.get(charges[bi], 0) + 1
-    disc = sum(x * x for x, _, _ in allsv[len(keep):])
+    total_sq = sum(x * x for x, _, _ in allsv)
+    disc = (sum(x * x for x, _, _ in allsv[len(keep):]) / total_sq) if total_sq > 0 else 0.0
     nb = QIndex(kind, [(q, kept[q]) for q in charges if q in kept])
     norm = math.sqrt(sum(x * x for x, _, _ in keep)) or 1.0
     Ai, Aj = {}, {}

@@ -85,3 +85,18 @@ def test_truncation_keeps_the_largest_singular_values():
     kept = np.einsum("sab,tbc->stac", A, B) * np.sqrt(np.sum(sv[:D] ** 2))  # undo the normalisation
     # the kept state is the best rank-D approximation: its overlap with T is the kept weight
     assert abs(np.sum(kept * T) - np.sum(sv[:D] ** 2)) < 1e-12
+
+
+def test_truncation_rule_of_truncate_svd():
+    """sigma >= cutoff * sigma_max, at most max_bond, at least one; relative discarded weight
+    (truncation/mod.rs:71-99)."""
+    kind, P, QA, QB, keys, offs, qs, psi = _case()
+    T = _dense(kind, psi, keys, offs, qs, P, QA, QB)
+    d = P.total_dim
+    M = T.transpose(0, 2, 1, 3).reshape(d * QA.total_dim, d * QB.total_dim)
+    sv = np.sort(np.linalg.svd(M, compute_uv=False))[::-1]
+    for cutoff, max_bond in ((0.5, 100), (0.2, 5), (2.0, 100)):
+        want = max(1, min(max_bond, int(np.sum(sv >= cutoff * sv[0]))))
+        _, _, nb, disc = split_two_site(kind, psi * 3.0, keys, offs, [P, P, QA, QB], max_bond, cutoff, True)
+        assert nb.total_dim == want, (cutoff, max_bond)
+        assert abs(disc - np.sum(sv[want:] ** 2) / np.sum(sv ** 2)) < 1e-12
