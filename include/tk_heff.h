@@ -305,6 +305,27 @@ typedef struct {
 tk_status tk_block_gemm_f64(tk_ctx* ctx, const tk_bst* a, const tk_bst* b, tk_bst_out* out);
 void tk_bst_free(tk_bst_out* t);
 
+/*
+ * The dense factorisations of LinAlgBackend (tk-linalg/src/traits.rs:63-148) on
+ * device matrices (tk_mat strides, real f64), with the faer backend's result
+ * conventions (tk-linalg/src/device/faer.rs:127-325).  Synchronous.
+ *   tk_svd_truncated_f64: svd_truncated_gesdd -- singular values descending,
+ *     rank = count of sigma >= cutoff * sigma_max up to max_rank, truncation
+ *     error = sum of the discarded sigma^2; U (m x rank) and Vt (rank x n)
+ *     row-major into device buffers of m*min(m,n) and min(m,n)*n doubles;
+ *     the kept singular values into s_host (min(m,n) doubles).
+ *   tk_eigh_lowest_f64: the k lowest eigenpairs of a symmetric matrix,
+ *     eigenvalues ascending (host), eigenvectors as the columns of an (n x k)
+ *     row-major device matrix; k > n is TK_ERR_INVALID_ARG (EighKTooLarge).
+ *   tk_qr_f64: thin QR, Q (m x k) and R (k x n) row-major, k = min(m, n).
+ */
+tk_status tk_svd_truncated_f64(tk_ctx* ctx, const tk_mat* a, int64_t max_rank, double cutoff, double* u_dev,
+                               double* s_host, double* vt_dev, int64_t* rank, double* truncation_error,
+                               void* stream);
+tk_status tk_eigh_lowest_f64(tk_ctx* ctx, const tk_mat* a, int64_t k, double* evals_host, double* evecs_dev,
+                             void* stream);
+tk_status tk_qr_f64(tk_ctx* ctx, const tk_mat* a, double* q_dev, double* r_dev, void* stream);
+
 /* SparseLinAlgBackend::spmv (tk-linalg/src/traits.rs:193-198): y = A x for
  * a rank-2 host tensor and host vectors (y fully overwritten). */
 tk_status tk_spmv_f64(tk_ctx* ctx, const tk_bst* a, const double* x, double* y);

@@ -86,7 +86,11 @@ tk_status tk_ctx_create(int32_t device, tk_ctx** out) {
     return TK_OK;
 }
 
-void tk_ctx_destroy(tk_ctx* ctx) { delete ctx; }
+void tk_ctx_destroy(tk_ctx* ctx) {
+    if (!ctx) return;
+    ctx_release_solver(ctx);
+    delete ctx;
+}
 
 tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
                                const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,

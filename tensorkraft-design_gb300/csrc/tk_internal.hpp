@@ -8,9 +8,11 @@
 
 #include "../../include/tk_heff.h"
 
-// Library context: the CUDA device it is bound to.
+// Library context: the CUDA device it is bound to, and the cuSOLVER handle of
+// the dense factorisations (created on first use).
 struct tk_ctx {
     int device = 0;
+    void* solver = nullptr;
 };
 
 namespace tk {
@@ -233,5 +235,7 @@ void env_layout(int kind, const QIndex& bra, const QIndex& mpo, const QIndex& ke
 
 // Thread-local last-error message.
 void set_error(const std::string& msg);
+// Releases the context's cuSOLVER handle (dense.cu).
+void ctx_release_solver(tk_ctx* ctx);
 
 }  // namespace tk

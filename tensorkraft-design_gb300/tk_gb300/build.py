@@ -60,7 +60,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    cmd = [NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    cuda_lib = str(Path(NVCC).resolve().parent.parent / "lib64")
+    cmd = [NVCC, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-L", cuda_lib, "-lcusolver",
+           "-Xlinker", "-rpath=" + cuda_lib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

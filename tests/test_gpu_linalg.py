@@ -76,3 +76,73 @@ def test_gemm_strided(lib_built, ta, tb):
     _abi.check(_abi.load().tk_gemm_f64(context(0), 0.5, C.byref(a), C.byref(b), 2.0, C.byref(c), None))
     want = 0.5 * ((A.T if ta else A) @ (B.T if tb else B)) + 2.0 * Cm
     assert np.abs(dC.cpu().numpy() - want).max() < 1e-11
+
+
+def _mat(t, rows, cols, rs, cs):
+    return _abi.tk_mat(C.c_void_p(t.data_ptr()), rows, cols, rs, cs, 0)
+
+
+@pytest.mark.parametrize("m,n,transposed", [(40, 25, False), (25, 40, False), (33, 33, True)])
+def test_svd_truncated_matches_numpy(lib_built, m, n, transposed):
+    """svd_truncated (traits.rs:63-104): singular values descending, the faer
+    truncation rule (device/faer.rs:127-179), U and Vt row-major; strided input."""
+    import torch
+
+    rng = np.random.default_rng(m + n)
+    A = rng.standard_normal((m, n)) @ np.diag(np.logspace(0, -6, n)) if m >= n else \
+        np.diag(np.logspace(0, -6, m)) @ rng.standard_normal((m, n))
+    src = torch.from_numpy(np.ascontiguousarray(A.T if transposed else A)).cuda()
+    mat = _mat(src, m, n, 1 if transposed else n, m if transposed else 1)
+    k = min(m, n)
+    sv_ref = np.linalg.svd(A, compute_uv=False)
+    for max_rank, cutoff in ((k, 0.0), (10, 0.0), (k, 1e-3)):
+        u = torch.empty(m * k, dtype=torch.float64).cuda()
+        vt = torch.empty(k * n, dtype=torch.float64).cuda()
+        s = np.zeros(k)
+        rank, err = C.c_int64(), C.c_double()
+        _abi.check(_abi.load().tk_svd_truncated_f64(context(0), C.byref(mat), max_rank, cutoff,
+                                                    C.c_void_p(u.data_ptr()), _abi.dptr(s),
+                                                    C.c_void_p(vt.data_ptr()), C.byref(rank), C.byref(err), None))
+        r = rank.value
+        want = int(min(max_rank, np.sum(sv_ref >= cutoff * sv_ref[0])))
+        assert r == want
+        assert np.allclose(s[:r], sv_ref[:r], rtol=1e-12, atol=1e-14)
+        assert abs(err.value - np.sum(sv_ref[r:] ** 2)) < 1e-12
+        U = u.cpu().numpy()[:m * r].reshape(m, r)
+        Vt = vt.cpu().numpy()[:r * n].reshape(r, n)
+        assert np.allclose(U.T @ U, np.eye(r), atol=1e-11)
+        assert np.allclose(Vt @ Vt.T, np.eye(r), atol=1e-11)
+        approx = U @ np.diag(s[:r]) @ Vt
+        assert np.linalg.norm(A - approx) ** 2 - np.sum(sv_ref[r:] ** 2) < 1e-10
+
+
+def test_eigh_lowest_and_qr(lib_built):
+    import torch
+
+    rng = np.random.default_rng(3)
+    B = rng.standard_normal((30, 30))
+    S = (B + B.T) / 2
+    st = torch.from_numpy(S).cuda()
+    ev = np.zeros(5)
+    vecs = torch.empty(30 * 5, dtype=torch.float64).cuda()
+    lib = _abi.load()
+    _abi.check(lib.tk_eigh_lowest_f64(context(0), C.byref(_mat(st, 30, 30, 30, 1)), 5, _abi.dptr(ev),
+                                      C.c_void_p(vecs.data_ptr()), None))
+    w = np.linalg.eigvalsh(S)
+    assert np.allclose(ev, w[:5], atol=1e-12)
+    V = vecs.cpu().numpy().reshape(30, 5)
+    assert np.allclose(S @ V, V * ev[None, :], atol=1e-10)
+    assert lib.tk_eigh_lowest_f64(context(0), C.byref(_mat(st, 30, 30, 30, 1)), 31, _abi.dptr(np.zeros(31)),
+                                  C.c_void_p(vecs.data_ptr()), None) == 1  # EighKTooLarge
+    for m, n in ((20, 12), (12, 20)):
+        A = rng.standard_normal((m, n))
+        at = torch.from_numpy(A).cuda()
+        k = min(m, n)
+        q = torch.empty(m * k, dtype=torch.float64).cuda()
+        r = torch.empty(k * n, dtype=torch.float64).cuda()
+        _abi.check(lib.tk_qr_f64(context(0), C.byref(_mat(at, m, n, n, 1)), C.c_void_p(q.data_ptr()),
+                                 C.c_void_p(r.data_ptr()), None))
+        Q, R = q.cpu().numpy().reshape(m, k), r.cpu().numpy().reshape(k, n)
+        assert np.allclose(Q.T @ Q, np.eye(k), atol=1e-12)
+        assert np.allclose(np.tril(R, -1), 0.0)
+        assert np.allclose(Q @ R, A, atol=1e-12)
