@@ -34,6 +34,14 @@ for _p in (str(ROOT), str(PKG)):
 import numpy as np  # noqa: E402
 
 METRIC = "H_eff matvec/s (two-site, D=2048 Hubbard U(1)xU(1))"
+# the metric and data description of each matvec workload (the first is the headline)
+WORKLOADS = {
+    "hubbard_d2048": (METRIC, "synthetic (seeded N(0,1) environments, Gaussian (N,2Sz) sector dims)"),
+    "heisenberg_d1024": ("H_eff matvec/s (two-site, D=1024 Heisenberg chain U(1))",
+                         "synthetic (seeded N(0,1) environments, Gaussian Sz sector dims)"),
+    "cylinder_d4096": ("H_eff matvec/s (two-site, D=4096 width-4 J1 cylinder U(1))",
+                       "synthetic (seeded N(0,1) environments, heavy-tailed Sz sector dims)"),
+}
 UNIT = "matvec/s"
 L2_BYTES = 129 * 1024 * 1024
 STAGES = ["stage1_L_psi", "stage2_wij_combine", "stage3_R"]
@@ -345,7 +353,7 @@ def run_reference(args):
     el = time.perf_counter() - t0
     v = steps / el
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "impl": "reference", "metric": WORKLOADS.get(args.workload, (METRIC,))[0], "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) environments, Gaussian sector dims)",
         "config": {"workload": args.workload, "block_dim": orc.total, "dense_dim": orc.dense_dim, "threads": cores},
@@ -404,6 +412,7 @@ def run_ours(args):
         prec_name = "bf16x3"
     n = plan.block_dim
     flops_total, alg_bytes = plan.cost()
+    launches_per_matvec = plan.launches()
     rng = np.random.default_rng(1 + rank)
     xh = rng.standard_normal(n)
     xh /= np.linalg.norm(xh)
@@ -513,10 +522,11 @@ def run_ours(args):
         cpu = {"value": v, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
                "sample": f"{runs} full matvecs of {args.workload} in {el:.1f} s, all host threads"}
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "metric": WORKLOADS[args.workload][0], "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup,
         "ms_per_step": max_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec_name == "fp64" else "bf16x3 (fp32 accumulate)",
-        "data": "synthetic (seeded N(0,1) environments, Gaussian (N,2Sz) sector dims)",
+        "data": WORKLOADS[args.workload][1],
         "config": {"workload": args.workload, "precision": prec_name, "block_dim": n, "dense_dim": plan.dense_dim,
                    "n_blocks": plan.n_blocks, "alg_gflop_per_matvec": flops_total / 1e9,
                    "alg_mbytes_per_matvec": alg_bytes / 1e6, "l2": "flushed between timed steps",
@@ -526,7 +536,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "api": "tk_heff2_apply_host_flat (pinned FlatBlockStorage host buffers)"},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": launches_per_matvec * args.steps,
         "clocks": clocks,
     }
     if y_fp is not None:

@@ -126,6 +126,10 @@ tk_status tk_heff2_dims(const tk_heff2_plan* plan, int64_t* dense_dim, int64_t* 
 tk_status tk_heff2_blocks(const tk_heff2_plan* plan, uint64_t* keys, int64_t* offsets);
 /* Algorithmic FP64 flops and bytes of one matvec, from the sector tables. */
 tk_status tk_heff2_cost(const tk_heff2_plan* plan, double* flops, double* bytes);
+/* Kernel launches one tk_heff2_apply (or tk_heff2_apply_complex) issues in
+ * the plan's current precision and schedule (no reference counterpart:
+ * launch accounting for benchmarks). */
+tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_apply);
 tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
 
 /* Launch schedule of the FP64 sector GEMMs.  TK_SCHED_GROUPED (default): all

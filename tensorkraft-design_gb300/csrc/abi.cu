@@ -251,6 +251,32 @@ static tk_status apply_fp64(tk_heff2_plan* p, const double* x, double* y, cudaSt
     return TK_OK;
 }
 
+static int per_block_launches(const DevGemm& g) {
+    int n = 0;
+    for (size_t t = 0; t + 1 < g.task_tile_begin.size(); ++t) n += g.task_tile_begin[t + 1] > g.task_tile_begin[t];
+    return n;
+}
+
+extern "C" tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_apply) {
+    if (!plan || !per_apply) {
+        set_error("tk_heff2_launches: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    const tk_heff2_plan* p = plan;
+    int n = 0;
+    if (p->is_complex) {
+        n = 4 * (p->g1.n_tiles > 0) + 2 * (p->n_jobs > 0) + 4 * (p->g3.n_tiles > 0);
+    } else if (p->precision == TK_PREC_BF16X3) {
+        n = tc_launches(*p->tc);
+    } else if (p->schedule == TK_SCHED_PER_BLOCK) {
+        n = per_block_launches(p->g1) + (p->n_jobs > 0) + per_block_launches(p->g3);
+    } else {
+        n = (p->g1.n_tiles > 0) + (p->n_jobs > 0) + (p->g3.n_tiles > 0);
+    }
+    *per_apply = n;
+    return TK_OK;
+}
+
 // The complex FP64 matvec: each stage's GEMM as four real launches over the
 // same tables (planar operands); the channel combine (real MPO) on each part.
 tk_status tk_heff2_apply_complex_s(tk_heff2_plan* p, const double* xr, const double* xi, double* yr, double* yi,

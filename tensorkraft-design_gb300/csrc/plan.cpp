@@ -340,7 +340,24 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
         err = "T1 column tables";
         return false;
     }
-    for (const TcTile& t : C.tiles1) {
+    for (const TcTile& t : C.tiles1x) {
+        if (t.b_cs <= 0 || t.kch <= 0 ||
+            (int64_t)t.b_row + (int64_t)(t.kch - 1) * t.b_cs + t.n_valid - 1 >= C.xq_rows) {
+            err = "tensor-core stage 1 split-copy operand";
+            return false;
+        }
+    }
+    for (const TcSplitJob& j : C.split) {
+        const int64_t nb = std::min<int64_t>(32, (int64_t)j.cols - j.b0);
+        const int64_t imax = (((int64_t)j.xrow + (int64_t)(j.a0 / kTcBK) * j.cstride + j.b0 + nb - 1) << 6) + 63;
+        if (j.rows <= 0 || j.cols <= 0 || j.src < 0 || j.src + (int64_t)j.rows * j.cols > T.total || j.xrow < 0 ||
+            j.cstride <= 0 || j.a0 < 0 || j.a0 >= j.rows || j.a0 % kTcBK != 0 || j.b0 < 0 || j.b0 >= j.cols ||
+            imax >= C.xq_rows * kTcBK) {
+            err = "tensor-core split job";
+            return false;
+        }
+    }
+    auto tile1_ok = [&](const TcTile& t) {
         if (t.mode != 2 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
             t.n_mma < t.n_valid || t.n_mma > kTcBN || t.n_mma % 16 != 0 || t.out_off < 0 || t.ldc < 0 ||
             t.out_off + t.n_valid > (int64_t)C.t1col_base.size() || t.a_row < 0 || t.b_row < 0) {
@@ -363,7 +380,12 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
                 return false;
             }
         }
-    }
+        return true;
+    };
+    for (const TcTile& t : C.tiles1)
+        if (!tile1_ok(t)) return false;
+    for (const TcTile& t : C.tiles1x)
+        if (!tile1_ok(t)) return false;
     for (const TcTile& t : C.tiles3) {
         if (t.n_mma < t.n_valid || t.n_mma > kTcBN || t.n_mma % 16 != 0) { err = "tensor-core stage 3 tile N"; return false; }
         if (t.mode != 1 || t.m_valid <= 0 || t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 ||
@@ -801,11 +823,33 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     C.xstride.push_back((int32_t)DB);
                 }
             }
+            // tall stacks: psi split once into a bf16 copy (K-major chunks,
+            // column b of block (p, B) on operand row xb + xcol + b of chunk 0)
+            const bool tall = (rows + kTcBM - 1) / kTcBM > kTcFuseMaxMTiles;
+            const int64_t xb = C.xq_rows;
+            if (tall) {
+                C.xq_rows += kch * cols;
+                for (size_t jx = 0; jx < xp.size(); ++jx) {
+                    TcSplitJob j{};
+                    j.src = SUB(xp[jx].first, a, xp[jx].second);
+                    j.rows = (int32_t)K;
+                    j.cols = (int32_t)QB.dim[xp[jx].second];
+                    j.xrow = (int32_t)(xb + xcol[jx]);
+                    j.cstride = (int32_t)cols;
+                    for (int32_t a0 = 0; a0 < j.rows; a0 += BK)
+                        for (int32_t b0 = 0; b0 < j.cols; b0 += 32) {
+                            j.a0 = a0;
+                            j.b0 = b0;
+                            C.split.push_back(j);
+                        }
+                }
+            }
             for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
                 for (int64_t n0 = 0; n0 < cols; n0 += kTcBN) {
                     TcTile t{};
                     t.a_row = (int32_t)(lb + m0); t.a_cs = (int32_t)rows;
-                    t.b_row = 0; t.b_cs = 0;
+                    t.b_row = tall ? (int32_t)(xb + n0) : 0;
+                    t.b_cs = tall ? (int32_t)cols : 0;
                     t.k_valid = (int32_t)K;
                     t.kch = kch;
                     t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
@@ -814,7 +858,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     t.mode = 2;
                     t.out_off = colbase0 + n0;
                     t.ldc = (int32_t)m0;
-                    C.tiles1.push_back(t);
+                    (tall ? C.tiles1x : C.tiles1).push_back(t);
                     C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
             for (size_t i = 0; i < lp.size(); ++i)
@@ -927,6 +971,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                 }
         }
         for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
+        for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
         for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
         // split the constant operands into bf16 hi + lo
         auto split = [](const std::vector<double>& v, std::vector<uint16_t>& hi, std::vector<uint16_t>& lo) {
@@ -940,7 +985,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
         };
         split(lq64, C.lq_hi, C.lq_lo);
         split(rq64, C.rq_hi, C.rq_lo);
-        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
+        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
             err = "tensor-core operand rows exceed 32 bits";
             return TK_ERR_UNSUPPORTED;
         }

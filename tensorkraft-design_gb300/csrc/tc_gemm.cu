@@ -4,12 +4,17 @@
 // a product a*b is evaluated as hi_a*hi_b + hi_a*lo_b + lo_a*hi_b with fp32
 // accumulation in tensor memory (the lo*lo term, ~2^-16 relative, is dropped).
 //
-// One matvec = three launches on one stream:
+// One matvec = three to five launches on one stream:
+//   split_psi_kernel   psi sub-blocks of tall stage-1 stacks -> bf16 hi/lo copy
+//   tc_gemm_kernel     stage 1 of the tall stacks, B operand from that copy
 //   tc_gemm1_kernel    stage 1, T1 = L_stack(A) * psi_A        (fp32 out); the
 //                      psi operand is read from the fp64 vector and split into
 //                      bf16 hi/lo in shared memory by the kernel itself
 //   combine_tc_kernel  W_i*W_j channel combine, T1 -> stage-3 A operand hi/lo
 //   tc_gemm_kernel     stage 3, y = T2_stack(B') * R_stack(B')^T (fp64 out via a row table)
+// A stage-1 stack of more than kTcFuseMaxMTiles row tiles would have every row
+// tile split the same psi columns again; those stacks (the large sectors of
+// wide bonds) take the split copy, made once per matvec, instead.
 //
 // tc_gemm_kernel: one CTA (4 warps) per 128 x 64 output tile.  Warp 0 lane 0
 // streams 64-wide K chunks of A_hi, A_lo, B_hi, B_lo with TMA (128-byte
@@ -516,6 +521,54 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
     }
 }
 
+constexpr int kSplitThreads = 128;  // split: threads per job
+
+// psi sub-block tile (64 a x 32 b of a row-major D_A x D_B block, a0 at a K
+// chunk boundary) -> 32 rows of the split copy (row = column b, 64 bf16 along
+// a), hi and lo.  The tile goes through shared memory so that psi is read
+// along b (256-byte row segments) and the copy written along a (four threads
+// per 128-byte row, 16-byte stores).  a past D_A is written as zero (K
+// padding of that column's own row).
+__global__ void __launch_bounds__(kSplitThreads) split_psi_kernel(const TcSplitJob* __restrict__ jobs,
+                                                                  const double* __restrict__ x,
+                                                                  __nv_bfloat16* __restrict__ xh,
+                                                                  __nv_bfloat16* __restrict__ xl) {
+    __shared__ double buf[kTcBK][33];
+    const TcSplitJob j = jobs[blockIdx.x];
+    grid_dep_launch();
+    const int na = min(kTcBK, j.rows - j.a0), nb = min(32, j.cols - j.b0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    grid_dep_wait();
+    double v[kTcBK / 4];
+#pragma unroll
+    for (int u = 0; u < kTcBK / 4; ++u) {
+        const int a = w + 4 * u;
+        v[u] = (a < na && lane < nb) ? x[j.src + (int64_t)(j.a0 + a) * j.cols + j.b0 + lane] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kTcBK / 4; ++u) buf[w + 4 * u][lane] = v[u];
+    __syncthreads();
+    const int b = threadIdx.x >> 2, ab = (threadIdx.x & 3) * 16;
+    if (b < nb) {
+        uint32_t hw[8], lw[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            __nv_bfloat16 h0, l0, h1, l1;
+            split2(buf[ab + 2 * i][b], h0, l0);
+            split2(buf[ab + 2 * i + 1][b], h1, l1);
+            hw[i] = pack2(h0, h1);
+            lw[i] = pack2(l0, l1);
+        }
+        const int64_t row = (int64_t)j.xrow + (int64_t)(j.a0 / kTcBK) * j.cstride + j.b0 + b;
+        uint4* ph = reinterpret_cast<uint4*>(xh + row * kTcBK + ab);
+        uint4* pl = reinterpret_cast<uint4*>(xl + row * kTcBK + ab);
+        ph[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        ph[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+        pl[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        pl[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+    }
+}
+
 constexpr int kCombThreads = 128;  // combine: threads per job
 
 // W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.  One
@@ -639,8 +692,10 @@ bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string
 struct TcPlan {
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
     __nv_bfloat16 *th = nullptr, *tl = nullptr;
+    __nv_bfloat16 *xh = nullptr, *xl = nullptr;  // split copy of psi (tall stage-1 stacks)
     float* t1 = nullptr;
-    TcTile *tiles1 = nullptr, *tiles3 = nullptr;
+    TcTile *tiles1 = nullptr, *tiles1x = nullptr, *tiles3 = nullptr;
+    TcSplitJob* split = nullptr;
     TcCombJob* jobs = nullptr;
     TcCombTerm* terms = nullptr;
     int64_t* yrow = nullptr;
@@ -649,12 +704,12 @@ struct TcPlan {
     int64_t* xsrc = nullptr;
     int32_t* xstride = nullptr;
     int* err = nullptr;
-    int n1 = 0, n3 = 0, njobs = 0;
-    int nst1 = 1, nst3 = 2;  // pipeline stages of the two GEMM launches
-    CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl;
+    int n1 = 0, n1x = 0, n3 = 0, nsplit = 0, njobs = 0;
+    int nst1 = 1, nst1x = 2, nst3 = 2;  // pipeline stages of the GEMM launches
+    CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl, mXh, mXl;
     ~TcPlan() {
-        void* ps[] = {lh,   ll,    rh,   rl,         th,           tl,   t1,      tiles1, tiles3,
-                      jobs, terms, yrow, t1col_base, t1col_stride, xsrc, xstride, err};
+        void* ps[] = {lh,    ll,    rh,   rl,         th,           tl,   xh,      xl,  t1, tiles1, tiles1x,
+                      tiles3, split, jobs, terms, yrow, t1col_base, t1col_stride, xsrc, xstride, err};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -681,7 +736,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     if ((e = put(&p->lh, bf(C.lq_hi))) != cudaSuccess || (e = put(&p->ll, bf(C.lq_lo))) != cudaSuccess ||
         (e = put(&p->rh, bf(C.rq_hi))) != cudaSuccess || (e = put(&p->rl, bf(C.rq_lo))) != cudaSuccess ||
         (e = zeros(&p->th, C.t2q_rows)) != cudaSuccess || (e = zeros(&p->tl, C.t2q_rows)) != cudaSuccess ||
+        (e = zeros(&p->xh, C.xq_rows)) != cudaSuccess || (e = zeros(&p->xl, C.xq_rows)) != cudaSuccess ||
         (e = put(&p->tiles1, C.tiles1)) != cudaSuccess || (e = put(&p->tiles3, C.tiles3)) != cudaSuccess ||
+        (e = put(&p->tiles1x, C.tiles1x)) != cudaSuccess || (e = put(&p->split, C.split)) != cudaSuccess ||
         (e = put(&p->xsrc, C.xsrc)) != cudaSuccess || (e = put(&p->xstride, C.xstride)) != cudaSuccess ||
         (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
         (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess ||
@@ -696,11 +753,15 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
     p->n1 = (int)C.tiles1.size();
+    p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
+    p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
+    p->nst1x = C.max_kch1x <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
+        !make_map(&p->mXh, p->xh, C.xq_rows, 16, err) || !make_map(&p->mXl, p->xl, C.xq_rows, 16, err) ||
         !make_map(&p->mTh, p->th, C.t2q_rows, kTcBM, err) || !make_map(&p->mTl, p->tl, C.t2q_rows, kTcBM, err) ||
         !make_map(&p->mRh, p->rh, C.rq_rows, 16, err) || !make_map(&p->mRl, p->rl, C.rq_rows, 16, err))
         return TK_ERR_CUDA;
@@ -752,6 +813,9 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
                            double* y, cudaStream_t s, int stage, std::string& err) {
     if (stage == 0) {
         const OutMap om{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride};
+        if (tc.nsplit > 0)
+            launch_pdl(split_psi_kernel, tc.nsplit, kSplitThreads, 0, s, (const TcSplitJob*)tc.split, x, tc.xh, tc.xl);
+        launch_tc_gemm(tc.nst1x, tc.n1x, tc.tiles1x, tc.mLh, tc.mLl, tc.mXh, tc.mXl, om, tc.err, s);
         if (tc.n1 > 0) {
             if (tc.nst1 == 1)
                 launch_pdl(tc_gemm1_kernel<1>, tc.n1, 128, smem_bytes(1), s, (const TcTile*)tc.tiles1, tc.mLh, tc.mLl,
@@ -813,6 +877,10 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 }
 
 int* tc_error_word(TcPlan& tc) { return tc.err; }
+
+int tc_launches(const TcPlan& tc) {
+    return (tc.nsplit > 0) + (tc.n1x > 0) + (tc.n1 > 0) + (tc.njobs > 0) + (tc.n3 > 0);
+}
 
 tk_status tc_check_error(TcPlan& tc, cudaStream_t s) {
     int h = 0;

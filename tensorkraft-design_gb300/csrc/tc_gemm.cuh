@@ -36,6 +36,8 @@ namespace tk {
 cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* bad, cudaStream_t s);
 // Device error word of the tensor-core kernels (0 = no bounded wait ran out).
 int* tc_error_word(TcPlan& tc);
+// Kernel launches of one split-precision matvec (tc_apply).
+int tc_launches(const TcPlan& tc);
 // Synchronises `s`, reads and clears the error word: TK_ERR_TIMEOUT if set.
 tk_status tc_check_error(TcPlan& tc, cudaStream_t s);
 }  // namespace tk

@@ -134,8 +134,11 @@ bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>
 // "stacks" that share one operand:
 //   stage 1, one stack per ket sector A of L: rows = every L slab (A', ws, A)
 //     stacked, columns = every psi sub-block (p, A, B) side by side, K = D_A
-//     (the psi operand is read and split straight from the fp64 vector by
-//     the stage-1 kernel, through the per-column tables xsrc / xstride);
+//     (stacks of at most kTcFuseMaxMTiles row tiles read and split the psi
+//     operand straight from the fp64 vector inside the stage-1 kernel,
+//     through the per-column tables xsrc / xstride; taller stacks, whose
+//     row tiles would each split the same columns again, take it from a
+//     bf16 hi/lo copy made once per matvec by the split kernel);
 //   stage 3, one stack per bra sector B' of R: rows = every y sub-block
 //     (p', A', B') stacked, columns = D_B', K = every R slab (B', ws, B)
 //     concatenated.
@@ -147,6 +150,7 @@ bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>
 constexpr int kTcBM = 128;  // rows per tensor-core tile (UMMA M)
 constexpr int kTcBN = 64;   // columns per tensor-core tile (UMMA N)
 constexpr int kTcBK = 64;   // K chunk (128 bytes of bf16: one swizzle atom)
+constexpr int kTcFuseMaxMTiles = 3;  // stage-1 stacks this tall (in row tiles) split psi in the GEMM kernel
 
 struct TcTile {
     int32_t a_row, a_cs;     // A operand row of chunk 0 at this tile's m0; rows between chunks
@@ -155,6 +159,15 @@ struct TcTile {
     int64_t out_off;         // mode 1: row-table index of m0; mode 2: column-table index of n0
     int32_t ldc, n0;         // mode 1: n0 = column offset added to the row table; mode 2: ldc = m0
     int32_t n_mma, k_valid;  // UMMA N (n_valid rounded up to 16, <= kTcBN); stage 1: K of the stack (D_A)
+};
+// psi sub-block -> stage-1 B operand of a tall stack (K-major chunks), hi/lo
+// split.  One job = one 64 (a) x 32 (b) tile of a D_A x D_B sub-block, a0 a
+// multiple of 64 (one K chunk).
+struct TcSplitJob {
+    int64_t src;             // flat offset of the (D_A x D_B) sub-block
+    int32_t rows, cols;      // D_A (becomes K), D_B (becomes N)
+    int32_t xrow, cstride;   // operand row of chunk 0 for column 0; rows between chunks
+    int32_t a0, b0;          // tile origin inside the sub-block
 };
 // T1 (fp32) -> stage-3 A operand (K-major chunks), hi/lo split.  One job =
 // rows [r0, r0 + rows) of one output slab, at most kTcCombMaxElems elements
@@ -170,9 +183,11 @@ struct TcCombTerm {
     float coef;
 };
 struct TcTables {
-    int64_t lq_rows = 0, rq_rows = 0, t2q_rows = 0, t1_total = 0;
+    int64_t lq_rows = 0, rq_rows = 0, xq_rows = 0, t2q_rows = 0, t1_total = 0;
     std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
     std::vector<TcTile> tiles1, tiles3;
+    std::vector<TcTile> tiles1x;       // stage-1 tiles of tall stacks (B operand from the split copy)
+    std::vector<TcSplitJob> split;     // psi -> split copy, tall stacks only
     std::vector<TcCombJob> jobs;
     std::vector<TcCombTerm> terms;
     std::vector<int64_t> yrow;  // y element offset of every stage-3 operand row
@@ -185,7 +200,7 @@ struct TcTables {
     std::vector<int64_t> xsrc;
     std::vector<int32_t> xstride;
     double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
-    int32_t max_kch1 = 0, max_kch3 = 0;
+    int32_t max_kch1 = 0, max_kch1x = 0, max_kch3 = 0;
 };
 
 // Everything the device needs for one two-site H_eff, built on the host.

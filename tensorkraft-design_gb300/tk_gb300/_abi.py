@@ -93,6 +93,7 @@ SIGNATURES = [
     ("tk_heff2_dims", C.c_int32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("tk_heff2_blocks", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
     ("tk_heff2_cost", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("tk_heff2_launches", C.c_int32, [C.c_void_p, C.POINTER(C.c_int32)]),
     ("tk_heff2_set_precision", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_set_schedule", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_profile", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,

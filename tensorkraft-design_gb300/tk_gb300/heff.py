@@ -216,6 +216,12 @@ class Heff2Plan:
         check(self._lib.tk_heff2_cost(self._h, C.byref(f), C.byref(b)))
         return f.value, b.value
 
+    def launches(self) -> int:
+        """Kernel launches of one apply in the current precision and schedule."""
+        n = C.c_int32()
+        check(self._lib.tk_heff2_launches(self._h, C.byref(n)))
+        return n.value
+
     def set_schedule(self, schedule: int):
         """FP64 GEMM launch schedule: _abi.SCHED_GROUPED or _abi.SCHED_PER_BLOCK."""
         check(self._lib.tk_heff2_set_schedule(self._h, schedule))
