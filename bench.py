@@ -464,20 +464,29 @@ def run_ours(args):
         y_fp = float(torch.linalg.norm(yb - y64) / torch.linalg.norm(y64))
         plan.set_precision(PREC_BF16X3)
     # end-to-end through the C ABI with pinned host buffers (H2D + matvec + D2H per step)
+    from tk_gb300 import _abi
+
     hx = torch.from_numpy(xh).pin_memory()
     hy = torch.empty_like(hx).pin_memory()
-    for _ in range(max(1, args.warmup)):
-        plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
-    if ws > 1:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = args.steps * ws / float(te.item())
+
+    def e2e_run(mode):
+        plan.set_host_io(mode)
+        for _ in range(max(1, args.warmup)):
+            plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
+        if ws > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
+        te = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
+        if ws > 1:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        return args.steps * ws / float(te.item())
+
+    # the three transfer forms, then the library's default (its per-plan choice)
+    e2e_modes = {name: e2e_run(m) for name, m in (("staged", _abi.HOST_IO_STAGED), ("direct", _abi.HOST_IO_DIRECT),
+                                                  ("direct_out", _abi.HOST_IO_DIRECT_OUT))}
+    e2e_value = e2e_run(_abi.HOST_IO_AUTO)
     lz = None
     if not args.no_lanczos and rank == 0:
         lz = lanczos_compare(plan, torch, dev, prec_name != "fp64")
@@ -535,7 +544,11 @@ def run_ours(args):
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
-                "api": "tk_heff2_apply_host_flat (pinned FlatBlockStorage host buffers)"},
+                "api": "tk_heff2_apply_host_flat (pinned FlatBlockStorage host buffers)",
+                "host_io": ("library default (TK_HOST_IO_AUTO): the stage-3 kernel writes y to the pinned host "
+                            "buffer; psi read from it directly when the split kernel does most psi reads, else "
+                            "copied in" if prec_name != "fp64" else "staged: H2D copy, matvec, D2H copy"),
+                "by_host_io": e2e_modes},
         "gpu_launches": launches_per_matvec * args.steps,
         "clocks": clocks,
     }

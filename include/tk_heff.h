@@ -130,6 +130,24 @@ tk_status tk_heff2_cost(const tk_heff2_plan* plan, double* flops, double* bytes)
  * the plan's current precision and schedule (no reference counterpart:
  * launch accounting for benchmarks). */
 tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_apply);
+/* How tk_heff2_apply_host_flat moves x and y (no reference counterpart).
+ * The direct forms apply when the plan runs split precision and the buffer
+ * is page-locked host memory mapped into the device address space
+ * (cudaHostAlloc / cudaHostRegister); otherwise that buffer is staged.
+ * TK_HOST_IO_STAGED: copy x into a device buffer, run, copy y back.
+ * TK_HOST_IO_DIRECT: the kernels read psi from x and write y in host memory
+ *   over the CPU-GPU link, overlapping the transfers with the GEMMs.
+ * TK_HOST_IO_DIRECT_OUT: x is copied in; the stage-3 kernel writes y to host
+ *   memory directly (every y element is written once).
+ * TK_HOST_IO_AUTO (default): DIRECT when most psi reads of the plan come from
+ *   the split kernel (tall stacks, one coalesced read per element), else
+ *   DIRECT_OUT (the in-GEMM psi split reads columns with a stride, which the
+ *   link serves poorly). */
+#define TK_HOST_IO_STAGED     0
+#define TK_HOST_IO_DIRECT     1
+#define TK_HOST_IO_DIRECT_OUT 2
+#define TK_HOST_IO_AUTO       3
+tk_status tk_heff2_set_host_io(tk_heff2_plan* plan, int32_t mode);
 tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
 
 /* Launch schedule of the FP64 sector GEMMs.  TK_SCHED_GROUPED (default): all

@@ -344,6 +344,39 @@ static tk_status ensure_host_staging(tk_heff2_plan* p) {
     if (!p->hy.p) TK_CUDA(p->hy.alloc(n));
     if (!p->pin_x) TK_CUDA(cudaMallocHost(&p->pin_x, sizeof(double) * n));
     if (!p->pin_y) TK_CUDA(cudaMallocHost(&p->pin_y, sizeof(double) * n));
+    if (!p->pin_err) {
+        TK_CUDA(cudaMallocHost(&p->pin_err, sizeof(int)));
+        *p->pin_err = 0;
+    }
+    return TK_OK;
+}
+
+// Device address of page-locked, mapped host memory; nullptr for anything else.
+static void* mapped_host_ptr(const void* h) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Queues the read-back of the tensor-core error word behind the matvec,
+// waits for the stream once, and reports a bounded wait that ran out.
+static tk_status finish_host_call(tk_heff2_plan* p, cudaStream_t s) {
+    const bool tc = p->precision == TK_PREC_BF16X3;
+    if (tc) TK_CUDA(cudaMemcpyAsync(p->pin_err, tc_error_word(*p->tc), sizeof(int), cudaMemcpyDeviceToHost, s));
+    TK_CUDA(cudaStreamSynchronize(s));
+    if (tc && *p->pin_err != 0) return tc_check_error(*p->tc, s);
+    return TK_OK;
+}
+
+tk_status tk_heff2_set_host_io(tk_heff2_plan* plan, int32_t mode) {
+    if (!plan || mode < TK_HOST_IO_STAGED || mode > TK_HOST_IO_AUTO) {
+        set_error("tk_heff2_set_host_io: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    plan->host_io = mode;
     return TK_OK;
 }
 
@@ -385,13 +418,15 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
     tk_status st = ensure_host_staging(plan);
     if (st != TK_OK) return st;
     cudaStream_t s = plan->stream;
-    TK_CUDA(cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, plan->precision);
+    int mode = plan->precision == TK_PREC_BF16X3 ? plan->host_io : TK_HOST_IO_STAGED;
+    if (mode == TK_HOST_IO_AUTO) mode = tc_prefers_direct_input(*plan->tc) ? TK_HOST_IO_DIRECT : TK_HOST_IO_DIRECT_OUT;
+    const double* dx = mode == TK_HOST_IO_DIRECT ? static_cast<const double*>(mapped_host_ptr(x)) : nullptr;
+    double* dy = mode != TK_HOST_IO_STAGED ? static_cast<double*>(mapped_host_ptr(y)) : nullptr;
+    if (!dx) TK_CUDA(cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    st = tk_heff2_apply_prec(plan, dx ? dx : plan->hx.p, dy ? dy : plan->hy.p, s, plan->precision);
     if (st != TK_OK) return st;
-    TK_CUDA(cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-    TK_CUDA(cudaStreamSynchronize(s));
-    if (plan->precision == TK_PREC_BF16X3) return tc_check_error(*plan->tc, s);
-    return TK_OK;
+    if (!dy) TK_CUDA(cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    return finish_host_call(plan, s);
 }
 
 tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {
@@ -410,8 +445,7 @@ tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {
         st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, plan->precision);
         if (st != TK_OK) return st;
         TK_CUDA(cudaMemcpyAsync(plan->pin_y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-        TK_CUDA(cudaStreamSynchronize(s));
-        if (plan->precision == TK_PREC_BF16X3 && (st = tc_check_error(*plan->tc, s)) != TK_OK) return st;
+        if ((st = finish_host_call(plan, s)) != TK_OK) return st;
     }
     return tk_heff2_flat_to_dense(plan, plan->pin_y, y);
 }

@@ -29,6 +29,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -706,6 +707,8 @@ struct TcPlan {
     int* err = nullptr;
     int n1 = 0, n1x = 0, n3 = 0, nsplit = 0, njobs = 0;
     int nst1 = 1, nst1x = 2, nst3 = 2;  // pipeline stages of the GEMM launches
+    // psi elements read per matvec by the in-GEMM split (every row tile) and by the split kernel
+    double psi_reads_fused = 0.0, psi_reads_split = 0.0;
     CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl, mXh, mXl;
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,         th,           tl,   xh,      xl,  t1, tiles1, tiles1x,
@@ -757,6 +760,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n3 = (int)C.tiles3.size();
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
+    for (const TcTile& t : C.tiles1) p->psi_reads_fused += (double)t.k_valid * t.n_valid;
+    for (const TcSplitJob& j : C.split)
+        p->psi_reads_split += (double)std::min(kTcBK, j.rows - j.a0) * std::min(32, j.cols - j.b0);
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
     p->nst1x = C.max_kch1x <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
@@ -877,6 +883,8 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 }
 
 int* tc_error_word(TcPlan& tc) { return tc.err; }
+
+bool tc_prefers_direct_input(const TcPlan& tc) { return tc.psi_reads_split >= tc.psi_reads_fused; }
 
 int tc_launches(const TcPlan& tc) {
     return (tc.nsplit > 0) + (tc.n1x > 0) + (tc.n1 > 0) + (tc.njobs > 0) + (tc.n3 > 0);

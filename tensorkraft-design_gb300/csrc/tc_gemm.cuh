@@ -38,6 +38,9 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 int* tc_error_word(TcPlan& tc);
 // Kernel launches of one split-precision matvec (tc_apply).
 int tc_launches(const TcPlan& tc);
+// True when most psi reads of a matvec come from the split kernel (coalesced,
+// one per element) rather than from the in-GEMM split (strided, per row tile).
+bool tc_prefers_direct_input(const TcPlan& tc);
 // Synchronises `s`, reads and clears the error word: TK_ERR_TIMEOUT if set.
 tk_status tc_check_error(TcPlan& tc, cudaStream_t s);
 }  // namespace tk

@@ -85,6 +85,8 @@ struct tk_heff2_plan {
     tk::DevBuf<double> hx, hy;
     double* pin_x = nullptr;
     double* pin_y = nullptr;
+    int* pin_err = nullptr;   // tensor-core error word, read back with the result
+    int host_io = TK_HOST_IO_AUTO;
     cudaStream_t stream = nullptr;
     // split-precision operands and state (tensor-core path)
     std::unique_ptr<tk::TcPlan, tk::TcPlanDeleter> tc;
@@ -102,6 +104,7 @@ struct tk_heff2_plan {
     ~tk_heff2_plan() {
         if (pin_x) cudaFreeHost(pin_x);
         if (pin_y) cudaFreeHost(pin_y);
+        if (pin_err) cudaFreeHost(pin_err);
         if (stream) cudaStreamDestroy(stream);
     }
 };

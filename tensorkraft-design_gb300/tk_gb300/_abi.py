@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "SECTOR_MISMATCH", 3: "OOM", 4: "C
                 6: "CANCELLED", 7: "UNSUPPORTED"}
 PREC_FP64, PREC_BF16X3 = 0, 1
 SCHED_GROUPED, SCHED_PER_BLOCK = 0, 1
+HOST_IO_STAGED, HOST_IO_DIRECT, HOST_IO_DIRECT_OUT, HOST_IO_AUTO = 0, 1, 2, 3
 
 
 class TkError(RuntimeError):
@@ -94,6 +95,7 @@ SIGNATURES = [
     ("tk_heff2_blocks", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
     ("tk_heff2_cost", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("tk_heff2_launches", C.c_int32, [C.c_void_p, C.POINTER(C.c_int32)]),
+    ("tk_heff2_set_host_io", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_set_precision", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_set_schedule", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_profile", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,

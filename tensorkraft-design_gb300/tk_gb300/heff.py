@@ -222,6 +222,10 @@ class Heff2Plan:
         check(self._lib.tk_heff2_launches(self._h, C.byref(n)))
         return n.value
 
+    def set_host_io(self, mode: int):
+        """Host-buffer matvec transfers: one of _abi.HOST_IO_STAGED / DIRECT / DIRECT_OUT / AUTO."""
+        check(self._lib.tk_heff2_set_host_io(self._h, mode))
+
     def set_schedule(self, schedule: int):
         """FP64 GEMM launch schedule: _abi.SCHED_GROUPED or _abi.SCHED_PER_BLOCK."""
         check(self._lib.tk_heff2_set_schedule(self._h, schedule))

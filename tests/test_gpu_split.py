@@ -106,3 +106,31 @@ def test_integer_pipe_conversions_match_hardware(lib_built):
     _abi.check(_abi.load().tk_check_split_conversions(context(0), C.c_void_p(x.data_ptr()), x.numel(),
                                                       C.byref(bad)))
     assert bad.value == 0
+
+
+def test_host_io_direct_matches_staged(lib_built):
+    """Split matvec from page-locked host buffers: the kernels reading psi and
+    writing y over the CPU-GPU link give the same bits as the staged copies."""
+    import torch
+
+    from tk_gb300 import _abi
+
+    p = small_problem("cylinder", 512)
+    plan = p.plan(precision=PREC_BF16X3)
+    x = np.random.default_rng(5).standard_normal(plan.block_dim)
+    hx = torch.from_numpy(x).pin_memory()
+    out = {}
+    modes = (_abi.HOST_IO_STAGED, _abi.HOST_IO_DIRECT, _abi.HOST_IO_DIRECT_OUT, _abi.HOST_IO_AUTO)
+    for mode in modes:
+        plan.set_host_io(mode)
+        hy = torch.full_like(hx, float("nan")).pin_memory()
+        plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
+        out[mode] = hy.numpy().copy()
+    for mode in modes[1:]:
+        assert np.array_equal(out[_abi.HOST_IO_STAGED], out[mode]), mode
+    assert rel_err(out[_abi.HOST_IO_AUTO], oracle_bs(p).apply(x)) < SPLIT_TOL
+    # pageable buffers fall back to staged copies in every mode
+    plan.set_host_io(_abi.HOST_IO_DIRECT)
+    y = np.zeros_like(x)
+    plan.apply_host_flat(x, y)
+    assert np.array_equal(y, out[_abi.HOST_IO_STAGED])
