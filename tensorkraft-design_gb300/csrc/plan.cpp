@@ -406,6 +406,13 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
             (size_t)j.term_end > C.terms.size()) { err = "tensor-core combine job"; return false; }
         for (int t = j.term_begin; t < j.term_end; ++t) {
             const TcCombTerm& c = C.terms[t];
+            if (t - j.term_begin < kTcCombInline) {
+                const TcCombTerm& d = j.inl[t - j.term_begin];
+                if (d.in_off != c.in_off || d.in_rs != c.in_rs || d.coef != c.coef) {
+                    err = "tensor-core combine inline term";
+                    return false;
+                }
+            }
             if (c.in_off < 0 || c.in_off + (int64_t)(j.r0 + j.rows - 1) * c.in_rs + j.cols - 1 >= C.t1_total) {
                 err = "tensor-core combine term";
                 return false;
@@ -940,6 +947,8 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                             }
                         }
                         j.term_end = (int32_t)C.terms.size();
+                        for (int q = 0; q < kTcCombInline && j.term_begin + q < j.term_end; ++q)
+                            j.inl[q] = C.terms[j.term_begin + q];
                         if (j.term_end > j.term_begin) {
                             // row chunks of at most kTcCombMaxElems elements
                             const int32_t all_rows = j.rows;

@@ -222,13 +222,17 @@ __device__ __forceinline__ void store_out(const TcTile& t, int row, int col, flo
         o.out64[o.rowtab[t.out_off + row] + t.n0 + col] = (double)v;
 }
 
+// Operands a launch may read before its dependency wait: they are plan
+// constants (the split L or R operand), not written by any kernel.
+constexpr int CONST_A = 1, CONST_B = 2;
+
 template <int NST>
 __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restrict__ tiles,
                                                          const __grid_constant__ CUtensorMap mAh,
                                                          const __grid_constant__ CUtensorMap mAl,
                                                          const __grid_constant__ CUtensorMap mBh,
                                                          const __grid_constant__ CUtensorMap mBl, const OutMap om,
-                                                         int* err) {
+                                                         int const_ops, int* err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
@@ -244,6 +248,22 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         for (int e = threadIdx.x; e < t.m_valid * t.n_valid; e += blockDim.x)
             store_out(t, e / t.n_valid, e % t.n_valid, 0.f, om);
         return;
+    }
+    // epilogue addressing from the (constant) plan tables, fetched up front:
+    // mode 2, lane c (+32) holds output column c's base and stride; mode 1,
+    // lane r holds the y offset of accumulator row 32 * warp + r
+    int64_t cb[2] = {0, 0};
+    int32_t cs[2] = {0, 0};
+    int64_t my_row = 0;
+    if (t.mode == 2) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (lane + 32 * h < t.n_valid) {
+                cb[h] = om.colbase[t.out_off + lane + 32 * h];
+                cs[h] = om.colstride[t.out_off + lane + 32 * h];
+            }
+    } else if (warp * 32 + lane < t.m_valid) {
+        my_row = om.rowtab[t.out_off + warp * 32 + lane];
     }
     if (threadIdx.x == 0) {
         for (int s = 0; s < NST; ++s) {
@@ -263,25 +283,49 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
+    const int nb16 = t.n_mma >> 4;  // 16-row B boxes per operand and chunk
+    const uint32_t chunk_bytes = 2 * A_BYTES + 2 * t.n_mma * kTcBK * 2;
+    const int npre = min(NST, t.kch);  // chunks whose ring slot is free from the start
+    auto load_a = [&](int c, uint8_t* st, uint64_t* bar) {
+        const int ya = t.a_row + c * t.a_cs;
+        tma_load_2d(st, &mAh, 0, ya, bar);
+        tma_load_2d(st + A_BYTES, &mAl, 0, ya, bar);
+    };
+    auto load_b = [&](int c, uint8_t* st, uint64_t* bar) {
+        const int yb = t.b_row + c * t.b_cs;
+        for (int i = 0; i < nb16; ++i) {
+            tma_load_2d(st + 2 * A_BYTES + i * 16 * 128, &mBh, 0, yb + 16 * i, bar);
+            tma_load_2d(st + 2 * A_BYTES + B_BYTES + i * 16 * 128, &mBl, 0, yb + 16 * i, bar);
+        }
+    };
+    if (warp == 0 && lane == 0) {
+        // the constant operand of the first chunks goes out before the
+        // dependency wait (it overlaps the previous kernel's tail)
+        for (int c = 0; c < npre; ++c) {
+            uint8_t* st = smem + c * STAGE_BYTES;
+            mbar_expect_tx(&full[c], chunk_bytes);
+            if (const_ops & CONST_A) load_a(c, st, &full[c]);
+            if (const_ops & CONST_B) load_b(c, st, &full[c]);
+        }
+    }
     grid_dep_wait();
     bool ok = true;
-    const int nb16 = t.n_mma >> 4;  // 16-row B boxes per operand and chunk
 
     if (warp == 0 && lane == 0) {
         // producer: TMA loads of the K chunks (A: one 128-row box; B: n_mma/16 16-row boxes)
         for (int c = 0; c < t.kch && ok; ++c) {
             const int s = c % NST;
-            if (c >= NST) ok = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
-            if (!ok) break;
             uint8_t* st = smem + s * STAGE_BYTES;
-            mbar_expect_tx(&full[s], 2 * A_BYTES + 2 * t.n_mma * kTcBK * 2);
-            const int ya = t.a_row + c * t.a_cs, yb = t.b_row + c * t.b_cs;
-            tma_load_2d(st, &mAh, 0, ya, &full[s]);
-            tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[s]);
-            for (int i = 0; i < nb16; ++i) {
-                tma_load_2d(st + 2 * A_BYTES + i * 16 * 128, &mBh, 0, yb + 16 * i, &full[s]);
-                tma_load_2d(st + 2 * A_BYTES + B_BYTES + i * 16 * 128, &mBl, 0, yb + 16 * i, &full[s]);
+            if (c < npre) {
+                if (!(const_ops & CONST_A)) load_a(c, st, &full[s]);
+                if (!(const_ops & CONST_B)) load_b(c, st, &full[s]);
+                continue;
             }
+            ok = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
+            if (!ok) break;
+            mbar_expect_tx(&full[s], chunk_bytes);
+            load_a(c, st, &full[s]);
+            load_b(c, st, &full[s]);
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer: three bf16 products per 16-wide K step
@@ -328,22 +372,14 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         __syncwarp();
         const int rend = min(t.m_valid, warp * 32 + 32);
         if (t.mode == 2) {
-            int64_t cb[2] = {0, 0};
-            int32_t cs[2] = {0, 0};
-#pragma unroll
-            for (int h = 0; h < 2; ++h)
-                if (lane + 32 * h < t.n_valid) {
-                    cb[h] = om.colbase[t.out_off + lane + 32 * h];
-                    cs[h] = om.colstride[t.out_off + lane + 32 * h];
-                }
             for (int r = warp * 32; r < rend; ++r)
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
                     if (lane + 32 * h < t.n_valid)
                         om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane + 32 * h];
         } else {
-            for (int r = warp * 32; r < rend; ++r) {
-                double* o = om.out64 + om.rowtab[t.out_off + r] + t.n0;
+            for (int r = warp * 32; r < rend; ++r) {  // warp-uniform trip count
+                double* o = om.out64 + __shfl_sync(0xffffffffu, my_row, r - warp * 32) + t.n0;
                 for (int col = lane; col < t.n_valid; col += 32) o[col] = f2d_bits(stile[r][col]);
             }
         }
@@ -370,7 +406,7 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
 // counts stay block-uniform (bounded waits are combined with
 // __syncthreads_and) so no thread can be left at a barrier.
 template <int NST>
-__global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restrict__ tiles,
+__global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restrict__ tiles,
                                                           const __grid_constant__ CUtensorMap mAh,
                                                           const __grid_constant__ CUtensorMap mAl,
                                                           const double* __restrict__ x,
@@ -411,7 +447,6 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    grid_dep_wait();
     const uint32_t idesc = make_idesc(t.n_mma);
     // B fill assignment: thread -> one tile column and every fill_step-th k pair
     const int tid = (int)threadIdx.x;
@@ -421,13 +456,34 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
     const bool fill_valid = fill_col >= 0 && fill_col < t.n_valid;
     const int64_t fill_src = fill_valid ? xsrc[t.out_off + fill_col] : 0;
     const int64_t fill_stp = fill_valid ? xstride[t.out_off + fill_col] : 0;
+    // epilogue: lane c (+32) holds output column c's T1 base and stride
+    int64_t cb[2] = {0, 0};
+    int32_t cs[2] = {0, 0};
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (lane + 32 * h < t.n_valid) {
+            cb[h] = om.colbase[t.out_off + lane + 32 * h];
+            cs[h] = om.colstride[t.out_off + lane + 32 * h];
+        }
+    // the L operand (a plan constant) of the first chunks goes out before the
+    // dependency wait, overlapping the previous kernel's tail
+    const int npre = min(NST, t.kch);
+    if (threadIdx.x == 0)
+        for (int c = 0; c < npre; ++c) {
+            uint8_t* st = smem + c * STAGE_BYTES;
+            mbar_expect_tx(&full[c], 2 * A_BYTES);
+            const int ya = t.a_row + c * t.a_cs;
+            tma_load_2d(st, &mAh, 0, ya, &full[c]);
+            tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[c]);
+        }
+    grid_dep_wait();
     for (int c = 0; c < t.kch; ++c) {
         const int s = c % NST;
         bool good = true;
         if (c >= NST) good = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
         if (!__syncthreads_and(good)) break;
         uint8_t* st = smem + s * STAGE_BYTES;
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && c >= npre) {
             mbar_expect_tx(&full[s], 2 * A_BYTES);
             const int ya = t.a_row + c * t.a_cs;
             tma_load_2d(st, &mAh, 0, ya, &full[s]);
@@ -440,30 +496,31 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
         const int ksteps = min(kTcBK / 16, (t.k_valid - kbase + 15) / 16);
         const int nkp = 8 * ksteps;  // k pairs holding data in this chunk
         if (fill_col >= 0) {
-            for (int kq0 = fill_kq0; kq0 < nkp; kq0 += 4 * fill_step) {
-                double v[4][2];
+            // a thread owns at most kFillPairs k pairs of a chunk (nkp <= 32,
+            // fill_step >= 2): every load of the chunk is in flight at once
+            constexpr int kFillPairs = kTcBK / 2 / 2;
+            double v[kFillPairs][2];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int kq = kq0 + u * fill_step;
+            for (int u = 0; u < kFillPairs; ++u) {
+                const int kq = fill_kq0 + u * fill_step;
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int k = kbase + 2 * kq + h;
-                        v[u][h] = (kq < nkp && fill_valid && k < t.k_valid) ? x[fill_src + (int64_t)k * fill_stp] : 0.0;
-                    }
+                for (int h = 0; h < 2; ++h) {
+                    const int k = kbase + 2 * kq + h;
+                    v[u][h] = (kq < nkp && fill_valid && k < t.k_valid) ? x[fill_src + (int64_t)k * fill_stp] : 0.0;
                 }
+            }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int kq = kq0 + u * fill_step;
-                    if (kq >= nkp) continue;
-                    __nv_bfloat16 h0, l0, h1, l1;
-                    split2(v[u][0], h0, l0);
-                    split2(v[u][1], h1, l1);
-                    const int n = fill_col, k = 2 * kq;
-                    const uint32_t off =
-                        (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
-                    *reinterpret_cast<uint32_t*>(bh + off) = pack2(h0, h1);
-                    *reinterpret_cast<uint32_t*>(bl + off) = pack2(l0, l1);
-                }
+            for (int u = 0; u < kFillPairs; ++u) {
+                const int kq = fill_kq0 + u * fill_step;
+                if (kq >= nkp) continue;
+                __nv_bfloat16 h0, l0, h1, l1;
+                split2(v[u][0], h0, l0);
+                split2(v[u][1], h1, l1);
+                const int n = fill_col, k = 2 * kq;
+                const uint32_t off =
+                    (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
+                *reinterpret_cast<uint32_t*>(bh + off) = pack2(h0, h1);
+                *reinterpret_cast<uint32_t*>(bl + off) = pack2(l0, l1);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -501,14 +558,6 @@ __global__ void __launch_bounds__(128, 1) tc_gemm1_kernel(const TcTile* __restri
         }
         __syncwarp();
         const int rend = min(t.m_valid, warp * 32 + 32);
-        int64_t cb[2] = {0, 0};
-        int32_t cs[2] = {0, 0};
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-            if (lane + 32 * h < t.n_valid) {
-                cb[h] = om.colbase[t.out_off + lane + 32 * h];
-                cs[h] = om.colstride[t.out_off + lane + 32 * h];
-            }
         for (int r = warp * 32; r < rend; ++r)
 #pragma unroll
             for (int h = 0; h < 2; ++h)
@@ -574,22 +623,68 @@ constexpr int kCombThreads = 128;  // combine: threads per job
 
 // W_i W_j channel combine: T1 (fp32) -> stage-3 A operand, bf16 hi/lo.  One
 // CTA per job (rows [r0, r0 + rows) of one output slab, at most
-// kTcCombMaxElems elements unless a single row is longer); its terms are
-// staged in shared memory and each thread owns U elements, so a thread has
+// kTcCombMaxElems elements unless a single row is longer).  A job of at most
+// kTcCombInline terms (most of them: a channel pair reached from one or two
+// others) reads its terms from its own descriptor; longer term lists are
+// staged in shared memory.  Each thread owns U elements, so a thread has
 // TU x U independent T1 loads in flight before the first use.  Elements run
 // in row-major order, contiguous in T1 and in the operand chunk.
-__global__ void __launch_bounds__(kCombThreads) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
                                                                   const TcCombTerm* __restrict__ terms,
                                                                   const float* __restrict__ t1,
                                                                   __nv_bfloat16* __restrict__ th,
                                                                   __nv_bfloat16* __restrict__ tl) {
-    constexpr int U = 4, TU = 4, TCH = 64;
+    constexpr int U = 4, TU = 2, TCH = 64;
     __shared__ TcCombTerm st[TCH];
     const TcCombJob j = jobs[blockIdx.x];
     grid_dep_launch();
     const int n = j.rows * j.cols;
     const int nterm = j.term_end - j.term_begin;
+    // the terms are plan constants: a job with at most TCH of them (and more
+    // than kTcCombInline) stages them before the dependency wait
+    const bool inl = nterm <= kTcCombInline;
+    const bool resident = !inl && nterm <= TCH;
+    if (resident && (int)threadIdx.x < nterm) st[threadIdx.x] = terms[j.term_begin + threadIdx.x];
     grid_dep_wait();
+    if (resident) __syncthreads();
+    if (inl) {
+        for (int e0 = 0; e0 < n; e0 += U * kCombThreads) {
+            bool valid[U];
+            int r[U], c[U];
+            float acc[U], v[kTcCombInline][U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + u * kCombThreads + threadIdx.x;
+                valid[u] = e < n;
+                const int rl = valid[u] ? e / j.cols : 0;
+                c[u] = valid[u] ? e - rl * j.cols : 0;
+                r[u] = j.r0 + rl;
+                acc[u] = 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < kTcCombInline; ++q)
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    v[q][u] = (q < nterm && valid[u])
+                                  ? __ldg(t1 + j.inl[q].in_off + (int64_t)r[u] * j.inl[q].in_rs + c[u])
+                                  : 0.f;
+#pragma unroll
+            for (int q = 0; q < kTcCombInline; ++q)
+                if (q < nterm)
+#pragma unroll
+                    for (int u = 0; u < U; ++u) acc[u] = fmaf(j.inl[q].coef, v[q][u], acc[u]);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (valid[u]) {
+                    const int k = j.k0 + c[u];
+                    const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r[u]) << 6) + (k & 63);
+                    const __nv_bfloat16 h = __float2bfloat16_rn(acc[u]);
+                    th[idx] = h;
+                    tl[idx] = __float2bfloat16_rn(acc[u] - __bfloat162float(h));
+                }
+        }
+        return;
+    }
     for (int e0 = 0; e0 < n; e0 += U * kCombThreads) {  // block-uniform trip count
         bool valid[U];
         int r[U], c[U];
@@ -605,9 +700,11 @@ __global__ void __launch_bounds__(kCombThreads) combine_tc_kernel(const TcCombJo
         }
         for (int t0 = 0; t0 < nterm; t0 += TCH) {
             const int tn = min(TCH, nterm - t0);
-            __syncthreads();
-            if (threadIdx.x < tn) st[threadIdx.x] = terms[j.term_begin + t0 + threadIdx.x];
-            __syncthreads();
+            if (!resident) {
+                __syncthreads();
+                if ((int)threadIdx.x < tn) st[threadIdx.x] = terms[j.term_begin + t0 + threadIdx.x];
+                __syncthreads();
+            }
             int t = 0;
             for (; t + TU <= tn; t += TU) {
                 float v[TU][U];
@@ -805,12 +902,13 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem,
 }
 
 void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, const CUtensorMap& al,
-                    const CUtensorMap& bh, const CUtensorMap& bl, const OutMap& om, int* err, cudaStream_t s) {
+                    const CUtensorMap& bh, const CUtensorMap& bl, const OutMap& om, int const_ops, int* err,
+                    cudaStream_t s) {
     if (n <= 0) return;
     if (nst == 1)
-        launch_pdl(tc_gemm_kernel<1>, n, 128, smem_bytes(1), s, tiles, ah, al, bh, bl, om, err);
+        launch_pdl(tc_gemm_kernel<1>, n, 128, smem_bytes(1), s, tiles, ah, al, bh, bl, om, const_ops, err);
     else
-        launch_pdl(tc_gemm_kernel<2>, n, 128, smem_bytes(2), s, tiles, ah, al, bh, bl, om, err);
+        launch_pdl(tc_gemm_kernel<2>, n, 128, smem_bytes(2), s, tiles, ah, al, bh, bl, om, const_ops, err);
 }
 
 }  // namespace
@@ -821,7 +919,7 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
         const OutMap om{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride};
         if (tc.nsplit > 0)
             launch_pdl(split_psi_kernel, tc.nsplit, kSplitThreads, 0, s, (const TcSplitJob*)tc.split, x, tc.xh, tc.xl);
-        launch_tc_gemm(tc.nst1x, tc.n1x, tc.tiles1x, tc.mLh, tc.mLl, tc.mXh, tc.mXl, om, tc.err, s);
+        launch_tc_gemm(tc.nst1x, tc.n1x, tc.tiles1x, tc.mLh, tc.mLl, tc.mXh, tc.mXl, om, CONST_A, tc.err, s);
         if (tc.n1 > 0) {
             if (tc.nst1 == 1)
                 launch_pdl(tc_gemm1_kernel<1>, tc.n1, 128, smem_bytes(1), s, (const TcTile*)tc.tiles1, tc.mLh, tc.mLl,
@@ -836,7 +934,7 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
                        (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
     } else {
         launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl,
-                       OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, tc.err, s);
+                       OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, CONST_B, tc.err, s);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) err = "tensor-core stage launch";

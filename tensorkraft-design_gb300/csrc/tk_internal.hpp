@@ -171,17 +171,20 @@ struct TcSplitJob {
 };
 // T1 (fp32) -> stage-3 A operand (K-major chunks), hi/lo split.  One job =
 // rows [r0, r0 + rows) of one output slab, at most kTcCombMaxElems elements
-// (one warp each).
-struct TcCombJob {
-    int32_t t2row, cstride;  // operand row of chunk 0 for slab row 0; rows between chunks
-    int32_t k0, rows, cols, term_begin, term_end, r0;
-};
-constexpr int kTcCombMaxElems = 512;
+// (one CTA each).  A job with at most kTcCombInline terms carries them in
+// its descriptor as well (no second dependent table read).
 struct TcCombTerm {
     int64_t in_off;
     int32_t in_rs;
     float coef;
 };
+constexpr int kTcCombInline = 2;
+struct TcCombJob {
+    int32_t t2row, cstride;  // operand row of chunk 0 for slab row 0; rows between chunks
+    int32_t k0, rows, cols, term_begin, term_end, r0;
+    TcCombTerm inl[kTcCombInline];  // terms[term_begin .. term_end) when there are at most kTcCombInline
+};
+constexpr int kTcCombMaxElems = 512;
 struct TcTables {
     int64_t lq_rows = 0, rq_rows = 0, xq_rows = 0, t2q_rows = 0, t1_total = 0;
     std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
