@@ -177,7 +177,10 @@ tk_status tk_heff2_apply(tk_heff2_plan* plan, const double* x_dev, double* y_dev
  * (s_i, s_j, a_L, a_R) layout of length dense_dim; y fully overwritten.
  * Synchronous. */
 tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y);
-/* Same on host vectors in the block layout (FlatBlockStorage), synchronous. */
+/* Same on host vectors in the block layout (FlatBlockStorage), synchronous.
+ * With page-locked x and y the call runs as one CUDA graph (transfers per
+ * tk_heff2_set_host_io, kernels, error-word read-back), instantiated on the
+ * first call and reused while x, y and the plan settings stay the same. */
 tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double* y);
 /* Dense <-> block layout conversion on the host. */
 tk_status tk_heff2_dense_to_flat(const tk_heff2_plan* plan, const double* dense, double* flat);

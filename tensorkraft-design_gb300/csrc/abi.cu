@@ -420,13 +420,58 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
     cudaStream_t s = plan->stream;
     int mode = plan->precision == TK_PREC_BF16X3 ? plan->host_io : TK_HOST_IO_STAGED;
     if (mode == TK_HOST_IO_AUTO) mode = tc_prefers_direct_input(*plan->tc) ? TK_HOST_IO_DIRECT : TK_HOST_IO_DIRECT_OUT;
-    const double* dx = mode == TK_HOST_IO_DIRECT ? static_cast<const double*>(mapped_host_ptr(x)) : nullptr;
-    double* dy = mode != TK_HOST_IO_STAGED ? static_cast<double*>(mapped_host_ptr(y)) : nullptr;
-    if (!dx) TK_CUDA(cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    st = tk_heff2_apply_prec(plan, dx ? dx : plan->hx.p, dy ? dy : plan->hy.p, s, plan->precision);
-    if (st != TK_OK) return st;
-    if (!dy) TK_CUDA(cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-    return finish_host_call(plan, s);
+    const double* mx = static_cast<const double*>(mapped_host_ptr(x));
+    double* my = static_cast<double*>(mapped_host_ptr(y));
+    const double* dx = mode == TK_HOST_IO_DIRECT ? mx : nullptr;
+    double* dy = mode != TK_HOST_IO_STAGED ? my : nullptr;
+    if (!mx || !my) {
+        // pageable buffers: plain stream-ordered copies (graphs take page-locked memory only)
+        TK_CUDA(cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, plan->precision);
+        if (st != TK_OK) return st;
+        TK_CUDA(cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        return finish_host_call(plan, s);
+    }
+    // page-locked buffers: the whole call (copies, kernels, error-word
+    // read-back) as one CUDA graph launch, re-instantiated when the buffers
+    // or settings change
+    const int key = ((mode * 4 + plan->precision) * 4 + plan->schedule) * 4 + (dx ? 2 : 0) + (dy ? 1 : 0);
+    if (!plan->host_exec || plan->host_gx != x || plan->host_gy != y || plan->host_gkey != key) {
+        if (plan->host_exec) {
+            cudaGraphExecDestroy(plan->host_exec);
+            plan->host_exec = nullptr;
+        }
+        TK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        tk_status cst = TK_OK;
+        cudaError_t ce = cudaSuccess;
+        if (!dx) ce = cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+        if (ce == cudaSuccess)
+            cst = tk_heff2_apply_prec(plan, dx ? dx : plan->hx.p, dy ? dy : plan->hy.p, s, plan->precision);
+        if (ce == cudaSuccess && cst == TK_OK && !dy)
+            ce = cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+        if (ce == cudaSuccess && cst == TK_OK && plan->precision == TK_PREC_BF16X3)
+            ce = cudaMemcpyAsync(plan->pin_err, tc_error_word(*plan->tc), sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+        if (cst != TK_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return cst;
+        }
+        if (ce == cudaSuccess) ce = ee;
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&plan->host_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            plan->host_exec = nullptr;
+            return cuda_fail("tk_heff2_apply_host_flat: graph capture", ce);
+        }
+        plan->host_gx = x;
+        plan->host_gy = y;
+        plan->host_gkey = key;
+    }
+    TK_CUDA(cudaGraphLaunch(plan->host_exec, s));
+    TK_CUDA(cudaStreamSynchronize(s));
+    if (plan->precision == TK_PREC_BF16X3 && *plan->pin_err != 0) return tc_check_error(*plan->tc, s);
+    return TK_OK;
 }
 
 tk_status tk_heff2_apply_host(tk_heff2_plan* plan, const double* x, double* y) {

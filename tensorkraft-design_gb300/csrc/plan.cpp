@@ -979,6 +979,18 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
         }
+        // heaviest tiles first (K chunks, then padded MMA area): a launch with
+        // more tiles than resident CTAs ends on a tail of light tiles
+        // (LPT order, as tk-linalg/src/tasks.rs:172-174 orders sector tasks)
+        auto lpt = [](std::vector<TcTile>& v) {
+            std::stable_sort(v.begin(), v.end(), [](const TcTile& a, const TcTile& b) {
+                if (a.kch != b.kch) return a.kch > b.kch;
+                return (int64_t)a.m_valid * a.n_mma > (int64_t)b.m_valid * b.n_mma;
+            });
+        };
+        lpt(C.tiles1);
+        lpt(C.tiles1x);
+        lpt(C.tiles3);
         for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
         for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
         for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);

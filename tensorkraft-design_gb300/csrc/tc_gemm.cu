@@ -139,16 +139,29 @@ __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::aft
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
+// 16 consecutive accumulator columns of this thread's TMEM lane (no wait).
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
+}
+
+// Accumulator row of this thread (n_mma <= kTcBN columns) -> srow: every
+// tcgen05.ld is issued before the one wait.  Warp-collective (n_mma is
+// uniform across the warp).
+__device__ __forceinline__ void tmem_row_to_smem(uint32_t tbase, int n_mma, float* srow) {
+    uint32_t r[kTcBN];
+#pragma unroll
+    for (int q = 0; q < kTcBN / 16; ++q)
+        if (16 * q < n_mma) tmem_ld16_nowait(tbase + 16 * q, r + 16 * q);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int q = 0; q < kTcBN / 16; ++q)
+        if (16 * q < n_mma)
+#pragma unroll
+            for (int i = 0; i < 16; ++i) srow[16 * q + i] = __uint_as_float(r[16 * q + i]);
 }
 
 // Conversions between fp64 and fp32 on the integer pipes.  This GPU's FP64
@@ -363,12 +376,7 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
         const int row = threadIdx.x;
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int c0 = 0; c0 < t.n_mma; c0 += 16) {
-            float v[16];
-            tmem_ld16(tbase + c0, v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) stile[row][c0 + j] = v[j];
-        }
+        tmem_row_to_smem(tbase, t.n_mma, stile[row]);
         __syncwarp();
         const int rend = min(t.m_valid, warp * 32 + 32);
         if (t.mode == 2) {
@@ -550,12 +558,7 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
         float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
         const int row = threadIdx.x;
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int c0 = 0; c0 < t.n_mma; c0 += 16) {
-            float v[16];
-            tmem_ld16(tbase + c0, v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) stile[row][c0 + j] = v[j];
-        }
+        tmem_row_to_smem(tbase, t.n_mma, stile[row]);
         __syncwarp();
         const int rend = min(t.m_valid, warp * 32 + 32);
         for (int r = warp * 32; r < rend; ++r)

@@ -87,6 +87,12 @@ struct tk_heff2_plan {
     double* pin_y = nullptr;
     int* pin_err = nullptr;   // tensor-core error word, read back with the result
     int host_io = TK_HOST_IO_AUTO;
+    // CUDA graph of the last host-buffer matvec (copies, kernels, error-word
+    // read-back), reused while the buffers and the plan settings repeat
+    cudaGraphExec_t host_exec = nullptr;
+    const void* host_gx = nullptr;
+    void* host_gy = nullptr;
+    int host_gkey = -1;
     cudaStream_t stream = nullptr;
     // split-precision operands and state (tensor-core path)
     std::unique_ptr<tk::TcPlan, tk::TcPlanDeleter> tc;
@@ -105,6 +111,7 @@ struct tk_heff2_plan {
         if (pin_x) cudaFreeHost(pin_x);
         if (pin_y) cudaFreeHost(pin_y);
         if (pin_err) cudaFreeHost(pin_err);
+        if (host_exec) cudaGraphExecDestroy(host_exec);
         if (stream) cudaStreamDestroy(stream);
     }
 };
