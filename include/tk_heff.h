@@ -330,6 +330,17 @@ typedef struct {
 tk_status tk_block_gemm_f64(tk_ctx* ctx, const tk_bst* a, const tk_bst* b, tk_bst_out* out);
 void tk_bst_free(tk_bst_out* t);
 
+/* All eigenpairs of `batch` symmetric n x n matrices (host memory, each
+ * matrix n*n doubles back to back; symmetric, so row- and column-major
+ * agree; the lower triangle is read): w_host[b*n + j] ascending eigenvalues
+ * of matrix b, z_host[b*n*n + i + j*n] component i of its eigenvector j
+ * (column-major).  One cuSOLVER batched call (syevBatched) on the device.
+ * Serves the density-matrix truncation of a two-site split, one matrix per
+ * bond charge padded to a common n (no reference counterpart; the reference
+ * diagonalises sector by sector on the CPU, truncation/mod.rs:71-99 via
+ * LinAlgBackend::svd_truncated). */
+tk_status tk_eigh_batched_f64(tk_ctx* ctx, int64_t n, int64_t batch, const double* a_host, double* w_host,
+                              double* z_host);
 /*
  * The dense factorisations of LinAlgBackend (tk-linalg/src/traits.rs:63-148) on
  * device matrices (tk_mat strides, real f64), with the faer backend's result

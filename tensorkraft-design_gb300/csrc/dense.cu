@@ -221,6 +221,60 @@ tk_status tk_eigh_lowest_f64(tk_ctx* ctx, const tk_mat* a, int64_t k, double* ev
     return TK_OK;
 }
 
+tk_status tk_eigh_batched_f64(tk_ctx* ctx, int64_t n, int64_t batch, const double* a_host, double* w_host,
+                              double* z_host) {
+    if (!ctx || n <= 0 || batch < 0 || (batch > 0 && (!a_host || !w_host || !z_host))) {
+        set_error("tk_eigh_batched_f64: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (batch == 0) return TK_OK;
+    Guard g(ctx->device);
+    cudaStream_t s = 0;
+    cusolverDnHandle_t h;
+    tk_status st = handle_of(ctx, s, &h, "tk_eigh_batched_f64");
+    if (st != TK_OK) return st;
+    cusolverDnParams_t params = nullptr;
+    cusolverStatus_t cs = cusolverDnCreateParams(&params);
+    if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail("tk_eigh_batched_f64: params", cs);
+    struct ParamsFree {
+        cusolverDnParams_t p;
+        ~ParamsFree() { cusolverDnDestroyParams(p); }
+    } pf{params};
+    const size_t nn = (size_t)n * (size_t)n * (size_t)batch;
+    Dev d;
+    double *A, *W;
+    int* info;
+    cudaError_t e;
+    if ((e = d.alloc(&A, nn)) != cudaSuccess || (e = d.alloc(&W, (size_t)n * batch)) != cudaSuccess ||
+        (e = d.alloc(&info, (size_t)batch)) != cudaSuccess)
+        return cuda_fail("tk_eigh_batched_f64: workspace", e);
+    if ((e = cudaMemcpyAsync(A, a_host, sizeof(double) * nn, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail("tk_eigh_batched_f64: upload", e);
+    size_t wdev = 0, whost = 0;
+    cs = cusolverDnXsyevBatched_bufferSize(h, params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F,
+                                           A, n, CUDA_R_64F, W, CUDA_R_64F, &wdev, &whost, batch);
+    if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail("syevBatched buffer size", cs);
+    uint8_t* work = nullptr;
+    if ((e = d.alloc(&work, wdev)) != cudaSuccess) return cuda_fail("tk_eigh_batched_f64: workspace", e);
+    std::vector<uint8_t> hwork(std::max<size_t>(whost, 1));
+    cs = cusolverDnXsyevBatched(h, params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, A, n,
+                                CUDA_R_64F, W, CUDA_R_64F, work, wdev, hwork.data(), whost, info, batch);
+    if (cs != CUSOLVER_STATUS_SUCCESS) return solver_fail("syevBatched", cs);
+    std::vector<int> hinfo((size_t)batch);
+    if ((e = cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(w_host, W, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(z_host, A, sizeof(double) * nn, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail("tk_eigh_batched_f64: download", e);
+    for (int64_t b = 0; b < batch; ++b)
+        if (hinfo[(size_t)b] != 0) {
+            set_error("tk_eigh_batched_f64: cuSOLVER info " + std::to_string(hinfo[(size_t)b]) + " for matrix " +
+                      std::to_string(b));
+            return hinfo[(size_t)b] > 0 ? TK_ERR_UNSUPPORTED : TK_ERR_INVALID_ARG;
+        }
+    return TK_OK;
+}
+
 tk_status tk_qr_f64(tk_ctx* ctx, const tk_mat* a, double* q_dev, double* r_dev, void* stream) {
     if (!ctx || !mat_ok(a) || !q_dev || !r_dev) {
         set_error("tk_qr_f64: invalid argument");

@@ -133,6 +133,7 @@ SIGNATURES = [
                                          C.POINTER(C.c_double), C.c_void_p]),
     ("tk_eigh_lowest_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_mat), C.c_int64, C.POINTER(C.c_double), C.c_void_p,
                                        C.c_void_p]),
+    ("tk_eigh_batched_f64", C.c_int32, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("tk_qr_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_mat), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("tk_check_split_conversions", C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_uint64)]),
     ("tk_env_layout", C.c_int32, [C.c_int32, C.POINTER(tk_qindex), C.POINTER(tk_qindex), C.POINTER(tk_qindex),

@@ -122,19 +122,25 @@ class QIndex:
     def n_sectors(self) -> int:
         return len(self.sectors)
 
+    def _lookup(self) -> dict:
+        # {charge: (offset, dim)}, rebuilt when the sector list object changes
+        cache = self.__dict__.get("_lookup_cache")
+        if cache is None or cache[0] is not self.sectors or cache[1] != len(self.sectors):
+            table, off = {}, 0
+            for sq, d in self.sectors:
+                table[sq] = (off, d)
+                off += d
+            cache = (self.sectors, len(self.sectors), table)
+            self.__dict__["_lookup_cache"] = cache
+        return cache[2]
+
     def offset_of(self, q):
-        off = 0
-        for sq, d in self.sectors:
-            if sq == tuple(q):
-                return off
-            off += d
-        return None
+        hit = self._lookup().get(tuple(q))
+        return None if hit is None else hit[0]
 
     def dim_of(self, q):
-        for sq, d in self.sectors:
-            if sq == tuple(q):
-                return d
-        return None
+        hit = self._lookup().get(tuple(q))
+        return None if hit is None else hit[1]
 
     def charges(self) -> np.ndarray:
         return np.array([list(q) for q, _ in self.sectors], dtype=np.int32).reshape(-1)
