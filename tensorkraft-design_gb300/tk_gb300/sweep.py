@@ -37,7 +37,7 @@ import numpy as np
 from . import _abi
 from ._abi import PREC_FP64, check
 from .heff import Heff2Plan, _Marshal, context, identity_mpo_site
-from .symmetry import QIndex, dual, fuse, identity, key_pack, key_unpack
+from .symmetry import QIndex, bit_width, dual, fuse, identity, key_pack, key_unpack, qn_pack
 
 
 def _torch():
@@ -385,19 +385,34 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
             ncol[q] = ncol.get(q, 0) + db
     charges = sorted(set(rows) & set(cols))
     M = {q: np.zeros((nrow[q], ncol[q]), dtype=psi.dtype) for q in charges}
-    for key, off in zip(keys, offs):
-        qsi, qsj, qa, qb = (tuple(x) for x in key_unpack(kind, int(key), 4))
-        ni, nj, da, db = PI.dim_of(qsi), PJ.dim_of(qsj), QA.dim_of(qa), QB.dim_of(qb)
+    # sector indices of every block from the packed keys (vectorised over the
+    # blocks: one leg field at a time through a lookup table of packed charges)
+    bw = bit_width(kind)
+    kk = np.asarray(keys, dtype=np.uint64)
+    sec = []
+    for leg_no, ix in enumerate((PI, PJ, QA, QB)):
+        lut = np.full(1 << bw, -1, dtype=np.int64)
+        for i, (q, _) in enumerate(ix.sectors):
+            lut[qn_pack(kind, q) & ((1 << bw) - 1)] = i
+        field = ((kk >> np.uint64(leg_no * bw)) & np.uint64((1 << bw) - 1)).astype(np.int64)
+        sec.append(lut[field].tolist())
+    pi_off = [PI.offset_of(q) for q, _ in PI.sectors]
+    pj_off = [PJ.offset_of(q) for q, _ in PJ.sectors]
+    for n_blk, off in enumerate(np.asarray(offs).tolist()):
+        si, sj, ia, ib = sec[0][n_blk], sec[1][n_blk], sec[2][n_blk], sec[3][n_blk]
+        qsi, ni = PI.sectors[si]
+        nj = PJ.sectors[sj][1]
+        qa, da = QA.sectors[ia]
+        qb, db = QB.sectors[ib]
         blk = psi[off:off + ni * nj * da * db].reshape(ni, nj, da, db)
         q = fuse(kind, qsi, qa)
+        Mq, rq, cq = M[q], rows[q], cols[q]
         for li in range(ni):
-            s = PI.offset_of(qsi) + li
+            s = pi_off[si] + li
             for lj in range(nj):
-                t = PJ.offset_of(qsj) + lj
-                r0, c0 = rows[q][(s, qa)], cols[q][(t, qb)]
-                M[q][r0:r0 + da, c0:c0 + db] = blk[li, lj]
+                r0, c0 = rq[(s, qa)], cq[(pj_off[sj] + lj, qb)]
+                Mq[r0:r0 + da, c0:c0 + db] = blk[li, lj]
     eig = {}
-    allsv = []
 
     def gram(q):
         return M[q] @ M[q].conj().T if to_right else M[q].conj().T @ M[q]
@@ -408,26 +423,30 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
         else:
             # one charge per pool thread, single-threaded BLAS each
             pairs = list(_pool().map(lambda q: np.linalg.eigh(gram(q)), charges))
+    svs = []
     for bi, q in enumerate(charges):
         w, Z = pairs[bi]
         w, Z = w[::-1], Z[:, ::-1]
         eig[q] = Z
-        allsv += [(math.sqrt(max(float(x), 0.0)), bi, j) for j, x in enumerate(w)]
-    allsv.sort(key=lambda t: (-t[0], t[1], t[2]))
+        svs.append(np.sqrt(np.maximum(np.asarray(w, dtype=np.float64), 0.0)))
+    # every singular value of every charge, ordered by (-sigma, charge, position)
+    sv = np.concatenate(svs) if svs else np.zeros(0)
+    sv_charge = np.repeat(np.arange(len(svs)), [len(x) for x in svs])
+    sv_pos = np.concatenate([np.arange(len(x)) for x in svs]) if svs else np.zeros(0, dtype=np.int64)
+    order = np.lexsort((sv_pos, sv_charge, -sv))
+    sv, sv_charge = sv[order], sv_charge[order]
     # truncate_svd (truncation/mod.rs:71-99): keep sigma >= cutoff * sigma_max, at most
     # max_bond, at least one; the error is the discarded share of sum sigma^2
-    thr = cutoff * (allsv[0][0] if allsv else 0.0)
-    nkeep = 0
-    while nkeep < min(max_bond, len(allsv)) and not allsv[nkeep][0] < thr:
-        nkeep += 1
-    keep = allsv[:max(nkeep, min(1, len(allsv)))]
-    kept = {}
-    for _, bi, _ in keep:
-        kept[charges[bi]] = kept.get(charges[bi], 0) + 1
-    total_sq = sum(x * x for x, _, _ in allsv)
-    disc = (sum(x * x for x, _, _ in allsv[len(keep):]) / total_sq) if total_sq > 0 else 0.0
+    thr = cutoff * (float(sv[0]) if len(sv) else 0.0)
+    nkeep = min(max_bond, int(np.count_nonzero(sv >= thr)))
+    nkeep = max(nkeep, min(1, len(sv)))
+    counts = np.bincount(sv_charge[:nkeep], minlength=len(charges))
+    kept = {charges[bi]: int(c) for bi, c in enumerate(counts) if c > 0}
+    sq = sv * sv
+    total_sq = float(sq.sum())
+    disc = float(sq[nkeep:].sum()) / total_sq if total_sq > 0 else 0.0
     nb = QIndex(kind, [(q, kept[q]) for q in charges if q in kept])
-    norm = math.sqrt(sum(x * x for x, _, _ in keep)) or 1.0
+    norm = math.sqrt(float(sq[:nkeep].sum())) or 1.0
     Ai, Aj = {}, {}
 
     def factors(item):
