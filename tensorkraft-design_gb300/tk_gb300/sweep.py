@@ -581,6 +581,72 @@ def mps_overlap(bra: list, ket: list) -> complex:
     return complex(sum(v[0, 0] for v in E.values())) if E else 0j
 
 
+def _qr_left(blocks: dict):
+    """Left QR step of one site: for every right charge q, the rows (s, a_L)
+    of all blocks (s, q_L, q) stacked in ascending block order form M_q =
+    Q_q R_q (thin).  Returns (Q blocks with right dimension k_q, {q: R_q})."""
+    groups = {}
+    for (qs, ql, qr) in sorted(blocks):
+        groups.setdefault(qr, []).append((qs, ql))
+    newb, Rs = {}, {}
+    for qr, members in groups.items():
+        mats = [blocks[(qs, ql, qr)] for qs, ql in members]
+        M = np.concatenate([m.reshape(-1, m.shape[2]) for m in mats], axis=0)
+        Qm, Rm = np.linalg.qr(M)
+        k = Qm.shape[1]
+        r0 = 0
+        for (qs, ql), m in zip(members, mats):
+            n = m.shape[0] * m.shape[1]
+            newb[(qs, ql, qr)] = Qm[r0:r0 + n].reshape(m.shape[0], m.shape[1], k)
+            r0 += n
+        Rs[qr] = Rm
+    return newb, Rs
+
+
+def canonicalize(sites: list, bonds: list, center: int, device: int = 0):
+    """Mixed-canonical form of a block-sparse MPS with the orthogonality
+    centre at `center` (mps/mod.rs:346-419: left_canonicalize,
+    right_canonicalize, mixed_canonicalize): sites left of the centre become
+    left isometries (sum_s A_s^H A_s = 1) by thin QR, sites right of it right
+    isometries by thin LQ, each factor absorbed into the neighbour towards the
+    centre.  The QR is taken per bond charge over all blocks of that charge
+    (mps/mod.rs:421-770 factors each block on its own, which leaves blocks of
+    one charge non-orthogonal to each other); a bond shrinks to
+    min(rows, cols) per charge.  Returns (sites, bonds); the state and its
+    norm are unchanged."""
+    n = len(sites)
+    sites, bonds = list(sites), list(bonds)
+    kind = sites[0].kind
+    P = sites[0].legs[0]
+    host = [t.blocks_host() for t in sites]
+    for i in range(0, min(center, n - 1)):
+        newb, Rs = _qr_left(host[i])
+        nb = QIndex(kind, [(q, R.shape[0]) for q, R in sorted(Rs.items())])
+        host[i] = newb
+        nxt = {}
+        for (qs, ql, qr), blk in host[i + 1].items():
+            if ql in Rs:
+                nxt[(qs, ql, qr)] = np.einsum("ka,sab->skb", Rs[ql], blk)
+        host[i + 1] = nxt
+        bonds[i + 1] = nb
+    for i in range(n - 1, center, -1):
+        # LQ of the (a_L) x (s, a_R) matrices = QR of the transposed blocks
+        tb = {(qs, qr, ql): np.ascontiguousarray(blk.transpose(0, 2, 1).conj())
+              for (qs, ql, qr), blk in host[i].items()}
+        newt, Rs = _qr_left(tb)
+        nb = QIndex(kind, [(q, R.shape[0]) for q, R in sorted(Rs.items())])
+        host[i] = {(qs, ql, qr): np.ascontiguousarray(b.transpose(0, 2, 1).conj())
+                   for (qs, qr, ql), b in newt.items()}
+        prv = {}
+        for (qs, ql, qr), blk in host[i - 1].items():
+            if qr in Rs:  # A_{i-1} L with L = R^H
+                prv[(qs, ql, qr)] = np.einsum("sab,kb->sak", blk, Rs[qr].conj())
+        host[i - 1] = prv
+        bonds[i] = nb
+    out = [SiteTensor.from_blocks(kind, [P, bonds[i], bonds[i + 1]], host[i], device) for i in range(n)]
+    return out, bonds
+
+
 @dataclass
 class SweepRecord:
     energies: list = field(default_factory=list)   # energy after each half sweep

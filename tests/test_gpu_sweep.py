@@ -121,6 +121,35 @@ def test_random_site_tensors_right_canonical(lib_built):
     assert abs(np.sum(A0 * A0) - 1.0) < 1e-12
 
 
+def test_canonicalize_mixed(lib_built):
+    """Per-charge QR / LQ canonicalisation (mps/mod.rs:346-419): left
+    isometries left of the centre, right isometries right of it, the state
+    unchanged (overlaps with the original), the bonds in the form the charges
+    allow."""
+    m = models.hubbard()
+    rng = np.random.default_rng(9)
+    sites, bonds = sweep.random_site_tensors(m, 6, 24, (6, 0), rng)
+    # break the canonical form: scale every block of each site by random factors
+    mixed = []
+    for t in sites:
+        blocks = {k: v * rng.uniform(0.5, 2.0) for k, v in t.blocks_host().items()}
+        mixed.append(sweep.SiteTensor.from_blocks(t.kind, t.legs, blocks))
+    ref = sweep.mps_overlap(mixed, mixed).real
+    for center in (5, 0, 2):
+        out, nb = sweep.canonicalize(mixed, bonds, center)
+        assert abs(sweep.mps_overlap(out, out).real - ref) < 1e-10 * ref
+        assert abs(sweep.mps_overlap(mixed, out).real - ref) < 1e-10 * ref
+        for i, t in enumerate(out):
+            A = t.to_dense()
+            assert A.shape[1] == nb[i].total_dim and A.shape[2] == nb[i + 1].total_dim
+            if i < center:
+                G = np.einsum("sab,sac->bc", A, A)
+                assert np.allclose(G, np.eye(G.shape[0]), atol=1e-12), (center, i)
+            elif i > center:
+                G = np.einsum("sab,scb->ac", A, A)
+                assert np.allclose(G, np.eye(G.shape[0]), atol=1e-12), (center, i)
+
+
 def test_device_sweeps_match_dense_driver(lib_built):
     m, mps = _chain("heisenberg", 12, 16, seed=5)
     mps2 = dmrg.DenseMPS(mps.kind, mps.phys, list(mps.bonds), [t.copy() for t in mps.tensors])
