@@ -176,21 +176,16 @@ __device__ __forceinline__ void tmem_row_to_smem(uint32_t tbase, int n_mma, floa
 __device__ __forceinline__ float d2f_bits(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-    const int e = (int)((b >> 52) & 0x7FF);
-    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-    if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (m ? 0x400000u : 0u));
-    int fe = e - 1023 + 127;
-    if (fe <= 0) return __uint_as_float(sign);
-    uint32_t mant = (uint32_t)(m >> 29);
-    const unsigned long long rem = m & ((1ull << 29) - 1), half = 1ull << 28;
-    if (rem > half || (rem == half && (mant & 1u))) {
-        if (++mant == (1u << 23)) {
-            mant = 0;
-            ++fe;
-        }
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    if (e - 897u < 254u) {
+        // normal fp32 range: add the round-to-nearest-even bias below the 23
+        // kept mantissa bits (a carry runs into the exponent), keep bits
+        // 29.. and rebias the exponent (1023 - 127 = 896) modulo 2^32
+        const unsigned long long r = b + (0x0FFFFFFFull + ((b >> 29) & 1ull));
+        return __uint_as_float((((uint32_t)(r >> 29)) - (896u << 23)) | sign);
     }
-    if (fe >= 255) return __uint_as_float(sign | 0x7F800000u);
-    return __uint_as_float(sign | ((uint32_t)fe << 23) | mant);
+    if (e == 0x7FFu) return __uint_as_float(sign | 0x7F800000u | ((b & 0xFFFFFFFFFFFFFull) ? 0x400000u : 0u));
+    return __uint_as_float(e > 896u ? (sign | 0x7F800000u) : sign);  // overflow, or zero / below 2^-126
 }
 
 // fp32 -> fp64, exact for every input (subnormal fp32 values are normalised).
@@ -211,12 +206,16 @@ __device__ __forceinline__ double f2d_bits(float f) {
     return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)m << 29)));
 }
 
-// x ~ hi + lo with hi = bf16(x32), lo = bf16(x32 - hi), x32 = fp32(x); the
-// difference is exact in fp32.
-__device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-    const float f = d2f_bits(x);
-    hi = __float2bfloat16_rn(f);
-    lo = __float2bfloat16_rn(f - __bfloat162float(hi));
+// Two elements at once: x ~ hi + lo with hi = bf16(x32), lo = bf16(x32 - hi),
+// x32 = fp32(x) (the difference is exact in fp32); the hi and lo of a and b
+// are packed in pairs, a in the low half.
+__device__ __forceinline__ void split2x2(double a, double b, uint32_t& hi, uint32_t& lo) {
+    const float fa = d2f_bits(a), fb = d2f_bits(b);
+    const __nv_bfloat162 h = __floats2bfloat162_rn(fa, fb);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(fa - hf.x, fb - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // Output addressing of a tile element (row, col) relative to the tile origin.
@@ -400,9 +399,6 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
     }
 }
 
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
-    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
 
 // Stage 1 with the psi operand built in shared memory.  The L stack (A) comes
 // in by TMA as in tc_gemm_kernel; the B tile (n_mma columns x 64 K) is read
@@ -521,14 +517,13 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
             for (int u = 0; u < kFillPairs; ++u) {
                 const int kq = fill_kq0 + u * fill_step;
                 if (kq >= nkp) continue;
-                __nv_bfloat16 h0, l0, h1, l1;
-                split2(v[u][0], h0, l0);
-                split2(v[u][1], h1, l1);
+                uint32_t hw, lw;
+                split2x2(v[u][0], v[u][1], hw, lw);
                 const int n = fill_col, k = 2 * kq;
                 const uint32_t off =
                     (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
-                *reinterpret_cast<uint32_t*>(bh + off) = pack2(h0, h1);
-                *reinterpret_cast<uint32_t*>(bl + off) = pack2(l0, l1);
+                *reinterpret_cast<uint32_t*>(bh + off) = hw;
+                *reinterpret_cast<uint32_t*>(bl + off) = lw;
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -605,13 +600,7 @@ __global__ void __launch_bounds__(kSplitThreads) split_psi_kernel(const TcSplitJ
     if (b < nb) {
         uint32_t hw[8], lw[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            __nv_bfloat16 h0, l0, h1, l1;
-            split2(buf[ab + 2 * i][b], h0, l0);
-            split2(buf[ab + 2 * i + 1][b], h1, l1);
-            hw[i] = pack2(h0, h1);
-            lw[i] = pack2(l0, l1);
-        }
+        for (int i = 0; i < 8; ++i) split2x2(buf[ab + 2 * i][b], buf[ab + 2 * i + 1][b], hw[i], lw[i]);
         const int64_t row = (int64_t)j.xrow + (int64_t)(j.a0 / kTcBK) * j.cstride + j.b0 + b;
         uint4* ph = reinterpret_cast<uint4*>(xh + row * kTcBK + ab);
         uint4* pl = reinterpret_cast<uint4*>(xl + row * kTcBK + ab);
