@@ -556,9 +556,9 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "api": "tk_heff2_apply_host_flat (pinned FlatBlockStorage host buffers)",
-                "host_io": ("library default (TK_HOST_IO_AUTO): the stage-3 kernel writes y to the pinned host "
-                            "buffer; psi read from it directly when the split kernel does most psi reads, else "
-                            "copied in" if prec_name != "fp64" else "staged: H2D copy, matvec, D2H copy"),
+                "host_io": ("library default (TK_HOST_IO_AUTO): psi copied in (in two halves overlapped with "
+                            "stage 1 where the plan allows), the stage-3 kernel writes y to the pinned host buffer"
+                            if prec_name != "fp64" else "staged: H2D copy, matvec, D2H copy"),
                 "by_host_io": e2e_modes},
         "gpu_launches": launches_per_matvec * args.steps,
         "clocks": clocks,

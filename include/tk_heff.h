@@ -139,10 +139,12 @@ tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_apply);
  *   over the CPU-GPU link, overlapping the transfers with the GEMMs.
  * TK_HOST_IO_DIRECT_OUT: x is copied in; the stage-3 kernel writes y to host
  *   memory directly (every y element is written once).
- * TK_HOST_IO_AUTO (default): DIRECT when most psi reads of the plan come from
- *   the split kernel (tall stacks, one coalesced read per element), else
- *   DIRECT_OUT (the in-GEMM psi split reads columns with a stride, which the
- *   link serves poorly). */
+ * TK_HOST_IO_AUTO (default): DIRECT_OUT (measured fastest on the Hubbard,
+ *   Heisenberg and cylinder workloads; the in-GEMM psi split reads columns
+ *   with a stride, which the link serves poorly under DIRECT).
+ * Whenever x is copied and every stage-1 stack splits psi inside the GEMM
+ * kernel, the copy runs in two halves on a second stream and the stage-1
+ * tiles that read only the first half start while the second is in flight. */
 #define TK_HOST_IO_STAGED     0
 #define TK_HOST_IO_DIRECT     1
 #define TK_HOST_IO_DIRECT_OUT 2

@@ -348,6 +348,38 @@ static tk_status ensure_host_staging(tk_heff2_plan* p) {
         TK_CUDA(cudaMallocHost(&p->pin_err, sizeof(int)));
         *p->pin_err = 0;
     }
+    if (!p->copy_stream) TK_CUDA(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+    if (!p->ev_fork) TK_CUDA(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+    for (cudaEvent_t& e : p->ev_half)
+        if (!e) TK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return TK_OK;
+}
+
+// Split matvec from a host buffer copied in two halves: the stage-1 tiles
+// that read only the first half run while the second half is in flight
+// (copy stream forked from and joined back into `s`), then the rest of
+// the matvec as usual.  Stream-ordered; used inside a graph capture.
+static tk_status enqueue_split_psi_halves(tk_heff2_plan* p, const double* x, double* y, int64_t x_split,
+                                          cudaStream_t s) {
+    const int64_t n = p->host.total;
+    const int64_t len[2] = {x_split, n - x_split};
+    TK_CUDA(cudaEventRecord(p->ev_fork, s));
+    TK_CUDA(cudaStreamWaitEvent(p->copy_stream, p->ev_fork, 0));
+    for (int h = 0; h < 2; ++h) {
+        const int64_t off = h == 0 ? 0 : x_split;
+        TK_CUDA(cudaMemcpyAsync(p->hx.p + off, x + off, sizeof(double) * len[h], cudaMemcpyHostToDevice,
+                                p->copy_stream));
+        TK_CUDA(cudaEventRecord(p->ev_half[h], p->copy_stream));
+    }
+    for (int h = 0; h < 2; ++h) {
+        TK_CUDA(cudaStreamWaitEvent(s, p->ev_half[h], 0));
+        TK_CUDA(tc_stage1_half(*p->tc, p->hx.p, h, s));
+    }
+    for (int stage = 1; stage < 3; ++stage) {
+        std::string err;
+        cudaError_t e = tc_apply_stage(*p->tc, p->host, p->jobs.p, p->n_jobs, p->terms.p, p->hx.p, y, s, stage, err);
+        if (e != cudaSuccess) return cuda_fail(err.c_str(), e);
+    }
     return TK_OK;
 }
 
@@ -419,7 +451,7 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
     if (st != TK_OK) return st;
     cudaStream_t s = plan->stream;
     int mode = plan->precision == TK_PREC_BF16X3 ? plan->host_io : TK_HOST_IO_STAGED;
-    if (mode == TK_HOST_IO_AUTO) mode = tc_prefers_direct_input(*plan->tc) ? TK_HOST_IO_DIRECT : TK_HOST_IO_DIRECT_OUT;
+    if (mode == TK_HOST_IO_AUTO) mode = TK_HOST_IO_DIRECT_OUT;
     const double* mx = static_cast<const double*>(mapped_host_ptr(x));
     double* my = static_cast<double*>(mapped_host_ptr(y));
     const double* dx = mode == TK_HOST_IO_DIRECT ? mx : nullptr;
@@ -441,12 +473,18 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
             cudaGraphExecDestroy(plan->host_exec);
             plan->host_exec = nullptr;
         }
+        int64_t x_split = 0;
+        const bool halves = !dx && plan->precision == TK_PREC_BF16X3 && tc_psi_halves(*plan->tc, &x_split);
         TK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         tk_status cst = TK_OK;
         cudaError_t ce = cudaSuccess;
-        if (!dx) ce = cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s);
-        if (ce == cudaSuccess)
-            cst = tk_heff2_apply_prec(plan, dx ? dx : plan->hx.p, dy ? dy : plan->hy.p, s, plan->precision);
+        if (halves) {
+            cst = enqueue_split_psi_halves(plan, x, dy ? dy : plan->hy.p, x_split, s);
+        } else {
+            if (!dx) ce = cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+            if (ce == cudaSuccess)
+                cst = tk_heff2_apply_prec(plan, dx ? dx : plan->hx.p, dy ? dy : plan->hy.p, s, plan->precision);
+        }
         if (ce == cudaSuccess && cst == TK_OK && !dy)
             ce = cudaMemcpyAsync(y, plan->hy.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess && cst == TK_OK && plan->precision == TK_PREC_BF16X3)

@@ -384,6 +384,18 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
     };
     for (const TcTile& t : C.tiles1)
         if (!tile1_ok(t)) return false;
+    if (C.n1_first < 0 || (size_t)C.n1_first > C.tiles1.size() || C.x_split < 0 || C.x_split > T.total) {
+        err = "tensor-core stage 1 psi halves";
+        return false;
+    }
+    for (int32_t i = 0; i < C.n1_first; ++i) {
+        const TcTile& t = C.tiles1[(size_t)i];
+        for (int c = 0; c < t.n_valid; ++c)
+            if (C.xsrc[t.out_off + c] + (int64_t)(t.k_valid - 1) * C.xstride[t.out_off + c] >= C.x_split) {
+                err = "tensor-core stage 1 tile reads past the first psi half";
+                return false;
+            }
+    }
     for (const TcTile& t : C.tiles1x)
         if (!tile1_ok(t)) return false;
     for (const TcTile& t : C.tiles3) {
@@ -781,6 +793,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
             return (((uint64_t)p * nA + ap) * nWL + ws) * nB + b;
         };
         int64_t t1off = 0;
+        std::vector<int64_t> tile1_xend;  // per tiles1 entry: end of the psi range it reads
         // stage 1: one stack per ket sector A
         for (int a = 0; a < nA; ++a) {
             std::vector<std::pair<int, int>> lp;   // (A', ws)
@@ -794,15 +807,20 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                         rows += QA.dim[ap] * WL.dim[ws];
                     }
             std::vector<std::pair<int64_t, int>> xp;  // (p, B)
-            std::vector<int64_t> xcol;
-            int64_t cols = 0;
             for (int64_t p = 0; p < P; ++p)
                 for (int b = 0; b < nB; ++b)
-                    if (SUB(p, a, b) >= 0) {
-                        xp.push_back({p, b});
-                        xcol.push_back(cols);
-                        cols += QB.dim[b];
-                    }
+                    if (SUB(p, a, b) >= 0) xp.push_back({p, b});
+            // columns in the order of their psi sub-blocks in the vector, so that
+            // a tile's columns come from a narrow range of psi
+            std::stable_sort(xp.begin(), xp.end(), [&](const std::pair<int64_t, int>& u, const std::pair<int64_t, int>& v) {
+                return SUB(u.first, a, u.second) < SUB(v.first, a, v.second);
+            });
+            std::vector<int64_t> xcol;
+            int64_t cols = 0;
+            for (const auto& pb : xp) {
+                xcol.push_back(cols);
+                cols += QB.dim[pb.second];
+            }
             if (rows == 0 || cols == 0) continue;
             const int64_t K = QA.dim[a];
             const int32_t kch = kchunks(K);
@@ -865,6 +883,16 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                     t.mode = 2;
                     t.out_off = colbase0 + n0;
                     t.ldc = (int32_t)m0;
+                    if (!tall) {
+                        // end of the psi range the tile reads (its columns' sub-blocks)
+                        int64_t xend = 0;
+                        for (size_t jx = 0; jx < xp.size(); ++jx) {
+                            const int64_t DB = QB.dim[xp[jx].second];
+                            if (xcol[jx] < n0 + t.n_valid && xcol[jx] + DB > n0)
+                                xend = std::max(xend, SUB(xp[jx].first, a, xp[jx].second) + K * DB);
+                        }
+                        tile1_xend.push_back(xend);
+                    }
                     (tall ? C.tiles1x : C.tiles1).push_back(t);
                     C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
@@ -988,7 +1016,25 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
                 return (int64_t)a.m_valid * a.n_mma > (int64_t)b.m_valid * b.n_mma;
             });
         };
-        lpt(C.tiles1);
+        // psi in two halves (a block boundary near the middle): the in-GEMM-split
+        // tiles that read only the first half go first, so a host-buffer matvec
+        // can start them while the second half is still being copied in
+        C.x_split = T.total;
+        for (int64_t o : T.blk_off)
+            if (2 * o >= T.total) {
+                C.x_split = o;
+                break;
+            }
+        {
+            std::vector<TcTile> first, second;
+            for (size_t i = 0; i < C.tiles1.size(); ++i)
+                (tile1_xend[i] <= C.x_split ? first : second).push_back(C.tiles1[i]);
+            lpt(first);
+            lpt(second);
+            C.n1_first = (int32_t)first.size();
+            C.tiles1 = first;
+            C.tiles1.insert(C.tiles1.end(), second.begin(), second.end());
+        }
         lpt(C.tiles1x);
         lpt(C.tiles3);
         for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);

@@ -795,9 +795,9 @@ struct TcPlan {
     int32_t* xstride = nullptr;
     int* err = nullptr;
     int n1 = 0, n1x = 0, n3 = 0, nsplit = 0, njobs = 0;
+    int n1_first = 0;       // tiles1[0, n1_first) read psi below x_split only
+    int64_t x_split = 0;
     int nst1 = 1, nst1x = 2, nst3 = 2;  // pipeline stages of the GEMM launches
-    // psi elements read per matvec by the in-GEMM split (every row tile) and by the split kernel
-    double psi_reads_fused = 0.0, psi_reads_split = 0.0;
     CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl, mXh, mXl;
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,         th,           tl,   xh,      xl,  t1, tiles1, tiles1x,
@@ -845,13 +845,12 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
     p->n1 = (int)C.tiles1.size();
+    p->n1_first = C.n1_first;
+    p->x_split = C.x_split;
     p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
-    for (const TcTile& t : C.tiles1) p->psi_reads_fused += (double)t.k_valid * t.n_valid;
-    for (const TcSplitJob& j : C.split)
-        p->psi_reads_split += (double)std::min(kTcBK, j.rows - j.a0) * std::min(32, j.cols - j.b0);
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
     p->nst1x = C.max_kch1x <= 1 ? 1 : 2;
     p->nst3 = C.max_kch3 <= 1 ? 1 : 2;
@@ -905,6 +904,34 @@ void launch_tc_gemm(int nst, int n, const TcTile* tiles, const CUtensorMap& ah, 
 
 }  // namespace
 
+namespace {
+
+void launch_stage1_fused(TcPlan& tc, const double* x, int first, int count, cudaStream_t s) {
+    if (count <= 0) return;
+    const OutMap om{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride};
+    const TcTile* tiles = tc.tiles1 + first;
+    if (tc.nst1 == 1)
+        launch_pdl(tc_gemm1_kernel<1>, count, 128, smem_bytes(1), s, tiles, tc.mLh, tc.mLl, x,
+                   (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+    else
+        launch_pdl(tc_gemm1_kernel<2>, count, 128, smem_bytes(2), s, tiles, tc.mLh, tc.mLl, x,
+                   (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+}
+
+}  // namespace
+
+bool tc_psi_halves(const TcPlan& tc, int64_t* x_split) {
+    if (tc.nsplit > 0 || tc.n1x > 0 || tc.n1_first <= 0 || tc.n1_first >= tc.n1) return false;
+    *x_split = tc.x_split;
+    return true;
+}
+
+cudaError_t tc_stage1_half(TcPlan& tc, const double* x, int half, cudaStream_t s) {
+    if (half == 0) launch_stage1_fused(tc, x, 0, tc.n1_first, s);
+    else launch_stage1_fused(tc, x, tc.n1_first, tc.n1 - tc.n1_first, s);
+    return cudaGetLastError();
+}
+
 cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, const CombTerm*, const double* x,
                            double* y, cudaStream_t s, int stage, std::string& err) {
     if (stage == 0) {
@@ -912,14 +939,7 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
         if (tc.nsplit > 0)
             launch_pdl(split_psi_kernel, tc.nsplit, kSplitThreads, 0, s, (const TcSplitJob*)tc.split, x, tc.xh, tc.xl);
         launch_tc_gemm(tc.nst1x, tc.n1x, tc.tiles1x, tc.mLh, tc.mLl, tc.mXh, tc.mXl, om, CONST_A, tc.err, s);
-        if (tc.n1 > 0) {
-            if (tc.nst1 == 1)
-                launch_pdl(tc_gemm1_kernel<1>, tc.n1, 128, smem_bytes(1), s, (const TcTile*)tc.tiles1, tc.mLh, tc.mLl,
-                           x, (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
-            else
-                launch_pdl(tc_gemm1_kernel<2>, tc.n1, 128, smem_bytes(2), s, (const TcTile*)tc.tiles1, tc.mLh, tc.mLl,
-                           x, (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
-        }
+        launch_stage1_fused(tc, x, 0, tc.n1, s);
     } else if (stage == 1) {
         if (tc.njobs > 0)
             launch_pdl(combine_tc_kernel, tc.njobs, kCombThreads, 0, s, (const TcCombJob*)tc.jobs,
@@ -973,8 +993,6 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 }
 
 int* tc_error_word(TcPlan& tc) { return tc.err; }
-
-bool tc_prefers_direct_input(const TcPlan& tc) { return tc.psi_reads_split >= tc.psi_reads_fused; }
 
 int tc_launches(const TcPlan& tc) {
     return (tc.nsplit > 0) + (tc.n1x > 0) + (tc.n1 > 0) + (tc.njobs > 0) + (tc.n3 > 0);

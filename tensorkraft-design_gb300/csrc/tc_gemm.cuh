@@ -38,9 +38,11 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 int* tc_error_word(TcPlan& tc);
 // Kernel launches of one split-precision matvec (tc_apply).
 int tc_launches(const TcPlan& tc);
-// True when most psi reads of a matvec come from the split kernel (coalesced,
-// one per element) rather than from the in-GEMM split (strided, per row tile).
-bool tc_prefers_direct_input(const TcPlan& tc);
+// True (and the split point) when stage 1 can run as two launches, the first
+// reading psi only below *x_split: every stack splits psi in the GEMM kernel.
+bool tc_psi_halves(const TcPlan& tc, int64_t* x_split);
+// Stage-1 tiles of one psi half (0: those reading below the split only; 1: the rest).
+cudaError_t tc_stage1_half(TcPlan& tc, const double* x, int half, cudaStream_t s);
 // Synchronises `s`, reads and clears the error word: TK_ERR_TIMEOUT if set.
 tk_status tc_check_error(TcPlan& tc, cudaStream_t s);
 }  // namespace tk

@@ -190,6 +190,9 @@ struct TcTables {
     std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
     std::vector<TcTile> tiles1, tiles3;
     std::vector<TcTile> tiles1x;       // stage-1 tiles of tall stacks (B operand from the split copy)
+    // tiles1[0, n1_first) read psi only below element x_split (a block boundary)
+    int32_t n1_first = 0;
+    int64_t x_split = 0;
     std::vector<TcSplitJob> split;     // psi -> split copy, tall stacks only
     std::vector<TcCombJob> jobs;
     std::vector<TcCombTerm> terms;

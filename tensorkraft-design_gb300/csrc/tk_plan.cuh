@@ -90,6 +90,8 @@ struct tk_heff2_plan {
     // CUDA graph of the last host-buffer matvec (copies, kernels, error-word
     // read-back), reused while the buffers and the plan settings repeat
     cudaGraphExec_t host_exec = nullptr;
+    cudaStream_t copy_stream = nullptr;  // the psi copy of a host-buffer matvec, in two halves
+    cudaEvent_t ev_fork = nullptr, ev_half[2] = {nullptr, nullptr};
     const void* host_gx = nullptr;
     void* host_gy = nullptr;
     int host_gkey = -1;
@@ -112,6 +114,10 @@ struct tk_heff2_plan {
         if (pin_y) cudaFreeHost(pin_y);
         if (pin_err) cudaFreeHost(pin_err);
         if (host_exec) cudaGraphExecDestroy(host_exec);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        for (cudaEvent_t e : ev_half)
+            if (e) cudaEventDestroy(e);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };
