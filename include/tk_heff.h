@@ -398,10 +398,9 @@ tk_status tk_heff2_two_site_product_complex(tk_heff2_plan* plan, const tk_bst* a
 
 /*
  * Self-check, no reference counterpart: the split-precision kernels convert
- * fp64 <-> fp32 from the IEEE 754 bit layouts on the integer pipes (the FP64
- * pipe of this GPU is narrow).  Compares those conversions with the hardware
- * ones on n device doubles (fp64 -> fp32 where the result is a normal fp32;
- * fp32 -> fp64 on the fp32 bit patterns taken from the doubles' bits) and
+ * psi from fp64 to fp32 from the IEEE 754 bit layouts on the integer pipes
+ * (the FP64 pipe of this GPU is narrow).  Compares that conversion with the
+ * hardware one on n device doubles (where the result is a normal fp32) and
  * writes the number of mismatches to *mismatches.  Synchronous.
  */
 tk_status tk_check_split_conversions(tk_ctx* ctx, const double* x_dev, int64_t n, uint64_t* mismatches);

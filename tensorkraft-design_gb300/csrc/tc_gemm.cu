@@ -164,10 +164,11 @@ __device__ __forceinline__ void tmem_row_to_smem(uint32_t tbase, int n_mma, floa
             for (int i = 0; i < 16; ++i) srow[16 * q + i] = __uint_as_float(r[16 * q + i]);
 }
 
-// Conversions between fp64 and fp32 on the integer pipes.  This GPU's FP64
-// pipe is narrow (a few operations per SM and clock) and the hardware
-// conversions issue to it, so the per-element conversions of the split
-// kernels are done from the IEEE 754 bit layouts instead.
+// fp64 -> fp32 on the integer pipes.  This GPU's FP64 pipe is narrow (a few
+// operations per SM and clock) and the hardware conversion issues to it, so
+// the per-element conversions of the psi split are done from the IEEE 754
+// bit layouts instead (fp32 -> fp64 in the epilogues, one per output
+// element, stays on the hardware conversion).
 //
 // fp64 -> fp32, round to nearest even (IEEE 754-2008 default rounding): equal
 // to __double2float_rn for every finite input whose result is a normal fp32;
@@ -188,23 +189,6 @@ __device__ __forceinline__ float d2f_bits(double x) {
     return __uint_as_float(e > 896u ? (sign | 0x7F800000u) : sign);  // overflow, or zero / below 2^-126
 }
 
-// fp32 -> fp64, exact for every input (subnormal fp32 values are normalised).
-__device__ __forceinline__ double f2d_bits(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-    const int e = (int)((u >> 23) & 0xFF);
-    uint32_t m = u & 0x7FFFFFu;
-    if (e == 0xFF) return __longlong_as_double((long long)(sign | (0x7FFull << 52) | ((unsigned long long)m << 29)));
-    if (e == 0) {
-        if (m == 0) return __longlong_as_double((long long)sign);
-        const int sh = __clz(m) - 8;  // bring the leading one to bit 23
-        m = (m << sh) & 0x7FFFFFu;
-        const unsigned long long de = (unsigned long long)(1 - 127 + 1023 - sh);
-        return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)m << 29)));
-    }
-    const unsigned long long de = (unsigned long long)(e - 127 + 1023);
-    return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)m << 29)));
-}
 
 // Two elements at once: x ~ hi + lo with hi = bf16(x32), lo = bf16(x32 - hi),
 // x32 = fp32(x) (the difference is exact in fp32); the hi and lo of a and b
@@ -377,17 +361,27 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
         tmem_row_to_smem(tbase, t.n_mma, stile[row]);
         __syncwarp();
-        const int rend = min(t.m_valid, warp * 32 + 32);
         if (t.mode == 2) {
+            const int rend = min(t.m_valid, warp * 32 + 32);
             for (int r = warp * 32; r < rend; ++r)
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
                     if (lane + 32 * h < t.n_valid)
                         om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane + 32 * h];
         } else {
-            for (int r = warp * 32; r < rend; ++r) {  // warp-uniform trip count
-                double* o = om.out64 + __shfl_sync(0xffffffffu, my_row, r - warp * 32) + t.n0;
-                for (int col = lane; col < t.n_valid; col += 32) o[col] = f2d_bits(stile[r][col]);
+            // y rows unrolled eight at a time (independent shuffle / shared-
+            // memory / store chains in flight); fp32 -> fp64 is exact, on the
+            // hardware conversion (the FP64 pipe is idle in this epilogue)
+#pragma unroll 8
+            for (int i = 0; i < 32; ++i) {
+                const int r = warp * 32 + i;
+                const int64_t rbase = __shfl_sync(0xffffffffu, my_row, i);  // every lane, every row
+                if (r < t.m_valid) {
+                    double* o = om.out64 + rbase + t.n0;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        if (lane + 32 * h < t.n_valid) o[lane + 32 * h] = (double)stile[r][lane + 32 * h];
+                }
             }
         }
     }
@@ -964,9 +958,8 @@ cudaError_t tc_apply(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs,
 
 namespace {
 
-// Counts inputs where the integer-pipe conversions differ from the hardware
-// ones: d2f_bits vs __double2float_rn (inputs with a normal fp32 result) and
-// f2d_bits vs the fp32 -> fp64 conversion (every fp32 value).
+// Counts inputs where the integer-pipe conversion differs from the hardware
+// one: d2f_bits vs __double2float_rn, on inputs with a normal fp32 result.
 __global__ void conversion_check_kernel(const double* __restrict__ x, int64_t n, unsigned long long* bad) {
     unsigned long long cnt = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -975,11 +968,6 @@ __global__ void conversion_check_kernel(const double* __restrict__ x, int64_t n,
         const float got = d2f_bits(v);
         const bool normal = fabsf(ref) >= 1.17549435e-38f && fabsf(ref) <= 3.40282347e38f;
         if (normal && __float_as_uint(ref) != __float_as_uint(got)) ++cnt;
-        const float f = __uint_as_float((uint32_t)(__double_as_longlong(v) >> 16));  // any fp32 bit pattern
-        if (f == f) {
-            const double dr = (double)f, dg = f2d_bits(f);
-            if (__double_as_longlong(dr) != __double_as_longlong(dg)) ++cnt;
-        }
     }
     if (cnt) atomicAdd(bad, cnt);
 }

@@ -32,7 +32,7 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables& host, const CombJob* d
 
 namespace tk {
 // Adds to *bad (device) the number of inputs where the split kernels' integer
-// fp64 <-> fp32 conversions differ from the hardware conversions.
+// fp64 -> fp32 conversion differs from the hardware conversion.
 cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* bad, cudaStream_t s);
 // Device error word of the tensor-core kernels (0 = no bounded wait ran out).
 int* tc_error_word(TcPlan& tc);
