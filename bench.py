@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--tdvp-steps", type=int, default=0, metavar="K",
                     help="also time K real-time TDVP steps of the impurity Green's function (Anderson chain, "
                          "16 sites, D=1024, dt=0.05, Krylov 16) after a split-precision DMRG ground state")
+    ap.add_argument("--rows", action="store_true",
+                    help="also time environment growth, the dense GEMM and the block GEMM beside CPU restatements")
     ap.add_argument("--compare-schedules", type=int, default=0, metavar="STEPS",
                     help="also time STEPS FP64 matvecs with one grouped launch per stage and with one launch "
                          "per sector block")
@@ -199,6 +201,101 @@ def tdvp_anderson(torch, steps: int, n: int = 16, D: int = 1024, dt: float = 0.0
     out["g_greater_0"] = norm * norm
     out["matvecs"] = rec2.matvecs
     out["max_bond"] = max(b.total_dim for b in dm.bonds)
+    return out
+
+
+def secondary_rows(torch, dev):
+    """Timings of the rows around the matvec, each beside a CPU restatement:
+    one left environment growth (contract_left_environment, FP64 grouped GEMM
+    on the device) at the Hubbard D=2048 bond and at D=512 (where the dense
+    numpy contraction of the oracle finishes in seconds); the dense GEMM of
+    LinAlgBackend::gemm (tk_gemm_f64, 4096^3) against cuBLAS DGEMM in the same
+    run; the rank-2 block GEMM of SparseLinAlgBackend::block_gemm
+    (tk_block_gemm_f64, host buffers in and out) on 15 U(1) sectors summing
+    to 1024 against numpy per-block products."""
+    import ctypes as C
+
+    import oracle.environments as oe
+    from tk_gb300 import _abi, models, sweep
+    from tk_gb300.heff import _Marshal, context
+    from tk_gb300.symmetry import U1, BlockSparseTensor, key_pack
+
+    out = {}
+
+    def ev_ms(fn, reps):
+        fn()
+        torch.cuda.synchronize(dev)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        e.synchronize()
+        return s.elapsed_time(e) / reps
+
+    rng = np.random.default_rng(5)
+    for scale in (1.0, 0.25):
+        p = models.workload("hubbard_d2048", scale=scale)
+        D = p.env_l.ket_idx.total_dim
+        bl = p.env_l.ket_idx
+        mid = models.gaussian_bond_u1u1(D, 31)
+        A = sweep.SiteTensor.from_dense(p.kind, [p.w_i.indices[0], bl, mid],
+                                        rng.standard_normal((p.w_i.indices[0].total_dim, D, D)), dev.index or 0)
+        Ld = sweep.DeviceEnv.from_dense(p.kind, p.env_l.data, bl, p.env_l.mpo_idx, bl, dev.index or 0)
+        ms = ev_ms(lambda: sweep.grow_left(Ld, A, p.w_i, device=dev.index or 0), 5)
+        row = {"D": D, "gpu_ms": ms}
+        if scale < 1:
+            Adense, Wd = A.to_dense(), p.w_i.to_dense()
+            t0 = time.perf_counter()
+            ref = oe.grow_left(p.env_l.data, Adense, Wd)
+            row["cpu_numpy_dense_ms"] = (time.perf_counter() - t0) * 1e3
+            got = sweep.grow_left(Ld, A, p.w_i, device=dev.index or 0).to_dense()
+            row["rel_err_vs_numpy"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        out[f"env_grow_left_hubbard_D{D}"] = row
+
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, n, dtype=torch.float64, device=dev)
+    ma = _abi.tk_mat(a.data_ptr(), n, n, n, 1, 0)
+    mb = _abi.tk_mat(b.data_ptr(), n, n, n, 1, 0)
+    mc = _abi.tk_mat_mut(c.data_ptr(), n, n, n, 1)
+    lib = _abi.load()
+    ctx = context(dev.index or 0)
+    t_ours = ev_ms(lambda: _abi.check(lib.tk_gemm_f64(ctx, 1.0, C.byref(ma), C.byref(mb), 0.0, C.byref(mc), None)), 3)
+    t_cublas = ev_ms(lambda: torch.matmul(a, b, out=c), 3)
+    flop = 2.0 * n ** 3
+    out["gemm_f64_4096"] = {"tk_gemm_f64_tflops": flop / t_ours / 1e9, "cublas_dgemm_tflops": flop / t_cublas / 1e9,
+                            "fraction_of_cublas": t_cublas / t_ours}
+
+    bond = models.gaussian_bond_u1(1024, 15, 3.0)
+    tens = []
+    for _ in range(2):
+        t = BlockSparseTensor([bond, bond], (0,), [0, 1])
+        for q, d in bond.sectors:
+            t.set_block([q, q], rng.standard_normal((d, d)))
+        tens.append(t)
+    m = _Marshal()
+    ba, bb = m.bst(tens[0]), m.bst(tens[1])
+
+    def block_gemm():
+        res = _abi.tk_bst_out()
+        _abi.check(lib.tk_block_gemm_f64(ctx, C.byref(ba), C.byref(bb), C.byref(res)))
+        lib.tk_bst_free(C.byref(res))
+
+    block_gemm()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        block_gemm()
+    t_blk = (time.perf_counter() - t0) / 5
+    t0 = time.perf_counter()
+    for _ in range(5):
+        for q, _d in bond.sectors:
+            tens[0].blocks[key_pack(U1, [q, q])] @ tens[1].blocks[key_pack(U1, [q, q])]
+    t_np = (time.perf_counter() - t0) / 5
+    flop = sum(2.0 * d ** 3 for _, d in bond.sectors)
+    out["block_gemm_u1_15_sectors_1024"] = {"gpu_ms_host_buffers": t_blk * 1e3, "cpu_numpy_ms": t_np * 1e3,
+                                            "gflop": flop / 1e9}
     return out
 
 
@@ -569,6 +666,8 @@ def run_ours(args):
         line["lanczos"] = lz
     if args.compare_schedules > 0:
         line["schedules"] = compare_schedules(plan, x, y, torch, dev, args.compare_schedules, flush)
+    if args.rows:
+        line["rows"] = secondary_rows(torch, dev)
     if args.dmrg:
         line["dmrg_cfg1"] = dmrg_cfg1(torch, args.dmrg_cpu)
     if args.sweeps > 0:

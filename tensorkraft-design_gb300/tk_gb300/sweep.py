@@ -39,6 +39,10 @@ from ._abi import PREC_FP64, check
 from .heff import Heff2Plan, _Marshal, context, identity_mpo_site
 from .symmetry import QIndex, bit_width, dual, fuse, identity, key_pack, key_unpack, qn_pack
 
+# pairwise contraction order with intermediates allowed to exceed the inputs (numpy's
+# default limit, the largest operand, falls back to one nested loop over every index)
+_PATH = ("greedy", 2 ** 34)
+
 
 def _torch():
     import torch
@@ -575,7 +579,7 @@ def mps_overlap(bra: list, ket: list) -> complex:
             blk_b = Bb.get((qs, ql, qr))
             if blk_b is None or ql not in E:
                 continue
-            t = np.einsum("sxa,xy,syb->ab", blk_a.conj(), E[ql], blk_b, optimize=True)
+            t = np.einsum("sxa,xy,syb->ab", blk_a.conj(), E[ql], blk_b, optimize=_PATH)
             nxt[qr] = nxt[qr] + t if qr in nxt else t
         E = nxt
     return complex(sum(v[0, 0] for v in E.values())) if E else 0j

@@ -11,6 +11,10 @@ from helpers import ed_heisenberg, models, oracle_dense_literal, small_problem
 from test_gpu_lanczos import matrix_plan
 from tk_gb300 import PREC_FP64, sweep
 
+# pairwise contraction order with intermediates allowed to exceed the inputs (numpy's
+# default limit, the largest operand, falls back to one nested loop over every index)
+_PATH = ("greedy", 2 ** 34)
+
 pytestmark = pytest.mark.gpu
 KATS = json.loads((Path(__file__).parent / "golden" / "reference_kats.json").read_text())
 
@@ -151,7 +155,7 @@ def test_complex_plan_matches_dense(lib_built):
     xd = plan.flat_to_dense(x.real) + 1j * plan.flat_to_dense(x.imag)
     d = Wi.shape[0]
     X = xd.reshape(d, d, Lm.shape[0], Rm.shape[0])
-    Y = np.einsum("pwa,stwv,uxvz,qzb,suab->txpq", Lm, Wi, Wj, Rm, X, optimize=True)
+    Y = np.einsum("pwa,stwv,uxvz,qzb,suab->txpq", Lm, Wi, Wj, Rm, X, optimize=_PATH)
     yr, yi = torch.empty(plan.block_dim, dtype=torch.float64).cuda(), torch.empty(plan.block_dim,
                                                                                  dtype=torch.float64).cuda()
     plan.apply_complex(_dev(x.real), _dev(x.imag), yr, yi)
