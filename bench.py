@@ -238,12 +238,16 @@ def secondary_rows(torch, dev):
         p = models.workload("hubbard_d2048", scale=scale)
         D = p.env_l.ket_idx.total_dim
         bl = p.env_l.ket_idx
-        mid = models.gaussian_bond_u1u1(D, 31)
+        # the right bond: the same (N, 2Sz) distribution (a site adds 0..2 particles and keeps
+        # N - 2Sz even, so every left sector reaches several right ones)
+        mid = models.gaussian_bond_u1u1(D, 30)
         A = sweep.SiteTensor.from_dense(p.kind, [p.w_i.indices[0], bl, mid],
                                         rng.standard_normal((p.w_i.indices[0].total_dim, D, D)), dev.index or 0)
+        if len(A.keys) == 0:
+            raise RuntimeError("environment-growth timing: the site tensor has no allowed block")
         Ld = sweep.DeviceEnv.from_dense(p.kind, p.env_l.data, bl, p.env_l.mpo_idx, bl, dev.index or 0)
         ms = ev_ms(lambda: sweep.grow_left(Ld, A, p.w_i, device=dev.index or 0), 5)
-        row = {"D": D, "gpu_ms": ms}
+        row = {"D": D, "site_blocks": int(len(A.keys)), "gpu_ms": ms}
         if scale < 1:
             Adense, Wd = A.to_dense(), p.w_i.to_dense()
             t0 = time.perf_counter()
