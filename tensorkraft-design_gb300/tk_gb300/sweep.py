@@ -607,8 +607,9 @@ def _qr_left(blocks: dict):
     return newb, Rs
 
 
-def canonicalize(sites: list, bonds: list, center: int, device: int = 0):
-    """Mixed-canonical form of a block-sparse MPS with the orthogonality
+def canonicalize_blocks(kind, blocks: list, bonds: list, center: int):
+    """Mixed-canonical form of a block-sparse MPS given as host blocks
+    ({(q_s, q_L, q_R): array (d_s, D_L, D_R)} per site) with the orthogonality
     centre at `center` (mps/mod.rs:346-419: left_canonicalize,
     right_canonicalize, mixed_canonicalize): sites left of the centre become
     left isometries (sum_s A_s^H A_s = 1) by thin QR, sites right of it right
@@ -616,13 +617,10 @@ def canonicalize(sites: list, bonds: list, center: int, device: int = 0):
     centre.  The QR is taken per bond charge over all blocks of that charge
     (mps/mod.rs:421-770 factors each block on its own, which leaves blocks of
     one charge non-orthogonal to each other); a bond shrinks to
-    min(rows, cols) per charge.  Returns (sites, bonds); the state and its
+    min(rows, cols) per charge.  Returns (blocks, bonds); the state and its
     norm are unchanged."""
-    n = len(sites)
-    sites, bonds = list(sites), list(bonds)
-    kind = sites[0].kind
-    P = sites[0].legs[0]
-    host = [t.blocks_host() for t in sites]
+    n = len(blocks)
+    host, bonds = [dict(b) for b in blocks], list(bonds)
     for i in range(0, min(center, n - 1)):
         newb, Rs = _qr_left(host[i])
         nb = QIndex(kind, [(q, R.shape[0]) for q, R in sorted(Rs.items())])
@@ -647,7 +645,15 @@ def canonicalize(sites: list, bonds: list, center: int, device: int = 0):
                 prv[(qs, ql, qr)] = np.einsum("sab,kb->sak", blk, Rs[qr].conj())
         host[i - 1] = prv
         bonds[i] = nb
-    out = [SiteTensor.from_blocks(kind, [P, bonds[i], bonds[i + 1]], host[i], device) for i in range(n)]
+    return host, bonds
+
+
+def canonicalize(sites: list, bonds: list, center: int, device: int = 0):
+    """canonicalize_blocks on device site tensors (SiteTensor in, SiteTensor out)."""
+    kind = sites[0].kind
+    P = sites[0].legs[0]
+    host, bonds = canonicalize_blocks(kind, [t.blocks_host() for t in sites], bonds, center)
+    out = [SiteTensor.from_blocks(kind, [P, bonds[i], bonds[i + 1]], host[i], device) for i in range(len(sites))]
     return out, bonds
 
 
