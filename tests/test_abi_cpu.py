@@ -83,7 +83,8 @@ def test_host_tables_self_check_cpu(lib_built):
         import pytest
 
         pytest.skip("CPU-only check (a GPU would create a real plan)")
-    for name, D in [("heisenberg", 40), ("hubbard", 48), ("cylinder", 96)]:
+    # the larger cases build tall stage-1 stacks (split copy) and psi halves
+    for name, D in [("heisenberg", 40), ("hubbard", 48), ("cylinder", 96), ("cylinder", 512), ("hubbard", 256)]:
         for all_sectors in (False, True):
             st, msg = _plan_status(small_problem(name, D), all_sectors)
             assert st == 4 and "cudaSetDevice" in msg, (name, st, msg)
