@@ -307,6 +307,19 @@ def dist_env():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest of the ranks' x (the timing of a replicas run is its
+    slowest rank); x itself without an initialised process group."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def oracle_for(prob):
     import oracle
 
@@ -558,11 +571,7 @@ def run_ours(args):
     clk.stop()
     if ws > 1:
         dist.barrier()
-    total_s = sum(step_ms) / 1e3
-    t = torch.tensor([total_s], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_s = float(t.item())
+    max_s = max_over_ranks(sum(step_ms) / 1e3, dev)
     value = args.steps * ws / max_s
     stage_ms /= prof_steps
     clocks = clk.summary(t_load, t_end)
@@ -590,10 +599,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(args.steps):
             plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
-        te = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
-        if ws > 1:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        return args.steps * ws / float(te.item())
+        return args.steps * ws / max_over_ranks(time.perf_counter() - t0, dev)
 
     # the three transfer forms, then the library's default (its per-plan choice)
     e2e_modes = {name: e2e_run(m) for name, m in (("staged", _abi.HOST_IO_STAGED), ("direct", _abi.HOST_IO_DIRECT),
