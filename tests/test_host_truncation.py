@@ -100,3 +100,33 @@ def test_truncation_rule_of_truncate_svd():
         _, _, nb, disc = split_two_site(kind, psi * 3.0, keys, offs, [P, P, QA, QB], max_bond, cutoff, True)
         assert nb.total_dim == want, (cutoff, max_bond)
         assert abs(disc - np.sum(sv[want:] ** 2) / np.sum(sv ** 2)) < 1e-12
+
+
+def test_complex_full_rank_reconstructs_and_is_isometric():
+    """Complex two-site vectors (real-time TDVP): the same per-charge
+    truncation with Hermitian density matrices."""
+    kind, P, QA, QB, keys, offs, qs, psi_r = _case()
+    psi = psi_r + 1j * np.random.default_rng(1).standard_normal(psi_r.shape)
+    psi /= np.linalg.norm(psi)
+    d = P.total_dim
+    T = np.zeros((d, d, QA.total_dim, QB.total_dim), dtype=complex)
+    for off, (qi, qj, qa, qb) in zip(offs, qs):
+        ni, nj, da, db = P.dim_of(qi), P.dim_of(qj), QA.dim_of(qa), QB.dim_of(qb)
+        oi, oj, oa, ob = P.offset_of(qi), P.offset_of(qj), QA.offset_of(qa), QB.offset_of(qb)
+        T[oi:oi + ni, oj:oj + nj, oa:oa + da, ob:ob + db] = psi[off:off + ni * nj * da * db].reshape(ni, nj, da, db)
+    for to_right in (True, False):
+        Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], 10_000, 0.0, to_right)
+        A = np.zeros((d, QA.total_dim, nb.total_dim), dtype=complex)
+        B = np.zeros((d, nb.total_dim, QB.total_dim), dtype=complex)
+        for (s, ql, qr), b in Ai.items():
+            A[P.offset_of(s):P.offset_of(s) + b.shape[0], QA.offset_of(ql):QA.offset_of(ql) + b.shape[1],
+              nb.offset_of(qr):nb.offset_of(qr) + b.shape[2]] = b
+        for (s, ql, qr), b in Aj.items():
+            B[P.offset_of(s):P.offset_of(s) + b.shape[0], nb.offset_of(ql):nb.offset_of(ql) + b.shape[1],
+              QB.offset_of(qr):QB.offset_of(qr) + b.shape[2]] = b
+        assert disc < 1e-24
+        assert np.allclose(np.einsum("sab,tbc->stac", A, B), T, atol=1e-12)
+        if to_right:
+            assert np.allclose(np.einsum("sab,sac->bc", A.conj(), A), np.eye(nb.total_dim), atol=1e-12)
+        else:
+            assert np.allclose(np.einsum("sab,scb->ac", B, B.conj()), np.eye(nb.total_dim), atol=1e-12)
