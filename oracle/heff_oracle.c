@@ -423,6 +423,9 @@ typedef struct {
     int64_t t1_total;
     int64_t* t2_off;               /* [P][nwr][nA][nB] */
     int64_t t2_total;
+    /* the non-empty tasks of each step, in descending-cost (LPT) order */
+    int64_t *task1, *task2, *task3;
+    int64_t n_task1, n_task2, n_task3;
     double* T1;
     double* T2;
     const double* L;
@@ -444,6 +447,7 @@ static int cmp_keyed4(const void* a, const void* b) {
 }
 
 void orc_bs_destroy(orc_bs_plan* p);
+static int build_tasks(orc_bs_plan* p);
 
 /* psi_flux may be NULL (all sectors). */
 orc_bs_plan* orc_bs_create(int kind, const orc_qindex* phys_i, const orc_qindex* phys_j,
@@ -584,7 +588,7 @@ orc_bs_plan* orc_bs_create(int kind, const orc_qindex* phys_i, const orc_qindex*
     p->t2_total = off;
     p->T1 = (double*)malloc(sizeof(double) * (size_t)(p->t1_total > 0 ? p->t1_total : 1));
     p->T2 = (double*)malloc(sizeof(double) * (size_t)(p->t2_total > 0 ? p->t2_total : 1));
-    if (!p->T1 || !p->T2) { orc_bs_destroy(p); return NULL; }
+    if (!p->T1 || !p->T2 || build_tasks(p) != 0) { orc_bs_destroy(p); return NULL; }
     return p;
 }
 
@@ -601,6 +605,7 @@ void orc_bs_destroy(orc_bs_plan* p) {
     free(p->secI); free(p->locI); free(p->secJ); free(p->locJ); free(p->dimSi); free(p->dimSj);
     free(p->blk); free(p->blk_off); free(p->blk_of); free(p->Lnz); free(p->Rnz); free(p->RT);
     free(p->Wij); free(p->t1_off); free(p->t2_off); free(p->T1); free(p->T2);
+    free(p->task1); free(p->task2); free(p->task3);
     free(p);
 }
 
@@ -614,89 +619,202 @@ static int64_t psi_sub(const orc_bs_plan* p, int64_t pp, int32_t a, int32_t b) {
     return p->blk_off[blk] + sub * p->dimA[a] * p->dimB[b];
 }
 
-/* x and y in the block layout; y fully overwritten. */
-int orc_bs_apply(orc_bs_plan* p, const double* x, double* y) {
-    int64_t P = p->P, nwl = p->nwl, nwr = p->nwr;
-    int32_t nA = p->nA, nB = p->nB;
-    int64_t n1 = P * nwl * nA * nB;
-    /* step 1: T1[p,wl,A',B] = sum_A L[A',wl,A] x[p,A,B] */
-    #pragma omp parallel for schedule(dynamic, 4)
-    for (int64_t id = 0; id < n1; ++id) {
-        int64_t o = p->t1_off[id];
-        if (o < 0) continue;
-        int32_t b = (int32_t)(id % nB);
-        int32_t ap = (int32_t)((id / nB) % nA);
-        int64_t wl = (id / ((int64_t)nB * nA)) % nwl;
-        int64_t pp = id / ((int64_t)nB * nA * nwl);
-        int64_t M = p->dimA[ap], N = p->dimB[b];
-        double* t = p->T1 + o;
-        memset(t, 0, sizeof(double) * (size_t)(M * N));
-        for (int32_t a = 0; a < nA; ++a) {
-            if (!p->Lnz[((int64_t)ap * nwl + wl) * nA + a]) continue;
-            int64_t xo = psi_sub(p, pp, a, b);
-            if (xo < 0) continue;
-            const double* xs = x + xo;
-            int64_t K = p->dimA[a];
+/*
+ * C[M x N] += A[M x K] B[K x N], row-major with leading dimensions lda, ldb,
+ * ldc.  This is the plain i-k-j loop, register-blocked: 4 x 4 tiles of C
+ * live in locals over panels of 256 k, so the 256 x 4 panel of B stays in L1
+ * while the row tiles stream past it.  Every element of C still adds its
+ * products one at a time in ascending k, which keeps the sums bit-identical
+ * to the unblocked loop on every host (ISO C mode keeps the compiler from
+ * contracting them into fused multiply-adds).  The per-task products of the
+ * reference's block GEMM go to faer's matmul
+ * (tk-linalg/src/device/faer.rs:475-482); this blocking stands in for that
+ * library's cache blocking.
+ */
+enum { ORC_MR = 4, ORC_NR = 4, ORC_KB = 256 };
+
+static void tile_mr(int64_t kb, const double* restrict A, int64_t lda, const double* restrict B, int64_t ldb,
+                    double* restrict C, int64_t ldc) {
+    double c[ORC_MR][ORC_NR];
+    for (int i = 0; i < ORC_MR; ++i)
+        for (int j = 0; j < ORC_NR; ++j) c[i][j] = C[i * ldc + j];
+    for (int64_t k = 0; k < kb; ++k) {
+        const double* b = B + k * ldb;
+        for (int i = 0; i < ORC_MR; ++i) {
+            const double a = A[i * lda + k];
+            for (int j = 0; j < ORC_NR; ++j) c[i][j] += a * b[j];
+        }
+    }
+    for (int i = 0; i < ORC_MR; ++i)
+        for (int j = 0; j < ORC_NR; ++j) C[i * ldc + j] = c[i][j];
+}
+
+static void tile_1(int64_t kb, const double* restrict A, const double* restrict B, int64_t ldb, double* restrict C) {
+    double c[ORC_NR];
+    for (int j = 0; j < ORC_NR; ++j) c[j] = C[j];
+    for (int64_t k = 0; k < kb; ++k) {
+        const double* b = B + k * ldb;
+        const double a = A[k];
+        for (int j = 0; j < ORC_NR; ++j) c[j] += a * b[j];
+    }
+    for (int j = 0; j < ORC_NR; ++j) C[j] = c[j];
+}
+
+static void gemm_acc(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B, int64_t ldb,
+                     double* C, int64_t ldc) {
+    for (int64_t k0 = 0; k0 < K; k0 += ORC_KB) {
+        const int64_t kb = K - k0 < ORC_KB ? K - k0 : ORC_KB;
+        int64_t j0 = 0;
+        for (; j0 + ORC_NR <= N; j0 += ORC_NR) {
+            int64_t i0 = 0;
+            for (; i0 + ORC_MR <= M; i0 += ORC_MR)
+                tile_mr(kb, A + i0 * lda + k0, lda, B + k0 * ldb + j0, ldb, C + i0 * ldc + j0, ldc);
+            for (; i0 < M; ++i0) tile_1(kb, A + i0 * lda + k0, B + k0 * ldb + j0, ldb, C + i0 * ldc + j0);
+        }
+        if (j0 < N)
             for (int64_t i = 0; i < M; ++i) {
-                const double* lrow = p->L + ((p->offA[ap] + i) * nwl + wl) * p->d_l + p->offA[a];
-                double* trow = t + i * N;
-                for (int64_t k = 0; k < K; ++k) {
-                    double lv = lrow[k];
-                    const double* xr = xs + k * N;
-                    for (int64_t j = 0; j < N; ++j) trow[j] += lv * xr[j];
+                double* c = C + i * ldc;
+                for (int64_t k = k0; k < k0 + kb; ++k) {
+                    const double a = A[i * lda + k];
+                    const double* b = B + k * ldb;
+                    for (int64_t j = j0; j < N; ++j) c[j] += a * b[j];
                 }
             }
+    }
+}
+
+/* Sector GEMM tasks of the three steps, ordered by descending cost (ties by
+ * task id) as the reference orders its block-GEMM tasks before handing them
+ * to its thread pool (tk-linalg/src/tasks.rs:172-174). */
+typedef struct { double cost; int64_t id; } orc_task;
+
+static int cmp_task(const void* a, const void* b) {
+    const orc_task *x = (const orc_task*)a, *y = (const orc_task*)b;
+    if (x->cost != y->cost) return x->cost > y->cost ? -1 : 1;
+    return x->id < y->id ? -1 : (x->id > y->id ? 1 : 0);
+}
+
+static int64_t* lpt_ids(orc_task* t, int64_t n) {
+    qsort(t, (size_t)n, sizeof(orc_task), cmp_task);
+    int64_t* ids = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    if (ids)
+        for (int64_t i = 0; i < n; ++i) ids[i] = t[i].id;
+    return ids;
+}
+
+static int build_tasks(orc_bs_plan* p) {
+    const int64_t P = p->P, nwl = p->nwl, nwr = p->nwr;
+    const int32_t nA = p->nA, nB = p->nB;
+    const int64_t n1 = P * nwl * nA * nB, n2 = P * nwr * nA * nB, n3 = P * nA * nB;
+    int64_t cap = n1 > n2 ? n1 : n2;
+    if (n3 > cap) cap = n3;
+    orc_task* t = (orc_task*)malloc(sizeof(orc_task) * (size_t)(cap > 0 ? cap : 1));
+    if (!t) return -1;
+    int64_t n = 0;
+    for (int64_t id = 0; id < n1; ++id) {
+        if (p->t1_off[id] < 0) continue;
+        const int32_t b = (int32_t)(id % nB), ap = (int32_t)((id / nB) % nA);
+        const int64_t wl = (id / ((int64_t)nB * nA)) % nwl, pp = id / ((int64_t)nB * nA * nwl);
+        double c = 0.0;
+        for (int32_t a = 0; a < nA; ++a)
+            if (p->Lnz[((int64_t)ap * nwl + wl) * nA + a] && psi_sub(p, pp, a, b) >= 0)
+                c += (double)p->dimA[ap] * p->dimA[a] * p->dimB[b];
+        t[n].cost = c; t[n].id = id; ++n;
+    }
+    p->n_task1 = n;
+    p->task1 = lpt_ids(t, n);
+    n = 0;
+    for (int64_t id = 0; id < n2; ++id) {
+        if (p->t2_off[id] < 0) continue;
+        const int32_t b = (int32_t)(id % nB), ap = (int32_t)((id / nB) % nA);
+        const int64_t wr = (id / ((int64_t)nB * nA)) % nwr, po = id / ((int64_t)nB * nA * nwr);
+        double c = 0.0;
+        for (int64_t pp = 0; pp < P; ++pp) for (int64_t wl = 0; wl < nwl; ++wl)
+            if (p->Wij[((pp * P + po) * nwl + wl) * nwr + wr] != 0.0 &&
+                p->t1_off[((pp * nwl + wl) * nA + ap) * nB + b] >= 0)
+                c += (double)p->dimA[ap] * p->dimB[b];
+        t[n].cost = c; t[n].id = id; ++n;
+    }
+    p->n_task2 = n;
+    p->task2 = lpt_ids(t, n);
+    n = 0;
+    for (int64_t id = 0; id < n3; ++id) {
+        const int32_t bp = (int32_t)(id % nB), ap = (int32_t)((id / nB) % nA);
+        const int64_t po = id / ((int64_t)nB * nA);
+        if (psi_sub(p, po, ap, bp) < 0) continue;
+        double c = 0.0;
+        for (int64_t wr = 0; wr < nwr; ++wr) for (int32_t b = 0; b < nB; ++b)
+            if (p->Rnz[((int64_t)bp * nwr + wr) * nB + b] && p->t2_off[((po * nwr + wr) * nA + ap) * nB + b] >= 0)
+                c += (double)p->dimA[ap] * p->dimB[bp] * p->dimB[b];
+        t[n].cost = c; t[n].id = id; ++n;
+    }
+    p->n_task3 = n;
+    p->task3 = lpt_ids(t, n);
+    free(t);
+    return (p->task1 && p->task2 && p->task3) ? 0 : -1;
+}
+
+/* x and y in the block layout; y fully overwritten. */
+int orc_bs_apply(orc_bs_plan* p, const double* x, double* y) {
+    const int64_t P = p->P, nwl = p->nwl, nwr = p->nwr;
+    const int32_t nA = p->nA, nB = p->nB;
+    (void)P;
+    /* step 1: T1[p,wl,A',B] = sum_A L[A',wl,A] x[p,A,B] */
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t t = 0; t < p->n_task1; ++t) {
+        const int64_t id = p->task1[t];
+        const int32_t b = (int32_t)(id % nB);
+        const int32_t ap = (int32_t)((id / nB) % nA);
+        const int64_t wl = (id / ((int64_t)nB * nA)) % nwl;
+        const int64_t pp = id / ((int64_t)nB * nA * nwl);
+        const int64_t M = p->dimA[ap], N = p->dimB[b];
+        double* t1 = p->T1 + p->t1_off[id];
+        memset(t1, 0, sizeof(double) * (size_t)(M * N));
+        for (int32_t a = 0; a < nA; ++a) {
+            if (!p->Lnz[((int64_t)ap * nwl + wl) * nA + a]) continue;
+            const int64_t xo = psi_sub(p, pp, a, b);
+            if (xo < 0) continue;
+            const double* l = p->L + ((p->offA[ap]) * nwl + wl) * p->d_l + p->offA[a];
+            gemm_acc(M, N, p->dimA[a], l, nwl * p->d_l, x + xo, N, t1, N);
         }
     }
     /* step 2: T2[p',wr,A',B] = sum_{p,wl} Wij[p,p',wl,wr] T1[p,wl,A',B] */
-    int64_t n2 = P * nwr * nA * nB;
-    #pragma omp parallel for schedule(dynamic, 4)
-    for (int64_t id = 0; id < n2; ++id) {
-        int64_t o = p->t2_off[id];
-        if (o < 0) continue;
-        int32_t b = (int32_t)(id % nB);
-        int32_t ap = (int32_t)((id / nB) % nA);
-        int64_t wr = (id / ((int64_t)nB * nA)) % nwr;
-        int64_t po = id / ((int64_t)nB * nA * nwr);
-        int64_t MN = p->dimA[ap] * p->dimB[b];
-        double* t2 = p->T2 + o;
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t t = 0; t < p->n_task2; ++t) {
+        const int64_t id = p->task2[t];
+        const int32_t b = (int32_t)(id % nB);
+        const int32_t ap = (int32_t)((id / nB) % nA);
+        const int64_t wr = (id / ((int64_t)nB * nA)) % nwr;
+        const int64_t po = id / ((int64_t)nB * nA * nwr);
+        const int64_t MN = p->dimA[ap] * p->dimB[b];
+        double* t2 = p->T2 + p->t2_off[id];
         memset(t2, 0, sizeof(double) * (size_t)MN);
-        for (int64_t pp = 0; pp < P; ++pp) for (int64_t wl = 0; wl < nwl; ++wl) {
-            double c = p->Wij[((pp * P + po) * nwl + wl) * nwr + wr];
+        for (int64_t pp = 0; pp < p->P; ++pp) for (int64_t wl = 0; wl < nwl; ++wl) {
+            const double c = p->Wij[((pp * p->P + po) * nwl + wl) * nwr + wr];
             if (c == 0.0) continue;
-            int64_t o1 = p->t1_off[((pp * nwl + wl) * nA + ap) * nB + b];
+            const int64_t o1 = p->t1_off[((pp * nwl + wl) * nA + ap) * nB + b];
             if (o1 < 0) continue;
             const double* t1 = p->T1 + o1;
             for (int64_t k = 0; k < MN; ++k) t2[k] += c * t1[k];
         }
     }
     /* step 3: y[p',A',B'] = sum_{wr,B} T2[p',wr,A',B] R[B',wr,B] */
-    int64_t ny = P * nA * nB;
-    #pragma omp parallel for schedule(dynamic, 2)
-    for (int64_t id = 0; id < ny; ++id) {
-        int32_t bp = (int32_t)(id % nB);
-        int32_t ap = (int32_t)((id / nB) % nA);
-        int64_t po = id / ((int64_t)nB * nA);
-        int64_t yo = psi_sub(p, po, ap, bp);
-        if (yo < 0) continue;
-        int64_t M = p->dimA[ap], N = p->dimB[bp];
-        double* ys = y + yo;
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t t = 0; t < p->n_task3; ++t) {
+        const int64_t id = p->task3[t];
+        const int32_t bp = (int32_t)(id % nB);
+        const int32_t ap = (int32_t)((id / nB) % nA);
+        const int64_t po = id / ((int64_t)nB * nA);
+        const int64_t M = p->dimA[ap], N = p->dimB[bp];
+        double* ys = y + psi_sub(p, po, ap, bp);
         memset(ys, 0, sizeof(double) * (size_t)(M * N));
         for (int64_t wr = 0; wr < nwr; ++wr) for (int32_t b = 0; b < nB; ++b) {
             if (!p->Rnz[((int64_t)bp * nwr + wr) * nB + b]) continue;
-            int64_t o2 = p->t2_off[((po * nwr + wr) * nA + ap) * nB + b];
+            const int64_t o2 = p->t2_off[((po * nwr + wr) * nA + ap) * nB + b];
             if (o2 < 0) continue;
-            const double* t2 = p->T2 + o2;
-            int64_t K = p->dimB[b];
-            for (int64_t i = 0; i < M; ++i) {
-                double* yrow = ys + i * N;
-                const double* trow = t2 + i * K;
-                for (int64_t k = 0; k < K; ++k) {
-                    double tv = trow[k];
-                    const double* rt = p->RT + (wr * p->d_r + p->offB[b] + k) * p->d_r + p->offB[bp];
-                    for (int64_t j = 0; j < N; ++j) yrow[j] += tv * rt[j];
-                }
-            }
+            const int64_t K = p->dimB[b];
+            gemm_acc(M, N, K, p->T2 + o2, K, p->RT + (wr * p->d_r + p->offB[b]) * p->d_r + p->offB[bp], p->d_r,
+                     ys, N);
         }
     }
     return 0;
