@@ -424,7 +424,7 @@ typedef struct {
     int64_t* t2_off;               /* [P][nwr][nA][nB] */
     int64_t t2_total;
     /* the non-empty tasks of each step, in descending-cost (LPT) order */
-    int64_t *task1, *task2, *task3;
+    struct orc_task *task1, *task2, *task3;
     int64_t n_task1, n_task2, n_task3;
     double* T1;
     double* T2;
@@ -684,34 +684,66 @@ static void gemm_acc(int64_t M, int64_t N, int64_t K, const double* A, int64_t l
 }
 
 /* Sector GEMM tasks of the three steps, ordered by descending cost (ties by
- * task id) as the reference orders its block-GEMM tasks before handing them
- * to its thread pool (tk-linalg/src/tasks.rs:172-174). */
-typedef struct { double cost; int64_t id; } orc_task;
+ * task id, then row) as the reference orders its block-GEMM tasks before
+ * handing them to its thread pool (tk-linalg/src/tasks.rs:172-174).  Step-1
+ * and step-3 tasks taller than ORC_ROWS rows are cut into row ranges, so a
+ * few large sectors still spread over all threads; a row range computes its
+ * rows exactly as the whole task would. */
+enum { ORC_ROWS = 64 };
+
+typedef struct orc_task { double cost; int64_t id; int32_t r0, r1; } orc_task;
+
+typedef struct { orc_task* t; int64_t n, cap; } orc_task_list;
 
 static int cmp_task(const void* a, const void* b) {
     const orc_task *x = (const orc_task*)a, *y = (const orc_task*)b;
     if (x->cost != y->cost) return x->cost > y->cost ? -1 : 1;
-    return x->id < y->id ? -1 : (x->id > y->id ? 1 : 0);
+    if (x->id != y->id) return x->id < y->id ? -1 : 1;
+    return x->r0 < y->r0 ? -1 : (x->r0 > y->r0 ? 1 : 0);
 }
 
-static int64_t* lpt_ids(orc_task* t, int64_t n) {
-    qsort(t, (size_t)n, sizeof(orc_task), cmp_task);
-    int64_t* ids = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
-    if (ids)
-        for (int64_t i = 0; i < n; ++i) ids[i] = t[i].id;
-    return ids;
+/* Appends the row ranges of one task of `rows` rows and total cost `cost`
+ * (one range of every row when `split` is 0); returns -1 when out of memory. */
+static int push_rows(orc_task_list* L, int64_t id, int64_t rows, double cost, int split) {
+    const int64_t step = (split && rows > ORC_ROWS) ? ORC_ROWS : (rows > 0 ? rows : 1);
+    const int64_t parts = rows > 0 ? (rows + step - 1) / step : 1;
+    if (L->n + parts > L->cap) {
+        int64_t cap = L->cap > 0 ? 2 * L->cap : 1024;
+        while (cap < L->n + parts) cap *= 2;
+        orc_task* t = (orc_task*)realloc(L->t, sizeof(orc_task) * (size_t)cap);
+        if (!t) return -1;
+        L->t = t;
+        L->cap = cap;
+    }
+    for (int64_t k = 0; k < parts; ++k) {
+        const int64_t r0 = k * step, r1 = r0 + step < rows ? r0 + step : rows;
+        orc_task* e = L->t + L->n++;
+        e->cost = rows > 0 ? cost * (double)(r1 - r0) / (double)rows : cost;
+        e->id = id;
+        e->r0 = (int32_t)r0;
+        e->r1 = (int32_t)r1;
+    }
+    return 0;
+}
+
+/* Sorts the list in LPT order and hands its array to the caller. */
+static orc_task* lpt_sorted(orc_task_list* L, int64_t* n) {
+    if (!L->t) L->t = (orc_task*)malloc(sizeof(orc_task));
+    if (L->t) qsort(L->t, (size_t)L->n, sizeof(orc_task), cmp_task);
+    *n = L->n;
+    orc_task* out = L->t;
+    L->t = NULL;
+    L->n = L->cap = 0;
+    return out;
 }
 
 static int build_tasks(orc_bs_plan* p) {
     const int64_t P = p->P, nwl = p->nwl, nwr = p->nwr;
     const int32_t nA = p->nA, nB = p->nB;
     const int64_t n1 = P * nwl * nA * nB, n2 = P * nwr * nA * nB, n3 = P * nA * nB;
-    int64_t cap = n1 > n2 ? n1 : n2;
-    if (n3 > cap) cap = n3;
-    orc_task* t = (orc_task*)malloc(sizeof(orc_task) * (size_t)(cap > 0 ? cap : 1));
-    if (!t) return -1;
-    int64_t n = 0;
-    for (int64_t id = 0; id < n1; ++id) {
+    orc_task_list L = {NULL, 0, 0};
+    int err = 0;
+    for (int64_t id = 0; id < n1 && !err; ++id) {
         if (p->t1_off[id] < 0) continue;
         const int32_t b = (int32_t)(id % nB), ap = (int32_t)((id / nB) % nA);
         const int64_t wl = (id / ((int64_t)nB * nA)) % nwl, pp = id / ((int64_t)nB * nA * nwl);
@@ -719,12 +751,10 @@ static int build_tasks(orc_bs_plan* p) {
         for (int32_t a = 0; a < nA; ++a)
             if (p->Lnz[((int64_t)ap * nwl + wl) * nA + a] && psi_sub(p, pp, a, b) >= 0)
                 c += (double)p->dimA[ap] * p->dimA[a] * p->dimB[b];
-        t[n].cost = c; t[n].id = id; ++n;
+        err = push_rows(&L, id, p->dimA[ap], c, 1);
     }
-    p->n_task1 = n;
-    p->task1 = lpt_ids(t, n);
-    n = 0;
-    for (int64_t id = 0; id < n2; ++id) {
+    p->task1 = lpt_sorted(&L, &p->n_task1);
+    for (int64_t id = 0; id < n2 && !err; ++id) {
         if (p->t2_off[id] < 0) continue;
         const int32_t b = (int32_t)(id % nB), ap = (int32_t)((id / nB) % nA);
         const int64_t wr = (id / ((int64_t)nB * nA)) % nwr, po = id / ((int64_t)nB * nA * nwr);
@@ -733,12 +763,10 @@ static int build_tasks(orc_bs_plan* p) {
             if (p->Wij[((pp * P + po) * nwl + wl) * nwr + wr] != 0.0 &&
                 p->t1_off[((pp * nwl + wl) * nA + ap) * nB + b] >= 0)
                 c += (double)p->dimA[ap] * p->dimB[b];
-        t[n].cost = c; t[n].id = id; ++n;
+        err = push_rows(&L, id, p->dimA[ap], c, 0);
     }
-    p->n_task2 = n;
-    p->task2 = lpt_ids(t, n);
-    n = 0;
-    for (int64_t id = 0; id < n3; ++id) {
+    p->task2 = lpt_sorted(&L, &p->n_task2);
+    for (int64_t id = 0; id < n3 && !err; ++id) {
         const int32_t bp = (int32_t)(id % nB), ap = (int32_t)((id / nB) % nA);
         const int64_t po = id / ((int64_t)nB * nA);
         if (psi_sub(p, po, ap, bp) < 0) continue;
@@ -746,42 +774,41 @@ static int build_tasks(orc_bs_plan* p) {
         for (int64_t wr = 0; wr < nwr; ++wr) for (int32_t b = 0; b < nB; ++b)
             if (p->Rnz[((int64_t)bp * nwr + wr) * nB + b] && p->t2_off[((po * nwr + wr) * nA + ap) * nB + b] >= 0)
                 c += (double)p->dimA[ap] * p->dimB[bp] * p->dimB[b];
-        t[n].cost = c; t[n].id = id; ++n;
+        err = push_rows(&L, id, p->dimA[ap], c, 1);
     }
-    p->n_task3 = n;
-    p->task3 = lpt_ids(t, n);
-    free(t);
-    return (p->task1 && p->task2 && p->task3) ? 0 : -1;
+    p->task3 = lpt_sorted(&L, &p->n_task3);
+    free(L.t);
+    return (!err && p->task1 && p->task2 && p->task3) ? 0 : -1;
 }
 
 /* x and y in the block layout; y fully overwritten. */
 int orc_bs_apply(orc_bs_plan* p, const double* x, double* y) {
-    const int64_t P = p->P, nwl = p->nwl, nwr = p->nwr;
+    const int64_t nwl = p->nwl, nwr = p->nwr;
     const int32_t nA = p->nA, nB = p->nB;
-    (void)P;
-    /* step 1: T1[p,wl,A',B] = sum_A L[A',wl,A] x[p,A,B] */
+    /* step 1: T1[p,wl,A',B] = sum_A L[A',wl,A] x[p,A,B], rows r0..r1 of A' */
     #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t t = 0; t < p->n_task1; ++t) {
-        const int64_t id = p->task1[t];
+        const orc_task* tk = p->task1 + t;
+        const int64_t id = tk->id, r0 = tk->r0, M = tk->r1 - tk->r0;
         const int32_t b = (int32_t)(id % nB);
         const int32_t ap = (int32_t)((id / nB) % nA);
         const int64_t wl = (id / ((int64_t)nB * nA)) % nwl;
         const int64_t pp = id / ((int64_t)nB * nA * nwl);
-        const int64_t M = p->dimA[ap], N = p->dimB[b];
-        double* t1 = p->T1 + p->t1_off[id];
+        const int64_t N = p->dimB[b];
+        double* t1 = p->T1 + p->t1_off[id] + r0 * N;
         memset(t1, 0, sizeof(double) * (size_t)(M * N));
         for (int32_t a = 0; a < nA; ++a) {
             if (!p->Lnz[((int64_t)ap * nwl + wl) * nA + a]) continue;
             const int64_t xo = psi_sub(p, pp, a, b);
             if (xo < 0) continue;
-            const double* l = p->L + ((p->offA[ap]) * nwl + wl) * p->d_l + p->offA[a];
+            const double* l = p->L + ((p->offA[ap] + r0) * nwl + wl) * p->d_l + p->offA[a];
             gemm_acc(M, N, p->dimA[a], l, nwl * p->d_l, x + xo, N, t1, N);
         }
     }
     /* step 2: T2[p',wr,A',B] = sum_{p,wl} Wij[p,p',wl,wr] T1[p,wl,A',B] */
     #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t t = 0; t < p->n_task2; ++t) {
-        const int64_t id = p->task2[t];
+        const int64_t id = p->task2[t].id;
         const int32_t b = (int32_t)(id % nB);
         const int32_t ap = (int32_t)((id / nB) % nA);
         const int64_t wr = (id / ((int64_t)nB * nA)) % nwr;
@@ -798,23 +825,24 @@ int orc_bs_apply(orc_bs_plan* p, const double* x, double* y) {
             for (int64_t k = 0; k < MN; ++k) t2[k] += c * t1[k];
         }
     }
-    /* step 3: y[p',A',B'] = sum_{wr,B} T2[p',wr,A',B] R[B',wr,B] */
+    /* step 3: y[p',A',B'] = sum_{wr,B} T2[p',wr,A',B] R[B',wr,B], rows r0..r1 of A' */
     #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t t = 0; t < p->n_task3; ++t) {
-        const int64_t id = p->task3[t];
+        const orc_task* tk = p->task3 + t;
+        const int64_t id = tk->id, r0 = tk->r0, M = tk->r1 - tk->r0;
         const int32_t bp = (int32_t)(id % nB);
         const int32_t ap = (int32_t)((id / nB) % nA);
         const int64_t po = id / ((int64_t)nB * nA);
-        const int64_t M = p->dimA[ap], N = p->dimB[bp];
-        double* ys = y + psi_sub(p, po, ap, bp);
+        const int64_t N = p->dimB[bp];
+        double* ys = y + psi_sub(p, po, ap, bp) + r0 * N;
         memset(ys, 0, sizeof(double) * (size_t)(M * N));
         for (int64_t wr = 0; wr < nwr; ++wr) for (int32_t b = 0; b < nB; ++b) {
             if (!p->Rnz[((int64_t)bp * nwr + wr) * nB + b]) continue;
             const int64_t o2 = p->t2_off[((po * nwr + wr) * nA + ap) * nB + b];
             if (o2 < 0) continue;
             const int64_t K = p->dimB[b];
-            gemm_acc(M, N, K, p->T2 + o2, K, p->RT + (wr * p->d_r + p->offB[b]) * p->d_r + p->offB[bp], p->d_r,
-                     ys, N);
+            gemm_acc(M, N, K, p->T2 + o2 + r0 * K, K, p->RT + (wr * p->d_r + p->offB[b]) * p->d_r + p->offB[bp],
+                     p->d_r, ys, N);
         }
     }
     return 0;
