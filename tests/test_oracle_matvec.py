@@ -52,3 +52,26 @@ def test_two_site_heisenberg_spectrum():
     p = exact_problem(models.heisenberg(), 2, 0, (0,))
     H = oracle_dense_literal(p)
     assert np.allclose(np.linalg.eigvalsh(H), [-0.75, 0.25, 0.25, 0.25])
+
+
+def test_blocksparse_large_sectors():
+    """Sectors taller than the restatement's 64-row task ranges and deeper than
+    its 256-wide k panels, with dimensions that are not multiples of its 4 x 4
+    register tiles (67, 301, 70), against a dense contraction in numpy:
+    y[t,v,p,q] = sum L[p,w,a] W_i[s,t,w,m] W_j[u,v,m,r] R[q,r,b] x[s,u,a,b]
+    (environments/mod.rs:540-578)."""
+    from tk_gb300.symmetry import QIndex
+
+    m = models.heisenberg()
+    b = QIndex(m.kind, [((-2,), 67), ((0,), 301), ((2,), 70)])
+    p = models.two_site_problem(m, b, b, 11, "heisenberg")
+    bs = oracle_bs(p)
+    x = np.random.default_rng(3).standard_normal(bs.total)
+    D = b.total_dim
+    xd = bs.to_dense(x).reshape(2, 2, D, D)
+    Wi, Wj = p.w_i.to_dense(), p.w_j.to_dense()
+    T = np.tensordot(xd, p.env_r.data, axes=([3], [2]))       # s u a q r
+    T = np.tensordot(p.env_l.data, T, axes=([2], [2]))        # p w s u q r
+    W2 = np.einsum("stwm,uvmr->suwrtv", Wi, Wj)
+    y = np.tensordot(T, W2, axes=([2, 3, 1, 5], [0, 1, 2, 3]))  # p q t v
+    assert rel_err(bs.to_dense(bs.apply(x)), y.transpose(2, 3, 0, 1).reshape(-1)) < 1e-13
