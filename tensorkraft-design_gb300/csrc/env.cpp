@@ -145,8 +145,9 @@ bool finish(GrowTables& G, int64_t n_env, int64_t n_site, int64_t n_out, bool le
 
 }  // namespace
 
-tk_status build_grow_tables(bool left, const QIndex& env_bra, const QIndex& env_mpo, const QIndex& env_ket,
-                            const Bst3& A, const Bst4& W, GrowTables& G, std::string& err) {
+static tk_status build_grow_tables_body(bool left, const QIndex& env_bra, const QIndex& env_mpo,
+                                        const QIndex& env_ket, const Bst3& A, const Bst4& W, GrowTables& G,
+                                        std::string& err) {
     G = GrowTables();
     const int kind = A.kind;
     const QIndex& P = A.legs[0];
@@ -397,7 +398,14 @@ tk_status build_grow_tables(bool left, const QIndex& env_bra, const QIndex& env_
     return TK_OK;
 }
 
-tk_status build_product_tables(const Heff2Tables& H, const Bst3& Ai, const Bst3& Aj, GemmTable& g, std::string& err) {
+tk_status build_grow_tables(bool left, const QIndex& env_bra, const QIndex& env_mpo, const QIndex& env_ket,
+                            const Bst3& A, const Bst4& W, GrowTables& G, std::string& err) {
+    return guard_host("environment growth tables", err,
+                      [&] { return build_grow_tables_body(left, env_bra, env_mpo, env_ket, A, W, G, err); });
+}
+
+static tk_status build_product_tables_body(const Heff2Tables& H, const Bst3& Ai, const Bst3& Aj, GemmTable& g,
+                                           std::string& err) {
     g = GemmTable();
     const int kind = Ai.kind;
     const QIndex& PI = Ai.legs[0];
@@ -450,6 +458,10 @@ tk_status build_product_tables(const Heff2Tables& H, const Bst3& Ai, const Bst3&
     gemm_lpt_order(g, kEnvTileM, kEnvTileN);
     if (!gemm_table_ok(g, Ai.total, Aj.total, H.total, "two-site product", err)) return TK_ERR_INVALID_ARG;
     return TK_OK;
+}
+
+tk_status build_product_tables(const Heff2Tables& H, const Bst3& Ai, const Bst3& Aj, GemmTable& g, std::string& err) {
+    return guard_host("two-site product tables", err, [&] { return build_product_tables_body(H, Ai, Aj, g, err); });
 }
 
 }  // namespace tk

@@ -20,7 +20,10 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <numeric>
+#include <system_error>
+#include <thread>
 #include <unordered_map>
 
 #include "tk_internal.hpp"
@@ -434,9 +437,72 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
     return true;
 }
 
-tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi,
-                             const tk_bst& wj_abi, const int32_t* psi_flux, int tile_m, int tile_n,
-                             Heff2Tables& T, std::string& err, const double* l_blocks, const double* r_blocks) {
+// One environment slab copied into a tensor-core operand stack: element
+// (r, kk) of the row-major [nr x len] slab is column k of the stack's row r,
+// k = k_off + kk, stored K-major in 64-wide chunks (chunk k / kTcBK holds
+// chunk_rows rows starting at row0 + (k / kTcBK) * chunk_rows).
+struct StackCopy {
+    const double* src;
+    int64_t nr, len, k_off, row0, chunk_rows;
+};
+
+// Fills the bf16 hi / lo stacks of `rows` rows x kTcBK from the copy jobs:
+// hi = bf16(v), lo = bf16(v - hi) (both rounded to nearest even through
+// fp32), zero where no slab lands.  Jobs write disjoint elements, so row
+// ranges of them run on several threads with the same result as one.
+static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, std::vector<uint16_t>& hi,
+                              std::vector<uint16_t>& lo) {
+    const int BK = kTcBK;
+    hi.assign((size_t)rows * BK, 0);
+    lo.assign((size_t)rows * BK, 0);
+    struct Item { size_t job; int64_t r0, r1; };
+    std::vector<Item> items;
+    int64_t total = 0;
+    const int64_t grain = 1 << 16;  // elements per work item
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        const int64_t len = std::max<int64_t>(1, jobs[j].len);
+        const int64_t step = std::max<int64_t>(1, grain / len);
+        for (int64_t r0 = 0; r0 < jobs[j].nr; r0 += step) items.push_back({j, r0, std::min(jobs[j].nr, r0 + step)});
+        total += jobs[j].nr * jobs[j].len;
+    }
+    uint16_t* H = hi.data();
+    uint16_t* L = lo.data();
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t it; (it = next.fetch_add(1)) < items.size();) {
+            const StackCopy& c = jobs[items[it].job];
+            for (int64_t r = items[it].r0; r < items[it].r1; ++r) {
+                const double* src = c.src + r * c.len;
+                for (int64_t kk = 0; kk < c.len; ++kk) {
+                    const int64_t k = c.k_off + kk;
+                    const size_t at = (size_t)(c.row0 + (k / BK) * c.chunk_rows + r) * BK + (size_t)(k % BK);
+                    const double v = src[kk];
+                    const uint16_t h = f32_to_bf16_bits((float)v);
+                    H[at] = h;
+                    L[at] = f32_to_bf16_bits((float)(v - (double)bf16_bits_to_f32(h)));
+                }
+            }
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    // one thread per 128 Ki elements, at most 16
+    const unsigned nt = (unsigned)std::min<int64_t>(std::min(hw, 16u), std::max<int64_t>(1, total >> 17));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (const std::system_error&) {
+            break;  // the calling thread still runs every remaining item
+        }
+    }
+    work();
+    for (std::thread& t : pool) t.join();
+}
+
+static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi,
+                                         const tk_bst& wj_abi, const int32_t* psi_flux, int tile_m, int tile_n,
+                                         Heff2Tables& T, std::string& err, const double* l_blocks,
+                                         const double* r_blocks) {
     Bst4 wi, wj;
     if (!bst4_from_abi(wi_abi, wi, "W_i", err)) return TK_ERR_INVALID_ARG;
     if (!bst4_from_abi(wj_abi, wj, "W_j", err)) return TK_ERR_INVALID_ARG;
@@ -785,7 +851,7 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
         C = TcTables();
         const int BK = kTcBK;
         auto kchunks = [&](int64_t K) { return (int32_t)((K + BK - 1) / BK); };
-        std::vector<double> lq64, rq64;
+        std::vector<StackCopy> lcopy, rcopy;
         // T1 pieces: key (p, A', ws, B) -> (offset of channel-0 row, row stride per a')
         struct Piece { uint64_t key; int64_t off; int32_t rs; };
         std::vector<Piece> pieces;
@@ -826,14 +892,10 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
             const int32_t kch = kchunks(K);
             const int64_t lb = C.lq_rows;
             C.lq_rows += kch * rows;
-            lq64.resize((size_t)C.lq_rows * BK, 0.0);
             for (size_t i = 0; i < lp.size(); ++i) {
                 int ap = lp[i].first, ws = lp[i].second;
-                const double* src = T.lbuf.data() + lblk[((size_t)ap * nWL + ws) * nA + a];
-                int64_t nr = QA.dim[ap] * WL.dim[ws];
-                for (int64_t r = 0; r < nr; ++r)
-                    for (int64_t k = 0; k < K; ++k)
-                        lq64[(size_t)(lb + (k / BK) * rows + lrow[i] + r) * BK + (k % BK)] = src[r * K + k];
+                lcopy.push_back({T.lbuf.data() + lblk[((size_t)ap * nWL + ws) * nA + a], QA.dim[ap] * WL.dim[ws], K, 0,
+                                 lb + lrow[i], rows});
             }
             // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B);
             // the B operand column b of block (p, B) is column b of the psi sub-block (D_A x D_B)
@@ -935,16 +997,10 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
             const int64_t rbase = C.rq_rows, t2b = C.t2q_rows, yb = (int64_t)C.yrow.size();
             C.rq_rows += kch * NB;
             C.t2q_rows += kch * rows;
-            rq64.resize((size_t)C.rq_rows * BK, 0.0);
             for (size_t i = 0; i < rp.size(); ++i) {
                 int ws = rp[i].first, b = rp[i].second;
-                const double* src = T.rbuf.data() + rblk[((size_t)bp * nWR + ws) * nB + b];
-                int64_t len = WR.dim[ws] * QB.dim[b];
-                for (int64_t r = 0; r < NB; ++r)
-                    for (int64_t kk = 0; kk < len; ++kk) {
-                        int64_t k = rk[i] + kk;
-                        rq64[(size_t)(rbase + (k / BK) * NB + r) * BK + (k % BK)] = src[r * len + kk];
-                    }
+                rcopy.push_back({T.rbuf.data() + rblk[((size_t)bp * nWR + ws) * nB + b], NB, WR.dim[ws] * QB.dim[b], rk[i],
+                                 rbase, NB});
             }
             for (size_t i = 0; i < yp.size(); ++i) {
                 int64_t po = yp[i].first;
@@ -1040,18 +1096,9 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
         for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
         for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
         for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
-        // split the constant operands into bf16 hi + lo
-        auto split = [](const std::vector<double>& v, std::vector<uint16_t>& hi, std::vector<uint16_t>& lo) {
-            hi.resize(v.size());
-            lo.resize(v.size());
-            for (size_t i = 0; i < v.size(); ++i) {
-                uint16_t h = f32_to_bf16_bits((float)v[i]);
-                hi[i] = h;
-                lo[i] = f32_to_bf16_bits((float)(v[i] - (double)bf16_bits_to_f32(h)));
-            }
-        };
-        split(lq64, C.lq_hi, C.lq_lo);
-        split(rq64, C.rq_hi, C.rq_lo);
+        // the constant operands as bf16 hi + lo stacks
+        fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
+        fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
         if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
             err = "tensor-core operand rows exceed 32 bits";
             return TK_ERR_UNSUPPORTED;
@@ -1072,6 +1119,14 @@ tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bs
         return TK_ERR_INVALID_ARG;
     }
     return TK_OK;
+}
+
+tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi, const tk_bst& wj_abi,
+                             const int32_t* psi_flux, int tile_m, int tile_n, Heff2Tables& T, std::string& err,
+                             const double* l_blocks, const double* r_blocks) {
+    return guard_host("sector tables", err, [&] {
+        return build_heff2_tables_body(envL, envR, wi_abi, wj_abi, psi_flux, tile_m, tile_n, T, err, l_blocks, r_blocks);
+    });
 }
 
 }  // namespace tk

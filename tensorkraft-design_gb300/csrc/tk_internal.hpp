@@ -3,6 +3,8 @@
 #pragma once
 #include <array>
 #include <cstdint>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -235,6 +237,25 @@ struct Heff2Tables {
 // bf16 bit pattern of a float, round to nearest even (NaN kept quiet).
 uint16_t f32_to_bf16_bits(float f);
 float bf16_bits_to_f32(uint16_t b);
+
+// Runs a host table builder and turns a C++ exception (a failed host
+// allocation above all) into a status code with `err` set: no exception may
+// cross the C ABI.
+template <class F>
+tk_status guard_host(const char* what, std::string& err, F&& build) {
+    try {
+        return build();
+    } catch (const std::bad_alloc&) {
+        err = std::string(what) + ": host allocation failed";
+        return TK_ERR_OOM;
+    } catch (const std::length_error&) {
+        err = std::string(what) + ": host tables too large";
+        return TK_ERR_OOM;
+    } catch (const std::exception& e) {
+        err = std::string(what) + ": " + e.what();
+        return TK_ERR_INVALID_ARG;
+    }
+}
 
 // Builds the tables; returns TK_OK or an error code with `err` set.  With
 // l_blocks / r_blocks (host copies of environments in the canonical block
