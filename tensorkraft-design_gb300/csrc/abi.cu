@@ -215,7 +215,8 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision) {
     if (!plan->tc) {
         std::string err;
         std::unique_ptr<TcPlan, TcPlanDeleter> tc;
-        tk_status st = tc_plan_create(plan->host, plan->lbuf.p, plan->rbuf.p, tc, err);
+        tk_status st = guard_host("split-precision plan", err,
+                                  [&] { return tc_plan_create(plan->host, plan->lbuf.p, plan->rbuf.p, tc, err); });
         if (st != TK_OK) {
             set_error("tk_heff2_set_precision: " + err);
             return st;
