@@ -107,3 +107,23 @@ def test_sector_mismatch_cpu(lib_built):
     p.w_j = models.cylinder_j1(4).bulk  # bond QIndex differs from the environment's
     st, msg = _plan_status(p)
     assert st == 2, (st, msg)
+
+
+def test_empty_two_site_space_cpu(lib_built):
+    """A flux no sector combination reaches: the host tables build (on a
+    machine without a GPU the call then stops at cudaSetDevice) and the
+    restatement's space is empty."""
+    import torch
+    from helpers import oracle_bs, small_problem
+
+    if torch.cuda.is_available():
+        import pytest
+
+        pytest.skip("CPU-only check")
+    p = small_problem("heisenberg", 12)
+    p.flux = (40,)
+    st, msg = _plan_status(p)
+    assert st == 4 and "cudaSetDevice" in msg, (st, msg)
+    bs = oracle_bs(p)
+    assert bs.total == 0 and bs.n_blocks == 0 and bs.flops() == 0.0
+    assert bs.apply(np.zeros(0)).shape == (0,)
