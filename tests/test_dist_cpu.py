@@ -72,3 +72,12 @@ def test_reference_arm_two_ranks():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["n_gpus"] == 2
+    # the contract's keys: the same metric as the GPU arm, a cpu_baseline describing this run,
+    # and an e2e equal to the line's own value with no host-device traffic
+    for k in ("metric", "unit", "steps", "warmup", "ms_per_step", "higher_is_better", "config", "dtype"):
+        assert k in d, k
+    assert d["unit"] == "matvec/s" and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == "heisenberg_d1024"
