@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--workload", default="hubbard_d2048")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16x3"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-one-core-seconds", type=float, default=5.0,
+                    help="budget of the one-thread CPU timing beside the all-threads baseline (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-lanczos", action="store_true")
     ap.add_argument("--dmrg", action="store_true",
@@ -327,6 +329,29 @@ def oracle_for(prob):
     return oracle.BlockSparseOracle(prob.kind, q(prob.w_i.indices[0]), q(prob.w_j.indices[0]), q(prob.env_l.ket_idx),
                                     q(prob.env_r.ket_idx), prob.flux, prob.w_i.to_dense(), prob.w_j.to_dense(),
                                     prob.env_l.data, prob.env_r.data)
+
+
+def cpu_baseline(prob, workload: str, seconds: float, one_core_seconds: float) -> dict:
+    """The oracle's block-sparse FP64 matvec timed on the host cores: all
+    threads (the reported value) and, when a single-thread matvec fits the
+    budget, one thread beside it."""
+    import oracle
+
+    orc = oracle_for(prob)
+    xc = np.random.default_rng(1).standard_normal(orc.total)
+    cores = oracle.num_threads()
+    v, runs, el = time_cpu(orc, xc, seconds)
+    out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{runs} full matvecs of {workload} in {el:.1f} s, all host threads"}
+    # a single thread is at most `cores` times slower; skip it when two matvecs would not fit
+    if one_core_seconds > 0 and 2.0 * cores / v <= one_core_seconds:
+        oracle.set_threads(1)
+        try:
+            v1, runs1, el1 = time_cpu(orc, xc, one_core_seconds)
+        finally:
+            oracle.set_threads(cores)
+        out["one_core"] = {"value": v1, "unit": UNIT, "sample": f"{runs1} full matvecs in {el1:.1f} s, one thread"}
+    return out
 
 
 def time_cpu(orc, x, seconds: float):
@@ -641,13 +666,7 @@ def run_ours(args):
                  "stage_ms": [float(v) for v in stage_ms], "stage_bytes": by, "stage_flops": fl})
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        import oracle
-
-        orc = oracle_for(prob)
-        xc = np.random.default_rng(1).standard_normal(orc.total)
-        v, runs, el = time_cpu(orc, xc, args.cpu_seconds)
-        cpu = {"value": v, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-               "sample": f"{runs} full matvecs of {args.workload} in {el:.1f} s, all host threads"}
+        cpu = cpu_baseline(prob, args.workload, args.cpu_seconds, args.cpu_one_core_seconds)
     line = {
         "metric": WORKLOADS[args.workload][0], "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup,
