@@ -19,3 +19,15 @@ def test_cpu_baseline_leg():
     assert d["one_core"]["value"] > 0 and d["one_core"]["unit"] == "matvec/s"
     assert oracle.num_threads() == cores  # the thread count is restored
     assert "one_core" not in bench.cpu_baseline(prob, "heisenberg_d1024", 0.1, 0.0)
+
+
+def test_traffic_table_covers_the_default_bench():
+    """The default bench line (Hubbard D=2048, split precision) finds the ncu
+    DRAM traffic of every stage it can name as the dominant one."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    for stage in bench.STAGES:
+        t = bench.traffic_for("hubbard_d2048", "bf16x3", stage)
+        assert isinstance(t, int) and t > 0, stage
+    assert bench.traffic_for("hubbard_d2048", "bf16x3", "no_such_kernel") is None
