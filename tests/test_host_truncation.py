@@ -130,3 +130,24 @@ def test_complex_full_rank_reconstructs_and_is_isometric():
             assert np.allclose(np.einsum("sab,sac->bc", A.conj(), A), np.eye(nb.total_dim), atol=1e-12)
         else:
             assert np.allclose(np.einsum("sab,scb->ac", B, B.conj()), np.eye(nb.total_dim), atol=1e-12)
+
+
+def test_tied_singular_values_keep_the_charges_that_sort_first():
+    """The deterministic sector assignment: every bond charge gets exactly one
+    singular value 1.0 (one unit entry in its block), so all of them tie, and
+    a bond of D states keeps the D charges that come first in charge order."""
+    kind, P, QA, QB, keys, offs, qs, psi0 = _case()
+    psi = np.zeros_like(psi0)
+    seen = []
+    for off, (qi, qj, qa, qb) in zip(offs, qs):
+        q = fuse(kind, qi, qa)
+        if q not in seen:
+            psi[off] = 1.0
+            seen.append(q)
+    assert len(seen) >= 4
+    for to_right in (True, False):
+        for D in (1, 2, 3):
+            Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], D, 0.5, to_right)
+            assert {q for q, _ in nb.sectors} == set(sorted(seen)[:D]), (to_right, D)
+            assert all(d == 1 for _, d in nb.sectors)
+            assert abs(disc - (len(seen) - D) / len(seen)) < 1e-14
