@@ -354,7 +354,7 @@ def eigh_batch_device(mats: list, device: int = 0, pad_step: int = 16) -> list:
 
 
 def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool,
-                   eigh_batch=None):
+                   eigh_batch=None, min_bond: int = 1):
     """Truncated decomposition of the two-site vector (plan block layout) per bond charge.
 
     Rows of M_q are (s_i, a_L) in global (state, index) order, columns (s_j,
@@ -365,8 +365,9 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     Its eigenvalues are the squared singular values of M_q; the kept set
     follows truncate_svd (truncation/mod.rs:71-99) on the singular values of
     all charges (ties broken by charge order then position): sigma >=
-    cutoff * sigma_max, at most `max_bond`, at least one; the returned error is
-    the discarded share of sum sigma^2.  The isometric factor is
+    cutoff * sigma_max, at most `max_bond`, then at least `min_bond`
+    (TruncationConfig::min_bond_dim, default 1) as far as there are singular
+    values; the returned error is the discarded share of sum sigma^2.  The isometric factor is
     orthonormal to rounding and the other factor is the exact projection of
     M_q (no division by small singular values).  `eigh_batch` (a list of
     symmetric matrices -> [(w ascending, Z)]) diagonalises the density
@@ -440,10 +441,11 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     order = np.lexsort((sv_pos, sv_charge, -sv))
     sv, sv_charge = sv[order], sv_charge[order]
     # truncate_svd (truncation/mod.rs:71-99): keep sigma >= cutoff * sigma_max, at most
-    # max_bond, at least one; the error is the discarded share of sum sigma^2
+    # max_bond, then at least min_bond but no more than there are; the error is the
+    # discarded share of sum sigma^2
     thr = cutoff * (float(sv[0]) if len(sv) else 0.0)
     nkeep = min(max_bond, int(np.count_nonzero(sv >= thr)))
-    nkeep = max(nkeep, min(1, len(sv)))
+    nkeep = min(max(nkeep, min_bond), len(sv))
     counts = np.bincount(sv_charge[:nkeep], minlength=len(charges))
     kept = {charges[bi]: int(c) for bi, c in enumerate(counts) if c > 0}
     sq = sv * sv

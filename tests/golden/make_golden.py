@@ -134,6 +134,19 @@ def main():
                       for d, s in [(4, 0), (3, 1), (7, 99), (12, 4242), (20, 9999), (16, 31337)]],
             "tol": 1e-6},
         "block_gemm": block_gemm_case(),
+        "truncate_svd": [
+            {"source": "tk-dmrg/src/truncation/mod.rs:185-202 (basic)", "rows": 3, "cols": 2,
+             "data": [3.0, 0.0, 0.0, 2.0, 0.0, 0.0], "max_bond_dim": 200, "svd_cutoff": 1e-12, "min_bond_dim": 1,
+             "bond_dim_new": 2, "n_discarded": 0, "truncation_error": 0.0, "error_atol": 1e-14,
+             "singular_values": [3.0, 2.0], "sv_atol": 1e-10},
+            {"source": "tk-dmrg/src/truncation/mod.rs:204-220 (with truncation)", "rows": 3, "cols": 3,
+             "data": [3.0, 0.0, 0.0, 0.0, 2.0, 0.0, 0.0, 0.0, 1.0], "max_bond_dim": 2, "svd_cutoff": 1e-12,
+             "min_bond_dim": 1, "bond_dim_new": 2, "n_discarded": 1, "truncation_error": 1.0 / 14.0,
+             "error_atol": 1e-10},
+            {"source": "tk-dmrg/src/truncation/mod.rs:222-236 (min_bond_dim)", "rows": 2, "cols": 2,
+             "data": [10.0, 0.0, 0.0, 1e-15], "max_bond_dim": 200, "svd_cutoff": 1e-10, "min_bond_dim": 2,
+             "bond_dim_new_at_least": 2},
+        ],
     }
     OUT.write_text(json.dumps(kats, indent=1))
     print(f"wrote {OUT}")

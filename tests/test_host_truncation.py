@@ -151,3 +151,37 @@ def test_tied_singular_values_keep_the_charges_that_sort_first():
             assert {q for q, _ in nb.sectors} == set(sorted(seen)[:D]), (to_right, D)
             assert all(d == 1 for _, d in nb.sectors)
             assert abs(disc - (len(seen) - D) / len(seen)) < 1e-14
+
+
+def test_truncate_svd_known_answers():
+    """The reference's truncate_svd tests (truncation/mod.rs:185-236, in
+    tests/golden/reference_kats.json) on a two-site vector with one charge
+    and one-dimensional physical legs, so that its single block is the
+    test's matrix: kept dimension, discarded count and error, and the kept
+    singular values (row norms of the right factor, rescaled)."""
+    import json
+    from pathlib import Path
+
+    kats = json.loads((Path(__file__).resolve().parent / "golden" / "reference_kats.json").read_text())
+    kind = 1  # U(1)
+    for case in kats["truncate_svd"]:
+        rows, cols = case["rows"], case["cols"]
+        P = QIndex(kind, [((0,), 1)])
+        QA, QB = QIndex(kind, [((0,), rows)]), QIndex(kind, [((0,), cols)])
+        keys, offs, _, total = _layout(kind, P, QA, QB)
+        assert total == rows * cols
+        psi = np.array(case["data"], dtype=np.float64)
+        Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], case["max_bond_dim"],
+                                          case["svd_cutoff"], True, min_bond=case["min_bond_dim"])
+        k = nb.total_dim
+        if "bond_dim_new_at_least" in case:
+            assert k >= case["bond_dim_new_at_least"], case["source"]
+            continue
+        assert k == case["bond_dim_new"], case["source"]
+        assert min(rows, cols) - k == case["n_discarded"], case["source"]
+        assert abs(disc - case["truncation_error"]) < case["error_atol"], case["source"]
+        if "singular_values" in case:
+            B = Aj[((0,), (0,), (0,))][0]  # (k, cols): sigma_r v_r^T / norm of the kept part
+            kept = np.sqrt((1.0 - disc) * float(psi @ psi))
+            sv = np.linalg.norm(B, axis=1) * kept
+            assert np.allclose(sv, case["singular_values"], atol=case["sv_atol"]), (sv, case["source"])
