@@ -127,3 +127,22 @@ def test_empty_two_site_space_cpu(lib_built):
     bs = oracle_bs(p)
     assert bs.total == 0 and bs.n_blocks == 0 and bs.flops() == 0.0
     assert bs.apply(np.zeros(0)).shape == (0,)
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/tk_heff.h compiles as ISO C11 on its own (no CUDA or C++ types),
+    which is what bindgen or cgo read."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    import pytest
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    inc = Path(__file__).resolve().parents[1] / "include"
+    src = tmp_path / "c_check.c"
+    src.write_text('#include "tk_heff.h"\nint main(void) { return (int)sizeof(tk_bst) + TK_OK; }\n')
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                        "-I", str(inc), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
