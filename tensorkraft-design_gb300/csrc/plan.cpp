@@ -488,6 +488,7 @@ static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, 
     // one thread per 128 Ki elements, at most 16
     const unsigned nt = (unsigned)std::min<int64_t>(std::min(hw, 16u), std::max<int64_t>(1, total >> 17));
     std::vector<std::thread> pool;
+    pool.reserve(nt);  // no reallocation (and no throw) once a thread runs
     for (unsigned t = 1; t < nt; ++t) {
         try {
             pool.emplace_back(work);
