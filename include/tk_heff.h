@@ -118,6 +118,25 @@ tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
                                tk_heff2_plan** out);
 void tk_heff2_plan_destroy(tk_heff2_plan* plan);
 
+/* Plan sizing without a GPU (no reference counterpart; for callers that
+ * pre-size device memory before the Krylov loop, as the specified
+ * SweepArena does, techspec/6_tech-spec_tk-dmrg.md:543-572): builds the
+ * plan's host tables exactly as tk_heff2_plan_create does and reports the
+ * block-layout length, the number of two-site blocks and the device bytes
+ * the plan holds for its tables, operands and intermediates in `precision`
+ * (eigensolver and host-call workspaces, allocated on first use, are not
+ * included).  Calls no CUDA API; any output pointer may be NULL. */
+tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                                  const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
+                                  int64_t* block_dim, int64_t* n_blocks, int64_t* device_bytes);
+/* Test hooks (no reference counterpart) for the TK_ERR_OOM paths: from the
+ * next call on, the countdown-th host-allocation checkpoint of the plan-table
+ * builders, or the countdown-th device allocation made for a plan, fails as
+ * if memory were exhausted (counted from 1; 0 disarms).  The failing call
+ * returns TK_ERR_OOM and releases what it had allocated. */
+void tk_debug_fail_host_alloc(int32_t countdown);
+void tk_debug_fail_device_alloc(int32_t countdown);
+
 /* dense_dim = d_i*d_j*D_L*D_R (the closure's `dim`); block_dim = length of
  * the block-layout vector; n_blocks = two-site blocks. */
 tk_status tk_heff2_dims(const tk_heff2_plan* plan, int64_t* dense_dim, int64_t* block_dim,
@@ -160,6 +179,22 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
 #define TK_SCHED_GROUPED   0
 #define TK_SCHED_PER_BLOCK 1
 tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule);
+
+/* Cooperative cancellation (DMRGEngine::run_with_cancel_flag,
+ * tk-dmrg/src/sweep/mod.rs:273-289, checks an AtomicBool before every step):
+ * `flag` points to a host int32 (NULL detaches it) that tk_lanczos_lowest,
+ * tk_davidson_lowest and tk_expm_krylov read before every restart, iteration
+ * or eighth Krylov step.  Once it reads non-zero the call waits for its
+ * stream, so that none of its work is left in flight, and returns
+ * TK_ERR_CANCELLED; the eigenvector buffer then holds the last iterate.  The
+ * flag is read with acquire ordering and may be set from any thread. */
+tk_status tk_heff2_set_cancel_flag(tk_heff2_plan* plan, const int32_t* flag);
+/* Test hook, no reference counterpart: writes `code` (non-zero) into the
+ * device error word of a split-precision plan's tensor-core kernels, as a
+ * bounded wait that ran out would.  The next call that reads the word back
+ * (tk_heff2_apply_host_flat, the eigensolvers) returns TK_ERR_TIMEOUT and
+ * clears it.  TK_ERR_UNSUPPORTED for an FP64 plan. */
+tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
 
 /* Per-stage kernel timing for roofline reports (no reference counterpart;
  * observability in the spirit of DMRGStats, tk-dmrg/src/sweep/mod.rs:85-111):
@@ -297,14 +332,16 @@ tk_status tk_gemm_f64(tk_ctx* ctx, double alpha, const tk_mat* a, const tk_mat* 
 /*
  * No counterpart in the reference.  tk_gemm_f64 for callers that cannot
  * allocate device memory at call time (a sweep running out of a pre-sized
- * arena, work recorded into a CUDA graph, latency-bound loops): same
- * arguments and result, but the kernel's tile tables live in a fixed 1 MiB
- * device array inside the library instead of per-call cudaMalloc'd buffers,
- * so nothing is allocated or freed and the call does not synchronise
- * (stream-ordered on `stream`).  At most 65 520 64x64 output tiles per call;
- * larger calls return TK_ERR_INVALID_ARG.  The first call on a device looks up
- * the array's address (make it before any stream capture).  Calls share the
- * array: calls on different streams that overlap on the GPU race on it.
+ * arena, a runtime that only hands over memory it manages, latency-bound
+ * loops): same arguments and result, but the kernel's tile tables live in a
+ * fixed 1 MiB device array inside the library instead of per-call
+ * cudaMalloc'd buffers, so nothing is allocated or freed and the call does
+ * not synchronise (stream-ordered on `stream`).  At most 65 520 64x64 output
+ * tiles per call; larger calls return TK_ERR_INVALID_ARG.  The first call on
+ * a device looks up the array's address (make it before any stream capture);
+ * that address is cached for the process, so the entry point must not be
+ * used again after cudaDeviceReset.  Calls share the array: calls on
+ * different streams that overlap on the GPU race on it.
  */
 tk_status tk_gemm_f64_noalloc(tk_ctx* ctx, double alpha, const tk_mat* a, const tk_mat* b,
                               double beta, tk_mat_mut* c, void* stream);

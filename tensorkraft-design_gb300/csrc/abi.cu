@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -20,12 +21,20 @@
 namespace tk {
 
 static thread_local std::string g_last_error;
+std::atomic<int> g_fail_device_alloc{0};
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
 tk_status cuda_fail(const char* op, cudaError_t e) {
     set_error(std::string(op) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
+}
+
+bool plan_cancelled(tk_heff2_plan* p, cudaStream_t s, const char* where) {
+    if (!p->cancel || __atomic_load_n(p->cancel, __ATOMIC_ACQUIRE) == 0) return false;
+    cudaStreamSynchronize(s);
+    set_error(std::string(where) + ": cancelled by the caller's flag");
+    return true;
 }
 
 namespace {
@@ -60,6 +69,10 @@ using namespace tk;
 extern "C" {
 
 int32_t tk_version(void) { return 1; }
+
+void tk_debug_fail_device_alloc(int32_t countdown) {
+    g_fail_device_alloc.store(countdown > 0 ? countdown : 0, std::memory_order_relaxed);
+}
 
 const char* tk_last_error(void) { return g_last_error.c_str(); }
 
@@ -100,6 +113,42 @@ tk_status tk_heff2_plan_create(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
         return TK_ERR_INVALID_ARG;
     }
     return plan_create_impl(ctx, env_l, env_r, w_i, w_j, psi_flux, precision, nullptr, nullptr, out);
+}
+
+tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i, const tk_bst* w_j,
+                                  const int32_t* psi_flux, int32_t precision, int64_t* block_dim, int64_t* n_blocks,
+                                  int64_t* device_bytes) {
+    if (!env_l || !env_r || !w_i || !w_j) {
+        set_error("tk_heff2_plan_footprint: null argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (precision != TK_PREC_FP64 && precision != TK_PREC_BF16X3) {
+        set_error("tk_heff2_plan_footprint: unknown precision");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::string err;
+    Heff2Tables H;
+    tk_status st = build_heff2_tables(*env_l, *env_r, *w_i, *w_j, psi_flux, kF64TileM, kF64TileN, H, err);
+    if (st != TK_OK) {
+        set_error("tk_heff2_plan_footprint: " + err);
+        return st;
+    }
+    auto vb = [](const auto& v) { return (double)v.size() * sizeof(v[0]); };
+    double b = 8.0 * ((double)H.lbuf.size() + H.rbuf.size() + std::max<int64_t>(H.t1_total, 1) +
+                      std::max<int64_t>(H.t2_total, 1));
+    for (const GemmTable* g : {&H.g1, &H.g3}) b += vb(g->tasks) + vb(g->segs) + 2.0 * vb(g->tiles);
+    b += vb(H.jobs) + vb(H.terms);
+    if (precision == TK_PREC_BF16X3) {
+        const TcTables& C = H.tc;
+        const double row = 2.0 * 2.0 * kTcBK;  // hi + lo bf16 per operand row
+        b += row * ((double)C.lq_rows + C.rq_rows + C.t2q_rows + C.xq_rows) + 4.0 * std::max<int64_t>(C.t1_total, 1);
+        b += vb(C.tiles1) + vb(C.tiles1x) + vb(C.tiles3) + vb(C.split) + vb(C.jobs) + vb(C.terms) + vb(C.yrow) +
+             vb(C.t1col_base) + vb(C.t1col_stride) + vb(C.xsrc) + vb(C.xstride) + sizeof(int);
+    }
+    if (block_dim) *block_dim = H.total;
+    if (n_blocks) *n_blocks = (int64_t)H.keys.size();
+    if (device_bytes) *device_bytes = (int64_t)b;
+    return TK_OK;
 }
 
 }  // extern "C"
@@ -306,6 +355,29 @@ tk_status tk_heff2_apply_complex(tk_heff2_plan* plan, const double* xr, const do
     return tk_heff2_apply_complex_s(plan, xr, xi, yr, yi, (cudaStream_t)stream);
 }
 
+tk_status tk_heff2_set_cancel_flag(tk_heff2_plan* plan, const int32_t* flag) {
+    if (!plan) {
+        set_error("tk_heff2_set_cancel_flag: null plan");
+        return TK_ERR_INVALID_ARG;
+    }
+    plan->cancel = flag;
+    return TK_OK;
+}
+
+tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code) {
+    if (!plan || code == 0) {
+        set_error("tk_heff2_inject_error_word: null plan or zero code");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (plan->precision != TK_PREC_BF16X3 || !plan->tc) {
+        set_error("tk_heff2_inject_error_word: the plan runs no tensor-core kernels");
+        return TK_ERR_UNSUPPORTED;
+    }
+    DeviceGuard g(plan->device);
+    TK_CUDA(cudaMemcpy(tc_error_word(*plan->tc), &code, sizeof(int32_t), cudaMemcpyHostToDevice));
+    return TK_OK;
+}
+
 tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
     if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK)) {
         set_error("tk_heff2_set_schedule: invalid argument");
@@ -469,7 +541,8 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
     // read-back) as one CUDA graph launch, re-instantiated when the buffers
     // or settings change
     const int key = ((mode * 4 + plan->precision) * 4 + plan->schedule) * 4 + (dx ? 2 : 0) + (dy ? 1 : 0);
-    if (!plan->host_exec || plan->host_gx != x || plan->host_gy != y || plan->host_gkey != key) {
+    if (!plan->host_exec || plan->host_gx != x || plan->host_gy != y || plan->host_gmx != mx ||
+        plan->host_gmy != my || plan->host_gkey != key) {
         if (plan->host_exec) {
             cudaGraphExecDestroy(plan->host_exec);
             plan->host_exec = nullptr;
@@ -505,6 +578,8 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
         }
         plan->host_gx = x;
         plan->host_gy = y;
+        plan->host_gmx = mx;
+        plan->host_gmy = my;
         plan->host_gkey = key;
     }
     TK_CUDA(cudaGraphLaunch(plan->host_exec, s));

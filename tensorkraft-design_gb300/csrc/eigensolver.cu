@@ -532,6 +532,7 @@ tk_status subspace_solve(tk_heff2_plan* p, const Ws& ws, Subspace& sp, const Sub
     int m = 1;
     double theta = G[0];
     for (int it = 0; it < cfg.max_iter; ++it) {
+        if (plan_cancelled(p, s, "davidson")) return TK_ERR_CANCELLED;
         // Ritz pair and residual
         theta = small_sym_lowest(G, m, M, cvec);
         if ((e = cudaMemcpyAsync(sc, cvec.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
@@ -701,6 +702,7 @@ tk_status expm_run(tk_heff2_plan* p, const Ws& ws, int nc, int64_t n, int m, dou
     }
     normalize_kernel<<<vgrid(nn), 256, 0, s>>>(ws.V, ws.V, MISC(ws), nn);
     for (int j = 0; j < m; ++j) {
+        if (j % 8 == 0 && plan_cancelled(p, s, "krylov exponential")) return TK_ERR_CANCELLED;
         double* vj = ws.V + (int64_t)j * nn;
         if (p->is_complex) {  // complex Hermitian H on (re; im): one complex matvec
             if ((st = tk_heff2_apply_complex_s(p, vj, vj + n, ws.w, ws.w + n, s)) != TK_OK) return st;
@@ -849,6 +851,7 @@ extern "C" tk_status tk_lanczos_lowest(tk_heff2_plan* p, const tk_lanczos_cfg* c
     int matvecs = 0, fp64_matvecs = 0, restarts = 0;
     double E = 0.0, rn = INFINITY;
     for (;;) {
+        if (plan_cancelled(p, s, "lanczos")) return TK_ERR_CANCELLED;
         // V_0 = x / |x|
         if ((e = multidot(ws, x, n, 1, x, MISC(ws) + 4, 1, s)) != cudaSuccess) return cuda_fail("multidot", e);
         normalize_kernel<<<vgrid(n), 256, 0, s>>>(ws.V, x, MISC(ws) + 4, n);

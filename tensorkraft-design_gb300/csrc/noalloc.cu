@@ -3,10 +3,10 @@
 //
 // Who needs it: callers that must not allocate device memory at call time.
 // A sweep that works out of a pre-sized arena (tensorkraft's SweepArena
-// design forbids allocation inside the Krylov loop), code that records the
-// call into a CUDA graph (cudaMalloc is not allowed in a capture), and
-// latency-bound loops where a cudaMalloc/cudaFree pair per call (what
-// tk_gemm_f64 does for its tile tables) costs more than the GEMM.
+// design forbids allocation inside the Krylov loop), a host runtime that
+// hands the library only the memory it manages itself, and latency-bound
+// loops where a cudaMalloc/cudaFree pair per call (what tk_gemm_f64 does for
+// its tile tables) costs more than the GEMM.
 //
 // How: the tile tables the grouped GEMM kernel reads live in one file-scope
 // device array, g_noalloc_gemm_scratch, of kNoallocScratchBytes (1 MiB), which
@@ -25,7 +25,11 @@
 //     tables: calls whose work overlaps on the GPU (different streams without
 //     ordering between them) race on it; calls on one stream are ordered;
 //   * the call is stream-ordered and does not synchronise: C is complete when
-//     the stream reaches the end of the call's work.
+//     the stream reaches the end of the call's work;
+//   * the array's address is cached per device for the life of the process:
+//     after cudaDeviceReset (or any reset of the device's primary context) the
+//     module is loaded again at another address, and this entry point must not
+//     be called again in that process.
 #include <cuda_runtime.h>
 
 #include <climits>

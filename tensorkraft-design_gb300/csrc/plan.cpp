@@ -30,6 +30,15 @@
 
 namespace tk {
 
+static std::atomic<int> g_fail_host_alloc{0};
+
+void host_alloc_checkpoint() {
+    int c = g_fail_host_alloc.load(std::memory_order_relaxed);
+    while (c > 0 && !g_fail_host_alloc.compare_exchange_weak(c, c - 1)) {
+    }
+    if (c == 1) throw std::bad_alloc();
+}
+
 int qn_ncomp(int kind) { return (kind == TK_QN_U1Z2 || kind == TK_QN_U1U1) ? 2 : 1; }
 
 int qn_bits(int kind) {
@@ -557,6 +566,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
     // --- fused two-site operator W_ij[p][p'][wl][wr] = sum_wm W_i W_j ---------
     std::vector<double> Wi, Wj;
     if (!mpo_dense(wi, Wi, err) || !mpo_dense(wj, Wj, err)) return TK_ERR_SECTOR_MISMATCH;
+    host_alloc_checkpoint();
     std::vector<double> Wij((size_t)(P * P * nwl * nwr), 0.0);
     for (int64_t si = 0; si < d_i; ++si)
         for (int64_t so = 0; so < d_i; ++so)
@@ -628,6 +638,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
     }
     T.total = off;
 
+    host_alloc_checkpoint();
     // --- non-zero environment slabs -------------------------------------------
     // L slab (A', ws, A) as [(a', w)][a]; R slab (B', ws, B) as [b'][(w, b)].
     const int nWL = WL.n(), nWR = WR.n();
@@ -686,6 +697,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
                     }
             }
 
+    host_alloc_checkpoint();
     // --- stage 1: T1(p, A', ws, B) = sum_A Lslab(A', ws, A) * psi(p, A, B) -----
     std::vector<int64_t> t1((size_t)P * nA * nWL * nB, -1);
     auto T1I = [&](int64_t p, int ap, int ws, int b) -> int64_t& {
@@ -732,6 +744,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
                 }
     T.t1_total = off;
 
+    host_alloc_checkpoint();
     // --- stage 2: T2(p', A', wsr, B)[a'][w][b] = sum W_ij * T1 -----------------
     std::vector<int> wl_sec(nwl), wr_sec(nwr);
     std::vector<int64_t> wl_loc(nwl), wr_loc(nwr);
@@ -814,6 +827,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
                 }
     T.t2_total = off;
 
+    host_alloc_checkpoint();
     // --- stage 3: y(p', A', B') = sum_{ws, B} T2(p', A', ws, B) * Rslab(B', ws, B)^T
     T.g3 = GemmTable();
     for (int64_t po = 0; po < P; ++po)
@@ -1098,6 +1112,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
         for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
         for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
         // the constant operands as bf16 hi + lo stacks
+        host_alloc_checkpoint();
         fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
         fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
         if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
@@ -1121,6 +1136,14 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
     }
     return TK_OK;
 }
+
+}  // namespace tk
+
+extern "C" void tk_debug_fail_host_alloc(int32_t countdown) {
+    tk::g_fail_host_alloc.store(countdown > 0 ? countdown : 0, std::memory_order_relaxed);
+}
+
+namespace tk {
 
 tk_status build_heff2_tables(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi, const tk_bst& wj_abi,
                              const int32_t* psi_flux, int tile_m, int tile_n, Heff2Tables& T, std::string& err,

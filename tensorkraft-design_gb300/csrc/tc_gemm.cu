@@ -731,7 +731,7 @@ template <class T>
 cudaError_t put(T** dst, const std::vector<T>& v) {
     *dst = nullptr;
     if (v.empty()) return cudaSuccess;
-    cudaError_t e = cudaMalloc((void**)dst, sizeof(T) * v.size());
+    cudaError_t e = dev_malloc((void**)dst, sizeof(T) * v.size());
     if (e != cudaSuccess) return e;
     return cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
 }
@@ -815,7 +815,7 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     auto zeros = [&](__nv_bfloat16** d, int64_t rows) -> cudaError_t {
         *d = nullptr;
         if (rows <= 0) return cudaSuccess;
-        cudaError_t r = cudaMalloc((void**)d, sizeof(__nv_bfloat16) * kTcBK * (size_t)rows);
+        cudaError_t r = dev_malloc((void**)d, sizeof(__nv_bfloat16) * kTcBK * (size_t)rows);
         if (r != cudaSuccess) return r;
         return cudaMemset(*d, 0, sizeof(__nv_bfloat16) * kTcBK * (size_t)rows);
     };
@@ -833,8 +833,8 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
-    if ((e = cudaMalloc((void**)&p->t1, sizeof(float) * (size_t)std::max<int64_t>(C.t1_total, 1))) != cudaSuccess ||
-        (e = cudaMalloc((void**)&p->err, sizeof(int))) != cudaSuccess || (e = cudaMemset(p->err, 0, sizeof(int))) != cudaSuccess) {
+    if ((e = dev_malloc((void**)&p->t1, sizeof(float) * (size_t)std::max<int64_t>(C.t1_total, 1))) != cudaSuccess ||
+        (e = dev_malloc((void**)&p->err, sizeof(int))) != cudaSuccess || (e = cudaMemset(p->err, 0, sizeof(int))) != cudaSuccess) {
         err = std::string("tensor-core workspace: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }

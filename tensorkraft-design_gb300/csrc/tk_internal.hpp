@@ -238,6 +238,11 @@ struct Heff2Tables {
 uint16_t f32_to_bf16_bits(float f);
 float bf16_bits_to_f32(uint16_t b);
 
+// Host-allocation checkpoint of the table builders: throws std::bad_alloc
+// at the countdown-th checkpoint once tk_debug_fail_host_alloc armed one
+// (test hook for the TK_ERR_OOM paths; a no-op otherwise).
+void host_alloc_checkpoint();
+
 // Runs a host table builder and turns a C++ exception (a failed host
 // allocation above all) into a status code with `err` set: no exception may
 // cross the C ABI.

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <memory>
 #include <vector>
 
@@ -10,6 +11,21 @@
 #include "tk_internal.hpp"
 
 namespace tk {
+
+// Device allocations of a plan.  With a countdown armed by
+// tk_debug_fail_device_alloc, the countdown-th allocation fails as if the
+// device were out of memory (test hook for the TK_ERR_OOM paths).
+extern std::atomic<int> g_fail_device_alloc;
+inline cudaError_t dev_malloc(void** p, size_t bytes) {
+    int c = g_fail_device_alloc.load(std::memory_order_relaxed);
+    while (c > 0 && !g_fail_device_alloc.compare_exchange_weak(c, c - 1)) {
+    }
+    if (c == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
 
 template <class T>
 struct DevBuf {
@@ -28,7 +44,7 @@ struct DevBuf {
         reset();
         n = count;
         if (count == 0) return cudaSuccess;
-        return cudaMalloc(&p, sizeof(T) * count);
+        return dev_malloc((void**)&p, sizeof(T) * count);
     }
     cudaError_t upload(const std::vector<T>& v) {
         cudaError_t e = alloc(v.size());
@@ -94,8 +110,14 @@ struct tk_heff2_plan {
     cudaEvent_t ev_fork = nullptr, ev_half[2] = {nullptr, nullptr};
     const void* host_gx = nullptr;
     void* host_gy = nullptr;
+    // device addresses of x and y's page-locked mappings when the graph was made
+    // (a buffer freed and re-registered at the same host address can map elsewhere)
+    const void* host_gmx = nullptr;
+    const void* host_gmy = nullptr;
     int host_gkey = -1;
     cudaStream_t stream = nullptr;
+    // host cancel flag (tk_heff2_set_cancel_flag), polled between eigensolver iterations
+    const int32_t* cancel = nullptr;
     // split-precision operands and state (tensor-core path)
     std::unique_ptr<tk::TcPlan, tk::TcPlanDeleter> tc;
     // Lanczos workspace (allocated on first use)
@@ -130,6 +152,10 @@ extern "C" tk_status tk_heff2_apply_complex_s(tk_heff2_plan* p, const double* xr
 
 namespace tk {
 tk_status cuda_fail(const char* op, cudaError_t e);
+// True once the plan's cancel flag (if any) reads non-zero: the solver waits
+// for its stream, so that none of its work is left in flight, records the
+// message and returns TK_ERR_CANCELLED.
+bool plan_cancelled(tk_heff2_plan* p, cudaStream_t s, const char* where);
 // Plan creation behind tk_heff2_plan_create / tk_heff2_plan_create_dev: with
 // l_blocks / r_blocks (host copies of canonical block-layout environments) the
 // environments' `data` pointers are not read.

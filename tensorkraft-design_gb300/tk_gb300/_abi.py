@@ -91,6 +91,13 @@ SIGNATURES = [
     ("tk_heff2_plan_create", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.POINTER(tk_env), C.POINTER(tk_bst),
                                          C.POINTER(tk_bst), C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_void_p)]),
     ("tk_heff2_plan_destroy", None, [C.c_void_p]),
+    ("tk_heff2_plan_footprint", C.c_int32, [C.POINTER(tk_env), C.POINTER(tk_env), C.POINTER(tk_bst),
+                                            C.POINTER(tk_bst), C.POINTER(C.c_int32), C.c_int32,
+                                            C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("tk_debug_fail_host_alloc", None, [C.c_int32]),
+    ("tk_debug_fail_device_alloc", None, [C.c_int32]),
+    ("tk_heff2_set_cancel_flag", C.c_int32, [C.c_void_p, C.c_void_p]),
+    ("tk_heff2_inject_error_word", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_dims", C.c_int32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("tk_heff2_blocks", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
     ("tk_heff2_cost", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

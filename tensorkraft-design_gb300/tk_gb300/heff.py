@@ -234,6 +234,17 @@ class Heff2Plan:
         check(self._lib.tk_heff2_set_precision(self._h, precision))
         self.precision = precision
 
+    def set_cancel_flag(self, flag):
+        """tk_heff2_set_cancel_flag: `flag` is a one-element int32 numpy array the
+        eigensolvers poll (non-zero cancels them with TK_ERR_CANCELLED), or None.
+        The plan keeps a reference to it while attached."""
+        if flag is None:
+            check(self._lib.tk_heff2_set_cancel_flag(self._h, None))
+        else:
+            assert flag.dtype == np.int32 and flag.size >= 1 and flag.flags.c_contiguous
+            check(self._lib.tk_heff2_set_cancel_flag(self._h, C.c_void_p(flag.ctypes.data)))
+        self._cancel = flag
+
     def apply(self, x, y, stream=None):
         """y = H x on device tensors (torch, float64, block layout)."""
         s = C.c_void_p(stream) if stream is not None else C.c_void_p(0)
@@ -314,6 +325,25 @@ class Heff2Plan:
         check(self._lib.tk_davidson_lowest(self._h, C.byref(cfg), x0p, C.c_void_p(evec.data_ptr()), C.byref(res), s))
         return EigenResult(res.eigenvalue, evec, bool(res.converged), res.matvec_count, res.residual_norm,
                            res.fp64_matvec_count, res.restarts)
+
+
+def plan_footprint(env_l: Environment, env_r: Environment, w_i: BlockSparseTensor, w_j: BlockSparseTensor,
+                   psi_flux=None, precision: int = PREC_FP64):
+    """tk_heff2_plan_footprint: (block_dim, n_blocks, device_bytes) of the plan
+    these inputs would make, from its host tables alone (no GPU needed)."""
+    lib = _abi.load()
+    m = _Marshal()
+    el, er = m.env(env_l), m.env(env_r)
+    bi, bj = m.bst(w_i), m.bst(w_j)
+    fl = None
+    if psi_flux is not None:
+        farr = np.array(list(psi_flux) + [0], dtype=np.int32)
+        m.keep.append(farr)
+        fl = _abi.i32ptr(farr)
+    bd, nb, db = C.c_int64(), C.c_int64(), C.c_int64()
+    check(lib.tk_heff2_plan_footprint(C.byref(el), C.byref(er), C.byref(bi), C.byref(bj), fl, precision,
+                                      C.byref(bd), C.byref(nb), C.byref(db)))
+    return bd.value, nb.value, db.value
 
 
 def build_heff_two_site(env_l: Environment, env_r: Environment, mpo: MPO, sites: tuple, psi_flux=None,

@@ -353,6 +353,33 @@ def eigh_batch_device(mats: list, device: int = 0, pad_step: int = 16) -> list:
     return out
 
 
+# Eigenvalues w of a charge's density matrix count as resolved above
+# _GRAM_FLOOR * n * w_max: a hundred times the backward error of a symmetric
+# eigensolver (about 8 n eps ||rho||), so that a resolved w carries at most 1 %
+# relative error (sigma = sqrt(w) at most 0.5 %).
+_GRAM_FLOOR = 800.0 * np.finfo(np.float64).eps
+
+
+def _charges_to_resolve(svs: list, floors: list, max_bond: int, cutoff: float) -> list:
+    """Charges whose singular values must come from an SVD instead of the
+    density matrix: those with unresolved values (sigma^2 below the charge's
+    floor) when such a value could change truncate_svd's choice, i.e. when it
+    could reach cutoff * sigma_max and the max_bond largest values are not all
+    resolved values certainly above it.  Otherwise every unresolved value is
+    discarded either way, as the SVD's would be."""
+    weak = [bi for bi, (s, f) in enumerate(zip(svs, floors)) if len(s) and float(s[-1]) ** 2 < f]
+    if not weak:
+        return []
+    smax = max((float(s[0]) for s in svs if len(s)), default=0.0)
+    upper = max(math.sqrt(2.0 * floors[bi]) for bi in weak)  # largest an unresolved sigma can be
+    if upper < cutoff * smax:
+        return []
+    sure = sum(int(np.count_nonzero(0.99 * s[s * s >= f] ** 2 > upper * upper)) for s, f in zip(svs, floors))
+    if sure >= max_bond:
+        return []
+    return weak
+
+
 def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool,
                    eigh_batch=None, min_bond: int = 1):
     """Truncated decomposition of the two-site vector (plan block layout) per bond charge.
@@ -362,7 +389,10 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     that becomes isometric (White's density-matrix truncation): moving right,
     rho = M_q M_q^T, A_i = its leading eigenvectors and A_j = A_i^T M_q;
     moving left, rho = M_q^T M_q, A_j = eigenvectors^T and A_i = M_q A_j^T.
-    Its eigenvalues are the squared singular values of M_q; the kept set
+    Its eigenvalues are the squared singular values of M_q down to about
+    1e-7 sigma_max; where smaller ones could change the kept set (a cutoff
+    below that level with max_bond not binding), the charges holding them are
+    decomposed by an SVD of M_q instead.  The kept set
     follows truncate_svd (truncation/mod.rs:71-99) on the singular values of
     all charges (ties broken by charge order then position): sigma >=
     cutoff * sigma_max, at most `max_bond`, then at least `min_bond`
@@ -428,12 +458,26 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
         else:
             # one charge per pool thread, single-threaded BLAS each
             pairs = list(_pool().map(lambda q: np.linalg.eigh(gram(q)), charges))
-    svs = []
+    svs, floors = [], []
     for bi, q in enumerate(charges):
         w, Z = pairs[bi]
-        w, Z = w[::-1], Z[:, ::-1]
+        w, Z = np.asarray(w, dtype=np.float64)[::-1], Z[:, ::-1]
         eig[q] = Z
-        svs.append(np.sqrt(np.maximum(np.asarray(w, dtype=np.float64), 0.0)))
+        svs.append(np.sqrt(np.maximum(w, 0.0)))
+        # a symmetric eigensolver resolves w only to about n eps ||rho||: below this
+        # floor the square root is not the singular value (sigma < ~1e-7 sigma_max)
+        floors.append(_GRAM_FLOOR * len(w) * float(w[0]) if len(w) else 0.0)
+    svd_charges = _charges_to_resolve(svs, floors, max_bond, cutoff)
+    if svd_charges:
+        # the singular values (and vectors) of those charges from an SVD of M_q itself,
+        # as truncate_svd takes them (truncation/mod.rs:68 through svd_truncated)
+        def svd(bi):
+            return bi, np.linalg.svd(M[charges[bi]], full_matrices=False)
+
+        with _SingleThreadBlas():
+            for bi, (U, s, Vh) in _pool().map(svd, svd_charges):
+                svs[bi] = s
+                eig[charges[bi]] = (U, s, Vh)
     # every singular value of every charge, ordered by (-sigma, charge, position)
     sv = np.concatenate(svs) if svs else np.zeros(0)
     sv_charge = np.repeat(np.arange(len(svs)), [len(x) for x in svs])
@@ -457,6 +501,11 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
 
     def factors(item):
         q, k = item
+        if isinstance(eig[q], tuple):  # charge resolved by an SVD: M_q = U s Vh
+            U, s, Vh = eig[q]
+            if to_right:
+                return q, k, U[:, :k], (s[:k, None] * Vh[:k]) / norm
+            return q, k, (U[:, :k] * s[None, :k]) / norm, Vh[:k]
         Z = eig[q][:, :k]
         if to_right:
             return q, k, Z, (Z.conj().T @ M[q]) / norm
@@ -659,6 +708,30 @@ def canonicalize(sites: list, bonds: list, center: int, device: int = 0):
     return out, bonds
 
 
+class SweepCancelled(RuntimeError):
+    """DmrgError::Cancelled (tk-dmrg/src/error.rs): the run's cancel flag was set."""
+
+
+class CancelFlag:
+    """The AtomicBool of DMRGEngine::run_with_cancel_flag
+    (tk-dmrg/src/sweep/mod.rs:273-289): a host int32 that the sweep reads
+    before every step and that each step's plan hands to its eigensolver
+    (tk_heff2_set_cancel_flag), so a long eigensolve stops too.  Set it from
+    any thread."""
+
+    def __init__(self):
+        self.word = np.zeros(1, dtype=np.int32)
+
+    def set(self):
+        self.word[0] = 1
+
+    def clear(self):
+        self.word[0] = 0
+
+    def is_set(self) -> bool:
+        return bool(self.word[0])
+
+
 @dataclass
 class SweepRecord:
     energies: list = field(default_factory=list)   # energy after each half sweep
@@ -715,16 +788,25 @@ class DeviceDMRG:
         inner = self.inner if plan.precision != PREC_FP64 else 0
         return plan.davidson(max_subspace=self.max_subspace, max_iter=self.max_iter, tol=self.tol, inner=inner, x0=x0)
 
-    def step(self, i: int, to_right: bool, max_bond: int, cutoff: float, rec: SweepRecord):
+    def step(self, i: int, to_right: bool, max_bond: int, cutoff: float, rec: SweepRecord, min_bond: int = 1,
+             cancel: "CancelFlag | None" = None):
         torch = _torch()
         t0 = time.perf_counter()
         plan = Heff2Plan.from_device_envs(self.L[i], self.R[i + 2], self.W[i], self.W[i + 1], self.zero,
                                           precision=self.precision, device=self.device)
+        if cancel is not None:
+            plan.set_cancel_flag(cancel.word)
         x0 = two_site_product(plan, self.sites[i], self.sites[i + 1])
         if float(torch.linalg.norm(x0)) == 0.0:
             x0 = None
         t1 = time.perf_counter()
-        r = self._solve(plan, x0)
+        try:
+            r = self._solve(plan, x0)
+        except _abi.TkError as exc:
+            if exc.status == 6:  # TK_ERR_CANCELLED: the site tensors are unchanged
+                plan.close()
+                raise SweepCancelled(str(exc)) from None
+            raise
         rec.matvecs += r.matvec_count
         rec.fp64_matvecs += r.fp64_matvec_count
         psi = r.eigenvector.cpu().numpy()
@@ -732,7 +814,7 @@ class DeviceDMRG:
         keys, offs = plan.blocks()
         legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
         Ai, Aj, nb, disc = split_two_site(self.kind, psi, keys, offs, legs, max_bond, cutoff, to_right,
-                                          eigh_batch=self.eigh_batch)
+                                          eigh_batch=self.eigh_batch, min_bond=min_bond)
         P = self.model.phys
         self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
         self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
@@ -792,7 +874,7 @@ class DeviceDMRG:
         plan.close()
 
     def tdvp_step(self, dt: float, max_bond: int, rec: "SweepRecord", cutoff: float = 1e-14,
-                  real_time: bool = False):
+                  real_time: bool = False, min_bond: int = 1):
         """One TDVP step by two-site projector splitting: a left-to-right and a
         right-to-left half sweep of dt/2 each; every two-site update evolves forward
         by exp(-(dt/2) H2) (imaginary time) or exp(-i (dt/2) H2) (real time, complex
@@ -822,7 +904,7 @@ class DeviceDMRG:
                 keys, offs = plan.blocks()
                 legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
                 Ai, Aj, nb, disc = split_two_site(self.kind, self._host(y), keys, offs, legs, max_bond, cutoff,
-                                                  to_right, eigh_batch=self.eigh_batch)
+                                                  to_right, eigh_batch=self.eigh_batch, min_bond=min_bond)
                 P = self.model.phys
                 self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
                 self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
@@ -880,14 +962,26 @@ class DeviceDMRG:
         for i in range(n - 1, site, -1):
             self.R[i] = grow_right(self.R[i + 1], self.sites[i], self.W[i], device=self.device)
 
-    def run(self, max_bond: int, sweeps: int, cutoff: float = 1e-14) -> SweepRecord:
+    def run(self, max_bond: int, sweeps: int, cutoff: float = 1e-14, min_bond: int = 1,
+            cancel: "CancelFlag | None" = None) -> SweepRecord:
+        """`sweeps` full sweeps (left to right, then back); the truncation of every
+        step follows TruncationConfig (max_bond_dim, svd_cutoff, min_bond_dim);
+        the reference's sweep builds it per step with min_bond_dim fixed at 1
+        (sweep/mod.rs:404-412), the default here.  With `cancel`, the flag is
+        read before every step (run_with_cancel_flag, sweep/mod.rs:287-289) and
+        by the step's eigensolver; once set, SweepCancelled is raised with the
+        MPS and environments as the last completed step left them, and
+        `self.record` holds what was measured until then."""
         rec = SweepRecord()
+        self.record = rec
         for _ in range(sweeps):
             for to_right, rng_ in ((True, range(0, self.n - 1)), (False, range(self.n - 2, -1, -1))):
                 t0 = time.perf_counter()
                 e, tmax = None, 0.0
                 for i in rng_:
-                    e, disc = self.step(i, to_right, max_bond, cutoff, rec)
+                    if cancel is not None and cancel.is_set():
+                        raise SweepCancelled(f"cancelled before the step at bond ({i}, {i + 1})")
+                    e, disc = self.step(i, to_right, max_bond, cutoff, rec, min_bond, cancel)
                     tmax = max(tmax, disc)
                 rec.seconds.append(time.perf_counter() - t0)
                 rec.energies.append(e)

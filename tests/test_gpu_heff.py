@@ -75,7 +75,8 @@ def test_device_apply_matches_oracle(lib_built, name, D):
     assert np.array_equal(y2, yd.cpu().numpy())
 
 
-@pytest.mark.parametrize("name", ["heisenberg_d1024", "hubbard_d2048"])
+# cylinder_d4096: 41 heavy-tailed sectors up to 1535 (the uneven-block stress case)
+@pytest.mark.parametrize("name", ["heisenberg_d1024", "hubbard_d2048", "cylinder_d4096"])
 def test_full_size_against_oracle(lib_built, name):
     """Full workload sizes: parity with the block-sparse oracle + symmetry and linearity."""
     torch = _torch()

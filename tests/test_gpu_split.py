@@ -38,7 +38,8 @@ def test_split_matvec_small(lib_built, name, D):
     assert rel_err(y, oracle_bs(p).apply(x)) < SPLIT_TOL
 
 
-@pytest.mark.parametrize("name", ["heisenberg_d1024", "hubbard_d2048"])
+# cylinder_d4096 runs the tall-stack stage 1 (split copy + TMA) on its large sectors
+@pytest.mark.parametrize("name", ["heisenberg_d1024", "hubbard_d2048", "cylinder_d4096"])
 def test_split_matvec_full(lib_built, name):
     p = models.workload(name)
     plan = p.plan(precision=PREC_BF16X3)
@@ -139,3 +140,20 @@ def test_host_io_direct_matches_staged(lib_built, name, D):
     assert np.array_equal(y, out[_abi.HOST_IO_STAGED])
     # and the device-buffer matvec gives the same bits
     assert np.array_equal(_run(plan, x), out[_abi.HOST_IO_STAGED])
+
+
+def test_refined_eigenpair_full_hubbard(lib_built):
+    """The metric's accuracy target at full size (Hubbard D=2048, 976 476
+    block elements): split-precision Lanczos with FP64 Jacobi-Davidson
+    refinement reaches the FP64 Lanczos eigenvalue to |dE| <= 1e-10, and its
+    FP64 residual meets the tolerance."""
+    p = models.workload("hubbard_d2048")
+    plan = p.plan(precision=PREC_FP64)
+    r64 = plan.lanczos(krylov_dim=30, max_restarts=40, tol=1e-9)
+    assert r64.converged
+    plan.set_precision(PREC_BF16X3)
+    r = plan.lanczos(krylov_dim=30, max_restarts=40, tol=1e-9, refine=30)
+    assert r.converged and r.residual_norm <= 1e-9
+    assert abs(r.eigenvalue - r64.eigenvalue) <= 1e-10, (r.eigenvalue, r64.eigenvalue)
+    # most matvecs ran in split precision
+    assert r.fp64_matvec_count < r.matvec_count

@@ -185,3 +185,51 @@ def test_truncate_svd_known_answers():
             kept = np.sqrt((1.0 - disc) * float(psi @ psi))
             sv = np.linalg.norm(B, axis=1) * kept
             assert np.allclose(sv, case["singular_values"], atol=case["sv_atol"]), (sv, case["source"])
+
+
+def test_exact_rank_keeps_exactly_the_rank():
+    """A rank-1 6 x 6 block with cutoff 1e-12: truncate_svd's SVD gives one
+    singular value and five at rounding level (< 1e-15 sigma_max), so it keeps
+    one state.  The density matrix alone resolves sigma only to ~1e-7 sigma_max,
+    which would keep noise states; the split takes those charges by SVD."""
+    kind = 1
+    P = QIndex(kind, [((0,), 1)])
+    QA, QB = QIndex(kind, [((0,), 6)]), QIndex(kind, [((0,), 6)])
+    keys, offs, _, total = _layout(kind, P, QA, QB)
+    rng = np.random.default_rng(4)
+    u, v = rng.standard_normal(6), rng.standard_normal(6)
+    psi = np.outer(u, v).reshape(-1)
+    for to_right in (True, False):
+        Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], 100, 1e-12, to_right)
+        assert nb.total_dim == 1, to_right
+        assert disc < 1e-28
+        A, B = _rebuild(Ai, Aj, nb, P, QA, QB)
+        rec = np.einsum("sab,tbc->stac", A, B).reshape(-1) * np.linalg.norm(psi)
+        assert np.allclose(rec, psi, atol=1e-13)
+
+
+def test_rank_deficient_charges_match_a_dense_svd():
+    """Several charges, each of a known rank below its size, cutoff 1e-12 and no
+    max_bond limit: the kept dimension per charge is that rank (what an SVD of
+    each charge block keeps), and the product of the factors is the state."""
+    kind, P, QA, QB, keys, offs, qs, _ = _case()
+    rng = np.random.default_rng(9)
+    psi = np.zeros(sum(int(np.prod([P.dim_of(a), P.dim_of(b), QA.dim_of(c), QB.dim_of(d)])) for a, b, c, d in qs))
+    T = np.zeros((P.total_dim, P.total_dim, QA.total_dim, QB.total_dim))
+    d = P.total_dim
+    # M = X Y with X (rows x 2), Y (2 x cols): every charge block has rank <= 2
+    X = rng.standard_normal((d * QA.total_dim, 2))
+    Y = rng.standard_normal((2, d * QB.total_dim))
+    Md = (X @ Y).reshape(d, QA.total_dim, d, QB.total_dim).transpose(0, 2, 1, 3)
+    for off, (qi, qj, qa, qb) in zip(offs, qs):
+        ni, nj, da, db = P.dim_of(qi), P.dim_of(qj), QA.dim_of(qa), QB.dim_of(qb)
+        oi, oj, oa, ob = P.offset_of(qi), P.offset_of(qj), QA.offset_of(qa), QB.offset_of(qb)
+        blk = Md[oi:oi + ni, oj:oj + nj, oa:oa + da, ob:ob + db]
+        psi[off:off + blk.size] = blk.reshape(-1)
+        T[oi:oi + ni, oj:oj + nj, oa:oa + da, ob:ob + db] = blk
+    for to_right in (True, False):
+        Ai, Aj, nb, disc = split_two_site(kind, psi, keys, offs, [P, P, QA, QB], 10_000, 1e-12, to_right)
+        assert all(k <= 2 for _, k in nb.sectors), nb.sectors
+        A, B = _rebuild(Ai, Aj, nb, P, QA, QB)
+        rec = np.einsum("sab,tbc->stac", A, B) * np.linalg.norm(psi)
+        assert np.allclose(rec, T, atol=1e-12)
