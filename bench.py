@@ -63,12 +63,16 @@ def parse():
     ap.add_argument("--dmrg", action="store_true",
                     help="also run the Heisenberg L=32, D=64, 4-sweep two-site DMRG (FP64 and split precision)")
     ap.add_argument("--dmrg-cpu", action="store_true", help="with --dmrg: also run it on the CPU oracle solver")
-    ap.add_argument("--sweeps", type=int, default=0, metavar="K",
-                    help="also time K device-resident two-site sweeps of the Hubbard chain (FP64 Davidson and "
-                         "split-precision Jacobi-Davidson from the same MPS, after --sweep-warmup split sweeps)")
+    ap.add_argument("--sweeps", type=int, default=1, metavar="K",
+                    help="time K device-resident two-site sweeps of the Hubbard chain (FP64 Davidson and "
+                         "split-precision Jacobi-Davidson from the same MPS, after --sweep-warmup split sweeps); "
+                         "0 skips them")
     ap.add_argument("--sweep-sites", type=int, default=64)
     ap.add_argument("--sweep-bond", type=int, default=2048)
-    ap.add_argument("--sweep-warmup", type=int, default=2)
+    ap.add_argument("--sweep-warmup", type=int, default=1)
+    ap.add_argument("--ref-seconds", type=float, default=8.0,
+                    help="--impl reference: time at least this long (and at least --steps matvecs)")
+    ap.add_argument("--cpu-child", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--tdvp-steps", type=int, default=0, metavar="K",
                     help="also time K real-time TDVP steps of the impurity Green's function (Anderson chain, "
                          "16 sites, D=1024, dt=0.05, Krylov 16) after a split-precision DMRG ground state")
@@ -322,36 +326,64 @@ def max_over_ranks(x: float, device) -> float:
     return float(t.item())
 
 
-def oracle_for(prob):
+CPU_BUILD = ("oracle/_build/liborc_timed.so: gcc -O3 -fopenmp -std=gnu11 -ffp-contract=fast -funroll-loops "
+             "(FMA contraction on)")
+
+
+def oracle_for(prob, timed: bool = False):
     import oracle
 
     q = lambda ix: ([list(c) for c, _ in ix.sectors], [d for _, d in ix.sectors])
     return oracle.BlockSparseOracle(prob.kind, q(prob.w_i.indices[0]), q(prob.w_j.indices[0]), q(prob.env_l.ket_idx),
                                     q(prob.env_r.ket_idx), prob.flux, prob.w_i.to_dense(), prob.w_j.to_dense(),
-                                    prob.env_l.data, prob.env_r.data)
+                                    prob.env_l.data, prob.env_r.data, timed=timed)
 
 
 def cpu_baseline(prob, workload: str, seconds: float, one_core_seconds: float) -> dict:
-    """The oracle's block-sparse FP64 matvec timed on the host cores: all
-    threads (the reported value) and, when a single-thread matvec fits the
-    budget, one thread beside it."""
+    """The oracle's block-sparse FP64 matvec (its FMA build) timed on the host
+    cores: all threads (the reported value) and, when a single-thread matvec
+    fits the budget, one thread beside it."""
     import oracle
 
-    orc = oracle_for(prob)
+    orc = oracle_for(prob, timed=True)
     xc = np.random.default_rng(1).standard_normal(orc.total)
-    cores = oracle.num_threads()
+    cores = oracle.num_threads(timed=True)
     v, runs, el = time_cpu(orc, xc, seconds)
-    out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+    out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "build": CPU_BUILD,
            "sample": f"{runs} full matvecs of {workload} in {el:.1f} s, all host threads"}
     # a single thread is at most `cores` times slower; skip it when two matvecs would not fit
     if one_core_seconds > 0 and 2.0 * cores / v <= one_core_seconds:
-        oracle.set_threads(1)
+        oracle.set_threads(1, timed=True)
         try:
             v1, runs1, el1 = time_cpu(orc, xc, one_core_seconds)
         finally:
-            oracle.set_threads(cores)
+            oracle.set_threads(cores, timed=True)
         out["one_core"] = {"value": v1, "unit": UNIT, "sample": f"{runs1} full matvecs in {el1:.1f} s, one thread"}
     return out
+
+
+def cpu_baseline_isolated(workload: str, seconds: float, one_core_seconds: float) -> dict:
+    """cpu_baseline in a fresh child process (no torch, no CUDA context, the
+    same process setup as the --impl reference arm), so that both arms time
+    the CPU under the same conditions."""
+    cmd = [sys.executable, str(Path(__file__).resolve()), "--cpu-child", "--workload", workload, "--cpu-seconds",
+           str(seconds), "--cpu-one-core-seconds", str(one_core_seconds)]
+    env = dict(os.environ)
+    for k in ("RANK", "LOCAL_RANK", "WORLD_SIZE"):
+        env.pop(k, None)
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError(f"CPU baseline child failed:\n{r.stderr[-2000:]}")
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    out["process"] = "child process without torch or CUDA"
+    return out
+
+
+def run_cpu_child(args):
+    from tk_gb300 import models
+
+    prob = models.workload(args.workload)
+    print(json.dumps(cpu_baseline(prob, args.workload, args.cpu_seconds, args.cpu_one_core_seconds)), flush=True)
 
 
 def time_cpu(orc, x, seconds: float):
@@ -461,6 +493,10 @@ def dgemm_peak_tflops(torch, dev):
     return 2.0 * n ** 3 / best / 1e12
 
 
+TRAFFIC_SOURCE = ("stored: profiles/ncu_traffic.json, dram__bytes_read.sum + dram__bytes_write.sum per launch from "
+                  "one ncu capture of the same workload and build (commands in profiles/), not measured in this run")
+
+
 def traffic_for(workload: str, precision: str, kernel: str):
     p = ROOT / "profiles" / "ncu_traffic.json"
     if not p.exists():
@@ -479,26 +515,30 @@ def run_reference(args):
     from tk_gb300 import models
 
     prob = models.workload(args.workload)
-    orc = oracle_for(prob)
+    orc = oracle_for(prob, timed=True)
     x = np.random.default_rng(1).standard_normal(orc.total)
     y = np.empty_like(x)
-    cores = oracle.num_threads()
+    cores = oracle.num_threads(timed=True)
     for _ in range(args.warmup):
         orc.apply_into(x, y)
-    steps = max(1, min(args.steps, 60))  # bounded CPU sample
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    # at least --steps matvecs and at least --ref-seconds (at most 60 s) of CPU work
+    steps, t0 = 0, time.perf_counter()
+    while True:
         orc.apply_into(x, y)
-    el = time.perf_counter() - t0
+        steps += 1
+        el = time.perf_counter() - t0
+        if (steps >= args.steps and el >= args.ref_seconds) or el >= 60.0:
+            break
     v = steps / el
     line = {
         "impl": "reference", "metric": WORKLOADS.get(args.workload, (METRIC,))[0], "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) environments, Gaussian sector dims)",
         "config": {"workload": args.workload, "block_dim": orc.total, "dense_dim": orc.dense_dim, "threads": cores},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{steps} full matvecs of {args.workload} (after {args.warmup} warm-up), "
-                                   "block-sparse FP64 restatement of build_heff_two_site, OpenMP over sector tasks"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "build": CPU_BUILD,
+                         "sample": f"{steps} full matvecs of {args.workload} in {el:.1f} s (after {args.warmup} "
+                                   "warm-up), block-sparse FP64 restatement of build_heff_two_site, OpenMP over "
+                                   "sector tasks"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gflops": orc.flops() * v / 1e9,
     }
@@ -601,6 +641,7 @@ def run_ours(args):
     stage_ms /= prof_steps
     clocks = clk.summary(t_load, t_end)
     y_fp = None
+    fp64 = None
     if prec_name != "fp64":
         yb = y.clone()
         plan.set_precision(PREC_FP64)
@@ -608,6 +649,18 @@ def run_ours(args):
         plan.apply(x, y64)
         torch.cuda.synchronize(dev)
         y_fp = float(torch.linalg.norm(yb - y64) / torch.linalg.norm(y64))
+        # the FP64 grouped path on the same workload and input, timed the same way
+        n64 = max(3, min(args.steps, 50))
+        ev64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n64)]
+        for e0, e1 in ev64:
+            flush.zero_()
+            e0.record()
+            plan.apply(x, y64, stream=stream)
+            e1.record()
+        torch.cuda.synchronize(dev)
+        t64 = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev64) / 1e3, dev)
+        fp64 = {"value": n64 * ws / t64, "unit": UNIT, "steps": n64, "ms_per_step": t64 / n64 * 1e3,
+                "launches_per_matvec": plan.launches(), "split_speedup": value / (n64 * ws / t64)}
         plan.set_precision(PREC_BF16X3)
     # end-to-end through the C ABI with pinned host buffers (H2D + matvec + D2H per step)
     from tk_gb300 import _abi
@@ -661,12 +714,13 @@ def run_ours(args):
         roof = {"bound": "tensor", "achieved": t_ach, "peak": tpeak, "unit": "TFLOP/s", "frac": t_ach / tpeak,
                 "peak_source": tsrc}
     roof.update({"kernel": STAGES[dom], "traffic": traffic_for(args.workload, prec_name, STAGES[dom]),
+                 "traffic_source": TRAFFIC_SOURCE,
                  "alg_bytes": by[dom], "alg_flops": fl[dom], "pipe_flops_per_byte": intensity, "ridge": ridge,
                  "tensor_achieved_tflops": t_ach * products, "tensor_peak_tflops": tpeak,
                  "stage_ms": [float(v) for v in stage_ms], "stage_bytes": by, "stage_flops": fl})
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(prob, args.workload, args.cpu_seconds, args.cpu_one_core_seconds)
+        cpu = cpu_baseline_isolated(args.workload, args.cpu_seconds, args.cpu_one_core_seconds)
     line = {
         "metric": WORKLOADS[args.workload][0], "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup,
@@ -691,6 +745,9 @@ def run_ours(args):
     }
     if y_fp is not None:
         line["split_vs_fp64_rel_err"] = y_fp
+    if fp64 is not None:
+        line["fp64_value"] = fp64["value"]
+        line["fp64"] = fp64
     if lz is not None:
         line["lanczos"] = lz
     if args.compare_schedules > 0:
@@ -700,8 +757,12 @@ def run_ours(args):
     if args.dmrg:
         line["dmrg_cfg1"] = dmrg_cfg1(torch, args.dmrg_cpu)
     if args.sweeps > 0:
-        line["sweeps_hubbard"] = sweep_hubbard(torch, args.sweep_sites, args.sweep_bond, args.sweep_warmup,
-                                               args.sweeps)
+        sw = sweep_hubbard(torch, args.sweep_sites, args.sweep_bond, args.sweep_warmup, args.sweeps)
+        line["sweeps_hubbard"] = sw
+        # the metric's second half: seconds per sweep at D=2048, split vs FP64, at |dE| <= 1e-10
+        line["sweep"] = {"fp64_seconds": sw["fp64"]["seconds_per_sweep"],
+                         "split_seconds": sw["bf16x3"]["seconds_per_sweep"], "speedup": sw["sweep_speedup"],
+                         "dE": sw["dE"], "dE_ok": bool(sw["dE"] <= 1e-10)}
     if args.tdvp_steps > 0:
         line["tdvp_anderson"] = tdvp_anderson(torch, args.tdvp_steps)
     print(json.dumps(line), flush=True)
@@ -712,7 +773,9 @@ def run_ours(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.cpu_child:
+        run_cpu_child(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -204,7 +204,10 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
  * (L x psi GEMMs), stage 2 (W_i W_j combine) and stage 3 (x R GEMMs) to
  * ms[0..2], the algorithmic flops of each stage to flops[0..2] and its
  * compulsory global-memory bytes (operands read once, results written once,
- * in the precision the plan runs) to bytes[0..2]; flops/bytes may be NULL. */
+ * in the precision the plan runs) to bytes[0..2]; flops/bytes may be NULL.
+ * In split precision the W_i W_j combine of narrow stage-3 stacks runs inside
+ * the stage-3 kernel; stage 2 then covers only the wide stacks' combine (0 ms
+ * and 0 bytes when there are none) and stage 3 the rest, T1 reads included. */
 tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, double* y_dev, void* stream,
                            int32_t reps, float* ms, double* flops, double* bytes);
 
@@ -364,10 +367,47 @@ typedef struct {
     int64_t* block_offsets;
     double* data;
     int64_t total;
+    /* charges / dims of legs that the library made (fused legs of a
+     * contraction); NULL when legs point into an input's QIndex */
+    int32_t* owned_charges;
+    int64_t* owned_dims;
 } tk_bst_out;
 
+/* Host tensors in, host tensor out (one copy in and one copy out through the
+ * context's page-locked staging and device scratch; no device allocation once
+ * the scratch has grown to the call's size).  Synchronous. */
 tk_status tk_block_gemm_f64(tk_ctx* ctx, const tk_bst* a, const tk_bst* b, tk_bst_out* out);
+/* The same on device buffers: a->data and b->data are device pointers in
+ * the FlatBlockStorage layout.  Fills the output layout (keys, offsets,
+ * total; out->data stays NULL) and, when c_dev is not NULL, computes C into
+ * c_dev (out->total doubles) on `stream`, waiting for it before returning
+ * (the tables live in the context's shared scratch).  Call once with
+ * c_dev = NULL to size the output buffer. */
+tk_status tk_block_gemm_f64_dev(tk_ctx* ctx, const tk_bst* a, const tk_bst* b, tk_bst_out* out, double* c_dev,
+                                void* stream);
+/* Releases the arrays of a tk_bst_out (keys, offsets, data, owned legs). */
 void tk_bst_free(tk_bst_out* t);
+
+/*
+ * One pairwise step of the block-sparse contraction executor:
+ * SparseContractionExecutor::execute_pairwise_sparse with reshape_for_gemm
+ * (tk-contract/src/sparse.rs:124-265).  A's legs a_legs[0..n) and B's legs
+ * b_legs[0..n) are contracted: each operand is permuted (free legs, then
+ * contracted legs, each in ascending leg order; contracted first for B),
+ * its free and its contracted legs are fused into one leg each
+ * (BlockSparseTensor::fuse_legs, tk-symmetry/src/block_sparse.rs:444-611:
+ * a fused leg is Incoming, sectors = distinct fused charges ascending,
+ * combinations in Cartesian order inside a sector; a single leg stays as it
+ * is), and the rank-2 operands are multiplied as by tk_block_gemm_f64.  The
+ * result is the rank-2 tensor (fused free legs of A, fused free legs of B)
+ * in FlatBlockStorage form; its fused legs are owned by `out` (released by
+ * tk_bst_free).  Host tensors in and out, ranks 1 to 8; the permutation, the
+ * fusion and the GEMM run on the device through the context's scratch.
+ * An operand without a free or without a contracted leg is
+ * TK_ERR_UNSUPPORTED.  Synchronous.
+ */
+tk_status tk_contract_pairwise_f64(tk_ctx* ctx, const tk_bst* a, const int32_t* a_legs, int32_t n_a,
+                                   const tk_bst* b, const int32_t* b_legs, int32_t n_b, tk_bst_out* out);
 
 /* All eigenpairs of `batch` symmetric n x n matrices (host memory, each
  * matrix n*n doubles back to back; symmetric, so row- and column-major
@@ -483,6 +523,46 @@ tk_status tk_env_grow_right(tk_ctx* ctx, const tk_env* env_r, const tk_bst* a, c
  * (sweep/mod.rs:390-396); this is the usual two-site guess instead. */
 tk_status tk_heff2_two_site_product(tk_heff2_plan* plan, const tk_bst* a_i, const tk_bst* a_j, double* psi_dev,
                                     void* stream);
+
+/*
+ * The two-site truncation's data path (no single reference counterpart: it
+ * moves the data for truncate_svd, tk-dmrg/src/truncation/mod.rs:56-127,
+ * applied to every bond charge of the two-site matrix
+ * M[(s_i, a_L), (s_j, a_R)], which is block diagonal in
+ * q = q(s_i) + q(a_L) = q(a_R) - q(s_j) for a flux-zero two-site vector).
+ * Rows of M_q: (s_i state, a_L sector), states then sectors ascending;
+ * columns (s_j state, a_R sector) likewise; charges ascending.
+ *   tk_split_plan_create: from the two-site block layout (legs s_i, s_j, a_L,
+ *     a_R; keys and offsets as tk_heff2_blocks returns them), host only.
+ *   tk_split_charges: the charges (ncomp int32 each) and the rows / columns
+ *     of each M_q; any array may be NULL.
+ *   tk_split_gather: every M_q from the device vector psi_dev, packed charge
+ *     after charge (row-major), copied to m_host (sum of rows x cols doubles;
+ *     page-locked memory copies fastest).  Synchronous on `stream`.
+ *   tk_split_set_kept: kept[i] states of charge i (0 .. min(rows, cols));
+ *     returns the block counts and lengths of the new site tensors A_i
+ *     (s_i, a_L, bond) and A_j (s_j, bond, a_R), bond = the charges with
+ *     kept[i] > 0, ascending.
+ *   tk_split_layout: their packed keys and block offsets (side 0: A_i, 1: A_j).
+ *   tk_split_factors: u_host packs U_q (rows x kept, row-major) and v_host
+ *     V_q (kept x cols, row-major) charge after charge (charges with kept 0
+ *     take no space); they are scattered into the device buffers ai_dev and
+ *     aj_dev (the caller scales them, e.g. A_i = U, A_j = S V^T / norm).
+ *     Synchronous on `stream`.
+ * The calls use the context's scratch and are not thread-safe per context.
+ */
+typedef struct tk_split_plan tk_split_plan;
+tk_status tk_split_plan_create(tk_ctx* ctx, int32_t qn_kind, const tk_qindex* legs, int64_t n_blocks,
+                               const uint64_t* keys, const int64_t* offsets, tk_split_plan** out);
+void tk_split_plan_destroy(tk_split_plan* split);
+tk_status tk_split_charges(const tk_split_plan* split, int32_t* n_charges, int32_t* charges, int64_t* rows,
+                           int64_t* cols);
+tk_status tk_split_gather(tk_split_plan* split, const double* psi_dev, double* m_host, void* stream);
+tk_status tk_split_set_kept(tk_split_plan* split, const int64_t* kept, int64_t* n_blocks_i, int64_t* total_i,
+                            int64_t* n_blocks_j, int64_t* total_j);
+tk_status tk_split_layout(const tk_split_plan* split, int32_t side, uint64_t* keys, int64_t* offsets);
+tk_status tk_split_factors(tk_split_plan* split, const double* u_host, const double* v_host, double* ai_dev,
+                           double* aj_dev, void* stream);
 
 #ifdef __cplusplus
 }

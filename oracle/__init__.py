@@ -7,8 +7,13 @@ parity status (integer bookkeeping pinned to the reference's known answers;
 matvec pinned to a literal transliteration and physics known answers, not to
 reference-run outputs -- the Rust reference cannot be built here).
 
-build() compiles heff_oracle.c with gcc (-O3 -fopenmp, no -march) into
-oracle/_build/liborc.so; load() binds it with ctypes.
+build() compiles heff_oracle.c twice with gcc: liborc.so, the checker
+(-O3 -fopenmp -std=c11: ISO C mode keeps floating-point contraction off, so
+its sums round the same on every host), and liborc_timed.so, the timed CPU
+baseline (-O3 -std=gnu11 -ffp-contract=fast -funroll-loops: multiply-adds
+fuse into FMA, as a tuned CPU build of the reference would; no -march, so the
+same flags build on x86-64 and on aarch64, whose base ISA has FMA and NEON).
+load() / load(timed=True) bind them with ctypes.
 """
 from __future__ import annotations
 
@@ -23,6 +28,9 @@ HERE = Path(__file__).resolve().parent
 SRC = HERE / "heff_oracle.c"
 BUILD = HERE / "_build"
 LIB = BUILD / "liborc.so"
+LIB_TIMED = BUILD / "liborc_timed.so"
+FLAGS = {LIB: ["-O3", "-fopenmp", "-std=c11"],
+         LIB_TIMED: ["-O3", "-fopenmp", "-std=gnu11", "-ffp-contract=fast", "-funroll-loops"]}
 
 
 class orc_qindex(C.Structure):
@@ -35,28 +43,33 @@ class orc_bst(C.Structure):
                 ("data", C.POINTER(C.c_double))]
 
 
-def build(force: bool = False) -> Path:
-    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
-        return LIB
+def _build_one(lib: Path, force: bool) -> Path:
+    if not force and lib.exists() and lib.stat().st_mtime >= SRC.stat().st_mtime:
+        return lib
     BUILD.mkdir(parents=True, exist_ok=True)
-    tmp = LIB.with_suffix(".so.tmp")
-    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-Wall", str(SRC), "-o", str(tmp), "-lm"]
+    tmp = lib.with_suffix(".so.tmp")
+    cmd = ["gcc", *FLAGS[lib], "-fPIC", "-shared", "-Wall", str(SRC), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
-_lib = None
+def build(force: bool = False) -> Path:
+    """Builds the checker and the timed baseline; returns the checker's path."""
+    _build_one(LIB_TIMED, force)
+    return _build_one(LIB, force)
 
 
-def load() -> C.CDLL:
-    global _lib
-    if _lib is not None:
-        return _lib
-    build()
-    lib = C.CDLL(str(LIB))
+_libs = {}
+
+
+def load(timed: bool = False) -> C.CDLL:
+    if timed in _libs:
+        return _libs[timed]
+    path = _build_one(LIB_TIMED if timed else LIB, False)
+    lib = C.CDLL(str(path))
     P = C.POINTER
     sig = {
         "orc_qn_pack": (C.c_uint64, [C.c_int, P(C.c_int32)]),
@@ -90,7 +103,7 @@ def load() -> C.CDLL:
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
-    _lib = lib
+    _libs[timed] = lib
     return lib
 
 
@@ -197,9 +210,11 @@ def heff_apply_dense(Wi, Wj, L, R, x) -> np.ndarray:
 
 
 class BlockSparseOracle:
-    """Block-sparse FP64 matvec in the FlatBlockStorage layout (the timed CPU baseline)."""
+    """Block-sparse FP64 matvec in the FlatBlockStorage layout.  timed=False:
+    the checker build; timed=True: the FMA build timed as the CPU baseline."""
 
-    def __init__(self, kind, phys_i, phys_j, bond_l, bond_r, flux, Wi, Wj, L, R):
+    def __init__(self, kind, phys_i, phys_j, bond_l, bond_r, flux, Wi, Wj, L, R, timed: bool = False):
+        self._lib = load(timed)
         self._kp = _Keep()
         kp = self._kp
         self.Wi = np.ascontiguousarray(Wi, dtype=np.float64)
@@ -212,7 +227,7 @@ class BlockSparseOracle:
         if flux is not None:
             self._flux = np.asarray(list(flux) + [0], dtype=np.int32)
             fl = self._flux.ctypes.data_as(C.POINTER(C.c_int32))
-        lib = load()
+        lib = self._lib
         self._h = lib.orc_bs_create(kind, C.byref(qi), C.byref(qj), C.byref(ql), C.byref(qr), fl,
                                     self.Wi.shape[2], self.Wi.shape[3], self.Wj.shape[3], _d(self.Wi), _d(self.Wj),
                                     _d(self.L), _d(self.R))
@@ -225,42 +240,42 @@ class BlockSparseOracle:
     def __del__(self):
         try:
             if self._h:
-                load().orc_bs_destroy(self._h)
+                self._lib.orc_bs_destroy(self._h)
         except Exception:
             pass
 
     def apply(self, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty(self.total)
-        load().orc_bs_apply(self._h, _d(x), _d(y))
+        self._lib.orc_bs_apply(self._h, _d(x), _d(y))
         return y
 
     def apply_into(self, x: np.ndarray, y: np.ndarray) -> None:
-        load().orc_bs_apply(self._h, _d(x), _d(y))
+        self._lib.orc_bs_apply(self._h, _d(x), _d(y))
 
     def flops(self) -> float:
-        return float(load().orc_bs_flops(self._h))
+        return float(self._lib.orc_bs_flops(self._h))
 
     def to_dense(self, xb):
         out = np.zeros(self.dense_dim)
-        load().orc_bs_to_dense(self._h, _d(np.ascontiguousarray(xb)), _d(out))
+        self._lib.orc_bs_to_dense(self._h, _d(np.ascontiguousarray(xb)), _d(out))
         return out
 
     def from_dense(self, xd):
         out = np.zeros(self.total)
-        load().orc_bs_from_dense(self._h, _d(np.ascontiguousarray(xd)), _d(out))
+        self._lib.orc_bs_from_dense(self._h, _d(np.ascontiguousarray(xd)), _d(out))
         return out
 
     def blocks(self):
         sec = np.zeros((self.n_blocks, 4), dtype=np.int32)
         off = np.zeros(self.n_blocks, dtype=np.int64)
-        load().orc_bs_blocks(self._h, sec.ctypes.data_as(C.POINTER(C.c_int32)), off.ctypes.data_as(C.POINTER(C.c_int64)))
+        self._lib.orc_bs_blocks(self._h, sec.ctypes.data_as(C.POINTER(C.c_int32)), off.ctypes.data_as(C.POINTER(C.c_int64)))
         return sec, off
 
 
-def set_threads(n: int) -> None:
-    load().orc_set_num_threads(n)
+def set_threads(n: int, timed: bool = False) -> None:
+    load(timed).orc_set_num_threads(n)
 
 
-def num_threads() -> int:
-    return int(load().orc_num_threads())
+def num_threads(timed: bool = False) -> int:
+    return int(load(timed).orc_num_threads())

@@ -30,6 +30,55 @@ tk_status cuda_fail(const char* op, cudaError_t e) {
     return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
 }
 
+tk_status ctx_stream(tk_ctx* ctx, void** out) {
+    if (!ctx->stream) {
+        cudaStream_t s = nullptr;
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail("context stream", e);
+        ctx->stream = s;
+    }
+    *out = ctx->stream;
+    return TK_OK;
+}
+
+tk_status ctx_dev_scratch(tk_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->dev_scratch_bytes) {
+        if (ctx->dev_scratch) {
+            if (ctx->stream) cudaStreamSynchronize((cudaStream_t)ctx->stream);
+            cudaFree(ctx->dev_scratch);
+            ctx->dev_scratch = nullptr;
+            ctx->dev_scratch_bytes = 0;
+        }
+        const size_t want = std::max<size_t>(bytes + bytes / 2, 1 << 20);
+        void* p = nullptr;
+        cudaError_t e = dev_malloc(&p, want);
+        if (e != cudaSuccess) return cuda_fail("context device scratch", e);
+        ctx->dev_scratch = p;
+        ctx->dev_scratch_bytes = want;
+    }
+    *out = ctx->dev_scratch;
+    return TK_OK;
+}
+
+tk_status ctx_host_stage(tk_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->host_stage_bytes) {
+        if (ctx->host_stage) {
+            if (ctx->stream) cudaStreamSynchronize((cudaStream_t)ctx->stream);
+            cudaFreeHost(ctx->host_stage);
+            ctx->host_stage = nullptr;
+            ctx->host_stage_bytes = 0;
+        }
+        const size_t want = std::max<size_t>(bytes + bytes / 2, 1 << 20);
+        void* p = nullptr;
+        cudaError_t e = cudaMallocHost(&p, want);
+        if (e != cudaSuccess) return cuda_fail("context host staging", e);
+        ctx->host_stage = p;
+        ctx->host_stage_bytes = want;
+    }
+    *out = ctx->host_stage;
+    return TK_OK;
+}
+
 bool plan_cancelled(tk_heff2_plan* p, cudaStream_t s, const char* where) {
     if (!p->cancel || __atomic_load_n(p->cancel, __ATOMIC_ACQUIRE) == 0) return false;
     cudaStreamSynchronize(s);
@@ -102,6 +151,13 @@ tk_status tk_ctx_create(int32_t device, tk_ctx** out) {
 void tk_ctx_destroy(tk_ctx* ctx) {
     if (!ctx) return;
     ctx_release_solver(ctx);
+    {
+        DeviceGuard g(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize((cudaStream_t)ctx->stream);
+        if (ctx->dev_scratch) cudaFree(ctx->dev_scratch);
+        if (ctx->host_stage) cudaFreeHost(ctx->host_stage);
+        if (ctx->stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
+    }
     delete ctx;
 }
 
@@ -652,9 +708,15 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
         if (p->precision == TK_PREC_BF16X3) {
             const TcTables& C = H.tc;
             const double b16 = 2.0 * 2.0 * kTcBK;  // hi + lo bf16 per operand row element x 64
+            // T1 reads of the combine kernel and of the fused stage 3, each at
+            // most all of T1 (a T1 element read by several terms counts once)
+            double comb_reads = 0.0;
+            for (const TcCombJob& j : C.jobs) comb_reads += (double)j.rows * j.cols * (j.term_end - j.term_begin);
+            const double t1_comb = 4.0 * std::min<double>((double)C.t1_total, comb_reads);
+            const double t1_fused = 4.0 * std::min<double>((double)C.t1_total, C.fill_term_elems);
             bytes[0] = 8.0 * H.total + b16 * (double)C.lq_rows + 4.0 * C.t1_total;
-            bytes[1] = 4.0 * C.t1_total + b16 * (double)C.t2q_rows;
-            bytes[2] = b16 * (double)C.t2q_rows + b16 * (double)C.rq_rows + 8.0 * H.total;
+            bytes[1] = C.jobs.empty() ? 0.0 : t1_comb + b16 * (double)C.t2q_rows;
+            bytes[2] = b16 * (double)C.t2q_rows + t1_fused + b16 * (double)C.rq_rows + 8.0 * H.total;
         } else {
             bytes[0] = 8.0 * ((double)H.lbuf.size() + H.total + H.t1_total);
             bytes[1] = 8.0 * ((double)H.t1_total + H.t2_total);

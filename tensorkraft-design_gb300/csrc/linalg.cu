@@ -19,7 +19,9 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "tk_bsgemm.hpp"
 #include "tk_internal.hpp"
+#include "tk_plan.cuh"
 
 using namespace tk;
 
@@ -71,61 +73,7 @@ struct Scratch {
         if (e_ != cudaSuccess) return fail(#op, e_);  \
     } while (0)
 
-void tiles_for(GemmTable& g, int task) {
-    const GemmTask& t = g.tasks[task];
-    for (int m0 = 0; m0 < t.M; m0 += kF64TileM)
-        for (int n0 = 0; n0 < t.N; n0 += kF64TileN) g.tiles.push_back({task, m0, n0, 0});
-}
-
-struct Rank2 {
-    int kind = 0;
-    QIndex legs[2];
-    int8_t dirs[2] = {0, 0};
-    Qn flux;
-    std::vector<uint64_t> keys;
-    std::vector<int64_t> offs;
-    std::vector<int> rs, cs;  // sector index per block
-    const double* data = nullptr;
-    int64_t total = 0;
-};
-
-bool rank2_from_abi(const tk_bst& t, Rank2& o, const char* name, std::string& err) {
-    if (t.rank != 2 || !t.legs || !qn_kind_valid(t.qn_kind)) {
-        err = std::string(name) + ": rank-2 tensor with a known quantum-number kind required";
-        return false;
-    }
-    o.kind = t.qn_kind;
-    for (int l = 0; l < 2; ++l) {
-        if (!qindex_from_abi(t.qn_kind, t.legs[l], o.legs[l], err)) return false;
-        o.dirs[l] = t.leg_dirs ? t.leg_dirs[l] : (int8_t)l;
-    }
-    if (t.flux)
-        for (int k = 0; k < qn_ncomp(t.qn_kind); ++k) o.flux.c[k] = t.flux[k];
-    if (t.n_blocks > 0 && (!t.keys || !t.block_offsets || !t.data)) {
-        err = std::string(name) + ": null block arrays";
-        return false;
-    }
-    o.data = t.data;
-    for (int64_t b = 0; b < t.n_blocks; ++b) {
-        Qn q[2];
-        key_unpack(t.qn_kind, t.keys[b], 2, q);
-        int r = o.legs[0].find(q[0]), c = o.legs[1].find(q[1]);
-        if (r < 0 || c < 0) {
-            err = std::string(name) + ": block key names a sector missing from its QIndex";
-            return false;
-        }
-        if (b > 0 && t.keys[b - 1] >= t.keys[b]) {
-            err = std::string(name) + ": keys not strictly ascending";
-            return false;
-        }
-        o.keys.push_back(t.keys[b]);
-        o.offs.push_back(t.block_offsets[b]);
-        o.rs.push_back(r);
-        o.cs.push_back(c);
-        o.total = std::max(o.total, t.block_offsets[b] + o.legs[0].dim[r] * o.legs[1].dim[c]);
-    }
-    return true;
-}
+void tiles_for(GemmTable& g, int task) { bsgemm_tiles_for(g, task); }
 
 }  // namespace
 
@@ -185,8 +133,60 @@ tk_status tk_gemm_f64(tk_ctx* ctx, double alpha, const tk_mat* a, const tk_mat* 
     return TK_OK;
 }
 
+// Output header of a block GEMM (legs of A's rows and B's columns, their
+// directions, the output flux) and its key / offset arrays; data unallocated.
+static tk_status fill_out_header(const tk_bst* a_abi, const tk_bst* b_abi, const Rank2& A, const Rank2& B,
+                                 const BlockGemmPlan& P, tk_bst_out* out, bool with_data) {
+    out->qn_kind = A.kind;
+    out->rank = 2;
+    out->legs[0] = a_abi->legs[0];
+    out->legs[1] = b_abi->legs[1];
+    out->leg_dirs[0] = A.dirs[0];
+    out->leg_dirs[1] = B.dirs[1];
+    out->flux[0] = P.target.c[0];
+    out->flux[1] = P.target.c[1];
+    out->n_blocks = (int64_t)P.okeys.size();
+    out->total = P.total;
+    out->keys = (uint64_t*)std::malloc(sizeof(uint64_t) * std::max<size_t>(P.okeys.size(), 1));
+    out->block_offsets = (int64_t*)std::malloc(sizeof(int64_t) * std::max<size_t>(P.ooffs.size(), 1));
+    out->data = with_data ? (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(P.total, 1)) : nullptr;
+    if (!out->keys || !out->block_offsets || (with_data && !out->data)) {
+        tk_bst_free(out);
+        set_error("block gemm: host allocation failed");
+        return TK_ERR_OOM;
+    }
+    std::copy(P.okeys.begin(), P.okeys.end(), out->keys);
+    std::copy(P.ooffs.begin(), P.ooffs.end(), out->block_offsets);
+    return TK_OK;
+}
+
+// Grouped-GEMM tables of a block GEMM, packed for one copy.
+struct TableBlob {
+    size_t tasks = 0, segs = 0, tiles = 0;
+};
+static TableBlob add_tables(Blob& b, const GemmTable& g) {
+    TableBlob t;
+    t.tasks = b.add(g.tasks.data(), sizeof(GemmTask) * g.tasks.size());
+    t.segs = b.add(g.segs.data(), sizeof(GemmSeg) * g.segs.size());
+    t.tiles = b.add(g.tiles.data(), sizeof(GemmTile) * g.tiles.size());
+    return t;
+}
+
+// Copies `blob` through the context's page-locked staging into its device
+// scratch on `s`; *dev receives the scratch base (at least blob.device_size()).
+static tk_status stage_blob(tk_ctx* ctx, const Blob& blob, cudaStream_t s, unsigned char** dev) {
+    void *d = nullptr, *h = nullptr;
+    tk_status st;
+    if ((st = ctx_dev_scratch(ctx, blob.device_size(), &d)) != TK_OK) return st;
+    if ((st = ctx_host_stage(ctx, std::max<size_t>(blob.bytes.size(), 1), &h)) != TK_OK) return st;
+    std::memcpy(h, blob.bytes.data(), blob.bytes.size());
+    if (!blob.bytes.empty()) CK(cudaMemcpyAsync(d, h, blob.bytes.size(), cudaMemcpyHostToDevice, s));
+    *dev = static_cast<unsigned char*>(d);
+    return TK_OK;
+}
+
 tk_status tk_block_gemm_f64(tk_ctx* ctx, const tk_bst* a_abi, const tk_bst* b_abi, tk_bst_out* out) {
-    if (!a_abi || !b_abi || !out) {
+    if (!ctx || !a_abi || !b_abi || !out) {
         set_error("tk_block_gemm_f64: null argument");
         return TK_ERR_INVALID_ARG;
     }
@@ -197,94 +197,76 @@ tk_status tk_block_gemm_f64(tk_ctx* ctx, const tk_bst* a_abi, const tk_bst* b_ab
         set_error("tk_block_gemm_f64: " + err);
         return TK_ERR_INVALID_ARG;
     }
-    if (A.kind != B.kind) {
-        set_error("tk_block_gemm_f64: quantum-number kinds differ");
+    BlockGemmPlan P;
+    tk_status st = guard_host("tk_block_gemm_f64", err, [&] { return block_gemm_plan(A, B, P, err); });
+    if (st != TK_OK) {
+        set_error("tk_block_gemm_f64: " + err);
+        return st;
+    }
+    if ((st = fill_out_header(a_abi, b_abi, A, B, P, out, true)) != TK_OK) return st;
+    if (P.total == 0) return TK_OK;
+    Guard gd(ctx->device);
+    // one host-to-device copy: A, B and the tables; C is written on the device
+    // and read back through the same staging buffer
+    Blob blob;
+    const size_t oa = blob.add(A.data, sizeof(double) * (size_t)A.total);
+    const size_t ob = blob.add(B.data, sizeof(double) * (size_t)B.total);
+    const TableBlob tb = add_tables(blob, P.g);
+    const size_t oc = blob.reserve(sizeof(double) * (size_t)P.total);
+    auto run = [&]() -> tk_status {
+        void* sp = nullptr;
+        tk_status s2;
+        if ((s2 = ctx_stream(ctx, &sp)) != TK_OK) return s2;
+        cudaStream_t s = (cudaStream_t)sp;
+        unsigned char* d = nullptr;
+        if ((s2 = ctx_host_stage(ctx, sizeof(double) * (size_t)P.total, &sp)) != TK_OK) return s2;
+        if ((s2 = stage_blob(ctx, blob, s, &d)) != TK_OK) return s2;
+        CK(launch_gemm_f64((const GemmTile*)(d + tb.tiles), (int)P.g.tiles.size(), (const GemmTask*)(d + tb.tasks),
+                           (const GemmSeg*)(d + tb.segs), (const double*)(d + oa), (const double*)(d + ob),
+                           (double*)(d + oc), s));
+        CK(cudaMemcpyAsync(ctx->host_stage, d + oc, sizeof(double) * (size_t)P.total, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        std::memcpy(out->data, ctx->host_stage, sizeof(double) * (size_t)P.total);
+        return TK_OK;
+    };
+    st = run();
+    if (st != TK_OK) tk_bst_free(out);
+    return st;
+}
+
+tk_status tk_block_gemm_f64_dev(tk_ctx* ctx, const tk_bst* a_abi, const tk_bst* b_abi, tk_bst_out* out,
+                                double* c_dev, void* stream) {
+    if (!ctx || !a_abi || !b_abi || !out) {
+        set_error("tk_block_gemm_f64_dev: null argument");
         return TK_ERR_INVALID_ARG;
     }
-    const int kind = A.kind;
-    const Qn target = qn_fuse(kind, A.flux, B.flux);
-    // Phase 1 (faer.rs:406-430): task generation per compatible pair.
-    std::map<uint64_t, std::vector<std::pair<int, int>>> by_out;
-    for (size_t i = 0; i < A.keys.size(); ++i)
-        for (size_t j = 0; j < B.keys.size(); ++j) {
-            const Qn& qa_col = A.legs[1].q[A.cs[i]];
-            const Qn& qb_row = B.legs[0].q[B.rs[j]];
-            if (qa_col != qb_row) continue;
-            Qn out_q[2] = {A.legs[0].q[A.rs[i]], B.legs[1].q[B.cs[j]]};
-            if (qn_fuse(kind, out_q[0], qn_dual(kind, out_q[1])) != target) continue;
-            if (A.legs[1].dim[A.cs[i]] != B.legs[0].dim[B.rs[j]]) {
-                set_error("tk_block_gemm_f64: contracted sector dimensions differ");
-                return TK_ERR_SECTOR_MISMATCH;
-            }
-            by_out[key_pack(kind, out_q, 2)].push_back({(int)i, (int)j});
-        }
-    // Output blocks in ascending key order (faer.rs:560-574).
-    GemmTable g;
-    std::vector<uint64_t> okeys;
-    std::vector<int64_t> ooffs;
-    int64_t total = 0;
-    for (auto& kv : by_out) {
-        const auto& pairs = kv.second;
-        int i0 = pairs[0].first, j0 = pairs[0].second;
-        int64_t M = A.legs[0].dim[A.rs[i0]], N = B.legs[1].dim[B.cs[j0]];
-        GemmTask t{};
-        t.M = (int32_t)M; t.N = (int32_t)N;
-        t.c_off = total; t.c_rs = (int32_t)N; t.c_cs = 1;
-        t.alpha = 1.0; t.beta = 0.0;
-        t.seg_begin = (int)g.segs.size();
-        for (auto& pr : pairs) {
-            int64_t K = A.legs[1].dim[A.cs[pr.first]];
-            GemmSeg s{};
-            s.a_off = A.offs[pr.first]; s.a_rs = (int32_t)K; s.a_cs = 1;
-            s.b_off = B.offs[pr.second]; s.b_rs = (int32_t)N; s.b_cs = 1;
-            s.K = (int32_t)K;
-            g.segs.push_back(s);
-        }
-        t.seg_end = (int)g.segs.size();
-        g.tasks.push_back(t);
-        tiles_for(g, (int)g.tasks.size() - 1);
-        okeys.push_back(kv.first);
-        ooffs.push_back(total);
-        total += M * N;
+    std::memset(out, 0, sizeof(*out));
+    std::string err;
+    Rank2 A, B;
+    if (!rank2_from_abi(*a_abi, A, "A", err) || !rank2_from_abi(*b_abi, B, "B", err)) {
+        set_error("tk_block_gemm_f64_dev: " + err);
+        return TK_ERR_INVALID_ARG;
     }
-    // Fill the output header.
-    out->qn_kind = kind;
-    out->rank = 2;
-    out->legs[0] = a_abi->legs[0];
-    out->legs[1] = b_abi->legs[1];
-    out->leg_dirs[0] = A.dirs[0];
-    out->leg_dirs[1] = B.dirs[1];
-    out->flux[0] = target.c[0];
-    out->flux[1] = target.c[1];
-    out->n_blocks = (int64_t)okeys.size();
-    out->total = total;
-    out->keys = (uint64_t*)std::malloc(sizeof(uint64_t) * std::max<size_t>(okeys.size(), 1));
-    out->block_offsets = (int64_t*)std::malloc(sizeof(int64_t) * std::max<size_t>(ooffs.size(), 1));
-    out->data = (double*)std::malloc(sizeof(double) * (size_t)std::max<int64_t>(total, 1));
-    if (!out->keys || !out->block_offsets || !out->data) {
-        tk_bst_free(out);
-        set_error("tk_block_gemm_f64: host allocation failed");
-        return TK_ERR_OOM;
+    BlockGemmPlan P;
+    tk_status st = guard_host("tk_block_gemm_f64_dev", err, [&] { return block_gemm_plan(A, B, P, err); });
+    if (st != TK_OK) {
+        set_error("tk_block_gemm_f64_dev: " + err);
+        return st;
     }
-    std::copy(okeys.begin(), okeys.end(), out->keys);
-    std::copy(ooffs.begin(), ooffs.end(), out->block_offsets);
-    if (total == 0) return TK_OK;
-    int dev = ctx ? ctx->device : 0;
-    Guard gd(dev);
-    Scratch sc;
-    double *da, *db, *dc;
-    GemmTask* dt; GemmSeg* ds; GemmTile* dl;
-    std::vector<double> ha(A.data, A.data + A.total), hb(B.data, B.data + B.total);
-    tk_status st = TK_OK;
+    if ((st = fill_out_header(a_abi, b_abi, A, B, P, out, false)) != TK_OK) return st;
+    if (!c_dev || P.total == 0) return TK_OK;
+    Guard gd(ctx->device);
+    Blob blob;
+    const TableBlob tb = add_tables(blob, P.g);
+    cudaStream_t s = (cudaStream_t)stream;
     auto run = [&]() -> tk_status {
-        CK(sc.put(ha, &da));
-        CK(sc.put(hb, &db));
-        CK(sc.make((size_t)total, &dc));
-        CK(sc.put(g.tasks, &dt));
-        CK(sc.put(g.segs, &ds));
-        CK(sc.put(g.tiles, &dl));
-        CK(launch_gemm_f64(dl, (int)g.tiles.size(), dt, ds, da, db, dc, nullptr));
-        CK(cudaMemcpy(out->data, dc, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost));
+        unsigned char* d = nullptr;
+        tk_status s2 = stage_blob(ctx, blob, s, &d);
+        if (s2 != TK_OK) return s2;
+        CK(launch_gemm_f64((const GemmTile*)(d + tb.tiles), (int)P.g.tiles.size(), (const GemmTask*)(d + tb.tasks),
+                           (const GemmSeg*)(d + tb.segs), A.data, B.data, c_dev, s));
+        // the tables live in the context's shared scratch: finish before returning
+        CK(cudaStreamSynchronize(s));
         return TK_OK;
     };
     st = run();
@@ -297,9 +279,13 @@ void tk_bst_free(tk_bst_out* t) {
     std::free(t->keys);
     std::free(t->block_offsets);
     std::free(t->data);
+    std::free(t->owned_charges);
+    std::free(t->owned_dims);
     t->keys = nullptr;
     t->block_offsets = nullptr;
     t->data = nullptr;
+    t->owned_charges = nullptr;
+    t->owned_dims = nullptr;
     t->n_blocks = 0;
     t->total = 0;
 }

@@ -422,6 +422,37 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
             if (y0 < 0 || y0 + t.n0 + t.n_valid - 1 >= T.total) { err = "tensor-core stage 3 output row"; return false; }
         }
     }
+    for (const TcTile& t : C.tiles3f) {
+        if (t.mode != 3 || t.n_mma < t.n_valid || t.n_mma > kTcBN || t.n_mma % 16 != 0 || t.m_valid <= 0 ||
+            t.n_valid <= 0 || t.m_valid > kTcBM || t.n_valid > kTcBN || t.kch < 0 || t.out_off < 0 ||
+            t.out_off + t.m_valid - 1 >= (int64_t)C.yrow.size() || t.b_row < 0 || t.fill0 < 0 ||
+            (size_t)t.fill0 + t.kch >= C.fill_chunk.size()) {
+            err = "tensor-core fused stage 3 tile";
+            return false;
+        }
+        for (int r = 0; r < t.m_valid; ++r) {
+            int64_t y0 = C.yrow[t.out_off + r];
+            if (y0 < 0 || y0 + t.n0 + t.n_valid - 1 >= T.total) { err = "tensor-core stage 3 output row"; return false; }
+        }
+        for (int c = 0; c < t.kch; ++c) {
+            const int32_t a = C.fill_chunk[(size_t)t.fill0 + c], b = C.fill_chunk[(size_t)t.fill0 + c + 1];
+            if (a < 0 || b < a || (size_t)b > C.fill_segs.size()) { err = "tensor-core fill chunk"; return false; }
+        }
+    }
+    for (const TcFillSeg& g : C.fill_segs) {
+        if (g.r0 < 0 || g.rows <= 0 || g.r0 + g.rows > kTcBM || g.k0 < 0 || g.cols <= 0 || g.k0 + g.cols > kTcBK ||
+            g.term_begin < 0 || g.term_end < g.term_begin || (size_t)g.term_end > C.fill_terms.size()) {
+            err = "tensor-core fill segment";
+            return false;
+        }
+        for (int32_t t = g.term_begin; t < g.term_end; ++t) {
+            const TcCombTerm& c = C.fill_terms[t];
+            if (c.in_off < 0 || c.in_rs < 0 || c.in_off + (int64_t)(g.rows - 1) * c.in_rs + g.cols - 1 >= C.t1_total) {
+                err = "tensor-core fill term";
+                return false;
+            }
+        }
+    }
     for (const TcCombJob& j : C.jobs) {
         int64_t kmax = (int64_t)j.k0 + j.cols - 1;
         int64_t imax = (((int64_t)j.t2row + (kmax >> 6) * j.cstride + j.r0 + j.rows - 1) << 6) + 63;
@@ -1009,14 +1040,25 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
                     }
             const int32_t kch = kchunks(K);
             const int64_t NB = QB.dim[bp];
+            // the combine fused into the GEMM when the stack has few column tiles
+            // (each column tile rebuilds the operand from T1)
+            const bool fuse = (NB + kTcBN - 1) / kTcBN <= kTcFuseMaxNTiles;
             const int64_t rbase = C.rq_rows, t2b = C.t2q_rows, yb = (int64_t)C.yrow.size();
             C.rq_rows += kch * NB;
-            C.t2q_rows += kch * rows;
+            if (!fuse) C.t2q_rows += kch * rows;
             for (size_t i = 0; i < rp.size(); ++i) {
                 int ws = rp[i].first, b = rp[i].second;
                 rcopy.push_back({T.rbuf.data() + rblk[((size_t)bp * nWR + ws) * nB + b], NB, WR.dim[ws] * QB.dim[b], rk[i],
                                  rbase, NB});
             }
+            // slabs of the A operand (T2): stack rows [row0, row0 + nr) x K columns
+            // [k0, k0 + nc), element (r, c) = sum_t coef_t * T1[in_off_t + r * in_rs_t + c]
+            struct Slab {
+                int64_t row0;
+                int32_t nr, k0, nc, tb, te;
+            };
+            std::vector<Slab> slabs;
+            std::vector<TcCombTerm> sterms;
             for (size_t i = 0; i < yp.size(); ++i) {
                 int64_t po = yp[i].first;
                 int ap = yp[i].second;
@@ -1026,13 +1068,8 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
                     int ws = rp[ri].first, b = rp[ri].second;
                     for (int64_t wloc = 0; wloc < WR.dim[ws]; ++wloc) {
                         int64_t wr = WR.off[ws] + wloc;
-                        TcCombJob j{};
-                        j.t2row = (int32_t)(t2b + yr[i]);
-                        j.cstride = (int32_t)rows;
-                        j.k0 = (int32_t)(rk[ri] + wloc * QB.dim[b]);
-                        j.rows = (int32_t)QA.dim[ap];
-                        j.cols = (int32_t)QB.dim[b];
-                        j.term_begin = (int32_t)C.terms.size();
+                        Slab sl{yr[i], (int32_t)QA.dim[ap], (int32_t)(rk[ri] + wloc * QB.dim[b]), (int32_t)QB.dim[b],
+                                (int32_t)sterms.size(), 0};
                         for (const Term& tm : byout[po * nwr + wr]) {
                             uint64_t key = pkey(tm.p, ap, wl_sec[tm.wl], b);
                             auto it = std::lower_bound(pieces.begin(), pieces.end(), key,
@@ -1042,41 +1079,85 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
                                 ct.in_off = it->off + wl_loc[tm.wl] * (int64_t)(it->rs / WL.dim[wl_sec[tm.wl]]);
                                 ct.in_rs = it->rs;
                                 ct.coef = (float)tm.c;
-                                C.terms.push_back(ct);
+                                sterms.push_back(ct);
                             }
                         }
-                        j.term_end = (int32_t)C.terms.size();
-                        for (int q = 0; q < kTcCombInline && j.term_begin + q < j.term_end; ++q)
-                            j.inl[q] = C.terms[j.term_begin + q];
-                        if (j.term_end > j.term_begin) {
-                            // row chunks of at most kTcCombMaxElems elements
-                            const int32_t all_rows = j.rows;
-                            const int32_t step = std::max<int32_t>(1, kTcCombMaxElems / std::max<int32_t>(1, j.cols));
-                            for (int32_t r0 = 0; r0 < all_rows; r0 += step) {
-                                j.r0 = r0;
-                                j.rows = std::min(step, all_rows - r0);
-                                C.jobs.push_back(j);
-                            }
-                        }
+                        sl.te = (int32_t)sterms.size();
+                        if (sl.te > sl.tb) slabs.push_back(sl);
                     }
                 }
             }
-            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
+            if (!fuse) {
+                // combine jobs: rows of one slab, at most kTcCombMaxElems elements each
+                for (const Slab& sl : slabs) {
+                    TcCombJob j{};
+                    j.t2row = (int32_t)(t2b + sl.row0);
+                    j.cstride = (int32_t)rows;
+                    j.k0 = sl.k0;
+                    j.cols = sl.nc;
+                    j.term_begin = (int32_t)C.terms.size();
+                    C.terms.insert(C.terms.end(), sterms.begin() + sl.tb, sterms.begin() + sl.te);
+                    j.term_end = (int32_t)C.terms.size();
+                    for (int q = 0; q < kTcCombInline && j.term_begin + q < j.term_end; ++q)
+                        j.inl[q] = C.terms[j.term_begin + q];
+                    const int32_t step = std::max<int32_t>(1, kTcCombMaxElems / std::max<int32_t>(1, j.cols));
+                    for (int32_t r0 = 0; r0 < sl.nr; r0 += step) {
+                        j.r0 = r0;
+                        j.rows = std::min(step, sl.nr - r0);
+                        C.jobs.push_back(j);
+                    }
+                }
+            }
+            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM) {
+                int32_t fill0 = -1;
+                if (fuse) {
+                    // fill segments of this row tile, chunk by chunk: every slab part
+                    // inside rows [m0, m0 + 128) and K chunk [64c, 64c + 64)
+                    fill0 = (int32_t)C.fill_chunk.size();
+                    for (int32_t c = 0; c < kch; ++c) {
+                        C.fill_chunk.push_back((int32_t)C.fill_segs.size());
+                        const int64_t ka = (int64_t)c * BK, kb = ka + BK;
+                        for (const Slab& sl : slabs) {
+                            const int64_t ra = std::max<int64_t>(sl.row0, m0);
+                            const int64_t rb = std::min<int64_t>(sl.row0 + sl.nr, m0 + kTcBM);
+                            const int64_t c0 = std::max<int64_t>(sl.k0, ka), c1 = std::min<int64_t>(sl.k0 + sl.nc, kb);
+                            if (ra >= rb || c0 >= c1) continue;
+                            TcFillSeg g{};
+                            g.r0 = (int16_t)(ra - m0);
+                            g.rows = (int16_t)(rb - ra);
+                            g.k0 = (int16_t)(c0 - ka);
+                            g.cols = (int16_t)(c1 - c0);
+                            g.term_begin = (int32_t)C.fill_terms.size();
+                            for (int32_t t = sl.tb; t < sl.te; ++t) {
+                                TcCombTerm ct = sterms[t];
+                                ct.in_off += (ra - sl.row0) * (int64_t)ct.in_rs + (c0 - sl.k0);
+                                C.fill_terms.push_back(ct);
+                            }
+                            g.term_end = (int32_t)C.fill_terms.size();
+                            C.fill_term_elems += (double)g.rows * g.cols * (g.term_end - g.term_begin);
+                            C.fill_segs.push_back(g);
+                        }
+                    }
+                    C.fill_chunk.push_back((int32_t)C.fill_segs.size());
+                }
                 for (int64_t n0 = 0; n0 < NB; n0 += kTcBN) {
                     TcTile t{};
-                    t.a_row = (int32_t)(t2b + m0); t.a_cs = (int32_t)rows;
+                    t.a_row = fuse ? 0 : (int32_t)(t2b + m0);
+                    t.a_cs = fuse ? 0 : (int32_t)rows;
                     t.b_row = (int32_t)(rbase + n0); t.b_cs = (int32_t)NB;
                     t.kch = kch;
                     t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
                     t.n_valid = (int32_t)std::min<int64_t>(kTcBN, NB - n0);
                     t.n_mma = (t.n_valid + 15) / 16 * 16;
-                    t.mode = 1;
+                    t.mode = fuse ? 3 : 1;
                     t.out_off = yb + m0;
                     t.ldc = 0;
                     t.n0 = (int32_t)n0;
-                    C.tiles3.push_back(t);
+                    t.fill0 = fill0;
+                    (fuse ? C.tiles3f : C.tiles3).push_back(t);
                     C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
                 }
+            }
         }
         // heaviest tiles first (K chunks, then padded MMA area): a launch with
         // more tiles than resident CTAs ends on a tail of light tiles
@@ -1108,9 +1189,11 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
         }
         lpt(C.tiles1x);
         lpt(C.tiles3);
+        lpt(C.tiles3f);
         for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
         for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
         for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
+        for (const TcTile& t : C.tiles3f) C.max_kch3f = std::max(C.max_kch3f, t.kch);
         // the constant operands as bf16 hi + lo stacks
         host_alloc_checkpoint();
         fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);

@@ -4,14 +4,18 @@
 // a product a*b is evaluated as hi_a*hi_b + hi_a*lo_b + lo_a*hi_b with fp32
 // accumulation in tensor memory (the lo*lo term, ~2^-16 relative, is dropped).
 //
-// One matvec = three to five launches on one stream:
+// One matvec = two to six launches on one stream:
 //   split_psi_kernel   psi sub-blocks of tall stage-1 stacks -> bf16 hi/lo copy
 //   tc_gemm_kernel     stage 1 of the tall stacks, B operand from that copy
 //   tc_gemm1_kernel    stage 1, T1 = L_stack(A) * psi_A        (fp32 out); the
 //                      psi operand is read from the fp64 vector and split into
 //                      bf16 hi/lo in shared memory by the kernel itself
 //   combine_tc_kernel  W_i*W_j channel combine, T1 -> stage-3 A operand hi/lo
-//   tc_gemm_kernel     stage 3, y = T2_stack(B') * R_stack(B')^T (fp64 out via a row table)
+//                      (stage-3 stacks of more than kTcFuseMaxNTiles column tiles)
+//   tc_gemm3f_kernel   stage 3 of the narrow stacks with the combine fused in:
+//                      T2 built in shared memory from T1, then y = T2 * R^T
+//   tc_gemm_kernel     stage 3 of the wide stacks, y = T2_stack(B') * R_stack(B')^T
+//                      (fp64 out via a row table)
 // A stage-1 stack of more than kTcFuseMaxMTiles row tiles would have every row
 // tile split the same psi columns again; those stacks (the large sectors of
 // wide bonds) take the split copy, made once per matvec, instead.
@@ -563,6 +567,193 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
     }
 }
 
+// Stage 3 with the W_i W_j combine fused in (stacks of at most
+// kTcFuseMaxNTiles column tiles).  The R operand (B) comes in by TMA as in
+// tc_gemm_kernel; the A operand, T2 = sum_t coef_t * T1, is built chunk by
+// chunk in shared memory by all eight warps from the fill segments of the
+// tile: the chunk is cleared, every segment element is summed in fp32 from
+// T1, split into bf16 hi / lo and stored in the 128-byte-swizzled K-major
+// layout a TMA load would give (row m at m * 128 bytes, its 16-byte chunk j
+// at position j ^ (m % 8)).  A two-stage ring lets chunk c + 1 be filled
+// while the MMAs of chunk c run.  Warps 0-3 read the accumulator back and
+// write y through the row table, as tc_gemm_kernel does.  Waits are bounded
+// and their trip counts block-uniform.
+constexpr int kFusedThreads = 256;
+constexpr int kFusedWarps = kFusedThreads / 32;
+
+template <int NST>
+__global__ void __launch_bounds__(kFusedThreads, 2) tc_gemm3f_kernel(const TcTile* __restrict__ tiles,
+                                                                    const int32_t* __restrict__ fill_chunk,
+                                                                    const TcFillSeg* __restrict__ segs,
+                                                                    const TcCombTerm* __restrict__ terms,
+                                                                    const float* __restrict__ t1,
+                                                                    const __grid_constant__ CUtensorMap mBh,
+                                                                    const __grid_constant__ CUtensorMap mBl,
+                                                                    const OutMap om, int* err) {
+    constexpr int U = 4;  // elements per lane in flight
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
+    uint64_t* empty = full + NST;
+    uint64_t* done = empty + NST;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    const TcTile t = tiles[blockIdx.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    grid_dep_launch();
+
+    if (t.kch == 0) {
+        grid_dep_wait();
+        for (int e = threadIdx.x; e < t.m_valid * t.n_valid; e += blockDim.x)
+            store_out(t, e / t.n_valid, e % t.n_valid, 0.f, om);
+        return;
+    }
+    int64_t my_row = 0;
+    if (warp < 4 && warp * 32 + lane < t.m_valid) my_row = om.rowtab[t.out_off + warp * 32 + lane];
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    const int nb16 = t.n_mma >> 4;
+    const uint32_t b_bytes = 2 * t.n_mma * kTcBK * 2;
+    auto load_b = [&](int c, uint8_t* st, uint64_t* bar) {
+        const int yb = t.b_row + c * t.b_cs;
+        for (int i = 0; i < nb16; ++i) {
+            tma_load_2d(st + 2 * A_BYTES + i * 16 * 128, &mBh, 0, yb + 16 * i, bar);
+            tma_load_2d(st + 2 * A_BYTES + B_BYTES + i * 16 * 128, &mBl, 0, yb + 16 * i, bar);
+        }
+    };
+    // the R operand (a plan constant) of the first chunks goes out before the
+    // dependency wait, overlapping the previous kernel's tail
+    const int npre = min(NST, t.kch);
+    if (threadIdx.x == 0)
+        for (int c = 0; c < npre; ++c) {
+            mbar_expect_tx(&full[c], b_bytes);
+            load_b(c, smem + c * STAGE_BYTES, &full[c]);
+        }
+    grid_dep_wait();
+    const uint32_t idesc = make_idesc(t.n_mma);
+    for (int c = 0; c < t.kch; ++c) {
+        const int s = c % NST;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        bool good = true;
+        if (c >= NST && threadIdx.x == 0) good = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
+        if (!__syncthreads_and(good)) break;
+        if (threadIdx.x == 0 && c >= npre) {
+            mbar_expect_tx(&full[s], b_bytes);
+            load_b(c, st, &full[s]);
+        }
+        // clear A hi / lo: positions no segment covers (K padding, slabs without
+        // terms, rows past the stack) must read as zero
+        {
+            uint4* z = reinterpret_cast<uint4*>(st);
+#pragma unroll
+            for (int i = 0; i < 2 * A_BYTES / 16 / kFusedThreads; ++i)
+                z[threadIdx.x + i * kFusedThreads] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncthreads();
+        const int sb = fill_chunk[t.fill0 + c], se = fill_chunk[t.fill0 + c + 1];
+        for (int g = sb + warp; g < se; g += kFusedWarps) {
+            const TcFillSeg sg = segs[g];
+            const int n = sg.rows * sg.cols;
+            const int tb = sg.term_begin, nt = sg.term_end - sg.term_begin;
+            for (int e0 = 0; e0 < n; e0 += 32 * U) {
+                int r[U], k[U];
+                bool v[U];
+                float acc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = e0 + u * 32 + lane;
+                    v[u] = e < n;
+                    r[u] = v[u] ? e / sg.cols : 0;
+                    k[u] = v[u] ? e - r[u] * sg.cols : 0;
+                    acc[u] = 0.f;
+                }
+                for (int q = 0; q < nt; ++q) {
+                    const TcCombTerm tm = terms[tb + q];
+                    float x[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+                        x[u] = v[u] ? __ldg(t1 + tm.in_off + (int64_t)r[u] * tm.in_rs + k[u]) : 0.f;
+#pragma unroll
+                    for (int u = 0; u < U; ++u) acc[u] = fmaf(tm.coef, x[u], acc[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (v[u]) {
+                        const int m = sg.r0 + r[u], kk = sg.k0 + k[u];
+                        const uint32_t off =
+                            (uint32_t)m * 128u + ((uint32_t)((kk >> 3) ^ (m & 7)) << 4) + (uint32_t)(kk & 7) * 2u;
+                        const __nv_bfloat16 h = __float2bfloat16_rn(acc[u]);
+                        *reinterpret_cast<__nv_bfloat16*>(st + off) = h;
+                        *reinterpret_cast<__nv_bfloat16*>(st + A_BYTES + off) =
+                            __float2bfloat16_rn(acc[u] - __bfloat162float(h));
+                    }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (warp == 1 && lane == 0) {
+            if (mbar_wait(&full[s], (c / NST) & 1, err, ERR_FULL_TIMEOUT)) {
+                fence_after();
+                const uint32_t sa = smem_u32(st);
+                const uint64_t ah = sw128_desc(sa), al = sw128_desc(sa + A_BYTES);
+                const uint64_t bh = sw128_desc(sa + 2 * A_BYTES), bl = sw128_desc(sa + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+                for (int kk = 0; kk < kTcBK / 16; ++kk) {
+                    const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+                    mma_bf16(tmem, ah + adv, bh + adv, idesc, (c | kk) != 0);
+                    mma_bf16(tmem, ah + adv, bl + adv, idesc, 1u);
+                    mma_bf16(tmem, al + adv, bh + adv, idesc, 1u);
+                }
+            }
+            mma_commit(&empty[s]);
+        }
+    }
+    if (warp == 1 && lane == 0) mma_commit(done);
+    __syncwarp();
+    const bool have = mbar_wait(done, 0, err, ERR_DONE_TIMEOUT);
+    fence_after();
+    const bool go = __all_sync(0xffffffffu, have);
+    if (go && warp < 4) {
+        float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
+        const int row = threadIdx.x;
+        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+        tmem_row_to_smem(tbase, t.n_mma, stile[row]);
+        __syncwarp();
+#pragma unroll 8
+        for (int i = 0; i < 32; ++i) {
+            const int r = warp * 32 + i;
+            const int64_t rbase = __shfl_sync(0xffffffffu, my_row, i);
+            if (r < t.m_valid) {
+                double* o = om.out64 + rbase + t.n0;
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    if (lane + 32 * h < t.n_valid) o[lane + 32 * h] = (double)stile[r][lane + 32 * h];
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
 constexpr int kSplitThreads = 128;  // split: threads per job
 
 // psi sub-block tile (64 a x 32 b of a row-major D_A x D_B block, a0 at a K
@@ -774,6 +965,11 @@ bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string
 }  // namespace
 
 struct TcPlan {
+    TcTile* tiles3f = nullptr;          // fused stage-3 tiles
+    int32_t* fill_chunk = nullptr;
+    TcFillSeg* fill_segs = nullptr;
+    TcCombTerm* fill_terms = nullptr;
+    int n3f = 0;
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
     __nv_bfloat16 *th = nullptr, *tl = nullptr;
     __nv_bfloat16 *xh = nullptr, *xl = nullptr;  // split copy of psi (tall stage-1 stacks)
@@ -795,7 +991,8 @@ struct TcPlan {
     CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl, mXh, mXl;
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,         th,           tl,   xh,      xl,  t1, tiles1, tiles1x,
-                      tiles3, split, jobs, terms, yrow, t1col_base, t1col_stride, xsrc, xstride, err};
+                      tiles3, split, jobs, terms, yrow, t1col_base, t1col_stride, xsrc, xstride, err,
+                      tiles3f, fill_chunk, fill_segs, fill_terms};
         for (void* p : ps)
             if (p) cudaFree(p);
     }
@@ -829,7 +1026,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = put(&p->jobs, C.jobs)) != cudaSuccess ||
         (e = put(&p->terms, C.terms)) != cudaSuccess || (e = put(&p->yrow, C.yrow)) != cudaSuccess ||
         (e = put(&p->t1col_base, C.t1col_base)) != cudaSuccess ||
-        (e = put(&p->t1col_stride, C.t1col_stride)) != cudaSuccess) {
+        (e = put(&p->t1col_stride, C.t1col_stride)) != cudaSuccess || (e = put(&p->tiles3f, C.tiles3f)) != cudaSuccess ||
+        (e = put(&p->fill_chunk, C.fill_chunk)) != cudaSuccess || (e = put(&p->fill_segs, C.fill_segs)) != cudaSuccess ||
+        (e = put(&p->fill_terms, C.fill_terms)) != cudaSuccess) {
         err = std::string("tensor-core operand upload: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
@@ -843,6 +1042,7 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->x_split = C.x_split;
     p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
+    p->n3f = (int)C.tiles3f.size();
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
@@ -860,6 +1060,8 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = cudaFuncSetAttribute(tc_gemm1_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
             cudaSuccess ||
         (e = cudaFuncSetAttribute(tc_gemm1_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm3f_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
             cudaSuccess) {
         err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return TK_ERR_CUDA;
@@ -939,6 +1141,13 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
             launch_pdl(combine_tc_kernel, tc.njobs, kCombThreads, 0, s, (const TcCombJob*)tc.jobs,
                        (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
     } else {
+        // fused tiles first: their dependency is stage 1 (T1); the TMA tiles read
+        // the combine's T2, complete before either launch starts its main loop
+        if (tc.n3f > 0)
+            launch_pdl(tc_gemm3f_kernel<2>, tc.n3f, kFusedThreads, smem_bytes(2), s, (const TcTile*)tc.tiles3f,
+                       (const int32_t*)tc.fill_chunk, (const TcFillSeg*)tc.fill_segs,
+                       (const TcCombTerm*)tc.fill_terms, (const float*)tc.t1, tc.mRh, tc.mRl,
+                       OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, tc.err);
         launch_tc_gemm(tc.nst3, tc.n3, tc.tiles3, tc.mTh, tc.mTl, tc.mRh, tc.mRl,
                        OutMap{nullptr, y, tc.yrow, nullptr, nullptr}, CONST_B, tc.err, s);
     }
@@ -983,7 +1192,7 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 int* tc_error_word(TcPlan& tc) { return tc.err; }
 
 int tc_launches(const TcPlan& tc) {
-    return (tc.nsplit > 0) + (tc.n1x > 0) + (tc.n1 > 0) + (tc.njobs > 0) + (tc.n3 > 0);
+    return (tc.nsplit > 0) + (tc.n1x > 0) + (tc.n1 > 0) + (tc.njobs > 0) + (tc.n3f > 0) + (tc.n3 > 0);
 }
 
 tk_status tc_check_error(TcPlan& tc, cudaStream_t s) {

@@ -1,6 +1,7 @@
 // tk_internal.hpp -- shared types of libtk_heff: quantum-number arithmetic,
 // flattened sector-GEMM task tables, and the host-side plan description.
 #pragma once
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <new>
@@ -10,11 +11,19 @@
 
 #include "../../include/tk_heff.h"
 
-// Library context: the CUDA device it is bound to, and the cuSOLVER handle of
-// the dense factorisations (created on first use).
+// Library context: the CUDA device it is bound to, the cuSOLVER handle of
+// the dense factorisations (created on first use), and the grow-only scratch
+// of the backend calls (block_gemm, spmv, gemm, pairwise contraction): one
+// device arena, one page-locked host staging buffer and a stream, so that
+// repeated calls allocate nothing once the arena has reached their size.
 struct tk_ctx {
     int device = 0;
     void* solver = nullptr;
+    void* dev_scratch = nullptr;
+    size_t dev_scratch_bytes = 0;
+    void* host_stage = nullptr;
+    size_t host_stage_bytes = 0;
+    void* stream = nullptr;  // cudaStream_t
 };
 
 namespace tk {
@@ -161,6 +170,20 @@ struct TcTile {
     int64_t out_off;         // mode 1: row-table index of m0; mode 2: column-table index of n0
     int32_t ldc, n0;         // mode 1: n0 = column offset added to the row table; mode 2: ldc = m0
     int32_t n_mma, k_valid;  // UMMA N (n_valid rounded up to 16, <= kTcBN); stage 1: K of the stack (D_A)
+    int32_t fill0, pad_;     // fused stage 3: chunk c's fill segments are fill_segs[fill_chunk[fill0 + c] ..)
+};
+// Fused stage 3 (the W_i W_j combine inside the stage-3 GEMM): a stage-3
+// stack of at most kTcFuseMaxNTiles column tiles builds its A operand (T2)
+// chunk by chunk in shared memory from T1 instead of reading a T2 written
+// by the combine kernel.  One fill segment = one rectangle of a chunk,
+// element (r, k) = sum_t coef_t * T1[in_off_t + r * in_rs_t + k], written to
+// tile row r0 + r, chunk column k0 + k (terms in TcTables::fill_terms, their
+// in_off at the segment's first element).
+constexpr int kTcFuseMaxNTiles = 2;
+struct TcFillSeg {
+    int16_t r0, rows;   // tile rows [r0, r0 + rows), r0 + rows <= kTcBM
+    int16_t k0, cols;   // chunk columns [k0, k0 + cols), k0 + cols <= kTcBK
+    int32_t term_begin, term_end;
 };
 // psi sub-block -> stage-1 B operand of a tall stack (K-major chunks), hi/lo
 // split.  One job = one 64 (a) x 32 (b) tile of a D_A x D_B sub-block, a0 a
@@ -198,6 +221,12 @@ struct TcTables {
     std::vector<TcSplitJob> split;     // psi -> split copy, tall stacks only
     std::vector<TcCombJob> jobs;
     std::vector<TcCombTerm> terms;
+    // fused stage 3: tiles (mode 3), their per-chunk segment ranges and segments
+    std::vector<TcTile> tiles3f;
+    std::vector<int32_t> fill_chunk;   // per fused tile: kch + 1 offsets into fill_segs
+    std::vector<TcFillSeg> fill_segs;
+    std::vector<TcCombTerm> fill_terms;
+    double fill_term_elems = 0.0;      // sum over fill segments of elements x terms (T1 reads)
     std::vector<int64_t> yrow;  // y element offset of every stage-3 operand row
     // T1 is stored per (stack A, column block (p, B)) as a row-major
     // [rows_A x D_B] matrix: element (r, c) of stack A sits at
@@ -208,7 +237,7 @@ struct TcTables {
     std::vector<int64_t> xsrc;
     std::vector<int32_t> xstride;
     double mma_flops = 0.0;     // padded tensor-core work of both stages (one product)
-    int32_t max_kch1 = 0, max_kch1x = 0, max_kch3 = 0;
+    int32_t max_kch1 = 0, max_kch1x = 0, max_kch3 = 0, max_kch3f = 0;
 };
 
 // Everything the device needs for one two-site H_eff, built on the host.
@@ -282,6 +311,31 @@ void env_layout(int kind, const QIndex& bra, const QIndex& mpo, const QIndex& ke
 
 // Thread-local last-error message.
 void set_error(const std::string& msg);
+// The context's scratch (abi.cu): device arena and page-locked staging of at
+// least `bytes` (grown by half again when too small, contents not kept), and
+// its stream (created on first use).  Return TK_OK or a status with the
+// message set.
+tk_status ctx_dev_scratch(tk_ctx* ctx, size_t bytes, void** out);
+tk_status ctx_host_stage(tk_ctx* ctx, size_t bytes, void** out);
+tk_status ctx_stream(tk_ctx* ctx, void** out);
+// Packs host arrays back to back (256-byte aligned) for one host-to-device copy.
+struct Blob {
+    std::vector<unsigned char> bytes;
+    size_t add(const void* p, size_t n) {
+        const size_t at = (bytes.size() + 255) & ~(size_t)255;
+        bytes.resize(at + n);
+        if (n) std::copy((const unsigned char*)p, (const unsigned char*)p + n, bytes.begin() + at);
+        return at;
+    }
+    size_t reserve(size_t n) {  // space without data (written on the device)
+        const size_t at = (bytes.size() + 255) & ~(size_t)255;
+        bytes.resize(at);
+        tail = at + n;
+        return at;
+    }
+    size_t tail = 0;  // end of the reserved space past bytes
+    size_t device_size() const { return std::max(bytes.size(), tail); }
+};
 // Releases the context's cuSOLVER handle (dense.cu).
 void ctx_release_solver(tk_ctx* ctx);
 

@@ -79,7 +79,8 @@ class tk_mat_mut(C.Structure):
 class tk_bst_out(C.Structure):
     _fields_ = [("qn_kind", C.c_int32), ("rank", C.c_int32), ("legs", tk_qindex * 2), ("leg_dirs", C.c_int8 * 2),
                 ("flux", C.c_int32 * 2), ("n_blocks", C.c_int64), ("keys", C.POINTER(C.c_uint64)),
-                ("block_offsets", C.POINTER(C.c_int64)), ("data", C.POINTER(C.c_double)), ("total", C.c_int64)]
+                ("block_offsets", C.POINTER(C.c_int64)), ("data", C.POINTER(C.c_double)), ("total", C.c_int64),
+                ("owned_charges", C.POINTER(C.c_int32)), ("owned_dims", C.POINTER(C.c_int64))]
 
 
 # (name, restype, argtypes) of every entry point declared in include/tk_heff.h
@@ -124,6 +125,11 @@ SIGNATURES = [
                                         C.POINTER(tk_mat_mut), C.c_void_p]),
     ("tk_block_gemm_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.POINTER(tk_bst_out)]),
     ("tk_bst_free", None, [C.POINTER(tk_bst_out)]),
+    ("tk_block_gemm_f64_dev", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.POINTER(tk_bst_out),
+                                          C.c_void_p, C.c_void_p]),
+    ("tk_contract_pairwise_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(C.c_int32), C.c_int32,
+                                             C.POINTER(tk_bst), C.POINTER(C.c_int32), C.c_int32,
+                                             C.POINTER(tk_bst_out)]),
     ("tk_spmv_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("tk_heff2_plan_create_dev_complex", C.c_int32, [C.c_void_p, C.POINTER(tk_env), C.c_void_p, C.POINTER(tk_env),
                                                      C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst),
@@ -155,6 +161,16 @@ SIGNATURES = [
                                       C.c_void_p, C.c_void_p]),
     ("tk_heff2_two_site_product", C.c_int32, [C.c_void_p, C.POINTER(tk_bst), C.POINTER(tk_bst), C.c_void_p,
                                               C.c_void_p]),
+    ("tk_split_plan_create", C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(tk_qindex), C.c_int64,
+                                         C.POINTER(C.c_uint64), C.POINTER(C.c_int64), C.POINTER(C.c_void_p)]),
+    ("tk_split_plan_destroy", None, [C.c_void_p]),
+    ("tk_split_charges", C.c_int32, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                                     C.POINTER(C.c_int64)]),
+    ("tk_split_gather", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("tk_split_set_kept", C.c_int32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("tk_split_layout", C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
+    ("tk_split_factors", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 
 _lib = None

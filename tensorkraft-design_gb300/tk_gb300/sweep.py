@@ -529,6 +529,124 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     return Ai, Aj, nb, disc
 
 
+def _select(svs: list, max_bond: int, cutoff: float, min_bond: int):
+    """truncate_svd's rule (truncation/mod.rs:71-99) on the singular values of all
+    charges, ties broken by charge order then position: sigma >= cutoff *
+    sigma_max, at most max_bond, then at least min_bond as far as there are
+    values.  Returns (kept count per charge, discarded share of sum sigma^2,
+    norm of the kept part)."""
+    sv = np.concatenate(svs) if svs else np.zeros(0)
+    sv_charge = np.repeat(np.arange(len(svs)), [len(x) for x in svs])
+    sv_pos = np.concatenate([np.arange(len(x)) for x in svs]) if svs else np.zeros(0, dtype=np.int64)
+    order = np.lexsort((sv_pos, sv_charge, -sv))
+    sv, sv_charge = sv[order], sv_charge[order]
+    thr = cutoff * (float(sv[0]) if len(sv) else 0.0)
+    nkeep = min(max_bond, int(np.count_nonzero(sv >= thr)))
+    nkeep = min(max(nkeep, min_bond), len(sv))
+    counts = np.bincount(sv_charge[:nkeep], minlength=len(svs)).astype(np.int64)
+    sq = sv * sv
+    total_sq = float(sq.sum())
+    disc = float(sq[nkeep:].sum()) / total_sq if total_sq > 0 else 0.0
+    norm = math.sqrt(float(sq[:nkeep].sum())) or 1.0
+    return counts, disc, norm
+
+
+_PINNED = {}
+
+
+def _pinned(device: int, name: str, n: int) -> np.ndarray:
+    """A page-locked float64 host buffer of at least n elements (grown, then reused)."""
+    torch = _torch()
+    buf = _PINNED.get((device, name))
+    if buf is None or buf.numel() < n:
+        buf = torch.empty(max(n, 1) + max(n, 1) // 4, dtype=torch.float64).pin_memory()
+        _PINNED[(device, name)] = buf
+    return buf.numpy()[:n]
+
+
+def split_two_site_device(kind, psi_dev, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool,
+                          min_bond: int = 1, device: int = 0):
+    """The two-site truncation of a real two-site vector that lives on the
+    device (the plan's block layout): every bond-charge block M_q is gathered
+    on the GPU and copied to the host once (tk_split_gather), decomposed by
+    LAPACK's SVD on a host thread pool (the SVD truncate_svd takes,
+    truncation/mod.rs:68), the kept set chosen by truncate_svd's rule over all
+    charges (_select), and the kept factors scattered into the new site
+    tensors on the GPU (tk_split_factors): A_i = U, A_j = S V^T / norm moving
+    right; A_i = U S / norm, A_j = V^T moving left.  Returns (A_i, A_j as
+    SiteTensor, new bond QIndex, discarded weight) like split_two_site."""
+    from .symmetry import ncomp
+
+    torch = _torch()
+    lib = _abi.load()
+    ctx = context(device)
+    m = _Marshal()
+    qlegs = (_abi.tk_qindex * 4)(*[m.qindex(ix) for ix in legs])
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    h = C.c_void_p()
+    check(lib.tk_split_plan_create(ctx, kind, qlegs, len(keys), _abi.u64ptr(keys), _abi.i64ptr(offs), C.byref(h)))
+    try:
+        n = C.c_int32()
+        check(lib.tk_split_charges(h, C.byref(n), None, None, None))
+        nq, nc = n.value, ncomp(kind)
+        ch = np.zeros(max(nq * nc, 1), dtype=np.int32)
+        rows = np.zeros(max(nq, 1), dtype=np.int64)
+        cols = np.zeros(max(nq, 1), dtype=np.int64)
+        check(lib.tk_split_charges(h, C.byref(n), _abi.i32ptr(ch), _abi.i64ptr(rows), _abi.i64ptr(cols)))
+        rows, cols = rows[:nq], cols[:nq]
+        moff = np.concatenate([[0], np.cumsum(rows * cols)]).astype(np.int64)
+        mbuf = _pinned(device, "split_m", int(moff[-1]))
+        check(lib.tk_split_gather(h, C.c_void_p(psi_dev.data_ptr()), C.c_void_p(mbuf.ctypes.data), None))
+
+        def svd(i):
+            return i, np.linalg.svd(mbuf[moff[i]:moff[i + 1]].reshape(rows[i], cols[i]), full_matrices=False)
+
+        # largest factorisations first on the pool (one BLAS thread each)
+        order = sorted(range(nq), key=lambda i: -int(rows[i] * cols[i] * min(rows[i], cols[i])))
+        with _SingleThreadBlas():
+            usv = dict(_pool().map(svd, order))
+        kept, disc, norm = _select([usv[i][1] for i in range(nq)], max_bond, cutoff, min_bond)
+        nbi, ti, nbj, tj = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib.tk_split_set_kept(h, _abi.i64ptr(kept), C.byref(nbi), C.byref(ti), C.byref(nbj), C.byref(tj)))
+        lay = []
+        for side, nb_ in ((0, nbi.value), (1, nbj.value)):
+            k_ = np.zeros(max(nb_, 1), dtype=np.uint64)
+            o_ = np.zeros(max(nb_, 1), dtype=np.int64)
+            check(lib.tk_split_layout(h, side, _abi.u64ptr(k_), _abi.i64ptr(o_)))
+            lay.append((k_[:nb_], o_[:nb_]))
+        ku = kept * rows
+        kv = kept * cols
+        ubuf = _pinned(device, "split_u", int(ku.sum()))
+        vbuf = _pinned(device, "split_v", int(kv.sum()))
+        uo = np.concatenate([[0], np.cumsum(ku)])
+        vo = np.concatenate([[0], np.cumsum(kv)])
+        for i in range(nq):
+            k = int(kept[i])
+            if k == 0:
+                continue
+            U, S, Vh = usv[i]
+            if to_right:
+                ubuf[uo[i]:uo[i + 1]] = U[:, :k].reshape(-1)
+                vbuf[vo[i]:vo[i + 1]] = ((S[:k, None] / norm) * Vh[:k]).reshape(-1)
+            else:
+                ubuf[uo[i]:uo[i + 1]] = (U[:, :k] * (S[None, :k] / norm)).reshape(-1)
+                vbuf[vo[i]:vo[i + 1]] = Vh[:k].reshape(-1)
+        dev = f"cuda:{device}"
+        ai = torch.empty(max(ti.value, 1), dtype=torch.float64, device=dev)
+        aj = torch.empty(max(tj.value, 1), dtype=torch.float64, device=dev)
+        check(lib.tk_split_factors(h, C.c_void_p(ubuf.ctypes.data), C.c_void_p(vbuf.ctypes.data),
+                                   C.c_void_p(ai.data_ptr()), C.c_void_p(aj.data_ptr()), None))
+    finally:
+        lib.tk_split_plan_destroy(h)
+    qs = [tuple(int(x) for x in ch[i * nc:(i + 1) * nc]) for i in range(nq)]
+    nb = QIndex(kind, [(qs[i], int(kept[i])) for i in range(nq) if kept[i] > 0])
+    PI, PJ, QA, QB = legs
+    Ai = SiteTensor(kind, [PI, QA, nb], lay[0][0], lay[0][1], ai)
+    Aj = SiteTensor(kind, [PJ, nb, QB], lay[1][0], lay[1][1], aj)
+    return Ai, Aj, nb, disc
+
+
 def random_site_tensors(model, n: int, max_bond: int, total, rng: np.random.Generator, width: float = 0.35,
                         device: int = 0):
     """Random right-canonical block-sparse MPS (no dense tensors): bond charges
@@ -749,13 +867,17 @@ class DeviceDMRG:
     solver: "davidson" (the reference sweep's default; split-precision plans
     use Jacobi-Davidson corrections with `inner` split-precision CG steps) or
     "lanczos" (split-precision plans refined by FP64 Jacobi-Davidson).
+    The two-site vector is truncated by split_two_site_device (blocks gathered
+    and factors scattered on the GPU, an SVD per bond charge on the host);
+    host_split=True takes the host density-matrix path split_two_site instead.
     device_eigh: the truncation's density matrices are diagonalised on the GPU
     in batches (eigh_batch_device) instead of by numpy on a host thread pool
     (the default: faster for the Hubbard D=2048 sweep on a 16-core host)."""
 
     def __init__(self, model, sites: list, bonds: list, precision: int = PREC_FP64, solver: str = "davidson",
                  tol: float = 1e-10, max_subspace: int = 60, max_iter: int = 1000, inner: int = 40,
-                 krylov: int = 20, restarts: int = 10, refine: int = 20, device: int = 0, device_eigh: bool = False):
+                 krylov: int = 20, restarts: int = 10, refine: int = 20, device: int = 0, device_eigh: bool = False,
+                 host_split: bool = False):
         self.model, self.kind = model, model.kind
         self.n = len(sites)
         self.sites, self.bonds = list(sites), list(bonds)
@@ -765,6 +887,7 @@ class DeviceDMRG:
         self.krylov, self.restarts, self.refine = krylov, restarts, refine
         self.device = device
         self.eigh_batch = (lambda mats: eigh_batch_device(mats, device)) if device_eigh else None
+        self.host_split = host_split or device_eigh
         self.zero = identity(self.kind)
         n = self.n
         self.L = [None] * (n + 1)
@@ -809,15 +932,18 @@ class DeviceDMRG:
             raise
         rec.matvecs += r.matvec_count
         rec.fp64_matvecs += r.fp64_matvec_count
-        psi = r.eigenvector.cpu().numpy()
         t2 = time.perf_counter()
         keys, offs = plan.blocks()
         legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
-        Ai, Aj, nb, disc = split_two_site(self.kind, psi, keys, offs, legs, max_bond, cutoff, to_right,
-                                          eigh_batch=self.eigh_batch, min_bond=min_bond)
         P = self.model.phys
-        self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
-        self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
+        if self.host_split:
+            Ai, Aj, nb, disc = split_two_site(self.kind, r.eigenvector.cpu().numpy(), keys, offs, legs, max_bond,
+                                              cutoff, to_right, eigh_batch=self.eigh_batch, min_bond=min_bond)
+            self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
+            self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
+        else:
+            self.sites[i], self.sites[i + 1], nb, disc = split_two_site_device(
+                self.kind, r.eigenvector, keys, offs, legs, max_bond, cutoff, to_right, min_bond, self.device)
         self.bonds[i + 1] = nb
         t3 = time.perf_counter()
         if to_right:
