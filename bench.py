@@ -586,9 +586,12 @@ def run_ours(args):
     prob = models.workload(args.workload)
     plan = prob.plan(precision=PREC_FP64, device=local)
     prec_name = "fp64"
+    tune = None
     if args.precision in ("auto", "bf16x3"):
         plan.set_precision(PREC_BF16X3)
         prec_name = "bf16x3"
+        # the autotuner times the candidate schedules on this workload and keeps the fastest
+        tune = plan.autotune(reps=10, use_cache=False)
     n = plan.block_dim
     flops_total, alg_bytes = plan.cost()
     launches_per_matvec = plan.launches()
@@ -748,6 +751,8 @@ def run_ours(args):
     if fp64 is not None:
         line["fp64_value"] = fp64["value"]
         line["fp64"] = fp64
+    if tune is not None:
+        line["autotune"] = tune
     if lz is not None:
         line["lanczos"] = lz
     if args.compare_schedules > 0:

@@ -196,6 +196,42 @@ tk_status tk_heff2_set_cancel_flag(tk_heff2_plan* plan, const int32_t* flag);
  * clears it.  TK_ERR_UNSUPPORTED for an FP64 plan. */
 tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
 
+/* Schedule of the split-precision kernels (no reference counterpart; the
+ * plan-time choices of the specification's autotuner):
+ *   tall_max_mtiles: stage-1 stacks (one per ket sector of L) of at most this
+ *     many 128-row tiles split psi inside the GEMM kernel; taller stacks take
+ *     a bf16 split copy of psi made once per matvec (default 3);
+ *   fuse_max_ntiles: stage-3 stacks of at most this many 64-column tiles run
+ *     the W_i W_j combine inside the stage-3 kernel instead of a separate
+ *     combine launch (default 0: never).
+ * tk_heff2_set_tc_options rebuilds the plan's split tables and operands;
+ * FP64 matvecs are unaffected.  TK_ERR_UNSUPPORTED for complex plans. */
+typedef struct {
+    int32_t tall_max_mtiles;
+    int32_t fuse_max_ntiles;
+} tk_tc_options;
+tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts);
+tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts);
+
+/* Autotuner (no reference counterpart; ARCHITECTURE.md's per-histogram
+ * schedule choice): times `reps` split-precision matvecs of every distinct
+ * candidate schedule on the plan's own sector tables (CUDA events on the
+ * plan's stream, after two warm-up matvecs) and keeps the fastest.  The
+ * choice is cached process-wide under the plan's sector-size histogram
+ * class (quantum-number kind, physical and MPO dimensions, sector counts and
+ * log2-bucketed sector sizes of both bonds); with use_cache a plan of a known
+ * class takes the cached choice without timing.  `out` receives the choice,
+ * its time and up to 8 candidates with their times (ms per matvec). */
+typedef struct {
+    tk_tc_options chosen;
+    float chosen_ms;
+    int32_t from_cache;
+    int32_t n_candidates;
+    tk_tc_options candidates[8];
+    float candidate_ms[8];
+} tk_autotune_result;
+tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_t use_cache, tk_autotune_result* out);
+
 /* Per-stage kernel timing for roofline reports (no reference counterpart;
  * observability in the spirit of DMRGStats, tk-dmrg/src/sweep/mod.rs:85-111):
  * runs `reps` complete matvecs y = H_eff x on `stream` -- the same launches

@@ -7,9 +7,12 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -434,6 +437,61 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code) {
     return TK_OK;
 }
 
+// Rebuilds the split tables and the tensor-core plan with `o`; the cached
+// CUDA graphs hold the old kernels' tables and are dropped.
+static tk_status apply_tc_options(tk_heff2_plan* plan, const TcOptions& o) {
+    std::string err;
+    tk_status st = rebuild_tc_tables(plan->host, o, err);
+    if (st != TK_OK) {
+        set_error("tc options: " + err);
+        return st;
+    }
+    if (plan->host_exec) {
+        cudaGraphExecDestroy(plan->host_exec);
+        plan->host_exec = nullptr;
+    }
+    plan->lz_graph.reset();
+    if (plan->tc) {
+        std::unique_ptr<TcPlan, TcPlanDeleter> tc;
+        st = guard_host("split-precision plan", err,
+                        [&] { return tc_plan_create(plan->host, plan->lbuf.p, plan->rbuf.p, tc, err); });
+        if (st != TK_OK) {
+            set_error("tc options: " + err);
+            plan->tc.reset();
+            plan->precision = TK_PREC_FP64;
+            return st;
+        }
+        plan->tc = std::move(tc);
+    }
+    return TK_OK;
+}
+
+tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts) {
+    if (!plan || !opts || opts->tall_max_mtiles < 1 || opts->fuse_max_ntiles < 0) {
+        set_error("tk_heff2_set_tc_options: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    if (plan->is_complex) {
+        set_error("tk_heff2_set_tc_options: complex plans run in FP64 only");
+        return TK_ERR_UNSUPPORTED;
+    }
+    DeviceGuard g(plan->device);
+    TcOptions o;
+    o.tall_max_mtiles = opts->tall_max_mtiles;
+    o.fuse_max_ntiles = opts->fuse_max_ntiles;
+    return apply_tc_options(plan, o);
+}
+
+tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts) {
+    if (!plan || !opts) {
+        set_error("tk_heff2_get_tc_options: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    opts->tall_max_mtiles = plan->host.tcopt.tall_max_mtiles;
+    opts->fuse_max_ntiles = plan->host.tcopt.fuse_max_ntiles;
+    return TK_OK;
+}
+
 tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
     if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK)) {
         set_error("tk_heff2_set_schedule: invalid argument");
@@ -765,5 +823,125 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
         }
     }
     for (int stage = 0; stage < 3; ++stage) ms[stage] = (float)(acc[stage] / reps);
+    return TK_OK;
+}
+
+namespace {
+
+// Sector-size histogram class of a plan: quantum-number kind, physical and
+// MPO dimensions, sector counts, and log2 buckets of the largest and the
+// mean sector size of both bonds.
+std::vector<int64_t> histogram_class(const tk_heff2_plan* p) {
+    const Heff2Tables& H = p->host;
+    std::vector<int64_t> key = {H.kind, H.d_i, H.d_j, H.nwl, H.nwr};
+    if (!H.tcsrc) return key;
+    for (const QIndex* q : {&H.tcsrc->QA, &H.tcsrc->QB}) {
+        int64_t mx = 0;
+        for (int64_t d : q->dim) mx = std::max(mx, d);
+        auto lg = [](double v) { return (int64_t)std::floor(2.0 * std::log2(std::max(v, 1.0))); };
+        key.push_back(q->n());
+        key.push_back(lg((double)mx));
+        key.push_back(lg(q->n() ? (double)q->total / q->n() : 0.0));
+    }
+    return key;
+}
+
+std::mutex g_tune_mutex;
+std::map<std::vector<int64_t>, TcOptions> g_tune_cache;
+
+}  // namespace
+
+extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_t use_cache,
+                                       tk_autotune_result* out) {
+    if (!plan || !out || reps < 1) {
+        set_error("tk_heff2_autotune: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    std::memset(out, 0, sizeof(*out));
+    if (plan->is_complex || plan->precision != TK_PREC_BF16X3 || !plan->tc) {
+        set_error("tk_heff2_autotune: tunes split-precision plans only");
+        return TK_ERR_UNSUPPORTED;
+    }
+    DeviceGuard g(plan->device);
+    const std::vector<int64_t> key = histogram_class(plan);
+    if (use_cache) {
+        TcOptions hit;
+        bool found = false;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                hit = it->second;
+                found = true;
+            }
+        }
+        if (found) {
+            tk_status st = TK_OK;
+            if (hit.tall_max_mtiles != plan->host.tcopt.tall_max_mtiles ||
+                hit.fuse_max_ntiles != plan->host.tcopt.fuse_max_ntiles)
+                st = apply_tc_options(plan, hit);
+            if (st != TK_OK) return st;
+            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles};
+            out->from_cache = 1;
+            return TK_OK;
+        }
+    }
+    const int64_t n = plan->host.total;
+    if (n == 0) return TK_OK;
+    tk_status st = ensure_host_staging(plan);
+    if (st != TK_OK) return st;
+    cudaStream_t s = plan->stream;
+    TK_CUDA(launch_fill_start_vector(plan->hx.p, n, s));
+    // candidate schedules; a candidate whose tables come out the same as an
+    // earlier one's is not timed again
+    const TcOptions cand[] = {{3, 0}, {3, 2}, {1 << 30, 0}, {1, 0}, {3, 1}};
+    std::vector<std::vector<size_t>> shapes;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TK_CUDA(cudaEventCreate(&e0));
+    TK_CUDA(cudaEventCreate(&e1));
+    struct EvFree {
+        cudaEvent_t a, b;
+        ~EvFree() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } evf{e0, e1};
+    TcOptions best = plan->host.tcopt;
+    float best_ms = 1e30f;
+    for (const TcOptions& c : cand) {
+        if ((st = apply_tc_options(plan, c)) != TK_OK) return st;
+        const TcTables& C = plan->host.tc;
+        std::vector<size_t> shape = {C.tiles1.size(), C.tiles1x.size(), C.split.size(), C.tiles3.size(),
+                                     C.tiles3f.size(), C.jobs.size()};
+        if (std::find(shapes.begin(), shapes.end(), shape) != shapes.end()) continue;
+        shapes.push_back(shape);
+        for (int w = 0; w < 2; ++w)
+            if ((st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, TK_PREC_BF16X3)) != TK_OK) return st;
+        TK_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r)
+            if ((st = tk_heff2_apply_prec(plan, plan->hx.p, plan->hy.p, s, TK_PREC_BF16X3)) != TK_OK) return st;
+        TK_CUDA(cudaEventRecord(e1, s));
+        TK_CUDA(cudaEventSynchronize(e1));
+        if ((st = tc_check_error(*plan->tc, s)) != TK_OK) return st;
+        float ms = 0.f;
+        TK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= (float)reps;
+        if (out->n_candidates < 8) {
+            out->candidates[out->n_candidates] = {c.tall_max_mtiles, c.fuse_max_ntiles};
+            out->candidate_ms[out->n_candidates] = ms;
+            ++out->n_candidates;
+        }
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    if ((st = apply_tc_options(plan, best)) != TK_OK) return st;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = best;
+    }
+    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles};
+    out->chosen_ms = best_ms;
     return TK_OK;
 }

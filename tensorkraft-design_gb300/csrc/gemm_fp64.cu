@@ -25,9 +25,14 @@ constexpr int BK = 16;
 constexpr int NT = 256;  // 16 x 16 threads
 
 // One E x E output tile (E = 64, 32 or 16): thread (tx, ty) owns the
-// (E/16) x (E/16) outputs (ty + 16 i, tx + 16 j).  Every output sums its
-// segments in order and k ascending inside each, whatever E is, so the tile
-// edge does not change the result.
+// (E/16) x (E/16) outputs (ty + 16 i, tx + 16 j); in a 16 x 16 tile the
+// threads are laid over the valid mv x nv outputs instead (thread t owns
+// (t / nv, t % nv)), so that a sector block of 13 x 13 keeps six warps
+// busy and leaves two idle rather than spreading its outputs over all eight.
+// Every output sums its segments in order and k ascending inside each, and
+// only the k < K of each segment are multiplied, whatever E and the mapping
+// are, so neither changes the result.  Warps without a valid output skip the
+// multiplications (the FP64 pipe is this GPU's bottleneck for these tiles).
 template <int E>
 __device__ __forceinline__ void gemm_tile(const GemmTile& tile, const GemmTask& task, const GemmSeg* __restrict__ segs,
                                           const double* __restrict__ A, const double* __restrict__ B,
@@ -35,7 +40,17 @@ __device__ __forceinline__ void gemm_tile(const GemmTile& tile, const GemmTask& 
                                           int accumulate) {
     constexpr int R = E / 16;
     const int tid = threadIdx.x;
-    const int tx = tid & 15, ty = tid >> 4;
+    const int mv = min(E, task.M - tile.m0), nv = min(E, task.N - tile.n0);
+    int tx = tid & 15, ty = tid >> 4;
+    bool mine = true;
+    if (E == 16) {
+        mine = tid < mv * nv;
+        ty = mine ? tid / nv : 0;
+        tx = mine ? tid - ty * nv : 0;
+    } else {
+        mine = ty < mv && tx < nv;
+    }
+    const bool warp_busy = __any_sync(0xffffffffu, mine);
     double acc[R][R];
 #pragma unroll
     for (int i = 0; i < R; ++i)
@@ -68,21 +83,27 @@ __device__ __forceinline__ void gemm_tile(const GemmTile& tile, const GemmTask& 
                 Bs[k][n] = v;
             }
             __syncthreads();
+            const int kl = min(BK, sg.K - k0);  // k past the segment's K would add zero products
+            if (warp_busy) {
 #pragma unroll
-            for (int k = 0; k < BK; ++k) {
-                double a[R], b[R];
+                for (int k = 0; k < BK; ++k) {
+                    if (k < kl) {
+                        double a[R], b[R];
 #pragma unroll
-                for (int i = 0; i < R; ++i) a[i] = As[k][ty + 16 * i];
+                        for (int i = 0; i < R; ++i) a[i] = As[k][ty + 16 * i];
 #pragma unroll
-                for (int j = 0; j < R; ++j) b[j] = Bs[k][tx + 16 * j];
+                        for (int j = 0; j < R; ++j) b[j] = Bs[k][tx + 16 * j];
 #pragma unroll
-                for (int i = 0; i < R; ++i)
+                        for (int i = 0; i < R; ++i)
 #pragma unroll
-                    for (int j = 0; j < R; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                            for (int j = 0; j < R; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                    }
+                }
             }
             __syncthreads();
         }
     }
+    if (!mine) return;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
         int gm = tile.m0 + ty + 16 * i;

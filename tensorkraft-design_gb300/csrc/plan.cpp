@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <atomic>
+#include <memory>
 #include <numeric>
 #include <system_error>
 #include <thread>
@@ -540,6 +541,336 @@ static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, 
     for (std::thread& t : pool) t.join();
 }
 
+// The split-precision (tensor-core) tables: both GEMM stages regrouped into
+// operand stacks (see TcTables), built from the sector structure of the
+// FP64 tables with the schedule options `o` (tall stage-1 stacks, fused stage
+// 3).  Rebuilt alone when a plan changes its options.
+static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOptions& o, std::string& err) {
+    using Term = TcSource::Term;
+    const int nA = X.nA, nB = X.nB, nWL = X.nWL, nWR = X.nWR;
+    const int64_t P = X.P, nwr = X.nwr;
+    const QIndex &QA = X.QA, &QB = X.QB, &WL = X.WL, &WR = X.WR;
+    const std::vector<int64_t>& lblk = X.lblk;
+    const std::vector<int64_t>& rblk = X.rblk;
+    const std::vector<std::vector<Term>>& byout = X.byout;
+    const std::vector<int>& wl_sec = X.wl_sec;
+    const std::vector<int64_t>& wl_loc = X.wl_loc;
+    auto SUB = [&](int64_t p, int a, int b) -> int64_t { return X.sub[((size_t)p * nA + a) * nB + b]; };
+    (void)WL;
+    {
+        TcTables& C = T.tc;
+        C = TcTables();
+        const int BK = kTcBK;
+        auto kchunks = [&](int64_t K) { return (int32_t)((K + BK - 1) / BK); };
+        std::vector<StackCopy> lcopy, rcopy;
+        // T1 pieces: key (p, A', ws, B) -> (offset of channel-0 row, row stride per a')
+        struct Piece { uint64_t key; int64_t off; int32_t rs; };
+        std::vector<Piece> pieces;
+        auto pkey = [&](int64_t p, int ap, int ws, int b) -> uint64_t {
+            return (((uint64_t)p * nA + ap) * nWL + ws) * nB + b;
+        };
+        int64_t t1off = 0;
+        std::vector<int64_t> tile1_xend;  // per tiles1 entry: end of the psi range it reads
+        // stage 1: one stack per ket sector A
+        for (int a = 0; a < nA; ++a) {
+            std::vector<std::pair<int, int>> lp;   // (A', ws)
+            std::vector<int64_t> lrow;
+            int64_t rows = 0;
+            for (int ap = 0; ap < nA; ++ap)
+                for (int ws = 0; ws < nWL; ++ws)
+                    if (lblk[((size_t)ap * nWL + ws) * nA + a] >= 0) {
+                        lp.push_back({ap, ws});
+                        lrow.push_back(rows);
+                        rows += QA.dim[ap] * WL.dim[ws];
+                    }
+            std::vector<std::pair<int64_t, int>> xp;  // (p, B)
+            for (int64_t p = 0; p < P; ++p)
+                for (int b = 0; b < nB; ++b)
+                    if (SUB(p, a, b) >= 0) xp.push_back({p, b});
+            // columns in the order of their psi sub-blocks in the vector, so that
+            // a tile's columns come from a narrow range of psi
+            std::stable_sort(xp.begin(), xp.end(), [&](const std::pair<int64_t, int>& u, const std::pair<int64_t, int>& v) {
+                return SUB(u.first, a, u.second) < SUB(v.first, a, v.second);
+            });
+            std::vector<int64_t> xcol;
+            int64_t cols = 0;
+            for (const auto& pb : xp) {
+                xcol.push_back(cols);
+                cols += QB.dim[pb.second];
+            }
+            if (rows == 0 || cols == 0) continue;
+            const int64_t K = QA.dim[a];
+            const int32_t kch = kchunks(K);
+            const int64_t lb = C.lq_rows;
+            C.lq_rows += kch * rows;
+            for (size_t i = 0; i < lp.size(); ++i) {
+                int ap = lp[i].first, ws = lp[i].second;
+                lcopy.push_back({T.lbuf.data() + lblk[((size_t)ap * nWL + ws) * nA + a], QA.dim[ap] * WL.dim[ws], K, 0,
+                                 lb + lrow[i], rows});
+            }
+            // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B);
+            // the B operand column b of block (p, B) is column b of the psi sub-block (D_A x D_B)
+            const int64_t colbase0 = (int64_t)C.t1col_base.size();
+            for (size_t jx = 0; jx < xp.size(); ++jx) {
+                const int64_t DB = QB.dim[xp[jx].second];
+                const int64_t src = SUB(xp[jx].first, a, xp[jx].second);
+                for (int64_t b = 0; b < DB; ++b) {
+                    C.t1col_base.push_back(t1off + xcol[jx] * rows + b);
+                    C.t1col_stride.push_back((int32_t)DB);
+                    C.xsrc.push_back(src + b);
+                    C.xstride.push_back((int32_t)DB);
+                }
+            }
+            // tall stacks: psi split once into a bf16 copy (K-major chunks,
+            // column b of block (p, B) on operand row xb + xcol + b of chunk 0)
+            const bool tall = (rows + kTcBM - 1) / kTcBM > o.tall_max_mtiles;
+            const int64_t xb = C.xq_rows;
+            if (tall) {
+                C.xq_rows += kch * cols;
+                for (size_t jx = 0; jx < xp.size(); ++jx) {
+                    TcSplitJob j{};
+                    j.src = SUB(xp[jx].first, a, xp[jx].second);
+                    j.rows = (int32_t)K;
+                    j.cols = (int32_t)QB.dim[xp[jx].second];
+                    j.xrow = (int32_t)(xb + xcol[jx]);
+                    j.cstride = (int32_t)cols;
+                    for (int32_t a0 = 0; a0 < j.rows; a0 += BK)
+                        for (int32_t b0 = 0; b0 < j.cols; b0 += 32) {
+                            j.a0 = a0;
+                            j.b0 = b0;
+                            C.split.push_back(j);
+                        }
+                }
+            }
+            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
+                for (int64_t n0 = 0; n0 < cols; n0 += kTcBN) {
+                    TcTile t{};
+                    t.a_row = (int32_t)(lb + m0); t.a_cs = (int32_t)rows;
+                    t.b_row = tall ? (int32_t)(xb + n0) : 0;
+                    t.b_cs = tall ? (int32_t)cols : 0;
+                    t.k_valid = (int32_t)K;
+                    t.kch = kch;
+                    t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
+                    t.n_valid = (int32_t)std::min<int64_t>(kTcBN, cols - n0);
+                    t.n_mma = (t.n_valid + 15) / 16 * 16;
+                    t.mode = 2;
+                    t.out_off = colbase0 + n0;
+                    t.ldc = (int32_t)m0;
+                    if (!tall) {
+                        // end of the psi range the tile reads (its columns' sub-blocks)
+                        int64_t xend = 0;
+                        for (size_t jx = 0; jx < xp.size(); ++jx) {
+                            const int64_t DB = QB.dim[xp[jx].second];
+                            if (xcol[jx] < n0 + t.n_valid && xcol[jx] + DB > n0)
+                                xend = std::max(xend, SUB(xp[jx].first, a, xp[jx].second) + K * DB);
+                        }
+                        tile1_xend.push_back(xend);
+                    }
+                    (tall ? C.tiles1x : C.tiles1).push_back(t);
+                    C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
+                }
+            for (size_t i = 0; i < lp.size(); ++i)
+                for (size_t jx = 0; jx < xp.size(); ++jx) {
+                    const int64_t DB = QB.dim[xp[jx].second];
+                    // channel-0 row of the slab, row stride per a' = dws rows of D_B
+                    pieces.push_back({pkey(xp[jx].first, lp[i].first, lp[i].second, xp[jx].second),
+                                      t1off + xcol[jx] * rows + lrow[i] * DB, (int32_t)(WL.dim[lp[i].second] * DB)});
+                }
+            t1off += rows * cols;
+        }
+        C.t1_total = t1off;
+        std::sort(pieces.begin(), pieces.end(), [](const Piece& x, const Piece& y) { return x.key < y.key; });
+        // stage 3: one stack per bra sector B' of R
+        for (int bp = 0; bp < nB; ++bp) {
+            std::vector<std::pair<int64_t, int>> yp;  // (p', A')
+            std::vector<int64_t> yr;
+            int64_t rows = 0;
+            for (int64_t p = 0; p < P; ++p)
+                for (int ap = 0; ap < nA; ++ap)
+                    if (SUB(p, ap, bp) >= 0) {
+                        yp.push_back({p, ap});
+                        yr.push_back(rows);
+                        rows += QA.dim[ap];
+                    }
+            if (rows == 0) continue;
+            std::vector<std::pair<int, int>> rp;  // (ws, B)
+            std::vector<int64_t> rk;
+            int64_t K = 0;
+            for (int ws = 0; ws < nWR; ++ws)
+                for (int b = 0; b < nB; ++b)
+                    if (rblk[((size_t)bp * nWR + ws) * nB + b] >= 0) {
+                        rp.push_back({ws, b});
+                        rk.push_back(K);
+                        K += WR.dim[ws] * QB.dim[b];
+                    }
+            const int32_t kch = kchunks(K);
+            const int64_t NB = QB.dim[bp];
+            // the combine fused into the GEMM when the stack has few column tiles
+            // (each column tile rebuilds the operand from T1)
+            const bool fuse = (NB + kTcBN - 1) / kTcBN <= o.fuse_max_ntiles;
+            const int64_t rbase = C.rq_rows, t2b = C.t2q_rows, yb = (int64_t)C.yrow.size();
+            C.rq_rows += kch * NB;
+            if (!fuse) C.t2q_rows += kch * rows;
+            for (size_t i = 0; i < rp.size(); ++i) {
+                int ws = rp[i].first, b = rp[i].second;
+                rcopy.push_back({T.rbuf.data() + rblk[((size_t)bp * nWR + ws) * nB + b], NB, WR.dim[ws] * QB.dim[b], rk[i],
+                                 rbase, NB});
+            }
+            // slabs of the A operand (T2): stack rows [row0, row0 + nr) x K columns
+            // [k0, k0 + nc), element (r, c) = sum_t coef_t * T1[in_off_t + r * in_rs_t + c]
+            struct Slab {
+                int64_t row0;
+                int32_t nr, k0, nc, tb, te;
+            };
+            std::vector<Slab> slabs;
+            std::vector<TcCombTerm> sterms;
+            for (size_t i = 0; i < yp.size(); ++i) {
+                int64_t po = yp[i].first;
+                int ap = yp[i].second;
+                int64_t yo = SUB(po, ap, bp);
+                for (int64_t r = 0; r < QA.dim[ap]; ++r) C.yrow.push_back(yo + r * NB);
+                for (size_t ri = 0; ri < rp.size(); ++ri) {
+                    int ws = rp[ri].first, b = rp[ri].second;
+                    for (int64_t wloc = 0; wloc < WR.dim[ws]; ++wloc) {
+                        int64_t wr = WR.off[ws] + wloc;
+                        Slab sl{yr[i], (int32_t)QA.dim[ap], (int32_t)(rk[ri] + wloc * QB.dim[b]), (int32_t)QB.dim[b],
+                                (int32_t)sterms.size(), 0};
+                        for (const Term& tm : byout[po * nwr + wr]) {
+                            uint64_t key = pkey(tm.p, ap, wl_sec[tm.wl], b);
+                            auto it = std::lower_bound(pieces.begin(), pieces.end(), key,
+                                                       [](const Piece& x, uint64_t k) { return x.key < k; });
+                            for (; it != pieces.end() && it->key == key; ++it) {
+                                TcCombTerm ct{};
+                                ct.in_off = it->off + wl_loc[tm.wl] * (int64_t)(it->rs / WL.dim[wl_sec[tm.wl]]);
+                                ct.in_rs = it->rs;
+                                ct.coef = (float)tm.c;
+                                sterms.push_back(ct);
+                            }
+                        }
+                        sl.te = (int32_t)sterms.size();
+                        if (sl.te > sl.tb) slabs.push_back(sl);
+                    }
+                }
+            }
+            if (!fuse) {
+                // combine jobs: rows of one slab, at most kTcCombMaxElems elements each
+                for (const Slab& sl : slabs) {
+                    TcCombJob j{};
+                    j.t2row = (int32_t)(t2b + sl.row0);
+                    j.cstride = (int32_t)rows;
+                    j.k0 = sl.k0;
+                    j.cols = sl.nc;
+                    j.term_begin = (int32_t)C.terms.size();
+                    C.terms.insert(C.terms.end(), sterms.begin() + sl.tb, sterms.begin() + sl.te);
+                    j.term_end = (int32_t)C.terms.size();
+                    for (int q = 0; q < kTcCombInline && j.term_begin + q < j.term_end; ++q)
+                        j.inl[q] = C.terms[j.term_begin + q];
+                    const int32_t step = std::max<int32_t>(1, kTcCombMaxElems / std::max<int32_t>(1, j.cols));
+                    for (int32_t r0 = 0; r0 < sl.nr; r0 += step) {
+                        j.r0 = r0;
+                        j.rows = std::min(step, sl.nr - r0);
+                        C.jobs.push_back(j);
+                    }
+                }
+            }
+            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM) {
+                int32_t fill0 = -1;
+                if (fuse) {
+                    // fill segments of this row tile, chunk by chunk: every slab part
+                    // inside rows [m0, m0 + 128) and K chunk [64c, 64c + 64)
+                    fill0 = (int32_t)C.fill_chunk.size();
+                    for (int32_t c = 0; c < kch; ++c) {
+                        C.fill_chunk.push_back((int32_t)C.fill_segs.size());
+                        const int64_t ka = (int64_t)c * BK, kb = ka + BK;
+                        for (const Slab& sl : slabs) {
+                            const int64_t ra = std::max<int64_t>(sl.row0, m0);
+                            const int64_t rb = std::min<int64_t>(sl.row0 + sl.nr, m0 + kTcBM);
+                            const int64_t c0 = std::max<int64_t>(sl.k0, ka), c1 = std::min<int64_t>(sl.k0 + sl.nc, kb);
+                            if (ra >= rb || c0 >= c1) continue;
+                            TcFillSeg g{};
+                            g.r0 = (int16_t)(ra - m0);
+                            g.rows = (int16_t)(rb - ra);
+                            g.k0 = (int16_t)(c0 - ka);
+                            g.cols = (int16_t)(c1 - c0);
+                            g.term_begin = (int32_t)C.fill_terms.size();
+                            for (int32_t t = sl.tb; t < sl.te; ++t) {
+                                TcCombTerm ct = sterms[t];
+                                ct.in_off += (ra - sl.row0) * (int64_t)ct.in_rs + (c0 - sl.k0);
+                                C.fill_terms.push_back(ct);
+                            }
+                            g.term_end = (int32_t)C.fill_terms.size();
+                            C.fill_term_elems += (double)g.rows * g.cols * (g.term_end - g.term_begin);
+                            C.fill_segs.push_back(g);
+                        }
+                    }
+                    C.fill_chunk.push_back((int32_t)C.fill_segs.size());
+                }
+                for (int64_t n0 = 0; n0 < NB; n0 += kTcBN) {
+                    TcTile t{};
+                    t.a_row = fuse ? 0 : (int32_t)(t2b + m0);
+                    t.a_cs = fuse ? 0 : (int32_t)rows;
+                    t.b_row = (int32_t)(rbase + n0); t.b_cs = (int32_t)NB;
+                    t.kch = kch;
+                    t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
+                    t.n_valid = (int32_t)std::min<int64_t>(kTcBN, NB - n0);
+                    t.n_mma = (t.n_valid + 15) / 16 * 16;
+                    t.mode = fuse ? 3 : 1;
+                    t.out_off = yb + m0;
+                    t.ldc = 0;
+                    t.n0 = (int32_t)n0;
+                    t.fill0 = fill0;
+                    (fuse ? C.tiles3f : C.tiles3).push_back(t);
+                    C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
+                }
+            }
+        }
+        // heaviest tiles first (K chunks, then padded MMA area): a launch with
+        // more tiles than resident CTAs ends on a tail of light tiles
+        // (LPT order, as tk-linalg/src/tasks.rs:172-174 orders sector tasks)
+        auto lpt = [](std::vector<TcTile>& v) {
+            std::stable_sort(v.begin(), v.end(), [](const TcTile& a, const TcTile& b) {
+                if (a.kch != b.kch) return a.kch > b.kch;
+                return (int64_t)a.m_valid * a.n_mma > (int64_t)b.m_valid * b.n_mma;
+            });
+        };
+        // psi in two halves (a block boundary near the middle): the in-GEMM-split
+        // tiles that read only the first half go first, so a host-buffer matvec
+        // can start them while the second half is still being copied in
+        C.x_split = T.total;
+        for (int64_t o : T.blk_off)
+            if (2 * o >= T.total) {
+                C.x_split = o;
+                break;
+            }
+        {
+            std::vector<TcTile> first, second;
+            for (size_t i = 0; i < C.tiles1.size(); ++i)
+                (tile1_xend[i] <= C.x_split ? first : second).push_back(C.tiles1[i]);
+            lpt(first);
+            lpt(second);
+            C.n1_first = (int32_t)first.size();
+            C.tiles1 = first;
+            C.tiles1.insert(C.tiles1.end(), second.begin(), second.end());
+        }
+        lpt(C.tiles1x);
+        lpt(C.tiles3);
+        lpt(C.tiles3f);
+        for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
+        for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
+        for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
+        for (const TcTile& t : C.tiles3f) C.max_kch3f = std::max(C.max_kch3f, t.kch);
+        // the constant operands as bf16 hi + lo stacks
+        host_alloc_checkpoint();
+        fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
+        fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
+        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
+            err = "tensor-core operand rows exceed 32 bits";
+            return TK_ERR_UNSUPPORTED;
+        }
+        }
+    return TK_OK;
+}
+
 static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR, const tk_bst& wi_abi,
                                          const tk_bst& wj_abi, const int32_t* psi_flux, int tile_m, int tile_n,
                                          Heff2Tables& T, std::string& err, const double* l_blocks,
@@ -784,7 +1115,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
     for (int s = 0; s < nWR; ++s)
         for (int64_t k = 0; k < WR.dim[s]; ++k) { wr_sec[WR.off[s] + k] = s; wr_loc[WR.off[s] + k] = k; }
     // non-zero W_ij terms grouped by (p', wr)
-    struct Term { int64_t p; int64_t wl; double c; };
+    using Term = TcSource::Term;
     std::vector<std::vector<Term>> byout((size_t)(P * nwr));
     int64_t nterms = 0;
     for (int64_t p = 0; p < P; ++p)
@@ -893,315 +1224,18 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
             }
     // --- split-precision regrouping (tensor-core stacks) ---------------------
     {
-        TcTables& C = T.tc;
-        C = TcTables();
-        const int BK = kTcBK;
-        auto kchunks = [&](int64_t K) { return (int32_t)((K + BK - 1) / BK); };
-        std::vector<StackCopy> lcopy, rcopy;
-        // T1 pieces: key (p, A', ws, B) -> (offset of channel-0 row, row stride per a')
-        struct Piece { uint64_t key; int64_t off; int32_t rs; };
-        std::vector<Piece> pieces;
-        auto pkey = [&](int64_t p, int ap, int ws, int b) -> uint64_t {
-            return (((uint64_t)p * nA + ap) * nWL + ws) * nB + b;
-        };
-        int64_t t1off = 0;
-        std::vector<int64_t> tile1_xend;  // per tiles1 entry: end of the psi range it reads
-        // stage 1: one stack per ket sector A
-        for (int a = 0; a < nA; ++a) {
-            std::vector<std::pair<int, int>> lp;   // (A', ws)
-            std::vector<int64_t> lrow;
-            int64_t rows = 0;
-            for (int ap = 0; ap < nA; ++ap)
-                for (int ws = 0; ws < nWL; ++ws)
-                    if (lblk[((size_t)ap * nWL + ws) * nA + a] >= 0) {
-                        lp.push_back({ap, ws});
-                        lrow.push_back(rows);
-                        rows += QA.dim[ap] * WL.dim[ws];
-                    }
-            std::vector<std::pair<int64_t, int>> xp;  // (p, B)
-            for (int64_t p = 0; p < P; ++p)
-                for (int b = 0; b < nB; ++b)
-                    if (SUB(p, a, b) >= 0) xp.push_back({p, b});
-            // columns in the order of their psi sub-blocks in the vector, so that
-            // a tile's columns come from a narrow range of psi
-            std::stable_sort(xp.begin(), xp.end(), [&](const std::pair<int64_t, int>& u, const std::pair<int64_t, int>& v) {
-                return SUB(u.first, a, u.second) < SUB(v.first, a, v.second);
-            });
-            std::vector<int64_t> xcol;
-            int64_t cols = 0;
-            for (const auto& pb : xp) {
-                xcol.push_back(cols);
-                cols += QB.dim[pb.second];
-            }
-            if (rows == 0 || cols == 0) continue;
-            const int64_t K = QA.dim[a];
-            const int32_t kch = kchunks(K);
-            const int64_t lb = C.lq_rows;
-            C.lq_rows += kch * rows;
-            for (size_t i = 0; i < lp.size(); ++i) {
-                int ap = lp[i].first, ws = lp[i].second;
-                lcopy.push_back({T.lbuf.data() + lblk[((size_t)ap * nWL + ws) * nA + a], QA.dim[ap] * WL.dim[ws], K, 0,
-                                 lb + lrow[i], rows});
-            }
-            // T1 of this stack: one row-major [rows x D_B] matrix per column block (p, B);
-            // the B operand column b of block (p, B) is column b of the psi sub-block (D_A x D_B)
-            const int64_t colbase0 = (int64_t)C.t1col_base.size();
-            for (size_t jx = 0; jx < xp.size(); ++jx) {
-                const int64_t DB = QB.dim[xp[jx].second];
-                const int64_t src = SUB(xp[jx].first, a, xp[jx].second);
-                for (int64_t b = 0; b < DB; ++b) {
-                    C.t1col_base.push_back(t1off + xcol[jx] * rows + b);
-                    C.t1col_stride.push_back((int32_t)DB);
-                    C.xsrc.push_back(src + b);
-                    C.xstride.push_back((int32_t)DB);
-                }
-            }
-            // tall stacks: psi split once into a bf16 copy (K-major chunks,
-            // column b of block (p, B) on operand row xb + xcol + b of chunk 0)
-            const bool tall = (rows + kTcBM - 1) / kTcBM > kTcFuseMaxMTiles;
-            const int64_t xb = C.xq_rows;
-            if (tall) {
-                C.xq_rows += kch * cols;
-                for (size_t jx = 0; jx < xp.size(); ++jx) {
-                    TcSplitJob j{};
-                    j.src = SUB(xp[jx].first, a, xp[jx].second);
-                    j.rows = (int32_t)K;
-                    j.cols = (int32_t)QB.dim[xp[jx].second];
-                    j.xrow = (int32_t)(xb + xcol[jx]);
-                    j.cstride = (int32_t)cols;
-                    for (int32_t a0 = 0; a0 < j.rows; a0 += BK)
-                        for (int32_t b0 = 0; b0 < j.cols; b0 += 32) {
-                            j.a0 = a0;
-                            j.b0 = b0;
-                            C.split.push_back(j);
-                        }
-                }
-            }
-            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM)
-                for (int64_t n0 = 0; n0 < cols; n0 += kTcBN) {
-                    TcTile t{};
-                    t.a_row = (int32_t)(lb + m0); t.a_cs = (int32_t)rows;
-                    t.b_row = tall ? (int32_t)(xb + n0) : 0;
-                    t.b_cs = tall ? (int32_t)cols : 0;
-                    t.k_valid = (int32_t)K;
-                    t.kch = kch;
-                    t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
-                    t.n_valid = (int32_t)std::min<int64_t>(kTcBN, cols - n0);
-                    t.n_mma = (t.n_valid + 15) / 16 * 16;
-                    t.mode = 2;
-                    t.out_off = colbase0 + n0;
-                    t.ldc = (int32_t)m0;
-                    if (!tall) {
-                        // end of the psi range the tile reads (its columns' sub-blocks)
-                        int64_t xend = 0;
-                        for (size_t jx = 0; jx < xp.size(); ++jx) {
-                            const int64_t DB = QB.dim[xp[jx].second];
-                            if (xcol[jx] < n0 + t.n_valid && xcol[jx] + DB > n0)
-                                xend = std::max(xend, SUB(xp[jx].first, a, xp[jx].second) + K * DB);
-                        }
-                        tile1_xend.push_back(xend);
-                    }
-                    (tall ? C.tiles1x : C.tiles1).push_back(t);
-                    C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
-                }
-            for (size_t i = 0; i < lp.size(); ++i)
-                for (size_t jx = 0; jx < xp.size(); ++jx) {
-                    const int64_t DB = QB.dim[xp[jx].second];
-                    // channel-0 row of the slab, row stride per a' = dws rows of D_B
-                    pieces.push_back({pkey(xp[jx].first, lp[i].first, lp[i].second, xp[jx].second),
-                                      t1off + xcol[jx] * rows + lrow[i] * DB, (int32_t)(WL.dim[lp[i].second] * DB)});
-                }
-            t1off += rows * cols;
-        }
-        C.t1_total = t1off;
-        std::sort(pieces.begin(), pieces.end(), [](const Piece& x, const Piece& y) { return x.key < y.key; });
-        // stage 3: one stack per bra sector B' of R
-        for (int bp = 0; bp < nB; ++bp) {
-            std::vector<std::pair<int64_t, int>> yp;  // (p', A')
-            std::vector<int64_t> yr;
-            int64_t rows = 0;
-            for (int64_t p = 0; p < P; ++p)
-                for (int ap = 0; ap < nA; ++ap)
-                    if (SUB(p, ap, bp) >= 0) {
-                        yp.push_back({p, ap});
-                        yr.push_back(rows);
-                        rows += QA.dim[ap];
-                    }
-            if (rows == 0) continue;
-            std::vector<std::pair<int, int>> rp;  // (ws, B)
-            std::vector<int64_t> rk;
-            int64_t K = 0;
-            for (int ws = 0; ws < nWR; ++ws)
-                for (int b = 0; b < nB; ++b)
-                    if (rblk[((size_t)bp * nWR + ws) * nB + b] >= 0) {
-                        rp.push_back({ws, b});
-                        rk.push_back(K);
-                        K += WR.dim[ws] * QB.dim[b];
-                    }
-            const int32_t kch = kchunks(K);
-            const int64_t NB = QB.dim[bp];
-            // the combine fused into the GEMM when the stack has few column tiles
-            // (each column tile rebuilds the operand from T1)
-            const bool fuse = (NB + kTcBN - 1) / kTcBN <= kTcFuseMaxNTiles;
-            const int64_t rbase = C.rq_rows, t2b = C.t2q_rows, yb = (int64_t)C.yrow.size();
-            C.rq_rows += kch * NB;
-            if (!fuse) C.t2q_rows += kch * rows;
-            for (size_t i = 0; i < rp.size(); ++i) {
-                int ws = rp[i].first, b = rp[i].second;
-                rcopy.push_back({T.rbuf.data() + rblk[((size_t)bp * nWR + ws) * nB + b], NB, WR.dim[ws] * QB.dim[b], rk[i],
-                                 rbase, NB});
-            }
-            // slabs of the A operand (T2): stack rows [row0, row0 + nr) x K columns
-            // [k0, k0 + nc), element (r, c) = sum_t coef_t * T1[in_off_t + r * in_rs_t + c]
-            struct Slab {
-                int64_t row0;
-                int32_t nr, k0, nc, tb, te;
-            };
-            std::vector<Slab> slabs;
-            std::vector<TcCombTerm> sterms;
-            for (size_t i = 0; i < yp.size(); ++i) {
-                int64_t po = yp[i].first;
-                int ap = yp[i].second;
-                int64_t yo = SUB(po, ap, bp);
-                for (int64_t r = 0; r < QA.dim[ap]; ++r) C.yrow.push_back(yo + r * NB);
-                for (size_t ri = 0; ri < rp.size(); ++ri) {
-                    int ws = rp[ri].first, b = rp[ri].second;
-                    for (int64_t wloc = 0; wloc < WR.dim[ws]; ++wloc) {
-                        int64_t wr = WR.off[ws] + wloc;
-                        Slab sl{yr[i], (int32_t)QA.dim[ap], (int32_t)(rk[ri] + wloc * QB.dim[b]), (int32_t)QB.dim[b],
-                                (int32_t)sterms.size(), 0};
-                        for (const Term& tm : byout[po * nwr + wr]) {
-                            uint64_t key = pkey(tm.p, ap, wl_sec[tm.wl], b);
-                            auto it = std::lower_bound(pieces.begin(), pieces.end(), key,
-                                                       [](const Piece& x, uint64_t k) { return x.key < k; });
-                            for (; it != pieces.end() && it->key == key; ++it) {
-                                TcCombTerm ct{};
-                                ct.in_off = it->off + wl_loc[tm.wl] * (int64_t)(it->rs / WL.dim[wl_sec[tm.wl]]);
-                                ct.in_rs = it->rs;
-                                ct.coef = (float)tm.c;
-                                sterms.push_back(ct);
-                            }
-                        }
-                        sl.te = (int32_t)sterms.size();
-                        if (sl.te > sl.tb) slabs.push_back(sl);
-                    }
-                }
-            }
-            if (!fuse) {
-                // combine jobs: rows of one slab, at most kTcCombMaxElems elements each
-                for (const Slab& sl : slabs) {
-                    TcCombJob j{};
-                    j.t2row = (int32_t)(t2b + sl.row0);
-                    j.cstride = (int32_t)rows;
-                    j.k0 = sl.k0;
-                    j.cols = sl.nc;
-                    j.term_begin = (int32_t)C.terms.size();
-                    C.terms.insert(C.terms.end(), sterms.begin() + sl.tb, sterms.begin() + sl.te);
-                    j.term_end = (int32_t)C.terms.size();
-                    for (int q = 0; q < kTcCombInline && j.term_begin + q < j.term_end; ++q)
-                        j.inl[q] = C.terms[j.term_begin + q];
-                    const int32_t step = std::max<int32_t>(1, kTcCombMaxElems / std::max<int32_t>(1, j.cols));
-                    for (int32_t r0 = 0; r0 < sl.nr; r0 += step) {
-                        j.r0 = r0;
-                        j.rows = std::min(step, sl.nr - r0);
-                        C.jobs.push_back(j);
-                    }
-                }
-            }
-            for (int64_t m0 = 0; m0 < rows; m0 += kTcBM) {
-                int32_t fill0 = -1;
-                if (fuse) {
-                    // fill segments of this row tile, chunk by chunk: every slab part
-                    // inside rows [m0, m0 + 128) and K chunk [64c, 64c + 64)
-                    fill0 = (int32_t)C.fill_chunk.size();
-                    for (int32_t c = 0; c < kch; ++c) {
-                        C.fill_chunk.push_back((int32_t)C.fill_segs.size());
-                        const int64_t ka = (int64_t)c * BK, kb = ka + BK;
-                        for (const Slab& sl : slabs) {
-                            const int64_t ra = std::max<int64_t>(sl.row0, m0);
-                            const int64_t rb = std::min<int64_t>(sl.row0 + sl.nr, m0 + kTcBM);
-                            const int64_t c0 = std::max<int64_t>(sl.k0, ka), c1 = std::min<int64_t>(sl.k0 + sl.nc, kb);
-                            if (ra >= rb || c0 >= c1) continue;
-                            TcFillSeg g{};
-                            g.r0 = (int16_t)(ra - m0);
-                            g.rows = (int16_t)(rb - ra);
-                            g.k0 = (int16_t)(c0 - ka);
-                            g.cols = (int16_t)(c1 - c0);
-                            g.term_begin = (int32_t)C.fill_terms.size();
-                            for (int32_t t = sl.tb; t < sl.te; ++t) {
-                                TcCombTerm ct = sterms[t];
-                                ct.in_off += (ra - sl.row0) * (int64_t)ct.in_rs + (c0 - sl.k0);
-                                C.fill_terms.push_back(ct);
-                            }
-                            g.term_end = (int32_t)C.fill_terms.size();
-                            C.fill_term_elems += (double)g.rows * g.cols * (g.term_end - g.term_begin);
-                            C.fill_segs.push_back(g);
-                        }
-                    }
-                    C.fill_chunk.push_back((int32_t)C.fill_segs.size());
-                }
-                for (int64_t n0 = 0; n0 < NB; n0 += kTcBN) {
-                    TcTile t{};
-                    t.a_row = fuse ? 0 : (int32_t)(t2b + m0);
-                    t.a_cs = fuse ? 0 : (int32_t)rows;
-                    t.b_row = (int32_t)(rbase + n0); t.b_cs = (int32_t)NB;
-                    t.kch = kch;
-                    t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
-                    t.n_valid = (int32_t)std::min<int64_t>(kTcBN, NB - n0);
-                    t.n_mma = (t.n_valid + 15) / 16 * 16;
-                    t.mode = fuse ? 3 : 1;
-                    t.out_off = yb + m0;
-                    t.ldc = 0;
-                    t.n0 = (int32_t)n0;
-                    t.fill0 = fill0;
-                    (fuse ? C.tiles3f : C.tiles3).push_back(t);
-                    C.mma_flops += 2.0 * kTcBM * t.n_mma * (double)kch * BK;
-                }
-            }
-        }
-        // heaviest tiles first (K chunks, then padded MMA area): a launch with
-        // more tiles than resident CTAs ends on a tail of light tiles
-        // (LPT order, as tk-linalg/src/tasks.rs:172-174 orders sector tasks)
-        auto lpt = [](std::vector<TcTile>& v) {
-            std::stable_sort(v.begin(), v.end(), [](const TcTile& a, const TcTile& b) {
-                if (a.kch != b.kch) return a.kch > b.kch;
-                return (int64_t)a.m_valid * a.n_mma > (int64_t)b.m_valid * b.n_mma;
-            });
-        };
-        // psi in two halves (a block boundary near the middle): the in-GEMM-split
-        // tiles that read only the first half go first, so a host-buffer matvec
-        // can start them while the second half is still being copied in
-        C.x_split = T.total;
-        for (int64_t o : T.blk_off)
-            if (2 * o >= T.total) {
-                C.x_split = o;
-                break;
-            }
-        {
-            std::vector<TcTile> first, second;
-            for (size_t i = 0; i < C.tiles1.size(); ++i)
-                (tile1_xend[i] <= C.x_split ? first : second).push_back(C.tiles1[i]);
-            lpt(first);
-            lpt(second);
-            C.n1_first = (int32_t)first.size();
-            C.tiles1 = first;
-            C.tiles1.insert(C.tiles1.end(), second.begin(), second.end());
-        }
-        lpt(C.tiles1x);
-        lpt(C.tiles3);
-        lpt(C.tiles3f);
-        for (const TcTile& t : C.tiles1) C.max_kch1 = std::max(C.max_kch1, t.kch);
-        for (const TcTile& t : C.tiles1x) C.max_kch1x = std::max(C.max_kch1x, t.kch);
-        for (const TcTile& t : C.tiles3) C.max_kch3 = std::max(C.max_kch3, t.kch);
-        for (const TcTile& t : C.tiles3f) C.max_kch3f = std::max(C.max_kch3f, t.kch);
-        // the constant operands as bf16 hi + lo stacks
-        host_alloc_checkpoint();
-        fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
-        fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
-        if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
-            err = "tensor-core operand rows exceed 32 bits";
-            return TK_ERR_UNSUPPORTED;
-        }
+        auto X = std::make_shared<TcSource>();
+        X->nA = nA; X->nB = nB; X->nWL = nWL; X->nWR = nWR; X->P = P; X->nwr = nwr;
+        X->QA = QA; X->QB = QB; X->WL = WL; X->WR = WR;
+        X->lblk = std::move(lblk);
+        X->rblk = std::move(rblk);
+        X->sub = std::move(sub);
+        X->byout = std::move(byout);
+        X->wl_sec = wl_sec;
+        X->wl_loc = wl_loc;
+        T.tcsrc = X;
+        const tk_status st = build_tc_tables(T, *X, T.tcopt, err);
+        if (st != TK_OK) return st;
     }
     lpt_order(T.g1, tile_m, tile_n);
     lpt_order(T.g3, tile_m, tile_n);
@@ -1218,6 +1252,32 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
         return TK_ERR_INVALID_ARG;
     }
     return TK_OK;
+}
+
+}  // namespace tk
+
+namespace tk {
+
+tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err) {
+    if (!T.tcsrc) {
+        err = "the plan keeps no sector structure to rebuild from";
+        return TK_ERR_UNSUPPORTED;
+    }
+    return guard_host("split-precision tables", err, [&]() -> tk_status {
+        TcTables saved = std::move(T.tc);
+        const TcOptions old = T.tcopt;
+        T.tcopt = o;
+        tk_status st = build_tc_tables(T, *T.tcsrc, o, err);
+        if (st == TK_OK && !validate_tables(T, err)) {
+            err = "internal table check failed: " + err;
+            st = TK_ERR_INVALID_ARG;
+        }
+        if (st != TK_OK) {
+            T.tc = std::move(saved);
+            T.tcopt = old;
+        }
+        return st;
+    });
 }
 
 }  // namespace tk

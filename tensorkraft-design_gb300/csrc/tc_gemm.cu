@@ -11,12 +11,12 @@
 //                      psi operand is read from the fp64 vector and split into
 //                      bf16 hi/lo in shared memory by the kernel itself
 //   combine_tc_kernel  W_i*W_j channel combine, T1 -> stage-3 A operand hi/lo
-//                      (stage-3 stacks of more than kTcFuseMaxNTiles column tiles)
+//                      (stage-3 stacks wider than TcOptions::fuse_max_ntiles column tiles)
 //   tc_gemm3f_kernel   stage 3 of the narrow stacks with the combine fused in:
 //                      T2 built in shared memory from T1, then y = T2 * R^T
 //   tc_gemm_kernel     stage 3 of the wide stacks, y = T2_stack(B') * R_stack(B')^T
 //                      (fp64 out via a row table)
-// A stage-1 stack of more than kTcFuseMaxMTiles row tiles would have every row
+// A stage-1 stack of more than TcOptions::tall_max_mtiles row tiles would have every row
 // tile split the same psi columns again; those stacks (the large sectors of
 // wide bonds) take the split copy, made once per matvec, instead.
 //
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
 }
 
 // Stage 3 with the W_i W_j combine fused in (stacks of at most
-// kTcFuseMaxNTiles column tiles).  The R operand (B) comes in by TMA as in
+// TcOptions::fuse_max_ntiles column tiles).  The R operand (B) comes in by TMA as in
 // tc_gemm_kernel; the A operand, T2 = sum_t coef_t * T1, is built chunk by
 // chunk in shared memory by all eight warps from the fill segments of the
 // tile: the chunk is cleared, every segment element is summed in fp32 from

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <array>
 #include <cstdint>
+#include <memory>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -145,7 +146,7 @@ bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>
 // "stacks" that share one operand:
 //   stage 1, one stack per ket sector A of L: rows = every L slab (A', ws, A)
 //     stacked, columns = every psi sub-block (p, A, B) side by side, K = D_A
-//     (stacks of at most kTcFuseMaxMTiles row tiles read and split the psi
+//     (stacks of at most TcOptions::tall_max_mtiles row tiles read and split the psi
 //     operand straight from the fp64 vector inside the stage-1 kernel,
 //     through the per-column tables xsrc / xstride; taller stacks, whose
 //     row tiles would each split the same columns again, take it from a
@@ -161,7 +162,6 @@ bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>
 constexpr int kTcBM = 128;  // rows per tensor-core tile (UMMA M)
 constexpr int kTcBN = 64;   // columns per tensor-core tile (UMMA N)
 constexpr int kTcBK = 64;   // K chunk (128 bytes of bf16: one swizzle atom)
-constexpr int kTcFuseMaxMTiles = 3;  // stage-1 stacks this tall (in row tiles) split psi in the GEMM kernel
 
 struct TcTile {
     int32_t a_row, a_cs;     // A operand row of chunk 0 at this tile's m0; rows between chunks
@@ -173,13 +173,12 @@ struct TcTile {
     int32_t fill0, pad_;     // fused stage 3: chunk c's fill segments are fill_segs[fill_chunk[fill0 + c] ..)
 };
 // Fused stage 3 (the W_i W_j combine inside the stage-3 GEMM): a stage-3
-// stack of at most kTcFuseMaxNTiles column tiles builds its A operand (T2)
-// chunk by chunk in shared memory from T1 instead of reading a T2 written
-// by the combine kernel.  One fill segment = one rectangle of a chunk,
-// element (r, k) = sum_t coef_t * T1[in_off_t + r * in_rs_t + k], written to
-// tile row r0 + r, chunk column k0 + k (terms in TcTables::fill_terms, their
-// in_off at the segment's first element).
-constexpr int kTcFuseMaxNTiles = 2;
+// stack of at most TcOptions::fuse_max_ntiles column tiles builds its A
+// operand (T2) chunk by chunk in shared memory from T1 instead of reading a
+// T2 written by the combine kernel.  One fill segment = one rectangle of a
+// chunk, element (r, k) = sum_t coef_t * T1[in_off_t + r * in_rs_t + k],
+// written to tile row r0 + r, chunk column k0 + k (terms in
+// TcTables::fill_terms, their in_off at the segment's first element).
 struct TcFillSeg {
     int16_t r0, rows;   // tile rows [r0, r0 + rows), r0 + rows <= kTcBM
     int16_t k0, cols;   // chunk columns [k0, k0 + cols), k0 + cols <= kTcBK
@@ -240,6 +239,34 @@ struct TcTables {
     int32_t max_kch1 = 0, max_kch1x = 0, max_kch3 = 0, max_kch3f = 0;
 };
 
+// Schedule options of the split-precision tables (the autotuner's knobs):
+//   tall_max_mtiles: stage-1 stacks of at most this many 128-row tiles split
+//     psi inside the GEMM kernel; taller ones take a split copy made once per
+//     matvec (every row tile would otherwise split the same columns again);
+//   fuse_max_ntiles: stage-3 stacks of at most this many column tiles run the
+//     W_i W_j combine inside the GEMM kernel (0: never; each column tile
+//     rebuilds the operand, so only narrow stacks qualify).
+struct TcOptions {
+    int32_t tall_max_mtiles = 3;
+    int32_t fuse_max_ntiles = 0;
+};
+
+// The sector structure the split-precision tables are built from, kept with
+// the host tables so that a plan can rebuild them with other options.
+struct TcSource {
+    struct Term {
+        int64_t p, wl;
+        double c;
+    };
+    int nA = 0, nB = 0, nWL = 0, nWR = 0;
+    int64_t P = 0, nwr = 0;
+    QIndex QA, QB, WL, WR;
+    std::vector<int64_t> lblk, rblk, sub;  // slab / two-site sub-block offsets (-1: absent)
+    std::vector<std::vector<Term>> byout;  // W_ij terms by (p', w_R)
+    std::vector<int> wl_sec;
+    std::vector<int64_t> wl_loc;
+};
+
 // Everything the device needs for one two-site H_eff, built on the host.
 struct Heff2Tables {
     int kind = 0;
@@ -261,7 +288,11 @@ struct Heff2Tables {
     int64_t n_wij_terms = 0;
     // split-precision (tensor-core) regrouping of the same work
     TcTables tc;
+    TcOptions tcopt;
+    std::shared_ptr<TcSource> tcsrc;
 };
+// Rebuilds T.tc with options `o` (T.tc and T.tcopt unchanged on failure).
+tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err);
 
 // bf16 bit pattern of a float, round to nearest even (NaN kept quiet).
 uint16_t f32_to_bf16_bits(float f);

@@ -76,6 +76,15 @@ class tk_mat_mut(C.Structure):
                 ("col_stride", C.c_int64)]
 
 
+class tk_tc_options(C.Structure):
+    _fields_ = [("tall_max_mtiles", C.c_int32), ("fuse_max_ntiles", C.c_int32)]
+
+
+class tk_autotune_result(C.Structure):
+    _fields_ = [("chosen", tk_tc_options), ("chosen_ms", C.c_float), ("from_cache", C.c_int32),
+                ("n_candidates", C.c_int32), ("candidates", tk_tc_options * 8), ("candidate_ms", C.c_float * 8)]
+
+
 class tk_bst_out(C.Structure):
     _fields_ = [("qn_kind", C.c_int32), ("rank", C.c_int32), ("legs", tk_qindex * 2), ("leg_dirs", C.c_int8 * 2),
                 ("flux", C.c_int32 * 2), ("n_blocks", C.c_int64), ("keys", C.POINTER(C.c_uint64)),
@@ -98,6 +107,9 @@ SIGNATURES = [
     ("tk_debug_fail_host_alloc", None, [C.c_int32]),
     ("tk_debug_fail_device_alloc", None, [C.c_int32]),
     ("tk_heff2_set_cancel_flag", C.c_int32, [C.c_void_p, C.c_void_p]),
+    ("tk_heff2_set_tc_options", C.c_int32, [C.c_void_p, C.POINTER(tk_tc_options)]),
+    ("tk_heff2_get_tc_options", C.c_int32, [C.c_void_p, C.POINTER(tk_tc_options)]),
+    ("tk_heff2_autotune", C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(tk_autotune_result)]),
     ("tk_heff2_inject_error_word", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_dims", C.c_int32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("tk_heff2_blocks", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),

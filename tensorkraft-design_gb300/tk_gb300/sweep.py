@@ -870,6 +870,8 @@ class DeviceDMRG:
     The two-site vector is truncated by split_two_site_device (blocks gathered
     and factors scattered on the GPU, an SVD per bond charge on the host);
     host_split=True takes the host density-matrix path split_two_site instead.
+    autotune: split-precision plans take the autotuner's schedule
+    (tk_heff2_autotune, timed once per sector-size histogram class).
     device_eigh: the truncation's density matrices are diagonalised on the GPU
     in batches (eigh_batch_device) instead of by numpy on a host thread pool
     (the default: faster for the Hubbard D=2048 sweep on a 16-core host)."""
@@ -877,7 +879,7 @@ class DeviceDMRG:
     def __init__(self, model, sites: list, bonds: list, precision: int = PREC_FP64, solver: str = "davidson",
                  tol: float = 1e-10, max_subspace: int = 60, max_iter: int = 1000, inner: int = 40,
                  krylov: int = 20, restarts: int = 10, refine: int = 20, device: int = 0, device_eigh: bool = False,
-                 host_split: bool = False):
+                 host_split: bool = False, autotune: bool = True):
         self.model, self.kind = model, model.kind
         self.n = len(sites)
         self.sites, self.bonds = list(sites), list(bonds)
@@ -888,6 +890,7 @@ class DeviceDMRG:
         self.device = device
         self.eigh_batch = (lambda mats: eigh_batch_device(mats, device)) if device_eigh else None
         self.host_split = host_split or device_eigh
+        self.autotune = autotune
         self.zero = identity(self.kind)
         n = self.n
         self.L = [None] * (n + 1)
@@ -917,6 +920,8 @@ class DeviceDMRG:
         t0 = time.perf_counter()
         plan = Heff2Plan.from_device_envs(self.L[i], self.R[i + 2], self.W[i], self.W[i + 1], self.zero,
                                           precision=self.precision, device=self.device)
+        if self.autotune and plan.precision != PREC_FP64:
+            plan.autotune(reps=3, use_cache=True)  # timed once per sector-size histogram class
         if cancel is not None:
             plan.set_cancel_flag(cancel.word)
         x0 = two_site_product(plan, self.sites[i], self.sites[i + 1])
