@@ -203,12 +203,16 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
  *     a bf16 split copy of psi made once per matvec (default 3);
  *   fuse_max_ntiles: stage-3 stacks of at most this many 64-column tiles run
  *     the W_i W_j combine inside the stage-3 kernel instead of a separate
- *     combine launch (default 0: never).
+ *     combine launch (default 0: never);
+ *   combine_warps: the separate combine runs as persistent warps that load
+ *     their next job while storing the current one (1) or as one CTA per job
+ *     (0, default).
  * tk_heff2_set_tc_options rebuilds the plan's split tables and operands;
  * FP64 matvecs are unaffected.  TK_ERR_UNSUPPORTED for complex plans. */
 typedef struct {
     int32_t tall_max_mtiles;
     int32_t fuse_max_ntiles;
+    int32_t combine_warps;
 } tk_tc_options;
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts);
 tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts);
@@ -218,8 +222,9 @@ tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts
  * candidate schedule on the plan's own sector tables (CUDA events on the
  * plan's stream, after two warm-up matvecs) and keeps the fastest.  The
  * choice is cached process-wide under the plan's sector-size histogram
- * class (quantum-number kind, physical and MPO dimensions, sector counts and
- * log2-bucketed sector sizes of both bonds); with use_cache a plan of a known
+ * class (quantum-number kind, physical and MPO dimensions, and for both bonds
+ * the log2 buckets of the sector count, the largest sector and the total
+ * dimension); with use_cache a plan of a known
  * class takes the cached choice without timing.  `out` receives the choice,
  * its time and up to 8 candidates with their times (ms per matvec). */
 typedef struct {

@@ -467,7 +467,8 @@ static tk_status apply_tc_options(tk_heff2_plan* plan, const TcOptions& o) {
 }
 
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts) {
-    if (!plan || !opts || opts->tall_max_mtiles < 1 || opts->fuse_max_ntiles < 0) {
+    if (!plan || !opts || opts->tall_max_mtiles < 1 || opts->fuse_max_ntiles < 0 || opts->combine_warps < 0 ||
+        opts->combine_warps > 1) {
         set_error("tk_heff2_set_tc_options: invalid argument");
         return TK_ERR_INVALID_ARG;
     }
@@ -479,6 +480,7 @@ tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts
     TcOptions o;
     o.tall_max_mtiles = opts->tall_max_mtiles;
     o.fuse_max_ntiles = opts->fuse_max_ntiles;
+    o.combine_warps = opts->combine_warps;
     return apply_tc_options(plan, o);
 }
 
@@ -489,6 +491,7 @@ tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts
     }
     opts->tall_max_mtiles = plan->host.tcopt.tall_max_mtiles;
     opts->fuse_max_ntiles = plan->host.tcopt.fuse_max_ntiles;
+    opts->combine_warps = plan->host.tcopt.combine_warps;
     return TK_OK;
 }
 
@@ -829,8 +832,9 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
 namespace {
 
 // Sector-size histogram class of a plan: quantum-number kind, physical and
-// MPO dimensions, sector counts, and log2 buckets of the largest and the
-// mean sector size of both bonds.
+// MPO dimensions, and for both bonds the log2 buckets of the sector count,
+// the largest sector and the total dimension (the bonds of one sweep's
+// middle share a class, so the timing is paid once per class).
 std::vector<int64_t> histogram_class(const tk_heff2_plan* p) {
     const Heff2Tables& H = p->host;
     std::vector<int64_t> key = {H.kind, H.d_i, H.d_j, H.nwl, H.nwr};
@@ -838,10 +842,10 @@ std::vector<int64_t> histogram_class(const tk_heff2_plan* p) {
     for (const QIndex* q : {&H.tcsrc->QA, &H.tcsrc->QB}) {
         int64_t mx = 0;
         for (int64_t d : q->dim) mx = std::max(mx, d);
-        auto lg = [](double v) { return (int64_t)std::floor(2.0 * std::log2(std::max(v, 1.0))); };
-        key.push_back(q->n());
+        auto lg = [](double v) { return (int64_t)std::floor(std::log2(std::max(v, 1.0))); };
+        key.push_back(lg((double)q->n()));
         key.push_back(lg((double)mx));
-        key.push_back(lg(q->n() ? (double)q->total / q->n() : 0.0));
+        key.push_back(lg((double)q->total));
     }
     return key;
 }
@@ -878,10 +882,11 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         if (found) {
             tk_status st = TK_OK;
             if (hit.tall_max_mtiles != plan->host.tcopt.tall_max_mtiles ||
-                hit.fuse_max_ntiles != plan->host.tcopt.fuse_max_ntiles)
+                hit.fuse_max_ntiles != plan->host.tcopt.fuse_max_ntiles ||
+                hit.combine_warps != plan->host.tcopt.combine_warps)
                 st = apply_tc_options(plan, hit);
             if (st != TK_OK) return st;
-            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles};
+            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles, hit.combine_warps};
             out->from_cache = 1;
             return TK_OK;
         }
@@ -894,7 +899,7 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
     TK_CUDA(launch_fill_start_vector(plan->hx.p, n, s));
     // candidate schedules; a candidate whose tables come out the same as an
     // earlier one's is not timed again
-    const TcOptions cand[] = {{3, 0}, {3, 2}, {1 << 30, 0}, {1, 0}, {3, 1}};
+    const TcOptions cand[] = {{3, 0, 0}, {3, 0, 1}, {3, 2, 0}, {1 << 30, 0, 0}, {1, 0, 0}, {1, 0, 1}, {3, 1, 1}};
     std::vector<std::vector<size_t>> shapes;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TK_CUDA(cudaEventCreate(&e0));
@@ -912,7 +917,7 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         if ((st = apply_tc_options(plan, c)) != TK_OK) return st;
         const TcTables& C = plan->host.tc;
         std::vector<size_t> shape = {C.tiles1.size(), C.tiles1x.size(), C.split.size(), C.tiles3.size(),
-                                     C.tiles3f.size(), C.jobs.size()};
+                                     C.tiles3f.size(), C.jobs.size(), C.jobs.empty() ? 0u : (size_t)c.combine_warps};
         if (std::find(shapes.begin(), shapes.end(), shape) != shapes.end()) continue;
         shapes.push_back(shape);
         for (int w = 0; w < 2; ++w)
@@ -927,7 +932,7 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         TK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         ms /= (float)reps;
         if (out->n_candidates < 8) {
-            out->candidates[out->n_candidates] = {c.tall_max_mtiles, c.fuse_max_ntiles};
+            out->candidates[out->n_candidates] = {c.tall_max_mtiles, c.fuse_max_ntiles, c.combine_warps};
             out->candidate_ms[out->n_candidates] = ms;
             ++out->n_candidates;
         }
@@ -941,7 +946,7 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache[key] = best;
     }
-    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles};
+    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles, best.combine_warps};
     out->chosen_ms = best_ms;
     return TK_OK;
 }

@@ -918,6 +918,104 @@ __global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCo
     }
 }
 
+// The same combine as persistent warps: every warp takes jobs j = w, w + W,
+// ... (W warps in the grid) and loads the T1 values of its next job before it
+// sums and stores the current one, so each warp keeps a job's loads in flight
+// while the previous job retires (one CTA per job pays every job's load
+// latency in full, in several waves of small CTAs).  Jobs of at most
+// kTcCombInline terms use their inline terms; longer ones read the rest from
+// the table.  Each lane owns elements lane + 32 u of the job (u < 16: jobs
+// have at most kTcCombMaxElems elements unless one row is longer, and a
+// longer row is walked in further passes).
+constexpr int kCombWarpU = kTcCombMaxElems / 32;
+
+struct CombPrefetch {
+    float v[kTcCombInline][kCombWarpU];
+};
+
+__device__ __forceinline__ void comb_warp_load(const TcCombJob& j, const float* __restrict__ t1, int lane, int e0,
+                                               CombPrefetch& p) {
+    const int n = j.rows * j.cols;
+    const int nterm = min(j.term_end - j.term_begin, kTcCombInline);
+#pragma unroll
+    for (int u = 0; u < kCombWarpU; ++u) {
+        const int e = e0 + u * 32 + lane;
+        const bool ok = e < n;
+        const int rl = ok ? e / j.cols : 0;
+        const int c = ok ? e - rl * j.cols : 0;
+        const int r = j.r0 + rl;
+#pragma unroll
+        for (int q = 0; q < kTcCombInline; ++q)
+            p.v[q][u] = (ok && q < nterm) ? __ldg(t1 + j.inl[q].in_off + (int64_t)r * j.inl[q].in_rs + c) : 0.f;
+    }
+}
+
+__device__ __forceinline__ void comb_warp_store(const TcCombJob& j, const TcCombTerm* __restrict__ terms,
+                                                const float* __restrict__ t1, int lane, int e0,
+                                                const CombPrefetch& p, __nv_bfloat16* __restrict__ th,
+                                                __nv_bfloat16* __restrict__ tl) {
+    const int n = j.rows * j.cols;
+    const int nterm = j.term_end - j.term_begin;
+#pragma unroll
+    for (int u = 0; u < kCombWarpU; ++u) {
+        const int e = e0 + u * 32 + lane;
+        if (e >= n) continue;
+        const int rl = e / j.cols;
+        const int c = e - rl * j.cols;
+        const int r = j.r0 + rl;
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < kTcCombInline; ++q)
+            if (q < nterm) acc = fmaf(j.inl[q].coef, p.v[q][u], acc);
+        for (int t = kTcCombInline; t < nterm; ++t) {  // terms past the inline ones
+            const TcCombTerm tm = terms[j.term_begin + t];
+            acc = fmaf(tm.coef, __ldg(t1 + tm.in_off + (int64_t)r * tm.in_rs + c), acc);
+        }
+        const int k = j.k0 + c;
+        const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r) << 6) + (k & 63);
+        const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+        th[idx] = h;
+        tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) combine_tc_warp_kernel(const TcCombJob* __restrict__ jobs, int njobs,
+                                                                const TcCombTerm* __restrict__ terms,
+                                                                const float* __restrict__ t1,
+                                                                __nv_bfloat16* __restrict__ th,
+                                                                __nv_bfloat16* __restrict__ tl) {
+    grid_dep_launch();
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int W = gridDim.x * (blockDim.x >> 5);
+    grid_dep_wait();
+    int j = w;
+    if (j >= njobs) return;
+    TcCombJob cur = jobs[j];
+    CombPrefetch pc;
+    comb_warp_load(cur, t1, lane, 0, pc);
+    while (true) {
+        const int jn = j + W;
+        TcCombJob nxt{};
+        CombPrefetch pn;
+        if (jn < njobs) {
+            nxt = jobs[jn];
+            comb_warp_load(nxt, t1, lane, 0, pn);
+        }
+        const int n = cur.rows * cur.cols;
+        comb_warp_store(cur, terms, t1, lane, 0, pc, th, tl);
+        for (int e0 = 32 * kCombWarpU; e0 < n; e0 += 32 * kCombWarpU) {  // one long row past 512 elements
+            CombPrefetch px;
+            comb_warp_load(cur, t1, lane, e0, px);
+            comb_warp_store(cur, terms, t1, lane, e0, px, th, tl);
+        }
+        if (jn >= njobs) break;
+        j = jn;
+        cur = nxt;
+        pc = pn;
+    }
+}
+
 template <class T>
 cudaError_t put(T** dst, const std::vector<T>& v) {
     *dst = nullptr;
@@ -970,6 +1068,7 @@ struct TcPlan {
     TcFillSeg* fill_segs = nullptr;
     TcCombTerm* fill_terms = nullptr;
     int n3f = 0;
+    bool comb_warps = false;            // persistent-warp combine (TcOptions::combine_warps)
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
     __nv_bfloat16 *th = nullptr, *tl = nullptr;
     __nv_bfloat16 *xh = nullptr, *xl = nullptr;  // split copy of psi (tall stage-1 stacks)
@@ -1043,6 +1142,7 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
     p->n3f = (int)C.tiles3f.size();
+    p->comb_warps = host.tcopt.combine_warps != 0;
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
@@ -1137,7 +1237,11 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
         launch_tc_gemm(tc.nst1x, tc.n1x, tc.tiles1x, tc.mLh, tc.mLl, tc.mXh, tc.mXl, om, CONST_A, tc.err, s);
         launch_stage1_fused(tc, x, 0, tc.n1, s);
     } else if (stage == 1) {
-        if (tc.njobs > 0)
+        if (tc.njobs > 0 && tc.comb_warps)
+            launch_pdl(combine_tc_warp_kernel, std::min(tc.njobs, 152 * 2 * 8) / 8 + 1, 256, 0, s,
+                       (const TcCombJob*)tc.jobs, tc.njobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1,
+                       tc.th, tc.tl);
+        else if (tc.njobs > 0)
             launch_pdl(combine_tc_kernel, tc.njobs, kCombThreads, 0, s, (const TcCombJob*)tc.jobs,
                        (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
     } else {

@@ -246,9 +246,12 @@ struct TcTables {
 //   fuse_max_ntiles: stage-3 stacks of at most this many column tiles run the
 //     W_i W_j combine inside the GEMM kernel (0: never; each column tile
 //     rebuilds the operand, so only narrow stacks qualify).
+//   combine_warps: the separate combine as persistent warps that prefetch
+//     their next job (1) or as one CTA per job (0).
 struct TcOptions {
     int32_t tall_max_mtiles = 3;
     int32_t fuse_max_ntiles = 0;
+    int32_t combine_warps = 0;
 };
 
 // The sector structure the split-precision tables are built from, kept with

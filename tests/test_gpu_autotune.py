@@ -11,7 +11,7 @@ from tk_gb300 import PREC_BF16X3
 
 pytestmark = pytest.mark.gpu
 SPLIT_TOL = 2e-4
-OPTIONS = [(3, 0), (3, 2), (1 << 30, 0), (1, 0), (3, 1), (1, 8)]
+OPTIONS = [(3, 0, 0), (3, 0, 1), (3, 2, 0), (1 << 30, 0, 1), (1, 0, 0), (3, 1, 1), (1, 8, 0)]
 
 
 def _run(plan, x):
@@ -30,21 +30,28 @@ def test_every_schedule_matches_the_oracle(lib_built, name, D):
     plan = p.plan(precision=PREC_BF16X3)
     x = np.random.default_rng(11).standard_normal(plan.block_dim)
     ref = oracle_bs(p).apply(x)
-    for tall, fuse in OPTIONS:
-        plan.set_tc_options(tall, fuse)
-        assert plan.tc_options() == {"tall_max_mtiles": tall, "fuse_max_ntiles": fuse}
+    ys = {}
+    for tall, fuse, warps in OPTIONS:
+        plan.set_tc_options(tall, fuse, warps)
+        assert plan.tc_options() == {"tall_max_mtiles": tall, "fuse_max_ntiles": fuse, "combine_warps": warps}
         y = _run(plan, x)
         assert np.isfinite(y).all()
-        assert rel_err(y, ref) < SPLIT_TOL, (tall, fuse)
+        assert rel_err(y, ref) < SPLIT_TOL, (tall, fuse, warps)
+        ys[(tall, fuse, warps)] = y
+    # the combine's two launch forms compute the same numbers, bit for bit
+    assert np.array_equal(ys[(3, 0, 0)], ys[(3, 0, 1)])
 
 
 def test_fused_stage3_full_size(lib_built):
-    """The fused combine + stage-3 kernel on the full Hubbard D=2048 workload."""
+    """The fused combine + stage-3 kernel and the persistent-warp combine on the
+    full Hubbard D=2048 workload."""
     p = models.workload("hubbard_d2048")
     plan = p.plan(precision=PREC_BF16X3)
-    plan.set_tc_options(3, 2)
     x = np.random.default_rng(3).standard_normal(plan.block_dim)
-    assert rel_err(_run(plan, x), oracle_bs(p).apply(x)) < SPLIT_TOL
+    ref = oracle_bs(p).apply(x)
+    for opts in ((3, 2, 0), (3, 0, 1)):
+        plan.set_tc_options(*opts)
+        assert rel_err(_run(plan, x), ref) < SPLIT_TOL, opts
 
 
 def test_autotune_keeps_the_fastest_and_caches(lib_built):
@@ -53,7 +60,7 @@ def test_autotune_keeps_the_fastest_and_caches(lib_built):
     r = plan.autotune(reps=3, use_cache=False)
     assert not r["from_cache"] and len(r["candidates"]) >= 2
     best = min(r["candidates"], key=lambda c: c["ms"])
-    assert r["chosen"] == {"tall_max_mtiles": best["tall_max_mtiles"], "fuse_max_ntiles": best["fuse_max_ntiles"]}
+    assert r["chosen"] == {k: best[k] for k in ("tall_max_mtiles", "fuse_max_ntiles", "combine_warps")}
     assert plan.tc_options() == r["chosen"]
     # a second plan of the same histogram class takes the cached choice
     plan2 = p.plan(precision=PREC_BF16X3)
