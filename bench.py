@@ -73,6 +73,9 @@ def parse():
     ap.add_argument("--ref-seconds", type=float, default=8.0,
                     help="--impl reference: time at least this long (and at least --steps matvecs)")
     ap.add_argument("--cpu-child", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: time the split-precision schedule candidates and keep the fastest; 0: the default "
+                         "schedule (for profiler launch lists)")
     ap.add_argument("--tdvp-steps", type=int, default=0, metavar="K",
                     help="also time K real-time TDVP steps of the impurity Green's function (Anderson chain, "
                          "16 sites, D=1024, dt=0.05, Krylov 16) after a split-precision DMRG ground state")
@@ -591,7 +594,8 @@ def run_ours(args):
         plan.set_precision(PREC_BF16X3)
         prec_name = "bf16x3"
         # the autotuner times the candidate schedules on this workload and keeps the fastest
-        tune = plan.autotune(reps=10, use_cache=False)
+        if args.autotune:
+            tune = plan.autotune(reps=10, use_cache=False)
     n = plan.block_dim
     flops_total, alg_bytes = plan.cost()
     launches_per_matvec = plan.launches()
