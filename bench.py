@@ -88,13 +88,15 @@ def parse():
 
 
 def compare_schedules(plan, x, y, torch, dev, steps: int, flush):
-    """FP64 matvec/s with the grouped launch and with one launch per output block."""
+    """FP64 matvec/s with the grouped launch, with one launch per output block
+    and on operand stacks."""
     from tk_gb300 import PREC_BF16X3, PREC_FP64, _abi
 
     prec = plan.precision
     plan.set_precision(PREC_FP64)
     out = {}
-    for name, sched in (("fp64_grouped", _abi.SCHED_GROUPED), ("fp64_per_block", _abi.SCHED_PER_BLOCK)):
+    for name, sched in (("fp64_grouped", _abi.SCHED_GROUPED), ("fp64_per_block", _abi.SCHED_PER_BLOCK),
+                        ("fp64_stacked", _abi.SCHED_STACKED)):
         plan.set_schedule(sched)
         plan.apply(x, y)
         torch.cuda.synchronize(dev)
@@ -111,6 +113,7 @@ def compare_schedules(plan, x, y, torch, dev, steps: int, flush):
     plan.set_schedule(_abi.SCHED_GROUPED)
     plan.set_precision(prec)
     out["grouped_speedup"] = out["fp64_grouped"] / out["fp64_per_block"]
+    out["stacked_speedup"] = out["fp64_stacked"] / out["fp64_grouped"]
     return out
 
 

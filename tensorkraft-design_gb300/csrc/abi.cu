@@ -348,6 +348,10 @@ static cudaError_t launch_per_block(const DevGemm& g, const double* A, const dou
 
 // The FP64 matvec: three stream-ordered stages.
 static tk_status apply_fp64(tk_heff2_plan* p, const double* x, double* y, cudaStream_t s) {
+    if (p->schedule == TK_SCHED_STACKED) {
+        TK_CUDA(f64stack_apply(*p->f64s, x, y, s));
+        return TK_OK;
+    }
     if (p->schedule == TK_SCHED_PER_BLOCK) {
         TK_CUDA(launch_per_block(p->g1, p->lbuf.p, x, p->t1.p, s));
         TK_CUDA(launch_combine_f64(p->jobs.p, p->n_jobs, p->terms.p, p->t1.p, p->t2.p, s));
@@ -377,6 +381,8 @@ extern "C" tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_a
         n = 4 * (p->g1.n_tiles > 0) + 2 * (p->n_jobs > 0) + 4 * (p->g3.n_tiles > 0);
     } else if (p->precision == TK_PREC_BF16X3) {
         n = tc_launches(*p->tc);
+    } else if (p->schedule == TK_SCHED_STACKED) {
+        n = f64stack_launches(*p->f64s);
     } else if (p->schedule == TK_SCHED_PER_BLOCK) {
         n = per_block_launches(p->g1) + (p->n_jobs > 0) + per_block_launches(p->g3);
     } else {
@@ -496,10 +502,29 @@ tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts
 }
 
 tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
-    if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK)) {
+    if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK && schedule != TK_SCHED_STACKED)) {
         set_error("tk_heff2_set_schedule: invalid argument");
         return TK_ERR_INVALID_ARG;
     }
+    if (schedule == TK_SCHED_STACKED && !plan->f64s) {
+        if (plan->is_complex) {
+            set_error("tk_heff2_set_schedule: the stacked schedule takes real plans only");
+            return TK_ERR_UNSUPPORTED;
+        }
+        DeviceGuard g(plan->device);
+        std::string err;
+        tk_status st = build_f64_stacks(plan->host, err);
+        if (st == TK_OK)
+            st = guard_host("stacked FP64 plan", err, [&] { return f64stack_create(plan->host.f64st, plan->f64s, err); });
+        // the device copy is the one that runs: the host tables go
+        plan->host.f64st = TcTables();
+        if (st != TK_OK) {
+            plan->f64s.reset();
+            set_error("tk_heff2_set_schedule: " + err);
+            return st;
+        }
+    }
+    if (plan->schedule != schedule) plan->lz_graph.reset();  // captured with the old schedule's kernels
     plan->schedule = schedule;
     return TK_OK;
 }
@@ -778,6 +803,10 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
             bytes[0] = 8.0 * H.total + b16 * (double)C.lq_rows + 4.0 * C.t1_total;
             bytes[1] = C.jobs.empty() ? 0.0 : t1_comb + b16 * (double)C.t2q_rows;
             bytes[2] = b16 * (double)C.t2q_rows + t1_fused + b16 * (double)C.rq_rows + 8.0 * H.total;
+        } else if (p->schedule == TK_SCHED_STACKED) {
+            f64stack_bytes(*p->f64s, bytes);
+            bytes[0] += 8.0 * H.total;
+            bytes[2] += 8.0 * H.total;
         } else {
             bytes[0] = 8.0 * ((double)H.lbuf.size() + H.total + H.t1_total);
             bytes[1] = 8.0 * ((double)H.t1_total + H.t2_total);
@@ -801,6 +830,8 @@ extern "C" tk_status tk_heff2_profile(tk_heff2_plan* plan, const double* x_dev, 
                 cudaError_t e = tc_apply_stage(*p->tc, p->host, p->jobs.p, p->n_jobs, p->terms.p, x_dev, y_dev, s,
                                                stage, err);
                 if (e != cudaSuccess) return cuda_fail(err.c_str(), e);
+            } else if (p->schedule == TK_SCHED_STACKED) {
+                TK_CUDA(f64stack_stage(*p->f64s, x_dev, y_dev, s, stage));
             } else if (stage == 0) {
                 if (p->schedule == TK_SCHED_PER_BLOCK)
                     TK_CUDA(launch_per_block(p->g1, p->lbuf.p, x_dev, p->t1.p, s));

@@ -343,11 +343,39 @@ bool comb_table_ok(const std::vector<CombJob>& jobs, const std::vector<CombTerm>
     return true;
 }
 
+static bool validate_tc(const Heff2Tables& T, const TcTables& C, std::string& err);
+
 static bool validate_tables(const Heff2Tables& T, std::string& err) {
     if (!gemm_table_ok(T.g1, (int64_t)T.lbuf.size(), T.total, T.t1_total, "stage 1", err)) return false;
     if (!gemm_table_ok(T.g3, T.t2_total, (int64_t)T.rbuf.size(), T.total, "stage 3", err)) return false;
     if (!comb_table_ok(T.jobs, T.terms, T.t1_total, T.t2_total, err)) return false;
-    const TcTables& C = T.tc;
+    return validate_tc(T, T.tc, err);
+}
+
+// Every access of the split (or stacked FP64) tables checked against its buffer.
+static bool validate_tc(const Heff2Tables& T, const TcTables& C, std::string& err) {
+    if (!C.term_coef64.empty() && C.term_coef64.size() != C.terms.size()) {
+        err = "FP64 combine coefficients";
+        return false;
+    }
+    // operand stacks: the last row a tile reads (TMA reads past the end
+    // would be zero-filled; the stacked FP64 kernels read them directly)
+    auto last_row = [](int32_t row, int32_t cs, int32_t kch, int32_t valid) {
+        return (int64_t)row + (int64_t)std::max(kch - 1, 0) * cs + valid - 1;
+    };
+    for (const TcTile& t : C.tiles3)
+        if (t.k_valid < 0 || t.k_valid > t.kch * kTcBK || t.a_cs < 0 || t.b_cs < 0 ||
+            (t.kch > 0 && (last_row(t.a_row, t.a_cs, t.kch, t.m_valid) >= C.t2q_rows ||
+                           last_row(t.b_row, t.b_cs, t.kch, t.n_valid) >= C.rq_rows))) {
+            err = "tensor-core stage 3 operand";
+            return false;
+        }
+    for (const std::vector<TcTile>* v : {&C.tiles1, &C.tiles1x})
+        for (const TcTile& t : *v)
+            if (t.a_cs < 0 || (t.kch > 0 && last_row(t.a_row, t.a_cs, t.kch, t.m_valid) >= C.lq_rows)) {
+                err = "tensor-core stage 1 operand";
+                return false;
+            }
     if (C.t1col_base.size() != C.t1col_stride.size() || C.xsrc.size() != C.t1col_base.size() ||
         C.xstride.size() != C.t1col_base.size()) {
         err = "T1 column tables";
@@ -541,11 +569,27 @@ static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, 
     for (std::thread& t : pool) t.join();
 }
 
+// The same stacks in FP64 (the stacked FP64 schedule): element for element
+// the environment values, zero where no slab lands.
+static void fill_stacks_f64(const std::vector<StackCopy>& jobs, int64_t rows, std::vector<double>& out) {
+    const int BK = kTcBK;
+    out.assign((size_t)rows * BK, 0.0);
+    for (const StackCopy& c : jobs)
+        for (int64_t r = 0; r < c.nr; ++r) {
+            const double* src = c.src + r * c.len;
+            for (int64_t kk = 0; kk < c.len; ++kk) {
+                const int64_t k = c.k_off + kk;
+                out[(size_t)(c.row0 + (k / BK) * c.chunk_rows + r) * BK + (size_t)(k % BK)] = src[kk];
+            }
+        }
+}
+
 // The split-precision (tensor-core) tables: both GEMM stages regrouped into
 // operand stacks (see TcTables), built from the sector structure of the
 // FP64 tables with the schedule options `o` (tall stage-1 stacks, fused stage
 // 3).  Rebuilt alone when a plan changes its options.
-static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOptions& o, std::string& err) {
+static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOptions& o, TcTables& C, bool fp64,
+                                 std::string& err) {
     using Term = TcSource::Term;
     const int nA = X.nA, nB = X.nB, nWL = X.nWL, nWR = X.nWR;
     const int64_t P = X.P, nwr = X.nwr;
@@ -558,7 +602,6 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
     auto SUB = [&](int64_t p, int a, int b) -> int64_t { return X.sub[((size_t)p * nA + a) * nB + b]; };
     (void)WL;
     {
-        TcTables& C = T.tc;
         C = TcTables();
         const int BK = kTcBK;
         auto kchunks = [&](int64_t K) { return (int32_t)((K + BK - 1) / BK); };
@@ -724,6 +767,7 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
             };
             std::vector<Slab> slabs;
             std::vector<TcCombTerm> sterms;
+            std::vector<double> scoef;  // the same coefficients in FP64
             for (size_t i = 0; i < yp.size(); ++i) {
                 int64_t po = yp[i].first;
                 int ap = yp[i].second;
@@ -745,6 +789,7 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
                                 ct.in_rs = it->rs;
                                 ct.coef = (float)tm.c;
                                 sterms.push_back(ct);
+                                scoef.push_back(tm.c);
                             }
                         }
                         sl.te = (int32_t)sterms.size();
@@ -762,6 +807,7 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
                     j.cols = sl.nc;
                     j.term_begin = (int32_t)C.terms.size();
                     C.terms.insert(C.terms.end(), sterms.begin() + sl.tb, sterms.begin() + sl.te);
+                    C.term_coef64.insert(C.term_coef64.end(), scoef.begin() + sl.tb, scoef.begin() + sl.te);
                     j.term_end = (int32_t)C.terms.size();
                     for (int q = 0; q < kTcCombInline && j.term_begin + q < j.term_end; ++q)
                         j.inl[q] = C.terms[j.term_begin + q];
@@ -811,6 +857,7 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
                     t.a_cs = fuse ? 0 : (int32_t)rows;
                     t.b_row = (int32_t)(rbase + n0); t.b_cs = (int32_t)NB;
                     t.kch = kch;
+                    t.k_valid = (int32_t)K;
                     t.m_valid = (int32_t)std::min<int64_t>(kTcBM, rows - m0);
                     t.n_valid = (int32_t)std::min<int64_t>(kTcBN, NB - n0);
                     t.n_mma = (t.n_valid + 15) / 16 * 16;
@@ -861,8 +908,13 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
         for (const TcTile& t : C.tiles3f) C.max_kch3f = std::max(C.max_kch3f, t.kch);
         // the constant operands as bf16 hi + lo stacks
         host_alloc_checkpoint();
-        fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
-        fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
+        if (fp64) {
+            fill_stacks_f64(lcopy, C.lq_rows, C.lq64);
+            fill_stacks_f64(rcopy, C.rq_rows, C.rq64);
+        } else {
+            fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
+            fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
+        }
         if (C.lq_rows > INT32_MAX || C.rq_rows > INT32_MAX || C.xq_rows > INT32_MAX || C.t2q_rows > INT32_MAX) {
             err = "tensor-core operand rows exceed 32 bits";
             return TK_ERR_UNSUPPORTED;
@@ -1234,7 +1286,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
         X->wl_sec = wl_sec;
         X->wl_loc = wl_loc;
         T.tcsrc = X;
-        const tk_status st = build_tc_tables(T, *X, T.tcopt, err);
+        const tk_status st = build_tc_tables(T, *X, T.tcopt, T.tc, false, err);
         if (st != TK_OK) return st;
     }
     lpt_order(T.g1, tile_m, tile_n);
@@ -1258,6 +1310,26 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
 
 namespace tk {
 
+tk_status build_f64_stacks(Heff2Tables& T, std::string& err) {
+    if (!T.tcsrc) {
+        err = "the plan keeps no sector structure to build from";
+        return TK_ERR_UNSUPPORTED;
+    }
+    return guard_host("stacked FP64 tables", err, [&]() -> tk_status {
+        TcOptions o;
+        o.tall_max_mtiles = 1 << 30;  // every stage-1 column read from psi through its table
+        o.fuse_max_ntiles = 0;        // every stage-3 stack reads a combined T2
+        TcTables C;
+        tk_status st = build_tc_tables(T, *T.tcsrc, o, C, true, err);
+        if (st == TK_OK && !validate_tc(T, C, err)) {
+            err = "internal table check failed: " + err;
+            st = TK_ERR_INVALID_ARG;
+        }
+        if (st == TK_OK) T.f64st = std::move(C);
+        return st;
+    });
+}
+
 tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err) {
     if (!T.tcsrc) {
         err = "the plan keeps no sector structure to rebuild from";
@@ -1267,7 +1339,7 @@ tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err
         TcTables saved = std::move(T.tc);
         const TcOptions old = T.tcopt;
         T.tcopt = o;
-        tk_status st = build_tc_tables(T, *T.tcsrc, o, err);
+        tk_status st = build_tc_tables(T, *T.tcsrc, o, T.tc, false, err);
         if (st == TK_OK && !validate_tables(T, err)) {
             err = "internal table check failed: " + err;
             st = TK_ERR_INVALID_ARG;

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <atomic>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "tc_gemm.cuh"
@@ -82,6 +83,20 @@ struct LanczosGraphDeleter {
     void operator()(LanczosGraph* g) const;
 };
 
+// The stacked FP64 schedule's device operands (stack_f64.cu), built from
+// Heff2Tables::f64st on the first TK_SCHED_STACKED request.
+struct F64Stack;
+struct F64StackDeleter {
+    void operator()(F64Stack* p) const;
+};
+tk_status f64stack_create(const TcTables& C, std::unique_ptr<F64Stack, F64StackDeleter>& out, std::string& err);
+// stage 0: T1 = L stacks * psi; 1: the W_i W_j combine into T2; 2: y = T2 * R stacks
+cudaError_t f64stack_stage(F64Stack& p, const double* x, double* y, cudaStream_t s, int stage);
+cudaError_t f64stack_apply(F64Stack& p, const double* x, double* y, cudaStream_t s);
+int f64stack_launches(const F64Stack& p);
+// Bytes per stage a stacked matvec must move, without the psi and y vectors.
+void f64stack_bytes(const F64Stack& p, double out[3]);
+
 }  // namespace tk
 
 struct tk_heff2_plan {
@@ -120,6 +135,8 @@ struct tk_heff2_plan {
     const int32_t* cancel = nullptr;
     // split-precision operands and state (tensor-core path)
     std::unique_ptr<tk::TcPlan, tk::TcPlanDeleter> tc;
+    // stacked FP64 operands (TK_SCHED_STACKED)
+    std::unique_ptr<tk::F64Stack, tk::F64StackDeleter> f64s;
     // Lanczos workspace (allocated on first use)
     tk::DevBuf<double> lz_basis, lz_w, lz_scal, lz_part, lz_vec;
     // FP64 search space of the Davidson / refinement solver (allocated on first use)

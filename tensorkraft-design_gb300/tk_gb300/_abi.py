@@ -16,7 +16,7 @@ TK_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "SECTOR_MISMATCH", 3: "OOM", 4: "CUDA", 5: "TIMEOUT",
                 6: "CANCELLED", 7: "UNSUPPORTED"}
 PREC_FP64, PREC_BF16X3 = 0, 1
-SCHED_GROUPED, SCHED_PER_BLOCK = 0, 1
+SCHED_GROUPED, SCHED_PER_BLOCK, SCHED_STACKED = 0, 1, 2
 HOST_IO_STAGED, HOST_IO_DIRECT, HOST_IO_DIRECT_OUT, HOST_IO_AUTO = 0, 1, 2, 3
 
 

@@ -227,7 +227,9 @@ class Heff2Plan:
         check(self._lib.tk_heff2_set_host_io(self._h, mode))
 
     def set_schedule(self, schedule: int):
-        """FP64 GEMM launch schedule: _abi.SCHED_GROUPED or _abi.SCHED_PER_BLOCK."""
+        """FP64 GEMM launch schedule: _abi.SCHED_GROUPED, _abi.SCHED_PER_BLOCK or
+        _abi.SCHED_STACKED (operand stacks as in the split path, built on the
+        first request; real plans only)."""
         check(self._lib.tk_heff2_set_schedule(self._h, schedule))
 
     def set_precision(self, precision: int):
