@@ -81,9 +81,11 @@ def parse():
                          "16 sites, D=1024, dt=0.05, Krylov 16) after a split-precision DMRG ground state")
     ap.add_argument("--rows", action="store_true",
                     help="also time environment growth, the dense GEMM and the block GEMM beside CPU restatements")
+    ap.add_argument("--fp64-schedule", default="stacked", choices=["grouped", "stacked"],
+                    help="launch schedule of the FP64 matvec (the fp64 line and the fp64 comparison)")
     ap.add_argument("--compare-schedules", type=int, default=0, metavar="STEPS",
-                    help="also time STEPS FP64 matvecs with one grouped launch per stage and with one launch "
-                         "per sector block")
+                    help="also time STEPS FP64 matvecs with one grouped launch per stage, with one launch "
+                         "per sector block and on operand stacks")
     return ap.parse_args()
 
 
@@ -93,6 +95,7 @@ def compare_schedules(plan, x, y, torch, dev, steps: int, flush):
     from tk_gb300 import PREC_BF16X3, PREC_FP64, _abi
 
     prec = plan.precision
+    sched_before = plan.schedule
     plan.set_precision(PREC_FP64)
     out = {}
     for name, sched in (("fp64_grouped", _abi.SCHED_GROUPED), ("fp64_per_block", _abi.SCHED_PER_BLOCK),
@@ -110,7 +113,7 @@ def compare_schedules(plan, x, y, torch, dev, steps: int, flush):
             e.synchronize()
             tot += s.elapsed_time(e) / 1e3
         out[name] = steps / tot
-    plan.set_schedule(_abi.SCHED_GROUPED)
+    plan.set_schedule(sched_before)
     plan.set_precision(prec)
     out["grouped_speedup"] = out["fp64_grouped"] / out["fp64_per_block"]
     out["stacked_speedup"] = out["fp64_stacked"] / out["fp64_grouped"]
@@ -591,6 +594,10 @@ def run_ours(args):
 
     prob = models.workload(args.workload)
     plan = prob.plan(precision=PREC_FP64, device=local)
+    from tk_gb300 import _abi
+
+    fp64_sched = {"grouped": _abi.SCHED_GROUPED, "stacked": _abi.SCHED_STACKED}[args.fp64_schedule]
+    plan.set_schedule(fp64_sched)
     prec_name = "fp64"
     tune = None
     if args.precision in ("auto", "bf16x3"):
@@ -659,7 +666,7 @@ def run_ours(args):
         plan.apply(x, y64)
         torch.cuda.synchronize(dev)
         y_fp = float(torch.linalg.norm(yb - y64) / torch.linalg.norm(y64))
-        # the FP64 grouped path on the same workload and input, timed the same way
+        # the FP64 path (--fp64-schedule) on the same workload and input, timed the same way
         n64 = max(3, min(args.steps, 50))
         ev64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n64)]
         for e0, e1 in ev64:
@@ -670,6 +677,7 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
         t64 = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev64) / 1e3, dev)
         fp64 = {"value": n64 * ws / t64, "unit": UNIT, "steps": n64, "ms_per_step": t64 / n64 * 1e3,
+                "schedule": args.fp64_schedule,
                 "launches_per_matvec": plan.launches(), "split_speedup": value / (n64 * ws / t64)}
         plan.set_precision(PREC_BF16X3)
     # end-to-end through the C ABI with pinned host buffers (H2D + matvec + D2H per step)

@@ -171,21 +171,24 @@ tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_apply);
 tk_status tk_heff2_set_host_io(tk_heff2_plan* plan, int32_t mode);
 tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
 
-/* Launch schedule of the FP64 sector GEMMs.  TK_SCHED_GROUPED (default): all
+/* Launch schedule of the FP64 sector GEMMs.  TK_SCHED_GROUPED: all
  * sector GEMMs of a stage in one grouped launch.  TK_SCHED_PER_BLOCK: one
  * launch per output block, the GPU analogue of the reference's one-task-at-a-
  * time block_gemm loop (tk-linalg/src/device/faer.rs:439-512), kept as the
- * baseline the grouped launch is measured against.  TK_SCHED_STACKED: the
- * sector GEMMs regrouped into operand stacks, one per ket sector of L and one
- * per bra sector of R (the split-precision path's grouping, in FP64), so
- * that the FP64 tiles are 128 x 64 over dense stacks instead of many small
- * sector tasks; its operands are built on the first request (real plans
- * only: TK_ERR_UNSUPPORTED for complex ones).  Every schedule computes the
- * same sums in FP64; they differ only in the order of the additions. */
+ * baseline the grouped launch is measured against.  TK_SCHED_STACKED (the
+ * default of real plans, built with the plan): the sector GEMMs regrouped
+ * into operand stacks, one per ket sector of L and one per bra sector of R
+ * (the split-precision path's grouping, in FP64), cut into pieces of at most
+ * 32 x 64 outputs that step over the stack columns their rows hold, so that
+ * nearly every FP64 FMA issued is one of the product's own.  Complex plans
+ * run TK_SCHED_GROUPED (TK_SCHED_STACKED: TK_ERR_UNSUPPORTED).  Every
+ * schedule computes the same sums in FP64; they differ only in the order of
+ * the additions. */
 #define TK_SCHED_GROUPED   0
 #define TK_SCHED_PER_BLOCK 1
 #define TK_SCHED_STACKED   2
 tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule);
+tk_status tk_heff2_get_schedule(const tk_heff2_plan* plan, int32_t* schedule);
 
 /* Cooperative cancellation (DMRGEngine::run_with_cancel_flag,
  * tk-dmrg/src/sweep/mod.rs:273-289, checks an AtomicBool before every step):

@@ -252,6 +252,9 @@ tk_status tk::plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
     TK_CUDA(p->terms.upload(H.terms));
     p->n_jobs = (int)H.jobs.size();
     p->precision = TK_PREC_FP64;
+    // the FP64 matvec of a real plan runs on operand stacks (TK_SCHED_STACKED)
+    tk_status s3 = tk_heff2_set_schedule(p.get(), TK_SCHED_STACKED);
+    if (s3 != TK_OK) return s3;
     if (precision != TK_PREC_FP64) {
         tk_status s2 = tk_heff2_set_precision(p.get(), precision);
         if (s2 != TK_OK) return s2;
@@ -526,6 +529,15 @@ tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
     }
     if (plan->schedule != schedule) plan->lz_graph.reset();  // captured with the old schedule's kernels
     plan->schedule = schedule;
+    return TK_OK;
+}
+
+tk_status tk_heff2_get_schedule(const tk_heff2_plan* plan, int32_t* schedule) {
+    if (!plan || !schedule) {
+        set_error("tk_heff2_get_schedule: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    *schedule = plan->schedule;
     return TK_OK;
 }
 

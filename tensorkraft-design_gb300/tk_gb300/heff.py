@@ -232,6 +232,13 @@ class Heff2Plan:
         first request; real plans only)."""
         check(self._lib.tk_heff2_set_schedule(self._h, schedule))
 
+    @property
+    def schedule(self) -> int:
+        """The FP64 launch schedule in use (real plans start on _abi.SCHED_STACKED)."""
+        s = C.c_int32()
+        check(self._lib.tk_heff2_get_schedule(self._h, C.byref(s)))
+        return s.value
+
     def set_precision(self, precision: int):
         check(self._lib.tk_heff2_set_precision(self._h, precision))
         self.precision = precision

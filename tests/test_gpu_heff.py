@@ -152,6 +152,8 @@ def test_per_block_schedule_matches_grouped(lib_built):
 
     p = small_problem("cylinder", 96)
     plan = p.plan()
+    assert plan.schedule == _abi.SCHED_STACKED  # the default of real plans
+    plan.set_schedule(_abi.SCHED_GROUPED)
     x = torch.from_numpy(np.random.default_rng(8).standard_normal(plan.block_dim)).cuda()
     y1, y2 = torch.empty_like(x), torch.empty_like(x)
     plan.apply(x, y1)

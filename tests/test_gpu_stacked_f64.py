@@ -25,7 +25,7 @@ def test_stacked_matches_oracle(lib_built, name, D):
     torch = _torch()
     p = small_problem(name, D)
     plan = p.plan()
-    plan.set_schedule(_abi.SCHED_STACKED)
+    assert plan.schedule == _abi.SCHED_STACKED  # the default of real plans
     assert plan.launches() <= 3
     bs = oracle_bs(p)
     x = np.random.default_rng(5).standard_normal(plan.block_dim)
@@ -58,6 +58,7 @@ def test_stacked_full_size(lib_built, name):
     X = torch.from_numpy(np.stack([x, u, 2.0 * x - 3.0 * u])).cuda()
     Y = torch.empty_like(X)
     yg = torch.empty_like(X[0])
+    plan.set_schedule(_abi.SCHED_GROUPED)
     plan.apply(X[0], yg)
     plan.set_schedule(_abi.SCHED_STACKED)
     for k in range(3):
@@ -74,6 +75,7 @@ def test_stacked_eigensolvers(lib_built):
     _torch()
     p = small_problem("hubbard", 64)
     plan = p.plan()
+    plan.set_schedule(_abi.SCHED_GROUPED)
     e_g = plan.lanczos(krylov_dim=40, max_restarts=20, tol=1e-11).eigenvalue
     plan.set_schedule(_abi.SCHED_STACKED)
     r = plan.lanczos(krylov_dim=40, max_restarts=20, tol=1e-11)
@@ -91,6 +93,7 @@ def test_stacked_profile_and_switching(lib_built):
     plan = p.plan()
     x = torch.from_numpy(np.random.default_rng(2).standard_normal(plan.block_dim)).cuda()
     y1, y2, y3 = (torch.empty_like(x) for _ in range(3))
+    plan.set_schedule(_abi.SCHED_GROUPED)
     plan.apply(x, y1)
     plan.set_schedule(_abi.SCHED_STACKED)
     ms, fl, by = plan.profile(x, y2, reps=2)
