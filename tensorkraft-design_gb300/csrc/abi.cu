@@ -216,7 +216,7 @@ tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, cons
 // tk_heff2_plan_create_dev (host copies of canonical block-layout ones).
 tk_status tk::plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
                                const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, const double* l_blocks,
-                               const double* r_blocks, tk_heff2_plan** out) {
+                               const double* r_blocks, tk_heff2_plan** out, bool stacked) {
     *out = nullptr;
     if (precision != TK_PREC_FP64 && precision != TK_PREC_BF16X3) {
         set_error("tk_heff2_plan_create: unknown precision");
@@ -253,8 +253,10 @@ tk_status tk::plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
     p->n_jobs = (int)H.jobs.size();
     p->precision = TK_PREC_FP64;
     // the FP64 matvec of a real plan runs on operand stacks (TK_SCHED_STACKED)
-    tk_status s3 = tk_heff2_set_schedule(p.get(), TK_SCHED_STACKED);
-    if (s3 != TK_OK) return s3;
+    if (stacked) {
+        tk_status s3 = tk_heff2_set_schedule(p.get(), TK_SCHED_STACKED);
+        if (s3 != TK_OK) return s3;
+    }
     if (precision != TK_PREC_FP64) {
         tk_status s2 = tk_heff2_set_precision(p.get(), precision);
         if (s2 != TK_OK) return s2;

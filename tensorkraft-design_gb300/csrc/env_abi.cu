@@ -218,9 +218,11 @@ tk_status tk_env_layout(int32_t qn_kind, const tk_qindex* bra, const tk_qindex* 
     return TK_OK;
 }
 
-tk_status tk_heff2_plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
-                                   const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
-                                   tk_heff2_plan** out) {
+// tk_heff2_plan_create_dev; `stacked` as in plan_create_impl (off for the
+// complex plans, whose FP64 matvec runs the grouped schedule).
+static tk_status plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                                 const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, tk_heff2_plan** out,
+                                 bool stacked) {
     if (!ctx || !env_l || !env_r || !w_i || !w_j || !out || !env_l->data || !env_r->data) {
         set_error("tk_heff2_plan_create_dev: null argument");
         return TK_ERR_INVALID_ARG;
@@ -250,7 +252,13 @@ tk_status tk_heff2_plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_en
         if (!rh.empty() && (e = cudaMemcpy(rh.data(), env_r->data, sizeof(double) * rh.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
             return cuda_fail("tk_heff2_plan_create_dev: read right environment", e);
     }
-    return plan_create_impl(ctx, env_l, env_r, w_i, w_j, psi_flux, precision, lh.data(), rh.data(), out);
+    return plan_create_impl(ctx, env_l, env_r, w_i, w_j, psi_flux, precision, lh.data(), rh.data(), out, stacked);
+}
+
+tk_status tk_heff2_plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
+                                   const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
+                                   tk_heff2_plan** out) {
+    return plan_create_dev(ctx, env_l, env_r, w_i, w_j, psi_flux, precision, out, true);
 }
 
 tk_status tk_env_grow_left(tk_ctx* ctx, const tk_env* env_l, const tk_bst* a, const tk_bst* w, double* out_dev,
@@ -280,7 +288,7 @@ tk_status tk_heff2_plan_create_dev_complex(tk_ctx* ctx, const tk_env* env_l, con
         set_error("tk_heff2_plan_create_dev_complex: null imaginary part");
         return TK_ERR_INVALID_ARG;
     }
-    tk_status st = tk_heff2_plan_create_dev(ctx, env_l, env_r, w_i, w_j, psi_flux, TK_PREC_FP64, out);
+    tk_status st = plan_create_dev(ctx, env_l, env_r, w_i, w_j, psi_flux, TK_PREC_FP64, out, false);
     if (st != TK_OK) return st;
     tk_heff2_plan* p = *out;
     Guard g(p->device);

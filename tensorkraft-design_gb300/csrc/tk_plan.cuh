@@ -175,8 +175,9 @@ tk_status cuda_fail(const char* op, cudaError_t e);
 bool plan_cancelled(tk_heff2_plan* p, cudaStream_t s, const char* where);
 // Plan creation behind tk_heff2_plan_create / tk_heff2_plan_create_dev: with
 // l_blocks / r_blocks (host copies of canonical block-layout environments) the
-// environments' `data` pointers are not read.
+// environments' `data` pointers are not read.  `stacked`: build the stacked
+// FP64 operands and make TK_SCHED_STACKED the plan's schedule (real plans).
 tk_status plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
                            const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, const double* l_blocks,
-                           const double* r_blocks, tk_heff2_plan** out);
+                           const double* r_blocks, tk_heff2_plan** out, bool stacked = true);
 }

@@ -114,6 +114,7 @@ def test_stacked_refuses_complex_plans(lib_built):
     dl = sweep.DeviceEnv.from_dense(p.kind, p.env_l.data + 0j, p.env_l.bra_idx, p.env_l.mpo_idx, p.env_l.ket_idx)
     dr = sweep.DeviceEnv.from_dense(p.kind, p.env_r.data + 0j, p.env_r.bra_idx, p.env_r.mpo_idx, p.env_r.ket_idx)
     plan = Heff2Plan.from_device_envs_complex(dl, dr, p.w_i, p.w_j, p.flux)
+    assert plan.schedule == _abi.SCHED_GROUPED
     with pytest.raises(TkError) as e:
         plan.set_schedule(_abi.SCHED_STACKED)
     assert _abi.STATUS_NAMES[e.value.status] == "UNSUPPORTED"
