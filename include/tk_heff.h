@@ -214,9 +214,12 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
  *   fuse_max_ntiles: stage-3 stacks of at most this many 64-column tiles run
  *     the W_i W_j combine inside the stage-3 kernel instead of a separate
  *     combine launch (default 0: never);
- *   combine_warps: the separate combine runs as persistent warps that load
- *     their next job while storing the current one (1) or as one CTA per job
- *     (0, default).
+ *   combine_warps: the form of the separate combine: one CTA per job (0,
+ *     default), persistent warps that load their next job while storing the
+ *     current one (1), or one warp per job whose lanes each take a strip of
+ *     eight columns of one row, loading its T1 values before summing any and
+ *     storing it as one 16-byte write per half (2).  Every form writes the
+ *     same T2 bits.
  * tk_heff2_set_tc_options rebuilds the plan's split tables and operands;
  * FP64 matvecs are unaffected.  TK_ERR_UNSUPPORTED for complex plans. */
 typedef struct {

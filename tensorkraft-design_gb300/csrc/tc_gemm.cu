@@ -805,8 +805,18 @@ constexpr int kCombThreads = 128;  // combine: threads per job
 // others) reads its terms from its own descriptor; longer term lists are
 // staged in shared memory.  Each thread owns U elements, so a thread has
 // TU x U independent T1 loads in flight before the first use.  Elements run
-// in row-major order, contiguous in T1 and in the operand chunk.
-__global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+// in row-major order, contiguous in T1 and in the operand chunk.  The kernel
+// is bound by its instruction issue: a thread walks its elements (tid, tid +
+// 128, ...) by one precomputed quotient and remainder of 128 instead of a
+// division per element, and (kWide false: T1 below 2^31 elements) forms
+// its T1 and operand offsets in 32 bits.
+template <bool kWide>
+__device__ __forceinline__ int64_t t1_off(int r, int rs, int c) {
+    return kWide ? (int64_t)r * rs + c : (int64_t)(r * rs + c);
+}
+
+template <bool kWide>
+__global__ void __launch_bounds__(kCombThreads, 16) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
                                                                   const TcCombTerm* __restrict__ terms,
                                                                   const float* __restrict__ t1,
                                                                   __nv_bfloat16* __restrict__ th,
@@ -822,29 +832,37 @@ __global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCo
     const bool inl = nterm <= kTcCombInline;
     const bool resident = !inl && nterm <= TCH;
     if (resident && (int)threadIdx.x < nterm) st[threadIdx.x] = terms[j.term_begin + threadIdx.x];
+    // element threadIdx.x's (row, column) in the job, and one step of kCombThreads elements
+    const int dq = kCombThreads / j.cols, dr = kCombThreads - dq * j.cols;
+    int rl = (int)threadIdx.x / j.cols, cl = (int)threadIdx.x - rl * j.cols;
     grid_dep_wait();
     if (resident) __syncthreads();
     if (inl) {
+        const float* src[kTcCombInline];
+#pragma unroll
+        for (int q = 0; q < kTcCombInline; ++q) src[q] = t1 + j.inl[q].in_off;
         for (int e0 = 0; e0 < n; e0 += U * kCombThreads) {
             bool valid[U];
             int r[U], c[U];
             float acc[U], v[kTcCombInline][U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const int e = e0 + u * kCombThreads + threadIdx.x;
-                valid[u] = e < n;
-                const int rl = valid[u] ? e / j.cols : 0;
-                c[u] = valid[u] ? e - rl * j.cols : 0;
+                valid[u] = e0 + u * kCombThreads + (int)threadIdx.x < n;
                 r[u] = j.r0 + rl;
+                c[u] = cl;
                 acc[u] = 0.f;
+                cl += dr;
+                rl += dq;
+                if (cl >= j.cols) {
+                    cl -= j.cols;
+                    ++rl;
+                }
             }
 #pragma unroll
             for (int q = 0; q < kTcCombInline; ++q)
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    v[q][u] = (q < nterm && valid[u])
-                                  ? __ldg(t1 + j.inl[q].in_off + (int64_t)r[u] * j.inl[q].in_rs + c[u])
-                                  : 0.f;
+                    v[q][u] = (q < nterm && valid[u]) ? __ldg(src[q] + t1_off<kWide>(r[u], j.inl[q].in_rs, c[u])) : 0.f;
 #pragma unroll
             for (int q = 0; q < kTcCombInline; ++q)
                 if (q < nterm)
@@ -854,7 +872,7 @@ __global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCo
             for (int u = 0; u < U; ++u)
                 if (valid[u]) {
                     const int k = j.k0 + c[u];
-                    const int64_t idx = (((int64_t)j.t2row + (int64_t)(k >> 6) * j.cstride + r[u]) << 6) + (k & 63);
+                    const int64_t idx = ((int64_t)(j.t2row + (k >> 6) * j.cstride + r[u]) << 6) + (k & 63);
                     const __nv_bfloat16 h = __float2bfloat16_rn(acc[u]);
                     th[idx] = h;
                     tl[idx] = __float2bfloat16_rn(acc[u] - __bfloat162float(h));
@@ -1016,6 +1034,80 @@ __global__ void __launch_bounds__(256, 2) combine_tc_warp_kernel(const TcCombJob
     }
 }
 
+// The same combine with one warp per job (TcOptions::combine_warps == 2).
+// The one-CTA-per-job form spends about ninety instructions per element (an
+// integer division, 64-bit index arithmetic and the job descriptor in every
+// thread) and keeps its issue slots three quarters busy.  Here a lane walks
+// elements lane, lane + 32, ... of its warp's job (consecutive lanes on
+// consecutive columns, so every load and store instruction stays coalesced),
+// stepping its (row, column) by one precomputed quotient and remainder of 32
+// instead of dividing, and issues the T1 loads of a group of four elements
+// before it sums them.  Elements sum their terms in table order with fmaf, as
+// the other forms do (bit-identical T2).  Four jobs per CTA.
+constexpr int kWjWarps = 4, kWjG = 4;  // jobs per CTA; elements per lane loaded together
+
+__global__ void __launch_bounds__(32 * kWjWarps) combine_tc_wj_kernel(const TcCombJob* __restrict__ jobs, int njobs,
+                                                                    const TcCombTerm* __restrict__ terms,
+                                                                    const float* __restrict__ t1,
+                                                                    __nv_bfloat16* __restrict__ th,
+                                                                    __nv_bfloat16* __restrict__ tl) {
+    const int lane = threadIdx.x & 31;
+    const int ji = blockIdx.x * kWjWarps + (threadIdx.x >> 5);
+    grid_dep_launch();
+    if (ji >= njobs) return;
+    const TcCombJob j = jobs[ji];  // a plan constant: read before the dependency wait
+    const int n = j.rows * j.cols;
+    const int nterm = j.term_end - j.term_begin;
+    const int dq = 32 / j.cols, dr = 32 - dq * j.cols;  // one step of 32 elements in (rows, columns)
+    int rl = lane / j.cols, c = lane - rl * j.cols;
+    const float* src0 = t1 + j.inl[0].in_off;
+    const float* src1 = t1 + j.inl[1].in_off;
+    const int rs0 = j.inl[0].in_rs, rs1 = j.inl[1].in_rs;
+    grid_dep_wait();
+    for (int e0 = 0; e0 < n; e0 += 32 * kWjG) {  // one pass unless one row is longer than the rest
+        float v0[kWjG], v1[kWjG];
+        const int rl_start = rl, c_start = c;
+#pragma unroll
+        for (int g = 0; g < kWjG; ++g) {
+            const bool ok = e0 + 32 * g + lane < n;
+            const int r = j.r0 + rl;
+            v0[g] = (ok && nterm > 0) ? __ldg(src0 + (r * rs0 + c)) : 0.f;
+            v1[g] = (ok && nterm > 1) ? __ldg(src1 + (r * rs1 + c)) : 0.f;
+            c += dr;
+            rl += dq;
+            if (c >= j.cols) {
+                c -= j.cols;
+                ++rl;
+            }
+        }
+        int rg = rl_start, cg = c_start;  // the same walk again for the sums and stores
+#pragma unroll
+        for (int g = 0; g < kWjG; ++g) {
+            if (e0 + 32 * g + lane < n) {
+                const int r = j.r0 + rg;
+                float acc = 0.f;
+                if (nterm > 0) acc = fmaf(j.inl[0].coef, v0[g], acc);
+                if (nterm > 1) acc = fmaf(j.inl[1].coef, v1[g], acc);
+                for (int t = kTcCombInline; t < nterm; ++t) {  // terms past the inline ones
+                    const TcCombTerm tm = terms[j.term_begin + t];
+                    acc = fmaf(tm.coef, __ldg(t1 + tm.in_off + (int64_t)r * tm.in_rs + cg), acc);
+                }
+                const int k = j.k0 + cg;
+                const int64_t idx = ((int64_t)(j.t2row + (k >> 6) * j.cstride + r) << 6) + (k & 63);
+                const __nv_bfloat16 h = __float2bfloat16_rn(acc);
+                th[idx] = h;
+                tl[idx] = __float2bfloat16_rn(acc - __bfloat162float(h));
+            }
+            cg += dr;
+            rg += dq;
+            if (cg >= j.cols) {
+                cg -= j.cols;
+                ++rg;
+            }
+        }
+    }
+}
+
 template <class T>
 cudaError_t put(T** dst, const std::vector<T>& v) {
     *dst = nullptr;
@@ -1068,7 +1160,8 @@ struct TcPlan {
     TcFillSeg* fill_segs = nullptr;
     TcCombTerm* fill_terms = nullptr;
     int n3f = 0;
-    bool comb_warps = false;            // persistent-warp combine (TcOptions::combine_warps)
+    int comb_form = 0;                  // TcOptions::combine_warps: 0 CTA per job, 1 warps, 2 warp per job
+    bool t1_wide = false;               // T1 holds 2^31 elements or more (64-bit combine offsets)
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
     __nv_bfloat16 *th = nullptr, *tl = nullptr;
     __nv_bfloat16 *xh = nullptr, *xl = nullptr;  // split copy of psi (tall stage-1 stacks)
@@ -1142,7 +1235,9 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
     p->n3f = (int)C.tiles3f.size();
-    p->comb_warps = host.tcopt.combine_warps != 0;
+    p->comb_form = host.tcopt.combine_warps;
+    p->t1_wide = C.t1_total > INT32_MAX;
+    if (p->comb_form == 2 && C.t1_total > INT32_MAX) p->comb_form = 0;  // form 2 indexes T1 rows in 32 bits
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
@@ -1237,13 +1332,17 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
         launch_tc_gemm(tc.nst1x, tc.n1x, tc.tiles1x, tc.mLh, tc.mLl, tc.mXh, tc.mXl, om, CONST_A, tc.err, s);
         launch_stage1_fused(tc, x, 0, tc.n1, s);
     } else if (stage == 1) {
-        if (tc.njobs > 0 && tc.comb_warps)
+        if (tc.njobs > 0 && tc.comb_form == 2)
+            launch_pdl(combine_tc_wj_kernel, (tc.njobs + kWjWarps - 1) / kWjWarps, 32 * kWjWarps, 0, s,
+                       (const TcCombJob*)tc.jobs, tc.njobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1,
+                       tc.th, tc.tl);
+        else if (tc.njobs > 0 && tc.comb_form == 1)
             launch_pdl(combine_tc_warp_kernel, std::min(tc.njobs, 152 * 2 * 8) / 8 + 1, 256, 0, s,
                        (const TcCombJob*)tc.jobs, tc.njobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1,
                        tc.th, tc.tl);
         else if (tc.njobs > 0)
-            launch_pdl(combine_tc_kernel, tc.njobs, kCombThreads, 0, s, (const TcCombJob*)tc.jobs,
-                       (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
+            launch_pdl(tc.t1_wide ? combine_tc_kernel<true> : combine_tc_kernel<false>, tc.njobs, kCombThreads, 0, s,
+                       (const TcCombJob*)tc.jobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
     } else {
         // fused tiles first: their dependency is stage 1 (T1); the TMA tiles read
         // the combine's T2, complete before either launch starts its main loop

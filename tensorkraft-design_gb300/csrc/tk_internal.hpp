@@ -248,8 +248,9 @@ struct TcTables {
 //   fuse_max_ntiles: stage-3 stacks of at most this many column tiles run the
 //     W_i W_j combine inside the GEMM kernel (0: never; each column tile
 //     rebuilds the operand, so only narrow stacks qualify).
-//   combine_warps: the separate combine as persistent warps that prefetch
-//     their next job (1) or as one CTA per job (0).
+//   combine_warps: the separate combine as one CTA per job (0), persistent
+//     warps that prefetch their next job (1), or one warp per job over
+//     eight-column strips (2).
 struct TcOptions {
     int32_t tall_max_mtiles = 3;
     int32_t fuse_max_ntiles = 0;

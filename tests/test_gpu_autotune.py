@@ -1,6 +1,6 @@
 """The split-precision schedule options and the autotuner: every candidate
 schedule (split copy for tall stage-1 stacks or not, the W_i W_j combine
-fused into the stage-3 kernel or not) gives the same matvec to the split
+fused into the stage-3 kernel or in one of its three separate forms) gives the same matvec to the split
 tolerance (2e-4 relative against the FP64 oracle), and the autotuner keeps
 the fastest timed candidate and caches it per sector-size histogram class."""
 import numpy as np
@@ -11,7 +11,7 @@ from tk_gb300 import PREC_BF16X3
 
 pytestmark = pytest.mark.gpu
 SPLIT_TOL = 2e-4
-OPTIONS = [(3, 0, 0), (3, 0, 1), (3, 2, 0), (1 << 30, 0, 1), (1, 0, 0), (3, 1, 1), (1, 8, 0)]
+OPTIONS = [(3, 0, 0), (3, 0, 1), (3, 0, 2), (3, 2, 0), (1 << 30, 0, 1), (1, 0, 0), (1, 0, 2), (3, 1, 1), (1, 8, 0)]
 
 
 def _run(plan, x):
@@ -38,8 +38,9 @@ def test_every_schedule_matches_the_oracle(lib_built, name, D):
         assert np.isfinite(y).all()
         assert rel_err(y, ref) < SPLIT_TOL, (tall, fuse, warps)
         ys[(tall, fuse, warps)] = y
-    # the combine's two launch forms compute the same numbers, bit for bit
+    # the combine's three launch forms compute the same numbers, bit for bit
     assert np.array_equal(ys[(3, 0, 0)], ys[(3, 0, 1)])
+    assert np.array_equal(ys[(3, 0, 0)], ys[(3, 0, 2)])
 
 
 def test_fused_stage3_full_size(lib_built):
@@ -49,9 +50,13 @@ def test_fused_stage3_full_size(lib_built):
     plan = p.plan(precision=PREC_BF16X3)
     x = np.random.default_rng(3).standard_normal(plan.block_dim)
     ref = oracle_bs(p).apply(x)
-    for opts in ((3, 2, 0), (3, 0, 1)):
+    y0 = _run(plan, x)
+    for opts in ((3, 2, 0), (3, 0, 1), (3, 0, 2)):
         plan.set_tc_options(*opts)
-        assert rel_err(_run(plan, x), ref) < SPLIT_TOL, opts
+        y = _run(plan, x)
+        assert rel_err(y, ref) < SPLIT_TOL, opts
+        if opts[1] == 0:
+            assert np.array_equal(y, y0), opts  # every combine form writes the same T2
 
 
 def test_autotune_keeps_the_fastest_and_caches(lib_built):
