@@ -816,7 +816,7 @@ __device__ __forceinline__ int64_t t1_off(int r, int rs, int c) {
 }
 
 template <bool kWide>
-__global__ void __launch_bounds__(kCombThreads, 16) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
                                                                   const TcCombTerm* __restrict__ terms,
                                                                   const float* __restrict__ t1,
                                                                   __nv_bfloat16* __restrict__ th,
