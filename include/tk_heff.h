@@ -216,16 +216,20 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
  *     combine launch (default 0: never);
  *   combine_warps: the form of the separate combine: one CTA per job (0,
  *     default), persistent warps that load their next job while storing the
- *     current one (1), or one warp per job whose lanes each take a strip of
- *     eight columns of one row, loading its T1 values before summing any and
- *     storing it as one 16-byte write per half (2).  Every form writes the
- *     same T2 bits.
+ *     current one (1), or one warp per job, consecutive lanes on consecutive
+ *     elements (2).  Every form writes the same T2 bits;
+ *   stage1_persistent: the stage-1 stacks that split psi inside the GEMM run
+ *     as one persistent, warp-specialised kernel (1: producer warps fill the
+ *     psi operand and issue the TMA and MMAs of tile i + 1 while epilogue
+ *     warps store tile i from the other of two TMEM accumulators) or as one
+ *     CTA per tile (0, default).  Both compute the same T1 bits.
  * tk_heff2_set_tc_options rebuilds the plan's split tables and operands;
  * FP64 matvecs are unaffected.  TK_ERR_UNSUPPORTED for complex plans. */
 typedef struct {
     int32_t tall_max_mtiles;
     int32_t fuse_max_ntiles;
     int32_t combine_warps;
+    int32_t stage1_persistent;
 } tk_tc_options;
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts);
 tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts);

@@ -479,7 +479,7 @@ static tk_status apply_tc_options(tk_heff2_plan* plan, const TcOptions& o) {
 
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts) {
     if (!plan || !opts || opts->tall_max_mtiles < 1 || opts->fuse_max_ntiles < 0 || opts->combine_warps < 0 ||
-        opts->combine_warps > 2) {
+        opts->combine_warps > 2 || opts->stage1_persistent < 0 || opts->stage1_persistent > 1) {
         set_error("tk_heff2_set_tc_options: invalid argument");
         return TK_ERR_INVALID_ARG;
     }
@@ -492,6 +492,7 @@ tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts
     o.tall_max_mtiles = opts->tall_max_mtiles;
     o.fuse_max_ntiles = opts->fuse_max_ntiles;
     o.combine_warps = opts->combine_warps;
+    o.stage1_persistent = opts->stage1_persistent;
     return apply_tc_options(plan, o);
 }
 
@@ -503,6 +504,7 @@ tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts
     opts->tall_max_mtiles = plan->host.tcopt.tall_max_mtiles;
     opts->fuse_max_ntiles = plan->host.tcopt.fuse_max_ntiles;
     opts->combine_warps = plan->host.tcopt.combine_warps;
+    opts->stage1_persistent = plan->host.tcopt.stage1_persistent;
     return TK_OK;
 }
 
@@ -928,10 +930,11 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
             tk_status st = TK_OK;
             if (hit.tall_max_mtiles != plan->host.tcopt.tall_max_mtiles ||
                 hit.fuse_max_ntiles != plan->host.tcopt.fuse_max_ntiles ||
-                hit.combine_warps != plan->host.tcopt.combine_warps)
+                hit.combine_warps != plan->host.tcopt.combine_warps ||
+                hit.stage1_persistent != plan->host.tcopt.stage1_persistent)
                 st = apply_tc_options(plan, hit);
             if (st != TK_OK) return st;
-            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles, hit.combine_warps};
+            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles, hit.combine_warps, hit.stage1_persistent};
             out->from_cache = 1;
             return TK_OK;
         }
@@ -944,7 +947,8 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
     TK_CUDA(launch_fill_start_vector(plan->hx.p, n, s));
     // candidate schedules; a candidate whose tables come out the same as an
     // earlier one's is not timed again
-    const TcOptions cand[] = {{3, 0, 0}, {3, 0, 2}, {3, 0, 1}, {3, 2, 0}, {1 << 30, 0, 0}, {1, 0, 0}, {1, 0, 2}};
+    const TcOptions cand[] = {{3, 0, 0, 0}, {3, 0, 0, 1}, {3, 0, 2, 0}, {3, 0, 1, 0},
+                              {3, 2, 0, 0}, {1 << 30, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 2, 0}};
     std::vector<std::vector<size_t>> shapes;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TK_CUDA(cudaEventCreate(&e0));
@@ -962,7 +966,8 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         if ((st = apply_tc_options(plan, c)) != TK_OK) return st;
         const TcTables& C = plan->host.tc;
         std::vector<size_t> shape = {C.tiles1.size(), C.tiles1x.size(), C.split.size(), C.tiles3.size(),
-                                     C.tiles3f.size(), C.jobs.size(), C.jobs.empty() ? 0u : (size_t)c.combine_warps};
+                                     C.tiles3f.size(), C.jobs.size(), C.jobs.empty() ? 0u : (size_t)c.combine_warps,
+                                     C.tiles1.empty() ? 0u : (size_t)c.stage1_persistent};
         if (std::find(shapes.begin(), shapes.end(), shape) != shapes.end()) continue;
         shapes.push_back(shape);
         for (int w = 0; w < 2; ++w)
@@ -977,7 +982,8 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         TK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         ms /= (float)reps;
         if (out->n_candidates < 8) {
-            out->candidates[out->n_candidates] = {c.tall_max_mtiles, c.fuse_max_ntiles, c.combine_warps};
+            out->candidates[out->n_candidates] = {c.tall_max_mtiles, c.fuse_max_ntiles, c.combine_warps,
+                                                  c.stage1_persistent};
             out->candidate_ms[out->n_candidates] = ms;
             ++out->n_candidates;
         }
@@ -991,7 +997,7 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache[key] = best;
     }
-    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles, best.combine_warps};
+    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles, best.combine_warps, best.stage1_persistent};
     out->chosen_ms = best_ms;
     return TK_OK;
 }

@@ -567,6 +567,228 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
     }
 }
 
+// Stage 1 as a persistent, warp-specialised kernel (TcOptions::stage1_persistent).
+// Each CTA (two per SM) walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// of the LPT-ordered list with two roles running side by side:
+//   warps 4-7 (producers): per 64-wide K chunk, thread 0 of warp 4 issues the
+//     TMA of the L operand, all 128 fill the psi operand (as tc_gemm1_kernel
+//     does), and lane 0 of warp 5 issues the MMAs into one of two TMEM
+//     accumulators (tile i uses accumulator i & 1) and commits the stage and,
+//     on a tile's last chunk, the accumulator;
+//   warps 0-3 (epilogue): wait for tile i's accumulator, read it into
+//     registers, release it, and write T1 through the column tables.
+// So the fill and MMAs of tile i + 1 run while tile i's epilogue stores, and
+// the TMEM allocation and barrier set-up are paid once per CTA.  Barriers:
+// full[s] (TMA bytes of stage s), sfree[s] (the MMAs reading stage s are
+// done), afull[b] (accumulator b holds a finished tile), afree[b] (the
+// epilogue has read accumulator b; 128 arrivals).  Every wait is bounded: on
+// a timeout the error word is set and the role leaves its loop (the
+// producers together, through a barrier reduction), the CTA waits (bounded)
+// for its own TMA and MMAs in flight, frees its TMEM and returns.
+constexpr int kP1Threads = 256;
+constexpr int kP1Stile = kTcBM * (kTcBN + 1) * 4;  // epilogue transpose buffer
+constexpr int p1_smem_bytes(int nst) { return nst * STAGE_BYTES + kP1Stile + 1024 + 256; }
+
+// AND of `v` over the `count` threads of named barrier `id` (all must arrive).
+__device__ __forceinline__ bool named_bar_and(int id, int count, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
+template <int NST>
+__global__ void __launch_bounds__(kP1Threads, 2) tc_gemm1p_kernel(const TcTile* __restrict__ tiles, int ntiles,
+                                                                  const __grid_constant__ CUtensorMap mAh,
+                                                                  const __grid_constant__ CUtensorMap mAl,
+                                                                  const double* __restrict__ x,
+                                                                  const int64_t* __restrict__ xsrc,
+                                                                  const int32_t* __restrict__ xstride,
+                                                                  const OutMap om, int* err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem + NST * STAGE_BYTES);
+    uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES + kP1Stile);
+    uint64_t* sfree = full + NST;
+    uint64_t* afull = sfree + NST;
+    uint64_t* afree = afull + 2;
+    uint64_t* done = afree + 2;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    grid_dep_launch();
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&sfree[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&afull[b], 1);
+            mbar_init(&afree[b], 128);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(2 * TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    if (warp >= 4) {
+        // ---------------------------------------------------------------- producers
+        const int ptid = (int)threadIdx.x - 128;
+        int g = 0;            // chunks issued by this CTA
+        int last_full = -1;   // last chunk whose TMA thread 0 issued (drained at the end)
+        bool ok = true;
+        bool waited = false;  // the dependency wait (psi is read from the first fill on)
+        for (int i = 0, ti = blockIdx.x; ok && ti < ntiles; ++i, ti += gridDim.x) {
+            const TcTile t = tiles[ti];
+            const int b = i & 1;
+            const uint32_t idesc = make_idesc(t.n_mma);
+            const int fill_step = 128 / t.n_mma;
+            const int fill_col = ptid < fill_step * t.n_mma ? ptid % t.n_mma : -1;
+            const int fill_kq0 = ptid / t.n_mma;
+            const bool fill_valid = fill_col >= 0 && fill_col < t.n_valid;
+            const int64_t fill_src = fill_valid ? xsrc[t.out_off + fill_col] : 0;
+            const int64_t fill_stp = fill_valid ? xstride[t.out_off + fill_col] : 0;
+            for (int c = 0; c < t.kch; ++c, ++g) {
+                const int s = g % NST;
+                bool good = true;
+                if (g >= NST) good = mbar_wait(&sfree[s], ((g / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
+                if (!named_bar_and(1, 128, good)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = smem + s * STAGE_BYTES;
+                if (ptid == 0) {
+                    // the L operand is a plan constant: it may load before the dependency wait
+                    mbar_expect_tx(&full[s], 2 * A_BYTES);
+                    const int ya = t.a_row + c * t.a_cs;
+                    tma_load_2d(st, &mAh, 0, ya, &full[s]);
+                    tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[s]);
+                    last_full = g;
+                }
+                if (!waited) {
+                    grid_dep_wait();
+                    waited = true;
+                }
+                uint8_t* bh = st + 2 * A_BYTES;
+                uint8_t* bl = bh + B_BYTES;
+                const int kbase = c * kTcBK;
+                const int ksteps = min(kTcBK / 16, (t.k_valid - kbase + 15) / 16);
+                const int nkp = 8 * ksteps;
+                if (fill_col >= 0) {
+                    constexpr int kFillPairs = kTcBK / 2 / 2;
+                    double v[kFillPairs][2];
+#pragma unroll
+                    for (int u = 0; u < kFillPairs; ++u) {
+                        const int kq = fill_kq0 + u * fill_step;
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int k = kbase + 2 * kq + h;
+                            v[u][h] = (kq < nkp && fill_valid && k < t.k_valid) ? x[fill_src + (int64_t)k * fill_stp]
+                                                                               : 0.0;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kFillPairs; ++u) {
+                        const int kq = fill_kq0 + u * fill_step;
+                        if (kq >= nkp) continue;
+                        uint32_t hw, lw;
+                        split2x2(v[u][0], v[u][1], hw, lw);
+                        const int n = fill_col, k = 2 * kq;
+                        const uint32_t off =
+                            (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
+                        *reinterpret_cast<uint32_t*>(bh + off) = hw;
+                        *reinterpret_cast<uint32_t*>(bl + off) = lw;
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                bool mok = true;
+                if (ptid == 32) {
+                    if (c == 0 && i >= 2) mok = mbar_wait(&afree[b], ((i >> 1) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
+                    if (mok) mok = mbar_wait(&full[s], (g / NST) & 1, err, ERR_FULL_TIMEOUT);
+                }
+                // the fill of every producer is in shared memory before the MMAs read it
+                if (!named_bar_and(1, 128, mok)) {
+                    ok = false;
+                    break;
+                }
+                if (ptid == 32) {
+                    fence_after();
+                    const uint32_t sa = smem_u32(st);
+                    const uint64_t ah = sw128_desc(sa), al = sw128_desc(sa + A_BYTES);
+                    const uint64_t bhd = sw128_desc(sa + 2 * A_BYTES), bld = sw128_desc(sa + 2 * A_BYTES + B_BYTES);
+                    const uint32_t acc = tmem + (uint32_t)(b * TMEM_COLS);
+                    for (int q = 0; q < ksteps; ++q) {
+                        const uint64_t adv = (uint64_t)((q * 32) >> 4);
+                        mma_bf16(acc, ah + adv, bhd + adv, idesc, (c | q) != 0);
+                        mma_bf16(acc, ah + adv, bld + adv, idesc, 1u);
+                        mma_bf16(acc, al + adv, bhd + adv, idesc, 1u);
+                    }
+                    mma_commit(&sfree[s]);
+                    if (c == t.kch - 1) mma_commit(&afull[b]);
+                }
+            }
+        }
+        if (!waited) grid_dep_wait();
+        // drain: the MMAs this CTA issued, and the TMA of the last chunk per stage
+        if (ptid == 32) {
+            mma_commit(done);
+            mbar_wait(done, 0, err, ERR_DONE_TIMEOUT);
+        }
+        if (ptid == 0)
+            for (int gg = max(0, last_full - NST + 1); gg <= last_full; ++gg)
+                mbar_wait(&full[gg % NST], (gg / NST) & 1, err, ERR_FULL_TIMEOUT);
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        grid_dep_wait();  // T1 may still be read by the previous matvec's combine
+        const uint32_t lanebase = (uint32_t)(warp * 32) << 16;
+        for (int i = 0, ti = blockIdx.x; ti < ntiles; ++i, ti += gridDim.x) {
+            const TcTile t = tiles[ti];
+            const int b = i & 1;
+            int64_t cb[2] = {0, 0};
+            int32_t cs[2] = {0, 0};
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (lane + 32 * h < t.n_valid) {
+                    cb[h] = om.colbase[t.out_off + lane + 32 * h];
+                    cs[h] = om.colstride[t.out_off + lane + 32 * h];
+                }
+            const bool have = mbar_wait(&afull[b], (i >> 1) & 1, err, ERR_DONE_TIMEOUT);
+            if (!__all_sync(0xffffffffu, have)) break;
+            fence_after();
+            tmem_row_to_smem(tmem + (uint32_t)(b * TMEM_COLS) + lanebase, t.n_mma, stile[threadIdx.x]);
+            fence_before();
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&afree[b])) : "memory");
+            __syncwarp();
+            const int rend = min(t.m_valid, warp * 32 + 32);
+            for (int r = warp * 32; r < rend; ++r)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    if (lane + 32 * h < t.n_valid)
+                        om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane + 32 * h];
+            __syncwarp();
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TMEM_COLS) : "memory");
+    }
+}
+
 // Stage 3 with the W_i W_j combine fused in (stacks of at most
 // TcOptions::fuse_max_ntiles column tiles).  The R operand (B) comes in by TMA as in
 // tc_gemm_kernel; the A operand, T2 = sum_t coef_t * T1, is built chunk by
@@ -1161,6 +1383,8 @@ struct TcPlan {
     TcCombTerm* fill_terms = nullptr;
     int n3f = 0;
     int comb_form = 0;                  // TcOptions::combine_warps: 0 CTA per job, 1 warps, 2 warp per job
+    bool p1 = false;                    // stage 1 as the persistent kernel (TcOptions::stage1_persistent)
+    int p1_ctas = 0;                    // its resident CTAs per SM x SMs
     bool t1_wide = false;               // T1 holds 2^31 elements or more (64-bit combine offsets)
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
     __nv_bfloat16 *th = nullptr, *tl = nullptr;
@@ -1236,6 +1460,7 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n3 = (int)C.tiles3.size();
     p->n3f = (int)C.tiles3f.size();
     p->comb_form = host.tcopt.combine_warps;
+    p->p1 = host.tcopt.stage1_persistent != 0;
     p->t1_wide = C.t1_total > INT32_MAX;
     if (p->comb_form == 2 && C.t1_total > INT32_MAX) p->comb_form = 0;  // form 2 indexes T1 rows in 32 bits
     p->nsplit = (int)C.split.size();
@@ -1257,9 +1482,26 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         (e = cudaFuncSetAttribute(tc_gemm1_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
             cudaSuccess ||
         (e = cudaFuncSetAttribute(tc_gemm3f_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
-            cudaSuccess) {
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1p_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  p1_smem_bytes(1))) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1p_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  p1_smem_bytes(2))) != cudaSuccess) {
         err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return TK_ERR_CUDA;
+    }
+    if (p->p1) {
+        int dev = 0, sms = 0, per_sm = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+            (e = p->nst1 == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_gemm1p_kernel<1>, kP1Threads,
+                                                                              p1_smem_bytes(1))
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_gemm1p_kernel<2>, kP1Threads,
+                                                                              p1_smem_bytes(2))) != cudaSuccess) {
+            err = std::string("persistent stage-1 occupancy: ") + cudaGetErrorString(e);
+            return TK_ERR_CUDA;
+        }
+        p->p1_ctas = std::max(1, per_sm) * std::max(1, sms);
     }
     out = std::move(p);
     return TK_OK;
@@ -1301,6 +1543,16 @@ void launch_stage1_fused(TcPlan& tc, const double* x, int first, int count, cuda
     if (count <= 0) return;
     const OutMap om{tc.t1, nullptr, nullptr, tc.t1col_base, tc.t1col_stride};
     const TcTile* tiles = tc.tiles1 + first;
+    if (tc.p1) {
+        const int grid = std::min(count, tc.p1_ctas);
+        if (tc.nst1 == 1)
+            launch_pdl(tc_gemm1p_kernel<1>, grid, kP1Threads, p1_smem_bytes(1), s, tiles, count, tc.mLh, tc.mLl, x,
+                       (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+        else
+            launch_pdl(tc_gemm1p_kernel<2>, grid, kP1Threads, p1_smem_bytes(2), s, tiles, count, tc.mLh, tc.mLl, x,
+                       (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+        return;
+    }
     if (tc.nst1 == 1)
         launch_pdl(tc_gemm1_kernel<1>, count, 128, smem_bytes(1), s, tiles, tc.mLh, tc.mLl, x,
                    (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);

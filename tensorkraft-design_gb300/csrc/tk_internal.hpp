@@ -249,12 +249,14 @@ struct TcTables {
 //     W_i W_j combine inside the GEMM kernel (0: never; each column tile
 //     rebuilds the operand, so only narrow stacks qualify).
 //   combine_warps: the separate combine as one CTA per job (0), persistent
-//     warps that prefetch their next job (1), or one warp per job over
-//     eight-column strips (2).
+//     warps that prefetch their next job (1), or one warp per job (2).
+//   stage1_persistent: the in-kernel-split stage 1 as a persistent,
+//     warp-specialised kernel (1) or one CTA per tile (0).
 struct TcOptions {
     int32_t tall_max_mtiles = 3;
     int32_t fuse_max_ntiles = 0;
     int32_t combine_warps = 0;
+    int32_t stage1_persistent = 0;
 };
 
 // The sector structure the split-precision tables are built from, kept with

@@ -243,16 +243,21 @@ class Heff2Plan:
         check(self._lib.tk_heff2_set_precision(self._h, precision))
         self.precision = precision
 
-    def set_tc_options(self, tall_max_mtiles: int = 3, fuse_max_ntiles: int = 0, combine_warps: int = 0):
+    def set_tc_options(self, tall_max_mtiles: int = 3, fuse_max_ntiles: int = 0, combine_warps: int = 0,
+                       stage1_persistent: int = 0):
         """tk_heff2_set_tc_options: the split-precision schedule (see tk_heff.h)."""
-        o = _abi.tk_tc_options(tall_max_mtiles, fuse_max_ntiles, combine_warps)
+        o = _abi.tk_tc_options(tall_max_mtiles, fuse_max_ntiles, combine_warps, stage1_persistent)
         check(self._lib.tk_heff2_set_tc_options(self._h, C.byref(o)))
+
+    @staticmethod
+    def _opts(o) -> dict:
+        return {"tall_max_mtiles": o.tall_max_mtiles, "fuse_max_ntiles": o.fuse_max_ntiles,
+                "combine_warps": o.combine_warps, "stage1_persistent": o.stage1_persistent}
 
     def tc_options(self) -> dict:
         o = _abi.tk_tc_options()
         check(self._lib.tk_heff2_get_tc_options(self._h, C.byref(o)))
-        return {"tall_max_mtiles": o.tall_max_mtiles, "fuse_max_ntiles": o.fuse_max_ntiles,
-                "combine_warps": o.combine_warps}
+        return self._opts(o)
 
     def autotune(self, reps: int = 5, use_cache: bool = True) -> dict:
         """tk_heff2_autotune: times the candidate split-precision schedules on this
@@ -260,8 +265,7 @@ class Heff2Plan:
         keeps the fastest.  Returns the choice and the candidates' ms per matvec."""
         r = _abi.tk_autotune_result()
         check(self._lib.tk_heff2_autotune(self._h, reps, 1 if use_cache else 0, C.byref(r)))
-        opt = lambda o: {"tall_max_mtiles": o.tall_max_mtiles, "fuse_max_ntiles": o.fuse_max_ntiles,
-                         "combine_warps": o.combine_warps}
+        opt = self._opts
         return {"chosen": opt(r.chosen), "chosen_ms": r.chosen_ms, "from_cache": bool(r.from_cache),
                 "candidates": [dict(opt(r.candidates[i]), ms=r.candidate_ms[i]) for i in range(r.n_candidates)]}
 

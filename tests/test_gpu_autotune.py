@@ -11,7 +11,8 @@ from tk_gb300 import PREC_BF16X3
 
 pytestmark = pytest.mark.gpu
 SPLIT_TOL = 2e-4
-OPTIONS = [(3, 0, 0), (3, 0, 1), (3, 0, 2), (3, 2, 0), (1 << 30, 0, 1), (1, 0, 0), (1, 0, 2), (3, 1, 1), (1, 8, 0)]
+OPTIONS = [(3, 0, 0, 0), (3, 0, 1, 0), (3, 0, 2, 0), (3, 0, 0, 1), (3, 2, 0, 0), (1 << 30, 0, 1, 1), (1, 0, 0, 0),
+           (1, 0, 2, 1), (3, 1, 1, 0), (1, 8, 0, 1)]
 
 
 def _run(plan, x):
@@ -31,16 +32,18 @@ def test_every_schedule_matches_the_oracle(lib_built, name, D):
     x = np.random.default_rng(11).standard_normal(plan.block_dim)
     ref = oracle_bs(p).apply(x)
     ys = {}
-    for tall, fuse, warps in OPTIONS:
-        plan.set_tc_options(tall, fuse, warps)
-        assert plan.tc_options() == {"tall_max_mtiles": tall, "fuse_max_ntiles": fuse, "combine_warps": warps}
+    for tall, fuse, warps, pers in OPTIONS:
+        plan.set_tc_options(tall, fuse, warps, pers)
+        assert plan.tc_options() == {"tall_max_mtiles": tall, "fuse_max_ntiles": fuse, "combine_warps": warps,
+                                     "stage1_persistent": pers}
         y = _run(plan, x)
         assert np.isfinite(y).all()
-        assert rel_err(y, ref) < SPLIT_TOL, (tall, fuse, warps)
-        ys[(tall, fuse, warps)] = y
-    # the combine's three launch forms compute the same numbers, bit for bit
-    assert np.array_equal(ys[(3, 0, 0)], ys[(3, 0, 1)])
-    assert np.array_equal(ys[(3, 0, 0)], ys[(3, 0, 2)])
+        assert rel_err(y, ref) < SPLIT_TOL, (tall, fuse, warps, pers)
+        ys[(tall, fuse, warps, pers)] = y
+    # the combine's three launch forms and both stage-1 kernels compute the same numbers, bit for bit
+    assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 1, 0)])
+    assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 2, 0)])
+    assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 0, 1)])
 
 
 def test_fused_stage3_full_size(lib_built):
@@ -51,7 +54,7 @@ def test_fused_stage3_full_size(lib_built):
     x = np.random.default_rng(3).standard_normal(plan.block_dim)
     ref = oracle_bs(p).apply(x)
     y0 = _run(plan, x)
-    for opts in ((3, 2, 0), (3, 0, 1), (3, 0, 2)):
+    for opts in ((3, 2, 0, 0), (3, 0, 1, 0), (3, 0, 2, 0), (3, 0, 0, 1)):
         plan.set_tc_options(*opts)
         y = _run(plan, x)
         assert rel_err(y, ref) < SPLIT_TOL, opts
@@ -65,7 +68,8 @@ def test_autotune_keeps_the_fastest_and_caches(lib_built):
     r = plan.autotune(reps=3, use_cache=False)
     assert not r["from_cache"] and len(r["candidates"]) >= 2
     best = min(r["candidates"], key=lambda c: c["ms"])
-    assert r["chosen"] == {k: best[k] for k in ("tall_max_mtiles", "fuse_max_ntiles", "combine_warps")}
+    assert r["chosen"] == {k: best[k] for k in ("tall_max_mtiles", "fuse_max_ntiles", "combine_warps",
+                                                "stage1_persistent")}
     assert plan.tc_options() == r["chosen"]
     # a second plan of the same histogram class takes the cached choice
     plan2 = p.plan(precision=PREC_BF16X3)
