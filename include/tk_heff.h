@@ -162,13 +162,20 @@ tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_apply);
  *   Heisenberg and cylinder workloads; the in-GEMM psi split reads columns
  *   with a stride, which the link serves poorly under DIRECT).
  * Whenever x is copied and every stage-1 stack splits psi inside the GEMM
- * kernel, the copy runs in two halves on a second stream and the stage-1
- * tiles that read only the first half start while the second is in flight. */
+ * kernel, the copy runs in pieces on a second stream (two by default,
+ * tk_heff2_set_psi_pieces) and the stage-1 tiles that read only the pieces
+ * already copied start while the rest is in flight. */
 #define TK_HOST_IO_STAGED     0
 #define TK_HOST_IO_DIRECT     1
 #define TK_HOST_IO_DIRECT_OUT 2
 #define TK_HOST_IO_AUTO       3
 tk_status tk_heff2_set_host_io(tk_heff2_plan* plan, int32_t mode);
+/* Host-buffer split matvec: psi is copied in `pieces` pieces (1, 2, 4 or 8;
+ * default 2) at block boundaries near equal shares, and the stage-1 tiles that
+ * read only the pieces already on the device start while the rest is in
+ * flight (when every stage-1 stack splits psi inside the GEMM kernel; else
+ * one copy).  Results are the same bits for every setting. */
+tk_status tk_heff2_set_psi_pieces(tk_heff2_plan* plan, int32_t pieces);
 tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
 
 /* Launch schedule of the FP64 sector GEMMs.  TK_SCHED_GROUPED: all

@@ -581,30 +581,30 @@ static tk_status ensure_host_staging(tk_heff2_plan* p) {
     }
     if (!p->copy_stream) TK_CUDA(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
     if (!p->ev_fork) TK_CUDA(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
-    for (cudaEvent_t& e : p->ev_half)
+    for (cudaEvent_t& e : p->ev_piece)
         if (!e) TK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return TK_OK;
 }
 
-// Split matvec from a host buffer copied in two halves: the stage-1 tiles
-// that read only the first half run while the second half is in flight
-// (copy stream forked from and joined back into `s`), then the rest of
-// the matvec as usual.  Stream-ordered; used inside a graph capture.
-static tk_status enqueue_split_psi_halves(tk_heff2_plan* p, const double* x, double* y, int64_t x_split,
-                                          cudaStream_t s) {
-    const int64_t n = p->host.total;
-    const int64_t len[2] = {x_split, n - x_split};
+// Split matvec from a host buffer copied in k pieces: the stage-1 tiles that
+// read only the first j pieces run while the later ones are in flight (copy
+// stream forked from and joined back into `s`), then the rest of the matvec
+// as usual.  Stream-ordered; used inside a graph capture.
+static tk_status enqueue_split_psi_pieces(tk_heff2_plan* p, const double* x, double* y, int k, const int64_t* x_cut,
+                                          const int32_t* n1_cut, cudaStream_t s) {
     TK_CUDA(cudaEventRecord(p->ev_fork, s));
     TK_CUDA(cudaStreamWaitEvent(p->copy_stream, p->ev_fork, 0));
-    for (int h = 0; h < 2; ++h) {
-        const int64_t off = h == 0 ? 0 : x_split;
-        TK_CUDA(cudaMemcpyAsync(p->hx.p + off, x + off, sizeof(double) * len[h], cudaMemcpyHostToDevice,
-                                p->copy_stream));
-        TK_CUDA(cudaEventRecord(p->ev_half[h], p->copy_stream));
+    for (int j = 0; j < k; ++j) {
+        const int64_t len = x_cut[j + 1] - x_cut[j];
+        if (len > 0)
+            TK_CUDA(cudaMemcpyAsync(p->hx.p + x_cut[j], x + x_cut[j], sizeof(double) * len, cudaMemcpyHostToDevice,
+                                    p->copy_stream));
+        TK_CUDA(cudaEventRecord(p->ev_piece[j], p->copy_stream));
     }
-    for (int h = 0; h < 2; ++h) {
-        TK_CUDA(cudaStreamWaitEvent(s, p->ev_half[h], 0));
-        TK_CUDA(tc_stage1_half(*p->tc, p->hx.p, h, s));
+    for (int j = 0; j < k; ++j) {
+        TK_CUDA(cudaStreamWaitEvent(s, p->ev_piece[j], 0));
+        if (n1_cut[j + 1] > n1_cut[j])
+            TK_CUDA(tc_stage1_range(*p->tc, p->hx.p, n1_cut[j], n1_cut[j + 1] - n1_cut[j], s));
     }
     for (int stage = 1; stage < 3; ++stage) {
         std::string err;
@@ -631,6 +631,15 @@ static tk_status finish_host_call(tk_heff2_plan* p, cudaStream_t s) {
     if (tc) TK_CUDA(cudaMemcpyAsync(p->pin_err, tc_error_word(*p->tc), sizeof(int), cudaMemcpyDeviceToHost, s));
     TK_CUDA(cudaStreamSynchronize(s));
     if (tc && *p->pin_err != 0) return tc_check_error(*p->tc, s);
+    return TK_OK;
+}
+
+tk_status tk_heff2_set_psi_pieces(tk_heff2_plan* plan, int32_t pieces) {
+    if (!plan || pieces < 1 || pieces > kTcPsiPieces || kTcPsiPieces % pieces != 0) {
+        set_error("tk_heff2_set_psi_pieces: invalid argument");
+        return TK_ERR_INVALID_ARG;
+    }
+    plan->psi_pieces = pieces;
     return TK_OK;
 }
 
@@ -698,20 +707,23 @@ tk_status tk_heff2_apply_host_flat(tk_heff2_plan* plan, const double* x, double*
     // page-locked buffers: the whole call (copies, kernels, error-word
     // read-back) as one CUDA graph launch, re-instantiated when the buffers
     // or settings change
-    const int key = ((mode * 4 + plan->precision) * 4 + plan->schedule) * 4 + (dx ? 2 : 0) + (dy ? 1 : 0);
+    const int key = (((mode * 4 + plan->precision) * 4 + plan->schedule) * 16 + plan->psi_pieces) * 4 + (dx ? 2 : 0) +
+                    (dy ? 1 : 0);
     if (!plan->host_exec || plan->host_gx != x || plan->host_gy != y || plan->host_gmx != mx ||
         plan->host_gmy != my || plan->host_gkey != key) {
         if (plan->host_exec) {
             cudaGraphExecDestroy(plan->host_exec);
             plan->host_exec = nullptr;
         }
-        int64_t x_split = 0;
-        const bool halves = !dx && plan->precision == TK_PREC_BF16X3 && tc_psi_halves(*plan->tc, &x_split);
+        int64_t x_cut[kTcPsiPieces + 1];
+        int32_t n1_cut[kTcPsiPieces + 1];
+        const bool pieces = !dx && plan->precision == TK_PREC_BF16X3 &&
+                            tc_psi_pieces(*plan->tc, plan->psi_pieces, x_cut, n1_cut);
         TK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         tk_status cst = TK_OK;
         cudaError_t ce = cudaSuccess;
-        if (halves) {
-            cst = enqueue_split_psi_halves(plan, x, dy ? dy : plan->hy.p, x_split, s);
+        if (pieces) {
+            cst = enqueue_split_psi_pieces(plan, x, dy ? dy : plan->hy.p, plan->psi_pieces, x_cut, n1_cut, s);
         } else {
             if (!dx) ce = cudaMemcpyAsync(plan->hx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, s);
             if (ce == cudaSuccess)

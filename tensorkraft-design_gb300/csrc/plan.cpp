@@ -425,17 +425,24 @@ static bool validate_tc(const Heff2Tables& T, const TcTables& C, std::string& er
     };
     for (const TcTile& t : C.tiles1)
         if (!tile1_ok(t)) return false;
-    if (C.n1_first < 0 || (size_t)C.n1_first > C.tiles1.size() || C.x_split < 0 || C.x_split > T.total) {
-        err = "tensor-core stage 1 psi halves";
+    if (C.x_cut[0] != 0 || C.x_cut[kTcPsiPieces] != T.total || C.n1_cut[0] != 0 ||
+        C.n1_cut[kTcPsiPieces] != (int32_t)C.tiles1.size()) {
+        err = "tensor-core stage 1 psi pieces";
         return false;
     }
-    for (int32_t i = 0; i < C.n1_first; ++i) {
-        const TcTile& t = C.tiles1[(size_t)i];
-        for (int c = 0; c < t.n_valid; ++c)
-            if (C.xsrc[t.out_off + c] + (int64_t)(t.k_valid - 1) * C.xstride[t.out_off + c] >= C.x_split) {
-                err = "tensor-core stage 1 tile reads past the first psi half";
-                return false;
-            }
+    for (int j = 0; j < kTcPsiPieces; ++j) {
+        if (C.x_cut[j + 1] < C.x_cut[j] || C.n1_cut[j + 1] < C.n1_cut[j]) {
+            err = "tensor-core stage 1 psi pieces";
+            return false;
+        }
+        for (int32_t i = C.n1_cut[j]; i < C.n1_cut[j + 1]; ++i) {
+            const TcTile& t = C.tiles1[(size_t)i];
+            for (int c = 0; c < t.n_valid; ++c)
+                if (C.xsrc[t.out_off + c] + (int64_t)(t.k_valid - 1) * C.xstride[t.out_off + c] >= C.x_cut[j + 1]) {
+                    err = "tensor-core stage 1 tile reads past its psi piece";
+                    return false;
+                }
+        }
     }
     for (const TcTile& t : C.tiles1x)
         if (!tile1_ok(t)) return false;
@@ -880,24 +887,32 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
                 return (int64_t)a.m_valid * a.n_mma > (int64_t)b.m_valid * b.n_mma;
             });
         };
-        // psi in two halves (a block boundary near the middle): the in-GEMM-split
-        // tiles that read only the first half go first, so a host-buffer matvec
-        // can start them while the second half is still being copied in
-        C.x_split = T.total;
-        for (int64_t o : T.blk_off)
-            if (2 * o >= T.total) {
-                C.x_split = o;
-                break;
-            }
+        // psi in kTcPsiPieces pieces (block boundaries near equal shares): the
+        // in-GEMM-split tiles go in the order of the piece their last psi read
+        // falls in, so a host-buffer matvec can start each group as soon as its
+        // piece is on the device while the later pieces are still being copied
         {
-            std::vector<TcTile> first, second;
-            for (size_t i = 0; i < C.tiles1.size(); ++i)
-                (tile1_xend[i] <= C.x_split ? first : second).push_back(C.tiles1[i]);
-            lpt(first);
-            lpt(second);
-            C.n1_first = (int32_t)first.size();
-            C.tiles1 = first;
-            C.tiles1.insert(C.tiles1.end(), second.begin(), second.end());
+            constexpr int KP = kTcPsiPieces;
+            C.x_cut[0] = 0;
+            C.x_cut[KP] = T.total;
+            size_t bi = 0;
+            for (int j = 1; j < KP; ++j) {
+                while (bi < T.blk_off.size() && (int64_t)KP * T.blk_off[bi] < (int64_t)j * T.total) ++bi;
+                C.x_cut[j] = bi < T.blk_off.size() ? T.blk_off[bi] : T.total;
+            }
+            std::vector<std::vector<TcTile>> groups(KP);
+            for (size_t i = 0; i < C.tiles1.size(); ++i) {
+                int j = 0;
+                while (j < KP - 1 && tile1_xend[i] > C.x_cut[j + 1]) ++j;
+                groups[(size_t)j].push_back(C.tiles1[i]);
+            }
+            C.tiles1.clear();
+            C.n1_cut[0] = 0;
+            for (int j = 0; j < KP; ++j) {
+                lpt(groups[(size_t)j]);
+                C.tiles1.insert(C.tiles1.end(), groups[(size_t)j].begin(), groups[(size_t)j].end());
+                C.n1_cut[j + 1] = (int32_t)C.tiles1.size();
+            }
         }
         lpt(C.tiles1x);
         lpt(C.tiles3);

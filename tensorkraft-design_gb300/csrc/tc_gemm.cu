@@ -1401,8 +1401,8 @@ struct TcPlan {
     int32_t* xstride = nullptr;
     int* err = nullptr;
     int n1 = 0, n1x = 0, n3 = 0, nsplit = 0, njobs = 0;
-    int n1_first = 0;       // tiles1[0, n1_first) read psi below x_split only
-    int64_t x_split = 0;
+    int32_t n1_cut[kTcPsiPieces + 1] = {};  // tiles1[n1_cut[j], n1_cut[j + 1]) read psi below x_cut[j + 1]
+    int64_t x_cut[kTcPsiPieces + 1] = {};
     int nst1 = 1, nst1x = 2, nst3 = 2;  // pipeline stages of the GEMM launches
     CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl, mXh, mXl;
     ~TcPlan() {
@@ -1454,8 +1454,8 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
     p->n1 = (int)C.tiles1.size();
-    p->n1_first = C.n1_first;
-    p->x_split = C.x_split;
+    std::copy(C.n1_cut, C.n1_cut + kTcPsiPieces + 1, p->n1_cut);
+    std::copy(C.x_cut, C.x_cut + kTcPsiPieces + 1, p->x_cut);
     p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
     p->n3f = (int)C.tiles3f.size();
@@ -1563,15 +1563,19 @@ void launch_stage1_fused(TcPlan& tc, const double* x, int first, int count, cuda
 
 }  // namespace
 
-bool tc_psi_halves(const TcPlan& tc, int64_t* x_split) {
-    if (tc.nsplit > 0 || tc.n1x > 0 || tc.n1_first <= 0 || tc.n1_first >= tc.n1) return false;
-    *x_split = tc.x_split;
+bool tc_psi_pieces(const TcPlan& tc, int k, int64_t* x_cut, int32_t* n1_cut) {
+    if (k < 2 || k > kTcPsiPieces || kTcPsiPieces % k != 0 || tc.nsplit > 0 || tc.n1x > 0 || tc.n1 <= 0)
+        return false;
+    const int step = kTcPsiPieces / k;
+    for (int j = 0; j <= k; ++j) {
+        x_cut[j] = tc.x_cut[j * step];
+        n1_cut[j] = tc.n1_cut[j * step];
+    }
     return true;
 }
 
-cudaError_t tc_stage1_half(TcPlan& tc, const double* x, int half, cudaStream_t s) {
-    if (half == 0) launch_stage1_fused(tc, x, 0, tc.n1_first, s);
-    else launch_stage1_fused(tc, x, tc.n1_first, tc.n1 - tc.n1_first, s);
+cudaError_t tc_stage1_range(TcPlan& tc, const double* x, int first, int count, cudaStream_t s) {
+    launch_stage1_fused(tc, x, first, count, s);
     return cudaGetLastError();
 }
 

@@ -38,11 +38,13 @@ cudaError_t tc_conversion_check(const double* x, int64_t n, unsigned long long* 
 int* tc_error_word(TcPlan& tc);
 // Kernel launches of one split-precision matvec (tc_apply).
 int tc_launches(const TcPlan& tc);
-// True (and the split point) when stage 1 can run as two launches, the first
-// reading psi only below *x_split: every stack splits psi in the GEMM kernel.
-bool tc_psi_halves(const TcPlan& tc, int64_t* x_split);
-// Stage-1 tiles of one psi half (0: those reading below the split only; 1: the rest).
-cudaError_t tc_stage1_half(TcPlan& tc, const double* x, int half, cudaStream_t s);
+// True when stage 1 can run as k launches over psi in k pieces (k divides
+// kTcPsiPieces; every stack splits psi in the GEMM kernel): x_cut[0..k] are the
+// piece boundaries in psi, and tiles1[n1_cut[j], n1_cut[j + 1]) read psi only
+// below x_cut[j + 1].
+bool tc_psi_pieces(const TcPlan& tc, int k, int64_t* x_cut, int32_t* n1_cut);
+// Stage-1 tiles [first, first + count) of the in-kernel-split list.
+cudaError_t tc_stage1_range(TcPlan& tc, const double* x, int first, int count, cudaStream_t s);
 // Synchronises `s`, reads and clears the error word: TK_ERR_TIMEOUT if set.
 tk_status tc_check_error(TcPlan& tc, cudaStream_t s);
 }  // namespace tk

@@ -209,6 +209,7 @@ struct TcCombJob {
     TcCombTerm inl[kTcCombInline];  // terms[term_begin .. term_end) when there are at most kTcCombInline
 };
 constexpr int kTcCombMaxElems = 512;
+constexpr int kTcPsiPieces = 8;
 struct TcTables {
     int64_t lq_rows = 0, rq_rows = 0, xq_rows = 0, t2q_rows = 0, t1_total = 0;
     std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
@@ -216,9 +217,12 @@ struct TcTables {
     std::vector<double> term_coef64;                   // FP64 coefficients of `terms`
     std::vector<TcTile> tiles1, tiles3;
     std::vector<TcTile> tiles1x;       // stage-1 tiles of tall stacks (B operand from the split copy)
-    // tiles1[0, n1_first) read psi only below element x_split (a block boundary)
-    int32_t n1_first = 0;
-    int64_t x_split = 0;
+    // psi in kTcPsiPieces pieces at block boundaries x_cut[0] = 0 < ... <
+    // x_cut[kTcPsiPieces] = |psi|: tiles1[n1_cut[j], n1_cut[j + 1]) read psi
+    // only below x_cut[j + 1] (a host-buffer matvec starts them once that much
+    // of psi is on the device)
+    int32_t n1_cut[kTcPsiPieces + 1] = {};
+    int64_t x_cut[kTcPsiPieces + 1] = {};
     std::vector<TcSplitJob> split;     // psi -> split copy, tall stacks only
     std::vector<TcCombJob> jobs;
     std::vector<TcCombTerm> terms;

@@ -121,8 +121,9 @@ struct tk_heff2_plan {
     // CUDA graph of the last host-buffer matvec (copies, kernels, error-word
     // read-back), reused while the buffers and the plan settings repeat
     cudaGraphExec_t host_exec = nullptr;
-    cudaStream_t copy_stream = nullptr;  // the psi copy of a host-buffer matvec, in two halves
-    cudaEvent_t ev_fork = nullptr, ev_half[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;  // the psi copy of a host-buffer matvec, in pieces
+    cudaEvent_t ev_fork = nullptr, ev_piece[tk::kTcPsiPieces] = {};
+    int psi_pieces = 2;  // host-buffer psi copy in this many pieces (tk_heff2_set_psi_pieces)
     const void* host_gx = nullptr;
     void* host_gy = nullptr;
     // device addresses of x and y's page-locked mappings when the graph was made
@@ -154,7 +155,7 @@ struct tk_heff2_plan {
         if (pin_err) cudaFreeHost(pin_err);
         if (host_exec) cudaGraphExecDestroy(host_exec);
         if (ev_fork) cudaEventDestroy(ev_fork);
-        for (cudaEvent_t e : ev_half)
+        for (cudaEvent_t e : ev_piece)
             if (e) cudaEventDestroy(e);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);

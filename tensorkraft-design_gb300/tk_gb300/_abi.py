@@ -119,6 +119,7 @@ SIGNATURES = [
     ("tk_heff2_set_host_io", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_set_precision", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_set_schedule", C.c_int32, [C.c_void_p, C.c_int32]),
+    ("tk_heff2_set_psi_pieces", C.c_int32, [C.c_void_p, C.c_int32]),
     ("tk_heff2_get_schedule", C.c_int32, [C.c_void_p, C.POINTER(C.c_int32)]),
     ("tk_heff2_profile", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                      C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_double)]),

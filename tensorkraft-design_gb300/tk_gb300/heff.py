@@ -226,6 +226,10 @@ class Heff2Plan:
         """Host-buffer matvec transfers: one of _abi.HOST_IO_STAGED / DIRECT / DIRECT_OUT / AUTO."""
         check(self._lib.tk_heff2_set_host_io(self._h, mode))
 
+    def set_psi_pieces(self, pieces: int):
+        """tk_heff2_set_psi_pieces: host-buffer psi copied in 1, 2, 4 or 8 pieces."""
+        check(self._lib.tk_heff2_set_psi_pieces(self._h, pieces))
+
     def set_schedule(self, schedule: int):
         """FP64 GEMM launch schedule: _abi.SCHED_GROUPED, _abi.SCHED_PER_BLOCK or
         _abi.SCHED_STACKED (operand stacks as in the split path, built on the

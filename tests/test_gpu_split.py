@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from helpers import exact_problem, models, oracle_bs, rel_err, small_problem
-from tk_gb300 import PREC_BF16X3, PREC_FP64
+from tk_gb300 import PREC_BF16X3, PREC_FP64, TkError
 
 pytestmark = pytest.mark.gpu
 SPLIT_TOL = 2e-4
@@ -110,8 +110,8 @@ def test_integer_pipe_conversions_match_hardware(lib_built):
 
 
 # cylinder D=512 has tall stage-1 stacks (split copy); hubbard D=64 has none,
-# so its staged psi copy runs in two halves overlapped with stage 1
-@pytest.mark.parametrize("name,D", [("cylinder", 512), ("hubbard", 64)])
+# so its staged psi copy runs in pieces overlapped with stage 1
+@pytest.mark.parametrize("name,D", [("cylinder", 512), ("hubbard", 64), ("hubbard", 256)])
 def test_host_io_direct_matches_staged(lib_built, name, D):
     """Split matvec from page-locked host buffers: the kernels reading psi and
     writing y over the CPU-GPU link give the same bits as the staged copies."""
@@ -132,6 +132,16 @@ def test_host_io_direct_matches_staged(lib_built, name, D):
         out[mode] = hy.numpy().copy()
     for mode in modes[1:]:
         assert np.array_equal(out[_abi.HOST_IO_STAGED], out[mode]), mode
+    # psi copied in 1, 2, 4 or 8 pieces: the same bits (the cached graph is rebuilt per setting)
+    for pieces in (1, 4, 8, 2):
+        plan.set_psi_pieces(pieces)
+        for mode in (_abi.HOST_IO_STAGED, _abi.HOST_IO_DIRECT_OUT):
+            plan.set_host_io(mode)
+            hy = torch.full_like(hx, float("nan")).pin_memory()
+            plan.apply_host_flat_ptr(hx.data_ptr(), hy.data_ptr())
+            assert np.array_equal(hy.numpy(), out[_abi.HOST_IO_STAGED]), (pieces, mode)
+    with pytest.raises(TkError):
+        plan.set_psi_pieces(3)
     assert rel_err(out[_abi.HOST_IO_AUTO], oracle_bs(p).apply(x)) < SPLIT_TOL
     # pageable buffers fall back to staged copies in every mode
     plan.set_host_io(_abi.HOST_IO_DIRECT)
