@@ -197,6 +197,16 @@ tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, cons
                       std::max<int64_t>(H.t2_total, 1));
     for (const GemmTable* g : {&H.g1, &H.g3}) b += vb(g->tasks) + vb(g->segs) + 2.0 * vb(g->tiles);
     b += vb(H.jobs) + vb(H.terms);
+    {
+        // the stacked FP64 operands every real plan builds: the same L, R and
+        // T2 stack rows as the split tables, in FP64, and T1 in FP64 (piece
+        // tables about one entry per 64 output rows of a tile)
+        const TcTables& C = H.tc;
+        b += 8.0 * kTcBK * ((double)C.lq_rows + C.rq_rows + std::max<int64_t>(C.t2q_rows, 1)) +
+             8.0 * std::max<int64_t>(C.t1_total, 1) + 2.0 * (vb(C.tiles1) + vb(C.tiles3)) + vb(C.jobs) +
+             vb(C.terms) + 8.0 * C.terms.size() + vb(C.yrow) + vb(C.t1col_base) + vb(C.t1col_stride) + vb(C.xsrc) +
+             vb(C.xstride);
+    }
     if (precision == TK_PREC_BF16X3) {
         const TcTables& C = H.tc;
         const double row = 2.0 * 2.0 * kTcBK;  // hi + lo bf16 per operand row
