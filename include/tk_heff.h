@@ -223,8 +223,9 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
  *     combine launch (default 0: never);
  *   combine_warps: the form of the separate combine: one CTA per job (0,
  *     default), persistent warps that load their next job while storing the
- *     current one (1), or one warp per job, consecutive lanes on consecutive
- *     elements (2).  Every form writes the same T2 bits;
+ *     current one (1), one warp per job, consecutive lanes on consecutive
+ *     elements (2), or one 64-thread CTA per job with eight elements per
+ *     thread (3).  Every form writes the same T2 bits;
  *   stage1_persistent: the stage-1 stacks that split psi inside the GEMM run
  *     as one persistent, warp-specialised kernel (1: producer warps fill the
  *     psi operand and issue the TMA and MMAs of tile i + 1 while epilogue

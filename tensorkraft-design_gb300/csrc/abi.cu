@@ -489,7 +489,7 @@ static tk_status apply_tc_options(tk_heff2_plan* plan, const TcOptions& o) {
 
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts) {
     if (!plan || !opts || opts->tall_max_mtiles < 1 || opts->fuse_max_ntiles < 0 || opts->combine_warps < 0 ||
-        opts->combine_warps > 2 || opts->stage1_persistent < 0 || opts->stage1_persistent > 1) {
+        opts->combine_warps > 3 || opts->stage1_persistent < 0 || opts->stage1_persistent > 1) {
         set_error("tk_heff2_set_tc_options: invalid argument");
         return TK_ERR_INVALID_ARG;
     }
@@ -969,8 +969,8 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
     TK_CUDA(launch_fill_start_vector(plan->hx.p, n, s));
     // candidate schedules; a candidate whose tables come out the same as an
     // earlier one's is not timed again
-    const TcOptions cand[] = {{3, 0, 0, 0}, {3, 0, 0, 1}, {3, 0, 2, 0}, {3, 0, 1, 0},
-                              {3, 2, 0, 0}, {1 << 30, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 2, 0}};
+    const TcOptions cand[] = {{3, 0, 0, 0}, {3, 0, 3, 0}, {3, 0, 0, 1}, {3, 0, 2, 0},
+                              {3, 0, 1, 0}, {3, 2, 0, 0}, {1 << 30, 0, 0, 0}, {1, 0, 0, 0}};
     std::vector<std::vector<size_t>> shapes;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TK_CUDA(cudaEventCreate(&e0));

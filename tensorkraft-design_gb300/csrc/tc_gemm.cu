@@ -1037,13 +1037,11 @@ __device__ __forceinline__ int64_t t1_off(int r, int rs, int c) {
     return kWide ? (int64_t)r * rs + c : (int64_t)(r * rs + c);
 }
 
-template <bool kWide>
-__global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCombJob* __restrict__ jobs,
-                                                                  const TcCombTerm* __restrict__ terms,
-                                                                  const float* __restrict__ t1,
-                                                                  __nv_bfloat16* __restrict__ th,
-                                                                  __nv_bfloat16* __restrict__ tl) {
-    constexpr int U = 4, TU = 2, TCH = 64;
+template <bool kWide, int kThreads = kCombThreads, int U = 4>
+__global__ void __launch_bounds__(kThreads, kThreads == 128 ? 12 : 16) combine_tc_kernel(
+    const TcCombJob* __restrict__ jobs, const TcCombTerm* __restrict__ terms, const float* __restrict__ t1,
+    __nv_bfloat16* __restrict__ th, __nv_bfloat16* __restrict__ tl) {
+    constexpr int TU = 2, TCH = 64;
     __shared__ TcCombTerm st[TCH];
     const TcCombJob j = jobs[blockIdx.x];
     grid_dep_launch();
@@ -1054,8 +1052,8 @@ __global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCo
     const bool inl = nterm <= kTcCombInline;
     const bool resident = !inl && nterm <= TCH;
     if (resident && (int)threadIdx.x < nterm) st[threadIdx.x] = terms[j.term_begin + threadIdx.x];
-    // element threadIdx.x's (row, column) in the job, and one step of kCombThreads elements
-    const int dq = kCombThreads / j.cols, dr = kCombThreads - dq * j.cols;
+    // element threadIdx.x's (row, column) in the job, and one step of kThreads elements
+    const int dq = kThreads / j.cols, dr = kThreads - dq * j.cols;
     int rl = (int)threadIdx.x / j.cols, cl = (int)threadIdx.x - rl * j.cols;
     grid_dep_wait();
     if (resident) __syncthreads();
@@ -1063,13 +1061,13 @@ __global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCo
         const float* src[kTcCombInline];
 #pragma unroll
         for (int q = 0; q < kTcCombInline; ++q) src[q] = t1 + j.inl[q].in_off;
-        for (int e0 = 0; e0 < n; e0 += U * kCombThreads) {
+        for (int e0 = 0; e0 < n; e0 += U * kThreads) {
             bool valid[U];
             int r[U], c[U];
             float acc[U], v[kTcCombInline][U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                valid[u] = e0 + u * kCombThreads + (int)threadIdx.x < n;
+                valid[u] = e0 + u * kThreads + (int)threadIdx.x < n;
                 r[u] = j.r0 + rl;
                 c[u] = cl;
                 acc[u] = 0.f;
@@ -1102,13 +1100,13 @@ __global__ void __launch_bounds__(kCombThreads, 12) combine_tc_kernel(const TcCo
         }
         return;
     }
-    for (int e0 = 0; e0 < n; e0 += U * kCombThreads) {  // block-uniform trip count
+    for (int e0 = 0; e0 < n; e0 += U * kThreads) {  // block-uniform trip count
         bool valid[U];
         int r[U], c[U];
         float acc[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int e = e0 + u * kCombThreads + threadIdx.x;
+            const int e = e0 + u * kThreads + threadIdx.x;
             valid[u] = e < n;
             const int rl = valid[u] ? e / j.cols : 0;
             c[u] = valid[u] ? e - rl * j.cols : 0;
@@ -1382,7 +1380,7 @@ struct TcPlan {
     TcFillSeg* fill_segs = nullptr;
     TcCombTerm* fill_terms = nullptr;
     int n3f = 0;
-    int comb_form = 0;                  // TcOptions::combine_warps: 0 CTA per job, 1 warps, 2 warp per job
+    int comb_form = 0;  // TcOptions::combine_warps: 0 CTA per job, 1 warps, 2 warp per job, 3 64-thread CTA per job
     bool p1 = false;                    // stage 1 as the persistent kernel (TcOptions::stage1_persistent)
     int p1_ctas = 0;                    // its resident CTAs per SM x SMs
     bool t1_wide = false;               // T1 holds 2^31 elements or more (64-bit combine offsets)
@@ -1596,6 +1594,9 @@ cudaError_t tc_apply_stage(TcPlan& tc, const Heff2Tables&, const CombJob*, int, 
             launch_pdl(combine_tc_warp_kernel, std::min(tc.njobs, 152 * 2 * 8) / 8 + 1, 256, 0, s,
                        (const TcCombJob*)tc.jobs, tc.njobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1,
                        tc.th, tc.tl);
+        else if (tc.njobs > 0 && tc.comb_form == 3)
+            launch_pdl(tc.t1_wide ? combine_tc_kernel<true, 64, 8> : combine_tc_kernel<false, 64, 8>, tc.njobs, 64, 0,
+                       s, (const TcCombJob*)tc.jobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);
         else if (tc.njobs > 0)
             launch_pdl(tc.t1_wide ? combine_tc_kernel<true> : combine_tc_kernel<false>, tc.njobs, kCombThreads, 0, s,
                        (const TcCombJob*)tc.jobs, (const TcCombTerm*)tc.terms, (const float*)tc.t1, tc.th, tc.tl);

@@ -253,7 +253,8 @@ struct TcTables {
 //     W_i W_j combine inside the GEMM kernel (0: never; each column tile
 //     rebuilds the operand, so only narrow stacks qualify).
 //   combine_warps: the separate combine as one CTA per job (0), persistent
-//     warps that prefetch their next job (1), or one warp per job (2).
+//     warps that prefetch their next job (1), one warp per job (2), or one
+//     64-thread CTA per job, eight elements per thread (3).
 //   stage1_persistent: the in-kernel-split stage 1 as a persistent,
 //     warp-specialised kernel (1) or one CTA per tile (0).
 struct TcOptions {

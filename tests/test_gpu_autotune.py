@@ -11,7 +11,7 @@ from tk_gb300 import PREC_BF16X3
 
 pytestmark = pytest.mark.gpu
 SPLIT_TOL = 2e-4
-OPTIONS = [(3, 0, 0, 0), (3, 0, 1, 0), (3, 0, 2, 0), (3, 0, 0, 1), (3, 2, 0, 0), (1 << 30, 0, 1, 1), (1, 0, 0, 0),
+OPTIONS = [(3, 0, 0, 0), (3, 0, 1, 0), (3, 0, 2, 0), (3, 0, 3, 0), (3, 0, 0, 1), (3, 2, 0, 0), (1 << 30, 0, 1, 1), (1, 0, 0, 0),
            (1, 0, 2, 1), (3, 1, 1, 0), (1, 8, 0, 1)]
 
 
@@ -40,9 +40,10 @@ def test_every_schedule_matches_the_oracle(lib_built, name, D):
         assert np.isfinite(y).all()
         assert rel_err(y, ref) < SPLIT_TOL, (tall, fuse, warps, pers)
         ys[(tall, fuse, warps, pers)] = y
-    # the combine's three launch forms and both stage-1 kernels compute the same numbers, bit for bit
+    # the combine's four launch forms and both stage-1 kernels compute the same numbers, bit for bit
     assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 1, 0)])
     assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 2, 0)])
+    assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 3, 0)])
     assert np.array_equal(ys[(3, 0, 0, 0)], ys[(3, 0, 0, 1)])
 
 
@@ -54,7 +55,7 @@ def test_fused_stage3_full_size(lib_built):
     x = np.random.default_rng(3).standard_normal(plan.block_dim)
     ref = oracle_bs(p).apply(x)
     y0 = _run(plan, x)
-    for opts in ((3, 2, 0, 0), (3, 0, 1, 0), (3, 0, 2, 0), (3, 0, 0, 1)):
+    for opts in ((3, 2, 0, 0), (3, 0, 1, 0), (3, 0, 2, 0), (3, 0, 3, 0), (3, 0, 0, 1)):
         plan.set_tc_options(*opts)
         y = _run(plan, x)
         assert rel_err(y, ref) < SPLIT_TOL, opts
