@@ -507,6 +507,35 @@ tk_status tk_eigh_lowest_f64(tk_ctx* ctx, const tk_mat* a, int64_t k, double* ev
                              void* stream);
 tk_status tk_qr_f64(tk_ctx* ctx, const tk_mat* a, double* q_dev, double* r_dev, void* stream);
 
+/*
+ * The same three factorisations for complex (C64) matrices, the reference's
+ * `LinAlgBackend<C64>` (traits.rs:63-148 for T = Complex<f64>; faer.rs conventions),
+ * in the planar form the rest of this interface uses for complex data:
+ * element (i, j) = re[i*row_stride + j*col_stride] + i * im[...], and
+ * `is_conjugated` makes the matrix stand for its elementwise conjugate
+ * (MatRef::is_conjugated).  Outputs are planar row-major device buffers of
+ * the real versions' shapes:
+ *   tk_svd_truncated_c64: A = U S V^H; U (m x rank), Vt = V^H (rank x n),
+ *     singular values (real) descending, the same rank rule and truncation
+ *     error as tk_svd_truncated_f64;
+ *   tk_eigh_lowest_c64: a Hermitian matrix (lower triangle read), the k lowest
+ *     eigenvalues (real, ascending) and eigenvectors as the columns of n x k;
+ *   tk_qr_c64: thin QR with Q unitary-column (m x k) and R upper (k x n).
+ */
+typedef struct {
+    const double* re;
+    const double* im;
+    int64_t rows, cols, row_stride, col_stride;
+    int32_t is_conjugated;
+} tk_cmat;
+tk_status tk_svd_truncated_c64(tk_ctx* ctx, const tk_cmat* a, int64_t max_rank, double cutoff, double* u_re,
+                               double* u_im, double* s_host, double* vt_re, double* vt_im, int64_t* rank,
+                               double* truncation_error, void* stream);
+tk_status tk_eigh_lowest_c64(tk_ctx* ctx, const tk_cmat* a, int64_t k, double* evals_host, double* evecs_re,
+                             double* evecs_im, void* stream);
+tk_status tk_qr_c64(tk_ctx* ctx, const tk_cmat* a, double* q_re, double* q_im, double* r_re, double* r_im,
+                    void* stream);
+
 /* SparseLinAlgBackend::spmv (tk-linalg/src/traits.rs:193-198): y = A x for
  * a rank-2 host tensor and host vectors (y fully overwritten). */
 tk_status tk_spmv_f64(tk_ctx* ctx, const tk_bst* a, const double* x, double* y);

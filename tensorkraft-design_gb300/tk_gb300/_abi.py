@@ -71,6 +71,11 @@ class tk_mat(C.Structure):
                 ("col_stride", C.c_int64), ("is_conjugated", C.c_int32)]
 
 
+class tk_cmat(C.Structure):
+    _fields_ = [("re", C.c_void_p), ("im", C.c_void_p), ("rows", C.c_int64), ("cols", C.c_int64),
+                ("row_stride", C.c_int64), ("col_stride", C.c_int64), ("is_conjugated", C.c_int32)]
+
+
 class tk_mat_mut(C.Structure):
     _fields_ = [("data", C.c_void_p), ("rows", C.c_int64), ("cols", C.c_int64), ("row_stride", C.c_int64),
                 ("col_stride", C.c_int64)]
@@ -163,6 +168,13 @@ SIGNATURES = [
                                        C.c_void_p]),
     ("tk_eigh_batched_f64", C.c_int32, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("tk_qr_f64", C.c_int32, [C.c_void_p, C.POINTER(tk_mat), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("tk_svd_truncated_c64", C.c_int32, [C.c_void_p, C.POINTER(tk_cmat), C.c_int64, C.c_double, C.c_void_p,
+                                         C.c_void_p, C.POINTER(C.c_double), C.c_void_p, C.c_void_p,
+                                         C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_void_p]),
+    ("tk_eigh_lowest_c64", C.c_int32, [C.c_void_p, C.POINTER(tk_cmat), C.c_int64, C.POINTER(C.c_double),
+                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("tk_qr_c64", C.c_int32, [C.c_void_p, C.POINTER(tk_cmat), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p]),
     ("tk_check_split_conversions", C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_uint64)]),
     ("tk_env_layout", C.c_int32, [C.c_int32, C.POINTER(tk_qindex), C.POINTER(tk_qindex), C.POINTER(tk_qindex),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_uint64), C.POINTER(C.c_int64),

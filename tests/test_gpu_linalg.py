@@ -146,3 +146,76 @@ def test_eigh_lowest_and_qr(lib_built):
         assert np.allclose(Q.T @ Q, np.eye(k), atol=1e-12)
         assert np.allclose(np.tril(R, -1), 0.0)
         assert np.allclose(Q @ R, A, atol=1e-12)
+
+
+def _cmat(re, im, rows, cols, rs, cs, conj=0):
+    return _abi.tk_cmat(re.data_ptr(), im.data_ptr(), rows, cols, rs, cs, conj)
+
+
+@pytest.mark.parametrize("m,n,transposed,conj", [(30, 18, False, 0), (18, 30, False, 1), (24, 24, True, 0)])
+def test_complex_svd_truncated_matches_numpy(lib_built, m, n, transposed, conj):
+    """svd_truncated for C64 (planar): A = U S V^H with the real version's rank rule;
+    strided and conjugated inputs."""
+    import torch
+
+    rng = np.random.default_rng(m * n + conj)
+    A = (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))) @ np.diag(np.logspace(0, -6, n))
+    stored = np.ascontiguousarray(A.T if transposed else A)
+    if conj:
+        stored = stored.conj()  # the matrix handed over is conj(A), flagged as conjugated
+    re = torch.from_numpy(stored.real.copy()).cuda()
+    im = torch.from_numpy(stored.imag.copy()).cuda()
+    mat = _cmat(re, im, m, n, 1 if transposed else n, m if transposed else 1, conj)
+    k = min(m, n)
+    sv_ref = np.linalg.svd(A, compute_uv=False)
+    for max_rank, cutoff in ((k, 0.0), (7, 0.0), (k, 1e-3)):
+        ur, ui = (torch.empty(m * k, dtype=torch.float64).cuda() for _ in range(2))
+        vr, vi = (torch.empty(k * n, dtype=torch.float64).cuda() for _ in range(2))
+        s = np.zeros(k)
+        rank, err = C.c_int64(), C.c_double()
+        _abi.check(_abi.load().tk_svd_truncated_c64(context(0), C.byref(mat), max_rank, cutoff,
+                                                    C.c_void_p(ur.data_ptr()), C.c_void_p(ui.data_ptr()),
+                                                    _abi.dptr(s), C.c_void_p(vr.data_ptr()),
+                                                    C.c_void_p(vi.data_ptr()), C.byref(rank), C.byref(err), None))
+        r = rank.value
+        assert r == int(min(max_rank, np.sum(sv_ref >= cutoff * sv_ref[0])))
+        assert np.allclose(s[:r], sv_ref[:r], rtol=1e-12, atol=1e-14)
+        assert abs(err.value - np.sum(sv_ref[r:] ** 2)) < 1e-12
+        U = (ur.cpu().numpy() + 1j * ui.cpu().numpy())[:m * r].reshape(m, r)
+        Vt = (vr.cpu().numpy() + 1j * vi.cpu().numpy())[:r * n].reshape(r, n)
+        assert np.allclose(U.conj().T @ U, np.eye(r), atol=1e-11)
+        assert np.allclose(Vt @ Vt.conj().T, np.eye(r), atol=1e-11)
+        assert np.linalg.norm(A - U @ np.diag(s[:r]) @ Vt) ** 2 - np.sum(sv_ref[r:] ** 2) < 1e-10
+
+
+def test_complex_eigh_lowest_and_qr(lib_built):
+    import torch
+
+    rng = np.random.default_rng(4)
+    B = rng.standard_normal((26, 26)) + 1j * rng.standard_normal((26, 26))
+    H = (B + B.conj().T) / 2
+    hr, hi = torch.from_numpy(H.real.copy()).cuda(), torch.from_numpy(H.imag.copy()).cuda()
+    lib = _abi.load()
+    ev = np.zeros(4)
+    vr, vi = (torch.empty(26 * 4, dtype=torch.float64).cuda() for _ in range(2))
+    _abi.check(lib.tk_eigh_lowest_c64(context(0), C.byref(_cmat(hr, hi, 26, 26, 26, 1)), 4, _abi.dptr(ev),
+                                      C.c_void_p(vr.data_ptr()), C.c_void_p(vi.data_ptr()), None))
+    assert np.allclose(ev, np.linalg.eigvalsh(H)[:4], atol=1e-12)
+    V = (vr.cpu().numpy() + 1j * vi.cpu().numpy()).reshape(26, 4)
+    assert np.allclose(H @ V, V * ev[None, :], atol=1e-10)
+    assert lib.tk_eigh_lowest_c64(context(0), C.byref(_cmat(hr, hi, 26, 26, 26, 1)), 27, _abi.dptr(np.zeros(27)),
+                                  C.c_void_p(vr.data_ptr()), C.c_void_p(vi.data_ptr()), None) == 1
+    for m, n in ((20, 12), (12, 20)):
+        A = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+        ar, ai = torch.from_numpy(A.real.copy()).cuda(), torch.from_numpy(A.imag.copy()).cuda()
+        k = min(m, n)
+        qr_, qi = (torch.empty(m * k, dtype=torch.float64).cuda() for _ in range(2))
+        rr, ri = (torch.empty(k * n, dtype=torch.float64).cuda() for _ in range(2))
+        _abi.check(lib.tk_qr_c64(context(0), C.byref(_cmat(ar, ai, m, n, n, 1)), C.c_void_p(qr_.data_ptr()),
+                                 C.c_void_p(qi.data_ptr()), C.c_void_p(rr.data_ptr()), C.c_void_p(ri.data_ptr()),
+                                 None))
+        Q = (qr_.cpu().numpy() + 1j * qi.cpu().numpy()).reshape(m, k)
+        R = (rr.cpu().numpy() + 1j * ri.cpu().numpy()).reshape(k, n)
+        assert np.allclose(Q.conj().T @ Q, np.eye(k), atol=1e-12)
+        assert np.allclose(np.tril(R, -1), 0.0)
+        assert np.allclose(Q @ R, A, atol=1e-12)
