@@ -566,20 +566,24 @@ def _pinned(device: int, name: str, n: int) -> np.ndarray:
 
 def split_two_site_device(kind, psi_dev, keys, offs, legs, max_bond: int, cutoff: float, to_right: bool,
                           min_bond: int = 1, device: int = 0):
-    """The two-site truncation of a real two-site vector that lives on the
-    device (the plan's block layout): every bond-charge block M_q is gathered
-    on the GPU and copied to the host once (tk_split_gather), decomposed by
-    LAPACK's SVD on a host thread pool (the SVD truncate_svd takes,
-    truncation/mod.rs:68), the kept set chosen by truncate_svd's rule over all
-    charges (_select), and the kept factors scattered into the new site
-    tensors on the GPU (tk_split_factors): A_i = U, A_j = S V^T / norm moving
-    right; A_i = U S / norm, A_j = V^T moving left.  Returns (A_i, A_j as
-    SiteTensor, new bond QIndex, discarded weight) like split_two_site."""
+    """The two-site truncation of a two-site vector that lives on the device
+    (the plan's block layout; a tensor, or a (real, imaginary) pair of tensors
+    for a complex vector): every bond-charge block M_q is gathered on the GPU
+    and copied to the host once (tk_split_gather, once per part), decomposed
+    by LAPACK's SVD on a host thread pool (the SVD truncate_svd takes,
+    truncation/mod.rs:68; complex M_q = U S V^H), the kept set chosen by
+    truncate_svd's rule over all charges (_select), and the kept factors
+    scattered into the new site tensors on the GPU (tk_split_factors, once per
+    part): A_i = U, A_j = S V^H / norm moving right; A_i = U S / norm,
+    A_j = V^H moving left.  Returns (A_i, A_j as SiteTensor, new bond QIndex,
+    discarded weight) like split_two_site."""
     from .symmetry import ncomp
 
     torch = _torch()
     lib = _abi.load()
     ctx = context(device)
+    cplx = isinstance(psi_dev, tuple)
+    parts = list(psi_dev) if cplx else [psi_dev]
     m = _Marshal()
     qlegs = (_abi.tk_qindex * 4)(*[m.qindex(ix) for ix in legs])
     keys = np.ascontiguousarray(keys, dtype=np.uint64)
@@ -596,11 +600,18 @@ def split_two_site_device(kind, psi_dev, keys, offs, legs, max_bond: int, cutoff
         check(lib.tk_split_charges(h, C.byref(n), _abi.i32ptr(ch), _abi.i64ptr(rows), _abi.i64ptr(cols)))
         rows, cols = rows[:nq], cols[:nq]
         moff = np.concatenate([[0], np.cumsum(rows * cols)]).astype(np.int64)
-        mbuf = _pinned(device, "split_m", int(moff[-1]))
-        check(lib.tk_split_gather(h, C.c_void_p(psi_dev.data_ptr()), C.c_void_p(mbuf.ctypes.data), None))
+        mbufs = []
+        for k_, part in enumerate(parts):
+            mb = _pinned(device, f"split_m{k_}", int(moff[-1]))
+            check(lib.tk_split_gather(h, C.c_void_p(part.data_ptr()), C.c_void_p(mb.ctypes.data), None))
+            mbufs.append(mb)
+
+        def block(i):
+            mq = mbufs[0][moff[i]:moff[i + 1]].reshape(rows[i], cols[i])
+            return mq + 1j * mbufs[1][moff[i]:moff[i + 1]].reshape(rows[i], cols[i]) if cplx else mq
 
         def svd(i):
-            return i, np.linalg.svd(mbuf[moff[i]:moff[i + 1]].reshape(rows[i], cols[i]), full_matrices=False)
+            return i, np.linalg.svd(block(i), full_matrices=False)
 
         # largest factorisations first on the pool (one BLAS thread each)
         order = sorted(range(nq), key=lambda i: -int(rows[i] * cols[i] * min(rows[i], cols[i])))
@@ -617,10 +628,14 @@ def split_two_site_device(kind, psi_dev, keys, offs, legs, max_bond: int, cutoff
             lay.append((k_[:nb_], o_[:nb_]))
         ku = kept * rows
         kv = kept * cols
-        ubuf = _pinned(device, "split_u", int(ku.sum()))
-        vbuf = _pinned(device, "split_v", int(kv.sum()))
         uo = np.concatenate([[0], np.cumsum(ku)])
         vo = np.concatenate([[0], np.cumsum(kv)])
+        if cplx:
+            ubuf = np.zeros(int(ku.sum()), dtype=np.complex128)
+            vbuf = np.zeros(int(kv.sum()), dtype=np.complex128)
+        else:  # real factors go straight into the page-locked buffers the scatter copies from
+            ubuf = _pinned(device, "split_u0", int(ku.sum()))
+            vbuf = _pinned(device, "split_v0", int(kv.sum()))
         for i in range(nq):
             k = int(kept[i])
             if k == 0:
@@ -633,17 +648,29 @@ def split_two_site_device(kind, psi_dev, keys, offs, legs, max_bond: int, cutoff
                 ubuf[uo[i]:uo[i + 1]] = (U[:, :k] * (S[None, :k] / norm)).reshape(-1)
                 vbuf[vo[i]:vo[i + 1]] = Vh[:k].reshape(-1)
         dev = f"cuda:{device}"
-        ai = torch.empty(max(ti.value, 1), dtype=torch.float64, device=dev)
-        aj = torch.empty(max(tj.value, 1), dtype=torch.float64, device=dev)
-        check(lib.tk_split_factors(h, C.c_void_p(ubuf.ctypes.data), C.c_void_p(vbuf.ctypes.data),
-                                   C.c_void_p(ai.data_ptr()), C.c_void_p(aj.data_ptr()), None))
+        out = []
+        for k_ in range(len(parts)):
+            if cplx:
+                up = _pinned(device, f"split_u{k_}", int(ku.sum()))
+                vp = _pinned(device, f"split_v{k_}", int(kv.sum()))
+                up[:] = ubuf.imag if k_ else ubuf.real
+                vp[:] = vbuf.imag if k_ else vbuf.real
+            else:
+                up, vp = ubuf, vbuf
+            ai = torch.empty(max(ti.value, 1), dtype=torch.float64, device=dev)
+            aj = torch.empty(max(tj.value, 1), dtype=torch.float64, device=dev)
+            check(lib.tk_split_factors(h, C.c_void_p(up.ctypes.data), C.c_void_p(vp.ctypes.data),
+                                       C.c_void_p(ai.data_ptr()), C.c_void_p(aj.data_ptr()), None))
+            out.append((ai, aj))
     finally:
         lib.tk_split_plan_destroy(h)
     qs = [tuple(int(x) for x in ch[i * nc:(i + 1) * nc]) for i in range(nq)]
     nb = QIndex(kind, [(qs[i], int(kept[i])) for i in range(nq) if kept[i] > 0])
     PI, PJ, QA, QB = legs
-    Ai = SiteTensor(kind, [PI, QA, nb], lay[0][0], lay[0][1], ai)
-    Aj = SiteTensor(kind, [PJ, nb, QB], lay[1][0], lay[1][1], aj)
+    im_i = out[1][0] if cplx else None
+    im_j = out[1][1] if cplx else None
+    Ai = SiteTensor(kind, [PI, QA, nb], lay[0][0], lay[0][1], out[0][0], im_i)
+    Aj = SiteTensor(kind, [PJ, nb, QB], lay[1][0], lay[1][1], out[0][1], im_j)
     return Ai, Aj, nb, disc
 
 
@@ -1034,11 +1061,16 @@ class DeviceDMRG:
                     energy = float(torch.dot(y, hy))
                 keys, offs = plan.blocks()
                 legs = [self.model.phys, self.model.phys, self.bonds[i], self.bonds[i + 2]]
-                Ai, Aj, nb, disc = split_two_site(self.kind, self._host(y), keys, offs, legs, max_bond, cutoff,
-                                                  to_right, eigh_batch=self.eigh_batch, min_bond=min_bond)
-                P = self.model.phys
-                self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
-                self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj, self.device)
+                if self.host_split:
+                    Ai, Aj, nb, disc = split_two_site(self.kind, self._host(y), keys, offs, legs, max_bond, cutoff,
+                                                      to_right, eigh_batch=self.eigh_batch, min_bond=min_bond)
+                    P = self.model.phys
+                    self.sites[i] = SiteTensor.from_blocks(self.kind, [P, self.bonds[i], nb], Ai, self.device)
+                    self.sites[i + 1] = SiteTensor.from_blocks(self.kind, [P, nb, self.bonds[i + 2]], Aj,
+                                                               self.device)
+                else:
+                    self.sites[i], self.sites[i + 1], nb, disc = split_two_site_device(
+                        self.kind, y, keys, offs, legs, max_bond, cutoff, to_right, min_bond, self.device)
                 self.bonds[i + 1] = nb
                 plan.close()
                 if to_right:

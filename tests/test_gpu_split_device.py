@@ -124,3 +124,35 @@ def test_matches_the_host_split(lib_built):
         hj = SiteTensor.from_blocks(kind, [P, hb, QB], Hj, 0)
         a, b = _product(Ai, Aj), _product(hi, hj)
         assert np.linalg.norm(a - b) < 1e-10 * np.linalg.norm(b)
+
+
+def test_complex_vector_reconstructs_and_truncates(lib_built):
+    """A complex two-site vector (real and imaginary parts on the device): full
+    rank reconstructs T, the factor on the growing side is an isometry in the
+    Hermitian sense, and a truncation keeps truncate_svd's count with the
+    weight of the discarded singular values of the complex matrix."""
+    kind, P, QA, QB, keys, offs, qs, psi = _case()
+    rng = np.random.default_rng(9)
+    psi_im = rng.standard_normal(psi.shape)
+    T = _dense(kind, psi, keys, offs, qs, P, QA, QB) + 1j * _dense(kind, psi_im, keys, offs, qs, P, QA, QB)
+    d = P.total_dim
+    M = T.transpose(0, 2, 1, 3).reshape(d * QA.total_dim, d * QB.total_dim)
+    sv = np.sort(np.linalg.svd(M, compute_uv=False))[::-1]
+    for to_right in (True, False):
+        Ai, Aj, nb, disc = split_two_site_device(kind, (_dev(psi), _dev(psi_im)), keys, offs, [P, P, QA, QB],
+                                                 10_000, 0.0, to_right)
+        assert Ai.is_complex and Aj.is_complex
+        A, B = Ai.to_dense(), Aj.to_dense()
+        assert disc < 1e-24
+        assert np.allclose(np.einsum("sab,tbc->stac", A, B), T, atol=1e-12)
+        if to_right:
+            assert np.allclose(np.einsum("sab,sac->bc", A.conj(), A), np.eye(nb.total_dim), atol=1e-12)
+        else:
+            assert np.allclose(np.einsum("sab,scb->ac", B, B.conj()), np.eye(nb.total_dim), atol=1e-12)
+    for cutoff, max_bond in ((0.3, 100), (0.0, 6)):
+        want = max(1, min(max_bond, int(np.sum(sv >= cutoff * sv[0]))))
+        Ai, Aj, nb, disc = split_two_site_device(kind, (_dev(psi), _dev(psi_im)), keys, offs, [P, P, QA, QB],
+                                                 max_bond, cutoff, True)
+        assert nb.total_dim == want
+        assert abs(disc - np.sum(sv[want:] ** 2) / np.sum(sv ** 2)) < 1e-12
+
