@@ -134,6 +134,8 @@ def test_complex_vector_reconstructs_and_truncates(lib_built):
     kind, P, QA, QB, keys, offs, qs, psi = _case()
     rng = np.random.default_rng(9)
     psi_im = rng.standard_normal(psi.shape)
+    scale = 1.0 / np.sqrt(np.sum(psi ** 2) + np.sum(psi_im ** 2))  # the split returns the normalised state
+    psi, psi_im = psi * scale, psi_im * scale
     T = _dense(kind, psi, keys, offs, qs, P, QA, QB) + 1j * _dense(kind, psi_im, keys, offs, qs, P, QA, QB)
     d = P.total_dim
     M = T.transpose(0, 2, 1, 3).reshape(d * QA.total_dim, d * QB.total_dim)
