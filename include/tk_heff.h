@@ -183,14 +183,14 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision);
  * launch per output block, the GPU analogue of the reference's one-task-at-a-
  * time block_gemm loop (tk-linalg/src/device/faer.rs:439-512), kept as the
  * baseline the grouped launch is measured against.  TK_SCHED_STACKED (the
- * default of real plans, built with the plan): the sector GEMMs regrouped
+ * default, built with the plan): the sector GEMMs regrouped
  * into operand stacks, one per ket sector of L and one per bra sector of R
  * (the split-precision path's grouping, in FP64), cut into pieces of at most
  * 32 x 64 outputs that step over the stack columns their rows hold, so that
- * nearly every FP64 FMA issued is one of the product's own.  Complex plans
- * run TK_SCHED_GROUPED (TK_SCHED_STACKED: TK_ERR_UNSUPPORTED).  Every
- * schedule computes the same sums in FP64; they differ only in the order of
- * the additions. */
+ * nearly every FP64 FMA issued is one of the product's own (complex plans:
+ * the same pieces with complex FMAs on planar operands; the default of
+ * complex plans too).  Every schedule computes the same sums in FP64; they
+ * differ only in the order of the additions. */
 #define TK_SCHED_GROUPED   0
 #define TK_SCHED_PER_BLOCK 1
 #define TK_SCHED_STACKED   2

@@ -392,7 +392,9 @@ extern "C" tk_status tk_heff2_launches(const tk_heff2_plan* plan, int32_t* per_a
     }
     const tk_heff2_plan* p = plan;
     int n = 0;
-    if (p->is_complex) {
+    if (p->is_complex && p->schedule == TK_SCHED_STACKED) {
+        n = f64stack_launches(*p->f64s) + (p->n_jobs > 0);  // the combine runs once per part
+    } else if (p->is_complex) {
         n = 4 * (p->g1.n_tiles > 0) + 2 * (p->n_jobs > 0) + 4 * (p->g3.n_tiles > 0);
     } else if (p->precision == TK_PREC_BF16X3) {
         n = tc_launches(*p->tc);
@@ -414,6 +416,10 @@ tk_status tk_heff2_apply_complex_s(tk_heff2_plan* p, const double* xr, const dou
     if (!p->is_complex) {
         set_error("complex matvec on a real plan");
         return TK_ERR_INVALID_ARG;
+    }
+    if (p->schedule == TK_SCHED_STACKED) {
+        TK_CUDA(f64stack_apply_complex(*p->f64s, xr, xi, yr, yi, s));
+        return TK_OK;
     }
     TK_CUDA(launch_gemm_c64(p->g1.tiles.p, p->g1.n_tiles, p->g1.tasks.p, p->g1.segs.p, p->lbuf.p, p->lbuf_im.p, xr, xi,
                             p->t1.p, p->t1_im.p, false, s));
@@ -524,13 +530,24 @@ tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
         return TK_ERR_INVALID_ARG;
     }
     if (schedule == TK_SCHED_STACKED && !plan->f64s) {
-        if (plan->is_complex) {
-            set_error("tk_heff2_set_schedule: the stacked schedule takes real plans only");
-            return TK_ERR_UNSUPPORTED;
-        }
         DeviceGuard g(plan->device);
         std::string err;
-        tk_status st = build_f64_stacks(plan->host, err);
+        // a complex plan's imaginary slabs live on the device only: host copies for the stacks
+        std::vector<double> lim, rim;
+        if (plan->is_complex) {
+            lim.resize(plan->lbuf_im.n);
+            rim.resize(plan->rbuf_im.n);
+            if (lim.size() != plan->host.lbuf.size() || rim.size() != plan->host.rbuf.size()) {
+                set_error("tk_heff2_set_schedule: imaginary environment slabs of another size");
+                return TK_ERR_INVALID_ARG;
+            }
+            if (!lim.empty()) TK_CUDA(cudaMemcpy(lim.data(), plan->lbuf_im.p, sizeof(double) * lim.size(),
+                                                 cudaMemcpyDeviceToHost));
+            if (!rim.empty()) TK_CUDA(cudaMemcpy(rim.data(), plan->rbuf_im.p, sizeof(double) * rim.size(),
+                                                 cudaMemcpyDeviceToHost));
+        }
+        tk_status st = build_f64_stacks(plan->host, err, plan->is_complex ? lim.data() : nullptr,
+                                        plan->is_complex ? rim.data() : nullptr);
         if (st == TK_OK)
             st = guard_host("stacked FP64 plan", err, [&] { return f64stack_create(plan->host.f64st, plan->f64s, err); });
         // the device copy is the one that runs: the host tables go

@@ -304,6 +304,13 @@ tk_status tk_heff2_plan_create_dev_complex(tk_ctx* ctx, const tk_env* env_l, con
         return cuda_fail("tk_heff2_plan_create_dev_complex", e);
     }
     p->is_complex = true;
+    // the complex FP64 matvec runs on operand stacks, as a real plan's does
+    st = tk_heff2_set_schedule(p, TK_SCHED_STACKED);
+    if (st != TK_OK) {
+        tk_heff2_plan_destroy(p);
+        *out = nullptr;
+        return st;
+    }
     return TK_OK;
 }
 

@@ -522,15 +522,12 @@ struct StackCopy {
     int64_t nr, len, k_off, row0, chunk_rows;
 };
 
-// Fills the bf16 hi / lo stacks of `rows` rows x kTcBK from the copy jobs:
-// hi = bf16(v), lo = bf16(v - hi) (both rounded to nearest even through
-// fp32), zero where no slab lands.  Jobs write disjoint elements, so row
-// ranges of them run on several threads with the same result as one.
-static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, std::vector<uint16_t>& hi,
-                              std::vector<uint16_t>& lo) {
+// Every element of the stack copies, (destination index, value), to `put`,
+// on up to 16 host threads (one per 128 Ki elements): the copies write
+// disjoint destinations, so the threads share no output element.
+template <class Put>
+static void for_stack_elements(const std::vector<StackCopy>& jobs, Put put) {
     const int BK = kTcBK;
-    hi.assign((size_t)rows * BK, 0);
-    lo.assign((size_t)rows * BK, 0);
     struct Item { size_t job; int64_t r0, r1; };
     std::vector<Item> items;
     int64_t total = 0;
@@ -541,8 +538,6 @@ static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, 
         for (int64_t r0 = 0; r0 < jobs[j].nr; r0 += step) items.push_back({j, r0, std::min(jobs[j].nr, r0 + step)});
         total += jobs[j].nr * jobs[j].len;
     }
-    uint16_t* H = hi.data();
-    uint16_t* L = lo.data();
     std::atomic<size_t> next{0};
     auto work = [&]() {
         for (size_t it; (it = next.fetch_add(1)) < items.size();) {
@@ -551,17 +546,12 @@ static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, 
                 const double* src = c.src + r * c.len;
                 for (int64_t kk = 0; kk < c.len; ++kk) {
                     const int64_t k = c.k_off + kk;
-                    const size_t at = (size_t)(c.row0 + (k / BK) * c.chunk_rows + r) * BK + (size_t)(k % BK);
-                    const double v = src[kk];
-                    const uint16_t h = f32_to_bf16_bits((float)v);
-                    H[at] = h;
-                    L[at] = f32_to_bf16_bits((float)(v - (double)bf16_bits_to_f32(h)));
+                    put((size_t)(c.row0 + (k / BK) * c.chunk_rows + r) * BK + (size_t)(k % BK), src[kk]);
                 }
             }
         }
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    // one thread per 128 Ki elements, at most 16
     const unsigned nt = (unsigned)std::min<int64_t>(std::min(hw, 16u), std::max<int64_t>(1, total >> 17));
     std::vector<std::thread> pool;
     pool.reserve(nt);  // no reallocation (and no throw) once a thread runs
@@ -576,19 +566,29 @@ static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, 
     for (std::thread& t : pool) t.join();
 }
 
+// Fills the bf16 hi / lo stacks of `rows` rows x kTcBK from the copy jobs:
+// hi = bf16(v), lo = bf16(v - hi) (both rounded to nearest even through
+// fp32), zero where no slab lands.  Jobs write disjoint elements, so row
+// ranges of them run on several threads with the same result as one.
+static void fill_split_stacks(const std::vector<StackCopy>& jobs, int64_t rows, std::vector<uint16_t>& hi,
+                              std::vector<uint16_t>& lo) {
+    hi.assign((size_t)rows * kTcBK, 0);
+    lo.assign((size_t)rows * kTcBK, 0);
+    uint16_t* H = hi.data();
+    uint16_t* L = lo.data();
+    for_stack_elements(jobs, [H, L](size_t at, double v) {
+        const uint16_t h = f32_to_bf16_bits((float)v);
+        H[at] = h;
+        L[at] = f32_to_bf16_bits((float)(v - (double)bf16_bits_to_f32(h)));
+    });
+}
+
 // The same stacks in FP64 (the stacked FP64 schedule): element for element
 // the environment values, zero where no slab lands.
 static void fill_stacks_f64(const std::vector<StackCopy>& jobs, int64_t rows, std::vector<double>& out) {
-    const int BK = kTcBK;
-    out.assign((size_t)rows * BK, 0.0);
-    for (const StackCopy& c : jobs)
-        for (int64_t r = 0; r < c.nr; ++r) {
-            const double* src = c.src + r * c.len;
-            for (int64_t kk = 0; kk < c.len; ++kk) {
-                const int64_t k = c.k_off + kk;
-                out[(size_t)(c.row0 + (k / BK) * c.chunk_rows + r) * BK + (size_t)(k % BK)] = src[kk];
-            }
-        }
+    out.assign((size_t)rows * kTcBK, 0.0);
+    double* O = out.data();
+    for_stack_elements(jobs, [O](size_t at, double v) { O[at] = v; });
 }
 
 // The split-precision (tensor-core) tables: both GEMM stages regrouped into
@@ -596,7 +596,8 @@ static void fill_stacks_f64(const std::vector<StackCopy>& jobs, int64_t rows, st
 // FP64 tables with the schedule options `o` (tall stage-1 stacks, fused stage
 // 3).  Rebuilt alone when a plan changes its options.
 static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOptions& o, TcTables& C, bool fp64,
-                                 std::string& err) {
+                                 std::string& err, const double* lbuf_im = nullptr,
+                                 const double* rbuf_im = nullptr) {
     using Term = TcSource::Term;
     const int nA = X.nA, nB = X.nB, nWL = X.nWL, nWR = X.nWR;
     const int64_t P = X.P, nwr = X.nwr;
@@ -926,6 +927,15 @@ static tk_status build_tc_tables(Heff2Tables& T, const TcSource& X, const TcOpti
         if (fp64) {
             fill_stacks_f64(lcopy, C.lq_rows, C.lq64);
             fill_stacks_f64(rcopy, C.rq_rows, C.rq64);
+            if (lbuf_im && rbuf_im) {
+                // imaginary parts of complex environments: the same copies from the
+                // same offsets of the imaginary slab arrays
+                std::vector<StackCopy> li(lcopy), ri(rcopy);
+                for (StackCopy& c : li) c.src = lbuf_im + (c.src - T.lbuf.data());
+                for (StackCopy& c : ri) c.src = rbuf_im + (c.src - T.rbuf.data());
+                fill_stacks_f64(li, C.lq_rows, C.lq64_im);
+                fill_stacks_f64(ri, C.rq_rows, C.rq64_im);
+            }
         } else {
             fill_split_stacks(lcopy, C.lq_rows, C.lq_hi, C.lq_lo);
             fill_split_stacks(rcopy, C.rq_rows, C.rq_hi, C.rq_lo);
@@ -1325,7 +1335,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
 
 namespace tk {
 
-tk_status build_f64_stacks(Heff2Tables& T, std::string& err) {
+tk_status build_f64_stacks(Heff2Tables& T, std::string& err, const double* lbuf_im, const double* rbuf_im) {
     if (!T.tcsrc) {
         err = "the plan keeps no sector structure to build from";
         return TK_ERR_UNSUPPORTED;
@@ -1335,7 +1345,7 @@ tk_status build_f64_stacks(Heff2Tables& T, std::string& err) {
         o.tall_max_mtiles = 1 << 30;  // every stage-1 column read from psi through its table
         o.fuse_max_ntiles = 0;        // every stage-3 stack reads a combined T2
         TcTables C;
-        tk_status st = build_tc_tables(T, *T.tcsrc, o, C, true, err);
+        tk_status st = build_tc_tables(T, *T.tcsrc, o, C, true, err, lbuf_im, rbuf_im);
         if (st == TK_OK && !validate_tc(T, C, err)) {
             err = "internal table check failed: " + err;
             st = TK_ERR_INVALID_ARG;

@@ -72,52 +72,81 @@ struct DenseMap {
     }
 };
 
-// acc[r] += sum over k < kl of As[k][m_r] * Bs[k][n_r], k ascending.  A full
-// step is unrolled; a short one loops exactly kl times, so that no FMA past
-// the segment's end is issued (predicated off, it would still hold the pipe).
-__device__ __forceinline__ void dense_kstep(const double (*As)[SBM + 1], const double (*Bs)[SBN + 1], int kl,
-                                            const DenseMap& d, int tid, double* acc) {
+// acc[r] += sum over k < kl of A[k][m_r] * B[k][n_r], k ascending; complex
+// (CPLX): (ar + i ai)(br + i bi) accumulated as re += ar br - ai bi and
+// im += ar bi + ai br.  A full step is unrolled; a short one loops exactly kl
+// times, so that no FMA past the segment's end is issued (predicated off, it
+// would still hold the pipe).
+template <bool CPLX>
+__device__ __forceinline__ void dense_kstep(const double (*Ar)[SBM + 1], const double (*Ai)[SBM + 1],
+                                            const double (*Br)[SBN + 1], const double (*Bi)[SBN + 1], int kl,
+                                            const DenseMap& d, int tid, double* accr, double* acci) {
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
         if (r < d.rounds) {
             const int e = min(tid + ST * r, d.total - 1);  // lanes past the end read a valid element
             const int m = e / d.nv, n = e - m * d.nv;
-            double s = acc[r];
+            double sr = accr[r], si = CPLX ? acci[r] : 0.0;
+            auto step = [&](int k) {
+                sr = fma(Ar[k][m], Br[k][n], sr);
+                if constexpr (CPLX) {
+                    sr = fma(-Ai[k][m], Bi[k][n], sr);
+                    si = fma(Ar[k][m], Bi[k][n], si);
+                    si = fma(Ai[k][m], Br[k][n], si);
+                }
+            };
             if (kl == SBK) {
 #pragma unroll
-                for (int k = 0; k < SBK; ++k) s = fma(As[k][m], Bs[k][n], s);
+                for (int k = 0; k < SBK; ++k) step(k);
             } else {
 #pragma unroll 1
-                for (int k = 0; k < kl; ++k) s = fma(As[k][m], Bs[k][n], s);
+                for (int k = 0; k < kl; ++k) step(k);
             }
-            acc[r] = s;
+            accr[r] = sr;
+            if constexpr (CPLX) acci[r] = si;
         }
     }
 }
 
-// k in [k0, k0 + kl) of the A operand (piece rows m < m_valid) into As.
-__device__ __forceinline__ void load_a(double (*As)[SBM + 1], const double* __restrict__ q, const F64Piece& t, int k0,
-                                       int kl, int tid) {
+// k in [k0, k0 + kl) of a stack operand (rows m < rows_valid of chunk-0 row
+// `row`, `cs` rows between chunks) into S[k][m].
+__device__ __forceinline__ void load_op_a(double (*S)[SBM + 1], const double* __restrict__ q, int32_t row, int32_t cs,
+                                          int rows_valid, int k0, int kl, int tid) {
 #pragma unroll
     for (int r = 0; r < SBM * SBK / ST; ++r) {
         const int e = tid + ST * r, k = e & 15, m = e >> 4, kk = k0 + k;
         double v = 0.0;
-        if (m < t.m_valid && k < kl) v = q[(((int64_t)t.a_row + (int64_t)(kk >> 6) * t.a_cs + m) << 6) + (kk & 63)];
-        As[k][m] = v;
+        if (m < rows_valid && k < kl) v = q[(((int64_t)row + (int64_t)(kk >> 6) * cs + m) << 6) + (kk & 63)];
+        S[k][m] = v;
     }
 }
 
+__device__ __forceinline__ void load_op_b(double (*S)[SBN + 1], const double* __restrict__ q, int32_t row, int32_t cs,
+                                          int rows_valid, int k0, int kl, int tid) {
+#pragma unroll
+    for (int r = 0; r < SBN * SBK / ST; ++r) {
+        const int e = tid + ST * r, k = e & 15, n = e >> 4, kk = k0 + k;
+        double v = 0.0;
+        if (n < rows_valid && k < kl) v = q[(((int64_t)row + (int64_t)(kk >> 6) * cs + n) << 6) + (kk & 63)];
+        S[k][n] = v;
+    }
+}
+
+// Stage 1: T1 = L stacks * psi (CPLX: both complex, planar).
+template <bool CPLX>
 __global__ void __launch_bounds__(ST, 4) stack_gemm1_f64_kernel(const F64Piece* __restrict__ pieces,
                                                                 const KSeg* __restrict__ segs,
                                                                 const double* __restrict__ lq,
+                                                                const double* __restrict__ lq_im,
                                                                 const double* __restrict__ x,
+                                                                const double* __restrict__ x_im,
                                                                 const int64_t* __restrict__ xsrc,
                                                                 const int32_t* __restrict__ xstride,
                                                                 const int64_t* __restrict__ colbase,
                                                                 const int32_t* __restrict__ colstride,
-                                                                double* __restrict__ t1) {
-    __shared__ double As[SBK][SBM + 1];
-    __shared__ double Bs[SBK][SBN + 1];
+                                                                double* __restrict__ t1, double* __restrict__ t1_im) {
+    __shared__ double Ar[SBK][SBM + 1], Br[SBK][SBN + 1];
+    __shared__ double Ai[CPLX ? SBK : 1][SBM + 1], Bi[CPLX ? SBK : 1][SBN + 1];
     const F64Piece t = pieces[blockIdx.x];
     const int tid = threadIdx.x;
     const int ln = tid & 63;  // the B column this thread loads
@@ -125,21 +154,24 @@ __global__ void __launch_bounds__(ST, 4) stack_gemm1_f64_kernel(const F64Piece* 
     const int64_t src = lv ? xsrc[t.out_off + ln] : 0;
     const int32_t str = lv ? xstride[t.out_off + ln] : 0;
     const DenseMap d(t.m_valid, t.n_valid, tid >> 5);
-    double acc[RPT];
+    double accr[RPT], acci[RPT];
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) acc[r] = 0.0;
+    for (int r = 0; r < RPT; ++r) accr[r] = acci[r] = 0.0;
     for (int sg = t.seg0; sg < t.seg0 + t.nseg; ++sg) {
         const KSeg g = segs[sg];
         for (int k0 = g.kb; k0 < g.ke; k0 += SBK) {
             const int kl = min(SBK, g.ke - k0);
-            load_a(As, lq, t, k0, kl, tid);
+            load_op_a(Ar, lq, t.a_row, t.a_cs, t.m_valid, k0, kl, tid);
+            if constexpr (CPLX) load_op_a(Ai, lq_im, t.a_row, t.a_cs, t.m_valid, k0, kl, tid);
 #pragma unroll
             for (int r = 0; r < SBN * SBK / ST; ++r) {
                 const int k = (tid >> 6) + 4 * r, kk = k0 + k;
-                Bs[k][ln] = (lv && k < kl) ? x[src + (int64_t)kk * str] : 0.0;
+                const bool ok = lv && k < kl;
+                Br[k][ln] = ok ? x[src + (int64_t)kk * str] : 0.0;
+                if constexpr (CPLX) Bi[k][ln] = ok ? x_im[src + (int64_t)kk * str] : 0.0;
             }
             __syncthreads();
-            dense_kstep(As, Bs, kl, d, tid, acc);
+            dense_kstep<CPLX>(Ar, Ai, Br, Bi, kl, d, tid, accr, acci);
             __syncthreads();
         }
     }
@@ -148,40 +180,43 @@ __global__ void __launch_bounds__(ST, 4) stack_gemm1_f64_kernel(const F64Piece* 
         const int e = tid + ST * r;
         if (r < d.rounds && e < d.total) {
             const int m = e / d.nv, n = e - m * d.nv;
-            t1[colbase[t.out_off + n] + (int64_t)(t.ldc + m) * colstride[t.out_off + n]] = acc[r];
+            const int64_t o = colbase[t.out_off + n] + (int64_t)(t.ldc + m) * colstride[t.out_off + n];
+            t1[o] = accr[r];
+            if constexpr (CPLX) t1_im[o] = acci[r];
         }
     }
 }
 
+// Stage 3: y = T2 stacks * R stacks^T (CPLX: both complex, planar).
+template <bool CPLX>
 __global__ void __launch_bounds__(ST, 4) stack_gemm3_f64_kernel(const F64Piece* __restrict__ pieces,
                                                                 const KSeg* __restrict__ segs,
                                                                 const double* __restrict__ t2,
+                                                                const double* __restrict__ t2_im,
                                                                 const double* __restrict__ rq,
+                                                                const double* __restrict__ rq_im,
                                                                 const int64_t* __restrict__ yrow,
-                                                                double* __restrict__ y) {
-    __shared__ double As[SBK][SBM + 1];
-    __shared__ double Bs[SBK][SBN + 1];
+                                                                double* __restrict__ y, double* __restrict__ y_im) {
+    __shared__ double Ar[SBK][SBM + 1], Br[SBK][SBN + 1];
+    __shared__ double Ai[CPLX ? SBK : 1][SBM + 1], Bi[CPLX ? SBK : 1][SBN + 1];
     const F64Piece t = pieces[blockIdx.x];
     const int tid = threadIdx.x;
     const DenseMap d(t.m_valid, t.n_valid, tid >> 5);
-    double acc[RPT];
+    double accr[RPT], acci[RPT];
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) acc[r] = 0.0;
+    for (int r = 0; r < RPT; ++r) accr[r] = acci[r] = 0.0;
     for (int sg = t.seg0; sg < t.seg0 + t.nseg; ++sg) {
         const KSeg g = segs[sg];
         for (int k0 = g.kb; k0 < g.ke; k0 += SBK) {
             const int kl = min(SBK, g.ke - k0);
-            load_a(As, t2, t, k0, kl, tid);
-#pragma unroll
-            for (int r = 0; r < SBN * SBK / ST; ++r) {
-                const int e = tid + ST * r, k = e & 15, n = e >> 4, kk = k0 + k;
-                double v = 0.0;
-                if (n < t.n_valid && k < kl)
-                    v = rq[(((int64_t)t.b_row + (int64_t)(kk >> 6) * t.b_cs + n) << 6) + (kk & 63)];
-                Bs[k][n] = v;
+            load_op_a(Ar, t2, t.a_row, t.a_cs, t.m_valid, k0, kl, tid);
+            load_op_b(Br, rq, t.b_row, t.b_cs, t.n_valid, k0, kl, tid);
+            if constexpr (CPLX) {
+                load_op_a(Ai, t2_im, t.a_row, t.a_cs, t.m_valid, k0, kl, tid);
+                load_op_b(Bi, rq_im, t.b_row, t.b_cs, t.n_valid, k0, kl, tid);
             }
             __syncthreads();
-            dense_kstep(As, Bs, kl, d, tid, acc);
+            dense_kstep<CPLX>(Ar, Ai, Br, Bi, kl, d, tid, accr, acci);
             __syncthreads();
         }
     }
@@ -190,7 +225,9 @@ __global__ void __launch_bounds__(ST, 4) stack_gemm3_f64_kernel(const F64Piece* 
         const int e = tid + ST * r;
         if (r < d.rounds && e < d.total) {
             const int m = e / d.nv, n = e - m * d.nv;
-            y[yrow[t.out_off + m] + t.n0 + n] = acc[r];
+            const int64_t o = yrow[t.out_off + m] + t.n0 + n;
+            y[o] = accr[r];
+            if constexpr (CPLX) y_im[o] = acci[r];
         }
     }
 }
@@ -333,6 +370,8 @@ bool stage3_pieces(const TcTables& C, std::vector<F64Piece>& out, std::vector<KS
 
 struct F64Stack {
     DevBuf<double> lq, rq, t1, t2, coef;
+    DevBuf<double> lq_im, rq_im, t1_im, t2_im;  // complex environments only
+    bool cplx = false;
     DevBuf<F64Piece> pieces1, pieces3;
     DevBuf<KSeg> segs;
     DevBuf<TcCombJob> jobs;
@@ -375,6 +414,18 @@ tk_status f64stack_create(const TcTables& C, std::unique_ptr<F64Stack, F64StackD
         err = std::string("stacked FP64 operands: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
     }
+    p->cplx = !C.lq64_im.empty() || !C.rq64_im.empty();
+    if (p->cplx &&
+        ((e = p->lq_im.upload(C.lq64_im)) != cudaSuccess || (e = p->rq_im.upload(C.rq64_im)) != cudaSuccess ||
+         (e = p->t1_im.alloc(p->t1.n)) != cudaSuccess || (e = p->t2_im.alloc(p->t2.n)) != cudaSuccess ||
+         (e = cudaMemset(p->t2_im.p, 0, sizeof(double) * p->t2_im.n)) != cudaSuccess)) {
+        err = std::string("stacked FP64 imaginary operands: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
+    }
+    if (p->cplx && (C.lq64_im.size() != C.lq64.size() || C.rq64_im.size() != C.rq64.size())) {
+        err = "stacked FP64 imaginary stacks of another size";
+        return TK_ERR_INVALID_ARG;
+    }
     // Bytes each stage must move at least: every stack element a piece reads
     // once (rows read by several column tiles count once), T1 written / read
     // once, T2 written / read once.
@@ -401,12 +452,14 @@ tk_status f64stack_create(const TcTables& C, std::unique_ptr<F64Stack, F64StackD
 
 cudaError_t f64stack_stage(F64Stack& p, const double* x, double* y, cudaStream_t s, int stage) {
     if (stage == 0 && p.n1 > 0)
-        stack_gemm1_f64_kernel<<<p.n1, ST, 0, s>>>(p.pieces1.p, p.segs.p, p.lq.p, x, p.xsrc.p, p.xstride.p,
-                                                   p.colbase.p, p.colstride.p, p.t1.p);
+        stack_gemm1_f64_kernel<false><<<p.n1, ST, 0, s>>>(p.pieces1.p, p.segs.p, p.lq.p, nullptr, x, nullptr,
+                                                          p.xsrc.p, p.xstride.p, p.colbase.p, p.colstride.p, p.t1.p,
+                                                          nullptr);
     else if (stage == 1 && p.njobs > 0)
         stack_combine_f64_kernel<<<p.njobs, 128, 0, s>>>(p.jobs.p, p.terms.p, p.coef.p, p.t1.p, p.t2.p);
     else if (stage == 2 && p.n3 > 0)
-        stack_gemm3_f64_kernel<<<p.n3, ST, 0, s>>>(p.pieces3.p, p.segs.p, p.t2.p, p.rq.p, p.yrow.p, y);
+        stack_gemm3_f64_kernel<false><<<p.n3, ST, 0, s>>>(p.pieces3.p, p.segs.p, p.t2.p, nullptr, p.rq.p, nullptr,
+                                                          p.yrow.p, y, nullptr);
     return cudaGetLastError();
 }
 
@@ -416,6 +469,23 @@ cudaError_t f64stack_apply(F64Stack& p, const double* x, double* y, cudaStream_t
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t f64stack_apply_complex(F64Stack& p, const double* xr, const double* xi, double* yr, double* yi,
+                                   cudaStream_t s) {
+    if (!p.cplx) return cudaErrorInvalidValue;
+    if (p.n1 > 0)
+        stack_gemm1_f64_kernel<true><<<p.n1, ST, 0, s>>>(p.pieces1.p, p.segs.p, p.lq.p, p.lq_im.p, xr, xi, p.xsrc.p,
+                                                         p.xstride.p, p.colbase.p, p.colstride.p, p.t1.p, p.t1_im.p);
+    if (p.njobs > 0) {
+        // the W_i W_j coefficients are real: the combine acts on each part
+        stack_combine_f64_kernel<<<p.njobs, 128, 0, s>>>(p.jobs.p, p.terms.p, p.coef.p, p.t1.p, p.t2.p);
+        stack_combine_f64_kernel<<<p.njobs, 128, 0, s>>>(p.jobs.p, p.terms.p, p.coef.p, p.t1_im.p, p.t2_im.p);
+    }
+    if (p.n3 > 0)
+        stack_gemm3_f64_kernel<true><<<p.n3, ST, 0, s>>>(p.pieces3.p, p.segs.p, p.t2.p, p.t2_im.p, p.rq.p, p.rq_im.p,
+                                                         p.yrow.p, yr, yi);
+    return cudaGetLastError();
 }
 
 int f64stack_launches(const F64Stack& p) { return (p.n1 > 0) + (p.njobs > 0) + (p.n3 > 0); }

@@ -214,6 +214,7 @@ struct TcTables {
     int64_t lq_rows = 0, rq_rows = 0, xq_rows = 0, t2q_rows = 0, t1_total = 0;
     std::vector<uint16_t> lq_hi, lq_lo, rq_hi, rq_lo;  // constant operands, split at plan time
     std::vector<double> lq64, rq64;                    // the same stacks in FP64 (stacked FP64 schedule)
+    std::vector<double> lq64_im, rq64_im;              // their imaginary parts (complex environments)
     std::vector<double> term_coef64;                   // FP64 coefficients of `terms`
     std::vector<TcTile> tiles1, tiles3;
     std::vector<TcTile> tiles1x;       // stage-1 tiles of tall stacks (B operand from the split copy)
@@ -307,8 +308,11 @@ struct Heff2Tables {
     TcTables f64st;
 };
 // Builds T.f64st: the stack tables with every stage-1 column read through
-// its psi table and no fused stage 3, the operand stacks in FP64.
-tk_status build_f64_stacks(Heff2Tables& T, std::string& err);
+// its psi table and no fused stage 3, the operand stacks in FP64 (and, for
+// complex environments, their imaginary parts from host copies of the
+// imaginary slab arrays, laid out like T.lbuf / T.rbuf).
+tk_status build_f64_stacks(Heff2Tables& T, std::string& err, const double* lbuf_im = nullptr,
+                           const double* rbuf_im = nullptr);
 // Rebuilds T.tc with options `o` (T.tc and T.tcopt unchanged on failure).
 tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err);
 

@@ -93,6 +93,9 @@ tk_status f64stack_create(const TcTables& C, std::unique_ptr<F64Stack, F64StackD
 // stage 0: T1 = L stacks * psi; 1: the W_i W_j combine into T2; 2: y = T2 * R stacks
 cudaError_t f64stack_stage(F64Stack& p, const double* x, double* y, cudaStream_t s, int stage);
 cudaError_t f64stack_apply(F64Stack& p, const double* x, double* y, cudaStream_t s);
+// The complex matvec (planar vectors) of a stack built from complex environments.
+cudaError_t f64stack_apply_complex(F64Stack& p, const double* xr, const double* xi, double* yr, double* yi,
+                                   cudaStream_t s);
 int f64stack_launches(const F64Stack& p);
 // Bytes per stage a stacked matvec must move, without the psi and y vectors.
 void f64stack_bytes(const F64Stack& p, double out[3]);

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from helpers import models, oracle_bs, rel_err, small_problem
-from tk_gb300 import TkError, _abi
+from tk_gb300 import _abi
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12  # FP64 vs the FP64 oracle, relative 2-norm (the sums run in another order)
@@ -107,14 +107,36 @@ def test_stacked_profile_and_switching(lib_built):
     assert rel_err(y2.cpu().numpy(), y1.cpu().numpy()) < 1e-13
 
 
-def test_stacked_refuses_complex_plans(lib_built):
+def test_stacked_complex_matches_grouped(lib_built):
+    """Complex environments: the stacked schedule (the default of complex plans
+    too) against the grouped one, and launches counted per schedule."""
+    import torch
+
     from tk_gb300 import Heff2Plan, sweep
 
-    p = small_problem("heisenberg", 10)
-    dl = sweep.DeviceEnv.from_dense(p.kind, p.env_l.data + 0j, p.env_l.bra_idx, p.env_l.mpo_idx, p.env_l.ket_idx)
-    dr = sweep.DeviceEnv.from_dense(p.kind, p.env_r.data + 0j, p.env_r.bra_idx, p.env_r.mpo_idx, p.env_r.ket_idx)
+    p = small_problem("hubbard", 40)
+    rng = np.random.default_rng(8)
+
+    def cplx_env(e):
+        im = rng.standard_normal(e.data.shape)
+        return e.data + 0.3j * (im - np.transpose(im, (2, 1, 0)))
+
+    dl = sweep.DeviceEnv.from_dense(p.kind, cplx_env(p.env_l), p.env_l.bra_idx, p.env_l.mpo_idx, p.env_l.ket_idx)
+    dr = sweep.DeviceEnv.from_dense(p.kind, cplx_env(p.env_r), p.env_r.bra_idx, p.env_r.mpo_idx, p.env_r.ket_idx)
     plan = Heff2Plan.from_device_envs_complex(dl, dr, p.w_i, p.w_j, p.flux)
-    assert plan.schedule == _abi.SCHED_GROUPED
-    with pytest.raises(TkError) as e:
-        plan.set_schedule(_abi.SCHED_STACKED)
-    assert _abi.STATUS_NAMES[e.value.status] == "UNSUPPORTED"
+    assert plan.schedule == _abi.SCHED_STACKED
+    n = plan.block_dim
+    xr = torch.from_numpy(rng.standard_normal(n)).cuda()
+    xi = torch.from_numpy(rng.standard_normal(n)).cuda()
+    out = {}
+    for sched in (_abi.SCHED_STACKED, _abi.SCHED_GROUPED):
+        plan.set_schedule(sched)
+        yr, yi = torch.full_like(xr, float("nan")), torch.full_like(xr, float("nan"))
+        plan.apply_complex(xr, xi, yr, yi)
+        torch.cuda.synchronize()
+        out[sched] = yr.cpu().numpy() + 1j * yi.cpu().numpy()
+        assert np.isfinite(out[sched]).all()
+    a, b = out[_abi.SCHED_STACKED], out[_abi.SCHED_GROUPED]
+    assert np.linalg.norm(a - b) < 1e-13 * np.linalg.norm(b)
+    plan.set_schedule(_abi.SCHED_STACKED)
+    assert plan.launches() <= 4
