@@ -188,6 +188,7 @@ tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, cons
     std::string err;
     Heff2Tables H;
     tk_status st = build_heff2_tables(*env_l, *env_r, *w_i, *w_j, psi_flux, kF64TileM, kF64TileN, H, err);
+    if (st == TK_OK) st = ensure_tc_tables(H, err);  // the stack sizes of both precisions come from them
     if (st != TK_OK) {
         set_error("tk_heff2_plan_footprint: " + err);
         return st;
@@ -338,8 +339,10 @@ tk_status tk_heff2_set_precision(tk_heff2_plan* plan, int32_t precision) {
     if (!plan->tc) {
         std::string err;
         std::unique_ptr<TcPlan, TcPlanDeleter> tc;
-        tk_status st = guard_host("split-precision plan", err,
-                                  [&] { return tc_plan_create(plan->host, plan->lbuf.p, plan->rbuf.p, tc, err); });
+        tk_status st = ensure_tc_tables(plan->host, err);
+        if (st == TK_OK)
+            st = guard_host("split-precision plan", err,
+                            [&] { return tc_plan_create(plan->host, plan->lbuf.p, plan->rbuf.p, tc, err); });
         if (st != TK_OK) {
             set_error("tk_heff2_set_precision: " + err);
             return st;

@@ -349,7 +349,7 @@ static bool validate_tables(const Heff2Tables& T, std::string& err) {
     if (!gemm_table_ok(T.g1, (int64_t)T.lbuf.size(), T.total, T.t1_total, "stage 1", err)) return false;
     if (!gemm_table_ok(T.g3, T.t2_total, (int64_t)T.rbuf.size(), T.total, "stage 3", err)) return false;
     if (!comb_table_ok(T.jobs, T.terms, T.t1_total, T.t2_total, err)) return false;
-    return validate_tc(T, T.tc, err);
+    return !T.tc_built || validate_tc(T, T.tc, err);
 }
 
 // Every access of the split (or stacked FP64) tables checked against its buffer.
@@ -1310,9 +1310,7 @@ static tk_status build_heff2_tables_body(const tk_env& envL, const tk_env& envR,
         X->byout = std::move(byout);
         X->wl_sec = wl_sec;
         X->wl_loc = wl_loc;
-        T.tcsrc = X;
-        const tk_status st = build_tc_tables(T, *X, T.tcopt, T.tc, false, err);
-        if (st != TK_OK) return st;
+        T.tcsrc = X;  // the split tables themselves are built on first use (ensure_tc_tables)
     }
     lpt_order(T.g1, tile_m, tile_n);
     lpt_order(T.g3, tile_m, tile_n);
@@ -1355,6 +1353,26 @@ tk_status build_f64_stacks(Heff2Tables& T, std::string& err, const double* lbuf_
     });
 }
 
+tk_status ensure_tc_tables(Heff2Tables& T, std::string& err) {
+    if (T.tc_built) return TK_OK;
+    if (!T.tcsrc) {
+        err = "the plan keeps no sector structure to build from";
+        return TK_ERR_UNSUPPORTED;
+    }
+    return guard_host("split-precision tables", err, [&]() -> tk_status {
+        tk_status st = build_tc_tables(T, *T.tcsrc, T.tcopt, T.tc, false, err);
+        if (st == TK_OK && !validate_tc(T, T.tc, err)) {
+            err = "internal table check failed: " + err;
+            st = TK_ERR_INVALID_ARG;
+        }
+        if (st == TK_OK)
+            T.tc_built = true;
+        else
+            T.tc = TcTables();
+        return st;
+    });
+}
+
 tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err) {
     if (!T.tcsrc) {
         err = "the plan keeps no sector structure to rebuild from";
@@ -1363,7 +1381,9 @@ tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err
     return guard_host("split-precision tables", err, [&]() -> tk_status {
         TcTables saved = std::move(T.tc);
         const TcOptions old = T.tcopt;
+        const bool was_built = T.tc_built;
         T.tcopt = o;
+        T.tc_built = true;
         tk_status st = build_tc_tables(T, *T.tcsrc, o, T.tc, false, err);
         if (st == TK_OK && !validate_tables(T, err)) {
             err = "internal table check failed: " + err;
@@ -1372,6 +1392,7 @@ tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err
         if (st != TK_OK) {
             T.tc = std::move(saved);
             T.tcopt = old;
+            T.tc_built = was_built;
         }
         return st;
     });

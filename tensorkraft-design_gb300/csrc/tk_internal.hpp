@@ -302,6 +302,7 @@ struct Heff2Tables {
     int64_t n_wij_terms = 0;
     // split-precision (tensor-core) regrouping of the same work
     TcTables tc;
+    bool tc_built = false;  // tc holds the tables of tcopt (built on first use)
     TcOptions tcopt;
     std::shared_ptr<TcSource> tcsrc;
     // the stacked FP64 schedule's tables (the split stacks in FP64; built on demand)
@@ -313,6 +314,9 @@ struct Heff2Tables {
 // imaginary slab arrays, laid out like T.lbuf / T.rbuf).
 tk_status build_f64_stacks(Heff2Tables& T, std::string& err, const double* lbuf_im = nullptr,
                            const double* rbuf_im = nullptr);
+// Builds T.tc with T.tcopt unless built already (the split tables of a plan
+// that never runs split precision are never built).
+tk_status ensure_tc_tables(Heff2Tables& T, std::string& err);
 // Rebuilds T.tc with options `o` (T.tc and T.tcopt unchanged on failure).
 tk_status rebuild_tc_tables(Heff2Tables& T, const TcOptions& o, std::string& err);
 
