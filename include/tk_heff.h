@@ -124,8 +124,9 @@ void tk_heff2_plan_destroy(tk_heff2_plan* plan);
  * plan's host tables exactly as tk_heff2_plan_create does and reports the
  * block-layout length, the number of two-site blocks and the device bytes
  * the plan holds for its tables, operands and intermediates in `precision`
- * (eigensolver and host-call workspaces, allocated on first use, are not
- * included).  Calls no CUDA API; any output pointer may be NULL. */
+ * with its default FP64 schedule (eigensolver and host-call workspaces and
+ * the grouped schedules' state, allocated on first use, are not included).
+ * Calls no CUDA API; any output pointer may be NULL. */
 tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
                                   const tk_bst* w_j, const int32_t* psi_flux, int32_t precision,
                                   int64_t* block_dim, int64_t* n_blocks, int64_t* device_bytes);

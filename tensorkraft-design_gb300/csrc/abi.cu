@@ -194,14 +194,13 @@ tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, cons
         return st;
     }
     auto vb = [](const auto& v) { return (double)v.size() * sizeof(v[0]); };
-    double b = 8.0 * ((double)H.lbuf.size() + H.rbuf.size() + std::max<int64_t>(H.t1_total, 1) +
-                      std::max<int64_t>(H.t2_total, 1));
-    for (const GemmTable* g : {&H.g1, &H.g3}) b += vb(g->tasks) + vb(g->segs) + 2.0 * vb(g->tiles);
-    b += vb(H.jobs) + vb(H.terms);
+    double b = 0.0;
     {
-        // the stacked FP64 operands every real plan builds: the same L, R and
-        // T2 stack rows as the split tables, in FP64, and T1 in FP64 (piece
-        // tables about one entry per 64 output rows of a tile)
+        // the stacked FP64 operands a plan builds (its default schedule): the
+        // same L, R and T2 stack rows as the split tables, in FP64, and T1 in
+        // FP64 (piece tables about one entry per 64 output rows of a tile).
+        // The grouped schedule's state is not counted: it is uploaded only
+        // when that schedule is chosen.
         const TcTables& C = H.tc;
         b += 8.0 * kTcBK * ((double)C.lq_rows + C.rq_rows + std::max<int64_t>(C.t2q_rows, 1)) +
              8.0 * std::max<int64_t>(C.t1_total, 1) + 2.0 * (vb(C.tiles1) + vb(C.tiles3)) + vb(C.jobs) +
@@ -222,6 +221,29 @@ tk_status tk_heff2_plan_footprint(const tk_env* env_l, const tk_env* env_r, cons
 }
 
 }  // extern "C"
+
+// The device state of the grouped and per-block FP64 schedules (environment
+// slabs, intermediates, GEMM and combine tables; for a complex plan also the
+// imaginary intermediates), uploaded on the first request for one of them.
+tk_status tk::ensure_grouped(tk_heff2_plan* p) {
+    if (p->grouped_ready) return TK_OK;
+    const Heff2Tables& H = p->host;
+    DeviceGuard g(p->device);
+    TK_CUDA(p->lbuf.upload(H.lbuf));
+    TK_CUDA(p->rbuf.upload(H.rbuf));
+    TK_CUDA(p->t1.alloc((size_t)std::max<int64_t>(H.t1_total, 1)));
+    TK_CUDA(p->t2.alloc((size_t)std::max<int64_t>(H.t2_total, 1)));
+    TK_CUDA(p->g1.upload(H.g1));
+    TK_CUDA(p->g3.upload(H.g3));
+    TK_CUDA(p->jobs.upload(H.jobs));
+    TK_CUDA(p->terms.upload(H.terms));
+    if (p->is_complex) {
+        TK_CUDA(p->t1_im.alloc(p->t1.n));
+        TK_CUDA(p->t2_im.alloc(p->t2.n));
+    }
+    p->grouped_ready = true;
+    return TK_OK;
+}
 
 // Shared by tk_heff2_plan_create (dense host environments) and
 // tk_heff2_plan_create_dev (host copies of canonical block-layout ones).
@@ -253,17 +275,11 @@ tk_status tk::plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* e
     p->device = ctx->device;
     const Heff2Tables& H = p->host;
     TK_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
-    TK_CUDA(p->lbuf.upload(H.lbuf));
-    TK_CUDA(p->rbuf.upload(H.rbuf));
-    TK_CUDA(p->t1.alloc((size_t)std::max<int64_t>(H.t1_total, 1)));
-    TK_CUDA(p->t2.alloc((size_t)std::max<int64_t>(H.t2_total, 1)));
-    TK_CUDA(p->g1.upload(H.g1));
-    TK_CUDA(p->g3.upload(H.g3));
-    TK_CUDA(p->jobs.upload(H.jobs));
-    TK_CUDA(p->terms.upload(H.terms));
+    // the grouped schedule's device state is uploaded when that schedule is chosen
     p->n_jobs = (int)H.jobs.size();
     p->precision = TK_PREC_FP64;
-    // the FP64 matvec of a real plan runs on operand stacks (TK_SCHED_STACKED)
+    // the FP64 matvec runs on operand stacks (TK_SCHED_STACKED); without
+    // `stacked` the caller sets the schedule before the plan is used
     if (stacked) {
         tk_status s3 = tk_heff2_set_schedule(p.get(), TK_SCHED_STACKED);
         if (s3 != TK_OK) return s3;
@@ -531,6 +547,13 @@ tk_status tk_heff2_set_schedule(tk_heff2_plan* plan, int32_t schedule) {
     if (!plan || (schedule != TK_SCHED_GROUPED && schedule != TK_SCHED_PER_BLOCK && schedule != TK_SCHED_STACKED)) {
         set_error("tk_heff2_set_schedule: invalid argument");
         return TK_ERR_INVALID_ARG;
+    }
+    if (schedule != TK_SCHED_STACKED) {
+        tk_status st = ensure_grouped(plan);
+        if (st != TK_OK) {
+            set_error("tk_heff2_set_schedule: " + std::string(tk_last_error()));
+            return st;
+        }
     }
     if (schedule == TK_SCHED_STACKED && !plan->f64s) {
         DeviceGuard g(plan->device);

@@ -218,8 +218,8 @@ tk_status tk_env_layout(int32_t qn_kind, const tk_qindex* bra, const tk_qindex* 
     return TK_OK;
 }
 
-// tk_heff2_plan_create_dev; `stacked` as in plan_create_impl (off for the
-// complex plans, whose FP64 matvec runs the grouped schedule).
+// tk_heff2_plan_create_dev; `stacked` as in plan_create_impl (off for complex
+// plans, which set their schedule once their imaginary parts are in place).
 static tk_status plan_create_dev(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
                                  const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, tk_heff2_plan** out,
                                  bool stacked) {
@@ -293,10 +293,8 @@ tk_status tk_heff2_plan_create_dev_complex(tk_ctx* ctx, const tk_env* env_l, con
     tk_heff2_plan* p = *out;
     Guard g(p->device);
     cudaError_t e;
-    const size_t nl = p->lbuf.n, nr = p->rbuf.n;
+    const size_t nl = p->host.lbuf.size(), nr = p->host.rbuf.size();
     if ((e = p->lbuf_im.alloc(nl)) != cudaSuccess || (e = p->rbuf_im.alloc(nr)) != cudaSuccess ||
-        (e = p->t1_im.alloc(std::max<size_t>(p->t1.n, 1))) != cudaSuccess ||
-        (e = p->t2_im.alloc(std::max<size_t>(p->t2.n, 1))) != cudaSuccess ||
         (nl && (e = cudaMemcpy(p->lbuf_im.p, env_l_im, sizeof(double) * nl, cudaMemcpyDeviceToDevice)) != cudaSuccess) ||
         (nr && (e = cudaMemcpy(p->rbuf_im.p, env_r_im, sizeof(double) * nr, cudaMemcpyDeviceToDevice)) != cudaSuccess)) {
         tk_heff2_plan_destroy(p);

@@ -112,6 +112,7 @@ struct tk_heff2_plan {
     bool is_complex = false;
     tk::DevBuf<double> lbuf_im, rbuf_im, t1_im, t2_im;
     tk::DevGemm g1, g3;
+    bool grouped_ready = false;  // lbuf, rbuf, t1, t2, g1, g3, jobs, terms uploaded (tk::ensure_grouped)
     tk::DevBuf<tk::CombJob> jobs;
     tk::DevBuf<tk::CombTerm> terms;
     int n_jobs = 0;
@@ -173,6 +174,8 @@ extern "C" tk_status tk_heff2_apply_complex_s(tk_heff2_plan* p, const double* xr
 
 namespace tk {
 tk_status cuda_fail(const char* op, cudaError_t e);
+// Uploads the grouped / per-block FP64 schedules' device state once.
+tk_status ensure_grouped(tk_heff2_plan* p);
 // True once the plan's cancel flag (if any) reads non-zero: the solver waits
 // for its stream, so that none of its work is left in flight, records the
 // message and returns TK_ERR_CANCELLED.
@@ -180,7 +183,8 @@ bool plan_cancelled(tk_heff2_plan* p, cudaStream_t s, const char* where);
 // Plan creation behind tk_heff2_plan_create / tk_heff2_plan_create_dev: with
 // l_blocks / r_blocks (host copies of canonical block-layout environments) the
 // environments' `data` pointers are not read.  `stacked`: build the stacked
-// FP64 operands and make TK_SCHED_STACKED the plan's schedule (real plans).
+// FP64 operands and make TK_SCHED_STACKED the plan's schedule; without it the
+// caller sets a schedule (tk_heff2_set_schedule) before the plan is used.
 tk_status plan_create_impl(tk_ctx* ctx, const tk_env* env_l, const tk_env* env_r, const tk_bst* w_i,
                            const tk_bst* w_j, const int32_t* psi_flux, int32_t precision, const double* l_blocks,
                            const double* r_blocks, tk_heff2_plan** out, bool stacked = true);
