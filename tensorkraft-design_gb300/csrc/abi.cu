@@ -1011,9 +1011,11 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
     cudaStream_t s = plan->stream;
     TK_CUDA(launch_fill_start_vector(plan->hx.p, n, s));
     // candidate schedules; a candidate whose tables come out the same as an
-    // earlier one's is not timed again
-    const TcOptions cand[] = {{3, 0, 0, 0}, {3, 0, 3, 0}, {3, 0, 0, 1}, {3, 0, 2, 0},
-                              {3, 0, 1, 0}, {3, 2, 0, 0}, {1 << 30, 0, 0, 0}, {1, 0, 0, 0}};
+    // earlier one's is not timed again.  The combine as persistent warps or one
+    // warp per job and the fused stage 3 stay settable (tk_heff2_set_tc_options)
+    // but are not timed here: 1.3-3.5x slower than the default on the Hubbard
+    // D=2048 bond, and every candidate costs a table rebuild inside a sweep
+    const TcOptions cand[] = {{3, 0, 0, 0}, {3, 0, 3, 0}, {3, 0, 0, 1}, {1 << 30, 0, 0, 0}, {1, 0, 0, 0}};
     std::vector<std::vector<size_t>> shapes;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TK_CUDA(cudaEventCreate(&e0));
