@@ -401,7 +401,7 @@ extern "C" tk_status tk_contract_pairwise_f64(tk_ctx* ctx, const tk_bst* a, cons
         const size_t og = blob.add(P.g.segs.data(), sizeof(GemmSeg) * P.g.segs.size());
         const size_t ol2 = blob.add(P.g.tiles.data(), sizeof(GemmTile) * P.g.tiles.size());
         // the fused operands and the result live on the device only, after the packed bytes
-        const size_t dev_fa = (blob.bytes.size() + 255) & ~(size_t)255;
+        const size_t dev_fa = (blob.size() + 255) & ~(size_t)255;
         const size_t dev_fb = (dev_fa + sizeof(double) * (size_t)FA.m.total + 255) & ~(size_t)255;
         const size_t dev_c = (dev_fb + sizeof(double) * (size_t)FB.m.total + 255) & ~(size_t)255;
         blob.tail = dev_c + sizeof(double) * (size_t)P.total;
@@ -411,11 +411,11 @@ extern "C" tk_status tk_contract_pairwise_f64(tk_ctx* ctx, const tk_bst* a, cons
         cudaStream_t s = (cudaStream_t)sp;
         void *dv = nullptr, *hv = nullptr;
         if ((s2 = ctx_dev_scratch(ctx, blob.device_size(), &dv)) != TK_OK) return s2;
-        if ((s2 = ctx_host_stage(ctx, std::max(blob.bytes.size(), sizeof(double) * (size_t)P.total), &hv)) != TK_OK)
+        if ((s2 = ctx_host_stage(ctx, std::max(blob.size(), sizeof(double) * (size_t)P.total), &hv)) != TK_OK)
             return s2;
         unsigned char* d = static_cast<unsigned char*>(dv);
-        std::memcpy(hv, blob.bytes.data(), blob.bytes.size());
-        CKC(cudaMemcpyAsync(d, hv, blob.bytes.size(), cudaMemcpyHostToDevice, s));
+        blob.copy_to(hv);
+        CKC(cudaMemcpyAsync(d, hv, blob.size(), cudaMemcpyHostToDevice, s));
         double* fa = (double*)(d + dev_fa);
         double* fb = (double*)(d + dev_fb);
         // blocks of a fused tensor that no source block reaches are zero

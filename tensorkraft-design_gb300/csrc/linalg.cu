@@ -178,9 +178,9 @@ static tk_status stage_blob(tk_ctx* ctx, const Blob& blob, cudaStream_t s, unsig
     void *d = nullptr, *h = nullptr;
     tk_status st;
     if ((st = ctx_dev_scratch(ctx, blob.device_size(), &d)) != TK_OK) return st;
-    if ((st = ctx_host_stage(ctx, std::max<size_t>(blob.bytes.size(), 1), &h)) != TK_OK) return st;
-    std::memcpy(h, blob.bytes.data(), blob.bytes.size());
-    if (!blob.bytes.empty()) CK(cudaMemcpyAsync(d, h, blob.bytes.size(), cudaMemcpyHostToDevice, s));
+    if ((st = ctx_host_stage(ctx, std::max<size_t>(blob.size(), 1), &h)) != TK_OK) return st;
+    blob.copy_to(h);
+    if (!(blob.size() == 0)) CK(cudaMemcpyAsync(d, h, blob.size(), cudaMemcpyHostToDevice, s));
     *dev = static_cast<unsigned char*>(d);
     return TK_OK;
 }

@@ -361,11 +361,11 @@ tk_status tk_split_gather(tk_split_plan* s, const double* psi_dev, double* m_hos
     void *dv = nullptr, *hv = nullptr;
     tk_status r;
     if ((r = ctx_dev_scratch(s->ctx, blob.device_size(), &dv)) != TK_OK) return r;
-    if ((r = ctx_host_stage(s->ctx, std::max<size_t>(blob.bytes.size(), 1), &hv)) != TK_OK) return r;
+    if ((r = ctx_host_stage(s->ctx, std::max<size_t>(blob.size(), 1), &hv)) != TK_OK) return r;
     unsigned char* d = static_cast<unsigned char*>(dv);
-    std::memcpy(hv, blob.bytes.data(), blob.bytes.size());
+    blob.copy_to(hv);
     double* m = (double*)(d + om);
-    CKS(cudaMemcpyAsync(d, hv, blob.bytes.size(), cudaMemcpyHostToDevice, st));
+    CKS(cudaMemcpyAsync(d, hv, blob.size(), cudaMemcpyHostToDevice, st));
     // elements of M_q that no psi block reaches are zero
     CKS(cudaMemsetAsync(m, 0, sizeof(double) * (size_t)s->m_total, st));
     CKS(launch_copy((const CopySeg*)(d + og), (int)s->gather.size(), s->gather_max, psi_dev, m, st));
@@ -413,10 +413,10 @@ tk_status tk_split_factors(tk_split_plan* s, const double* u_host, const double*
     void *dv = nullptr, *hv = nullptr;
     tk_status r;
     if ((r = ctx_dev_scratch(s->ctx, blob.device_size(), &dv)) != TK_OK) return r;
-    if ((r = ctx_host_stage(s->ctx, std::max<size_t>(blob.bytes.size(), 1), &hv)) != TK_OK) return r;
+    if ((r = ctx_host_stage(s->ctx, std::max<size_t>(blob.size(), 1), &hv)) != TK_OK) return r;
     unsigned char* d = static_cast<unsigned char*>(dv);
-    std::memcpy(hv, blob.bytes.data(), blob.bytes.size());
-    CKS(cudaMemcpyAsync(d, hv, blob.bytes.size(), cudaMemcpyHostToDevice, st));
+    blob.copy_to(hv);
+    CKS(cudaMemcpyAsync(d, hv, blob.size(), cudaMemcpyHostToDevice, st));
     CKS(launch_copy((const CopySeg*)(d + osu), (int)s->scat_u.size(), s->scat_u_max, (const double*)(d + ou), ai_dev, st));
     CKS(launch_copy((const CopySeg*)(d + osv), (int)s->scat_v.size(), s->scat_v_max, (const double*)(d + ov), aj_dev, st));
     // the packs live in the context's shared scratch: finish before returning

@@ -90,6 +90,51 @@ inline void bsgemm_tiles_for(GemmTable& g, int task) {
         for (int n0 = 0; n0 < t.N; n0 += 64) g.tiles.push_back({task, m0, n0, 0});
 }
 
+// Smaller square tiles for small products.  With fewer 64 x 64 tiles than
+// the GPU holds, most SMs would sit idle while a few run a whole tile over
+// the full K (this GPU's FP64 pipe retires two FMAs per clock per SM, so one
+// 64 x 64 x 130 tile is ~0.13 ms on one SM): the tasks whose tiles are the
+// heaviest (edge^2 x K) go to the next smaller edge (32, then 16) until there
+// are `target` tiles or every task is at the smallest edge; then the tiles
+// go out longest first.  Each output element still comes from one tile that
+// sums the task's segments in the same order.
+inline void bsgemm_retile(GemmTable& g, size_t target) {
+    const size_t nt = g.tasks.size();
+    std::vector<int> cls(nt, 0);
+    std::vector<double> ktot(nt, 0.0);
+    for (size_t t = 0; t < nt; ++t)
+        for (int s = g.tasks[t].seg_begin; s < g.tasks[t].seg_end; ++s) ktot[t] += g.segs[(size_t)s].K;
+    auto ntiles = [&](size_t t, int c) {
+        const int e = 64 >> c;
+        return (size_t)((g.tasks[t].M + e - 1) / e) * (size_t)((g.tasks[t].N + e - 1) / e);
+    };
+    size_t total = 0;
+    for (size_t t = 0; t < nt; ++t) total += ntiles(t, 0);
+    while (total < target) {
+        size_t best = nt;
+        double best_cost = 0.0;
+        for (size_t t = 0; t < nt; ++t) {
+            if (cls[t] + 1 >= kGemmTileClasses) continue;
+            const double e = (double)(64 >> cls[t]);
+            const double c = e * e * ktot[t];
+            if (best == nt || c > best_cost) {
+                best = t;
+                best_cost = c;
+            }
+        }
+        if (best == nt) break;
+        total += ntiles(best, cls[best] + 1) - ntiles(best, cls[best]);
+        ++cls[best];
+    }
+    g.tiles.clear();
+    for (size_t t = 0; t < nt; ++t) {
+        const int e = 64 >> cls[t];
+        for (int m0 = 0; m0 < g.tasks[t].M; m0 += e)
+            for (int n0 = 0; n0 < g.tasks[t].N; n0 += e) g.tiles.push_back({(int)t, m0, n0, cls[t]});
+    }
+    gemm_lpt_order(g, 64, 64);
+}
+
 // TK_OK, TK_ERR_INVALID_ARG (kinds differ) or TK_ERR_SECTOR_MISMATCH
 // (matched contracted sectors of different dimensions), with `err` set.
 inline tk_status block_gemm_plan(const Rank2& A, const Rank2& B, BlockGemmPlan& P, std::string& err) {
@@ -149,6 +194,7 @@ inline tk_status block_gemm_plan(const Rank2& A, const Rank2& B, BlockGemmPlan& 
         P.ooffs.push_back(P.total);
         P.total += M * N;
     }
+    bsgemm_retile(P.g, 2 * 152);
     return TK_OK;
 }
 

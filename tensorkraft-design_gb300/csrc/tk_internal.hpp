@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <array>
 #include <cstdint>
+#include <cstring>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -377,21 +378,35 @@ tk_status ctx_host_stage(tk_ctx* ctx, size_t bytes, void** out);
 tk_status ctx_stream(tk_ctx* ctx, void** out);
 // Packs host arrays back to back (256-byte aligned) for one host-to-device copy.
 struct Blob {
-    std::vector<unsigned char> bytes;
+    // The pieces of one host-to-device transfer: each piece is recorded with
+    // its source, and copy_to() copies every source once, straight into the
+    // page-locked staging buffer (the sources must outlive that call).
+    struct Ref {
+        size_t at;
+        const void* p;
+        size_t n;
+    };
+    std::vector<Ref> refs;
+    size_t end = 0;   // end of the transferred bytes
+    size_t tail = 0;  // end of the reserved space past them (written on the device)
     size_t add(const void* p, size_t n) {
-        const size_t at = (bytes.size() + 255) & ~(size_t)255;
-        bytes.resize(at + n);
-        if (n) std::copy((const unsigned char*)p, (const unsigned char*)p + n, bytes.begin() + at);
+        const size_t at = (end + 255) & ~(size_t)255;
+        if (n) refs.push_back({at, p, n});
+        end = at + n;
         return at;
     }
     size_t reserve(size_t n) {  // space without data (written on the device)
-        const size_t at = (bytes.size() + 255) & ~(size_t)255;
-        bytes.resize(at);
+        const size_t at = (end + 255) & ~(size_t)255;
+        end = at;
         tail = at + n;
         return at;
     }
-    size_t tail = 0;  // end of the reserved space past bytes
-    size_t device_size() const { return std::max(bytes.size(), tail); }
+    size_t size() const { return end; }
+    size_t device_size() const { return std::max(end, tail); }
+    void copy_to(void* dst) const {
+        unsigned char* d = static_cast<unsigned char*>(dst);
+        for (const Ref& r : refs) std::memcpy(d + r.at, r.p, r.n);
+    }
 };
 // Releases the context's cuSOLVER handle (dense.cu).
 void ctx_release_solver(tk_ctx* ctx);
