@@ -231,7 +231,11 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code);
  *     as one persistent, warp-specialised kernel (1: producer warps fill the
  *     psi operand and issue the TMA and MMAs of tile i + 1 while epilogue
  *     warps store tile i from the other of two TMEM accumulators) or as one
- *     CTA per tile (0, default).  Both compute the same T1 bits.
+ *     CTA per tile (0, default).  Both compute the same T1 bits;
+ *   stage1_narrow: the one-CTA-per-tile stage 1 takes the K of a stack in
+ *     32-wide chunks through one 24 KB shared-memory stage, eight CTAs per SM
+ *     (1), or in 64-wide chunks, four CTAs per SM (0, default); the same MMAs
+ *     in the same order, so the same T1 bits.  Ignored with stage1_persistent.
  * tk_heff2_set_tc_options rebuilds the plan's split tables and operands;
  * FP64 matvecs are unaffected.  TK_ERR_UNSUPPORTED for complex plans. */
 typedef struct {
@@ -239,6 +243,7 @@ typedef struct {
     int32_t fuse_max_ntiles;
     int32_t combine_warps;
     int32_t stage1_persistent;
+    int32_t stage1_narrow;
 } tk_tc_options;
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts);
 tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts);

@@ -514,7 +514,8 @@ static tk_status apply_tc_options(tk_heff2_plan* plan, const TcOptions& o) {
 
 tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts) {
     if (!plan || !opts || opts->tall_max_mtiles < 1 || opts->fuse_max_ntiles < 0 || opts->combine_warps < 0 ||
-        opts->combine_warps > 3 || opts->stage1_persistent < 0 || opts->stage1_persistent > 1) {
+        opts->combine_warps > 3 || opts->stage1_persistent < 0 || opts->stage1_persistent > 1 ||
+        opts->stage1_narrow < 0 || opts->stage1_narrow > 1) {
         set_error("tk_heff2_set_tc_options: invalid argument");
         return TK_ERR_INVALID_ARG;
     }
@@ -528,6 +529,7 @@ tk_status tk_heff2_set_tc_options(tk_heff2_plan* plan, const tk_tc_options* opts
     o.fuse_max_ntiles = opts->fuse_max_ntiles;
     o.combine_warps = opts->combine_warps;
     o.stage1_persistent = opts->stage1_persistent;
+    o.stage1_narrow = opts->stage1_narrow;
     return apply_tc_options(plan, o);
 }
 
@@ -540,6 +542,7 @@ tk_status tk_heff2_get_tc_options(const tk_heff2_plan* plan, tk_tc_options* opts
     opts->fuse_max_ntiles = plan->host.tcopt.fuse_max_ntiles;
     opts->combine_warps = plan->host.tcopt.combine_warps;
     opts->stage1_persistent = plan->host.tcopt.stage1_persistent;
+    opts->stage1_narrow = plan->host.tcopt.stage1_narrow;
     return TK_OK;
 }
 
@@ -996,10 +999,12 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
             if (hit.tall_max_mtiles != plan->host.tcopt.tall_max_mtiles ||
                 hit.fuse_max_ntiles != plan->host.tcopt.fuse_max_ntiles ||
                 hit.combine_warps != plan->host.tcopt.combine_warps ||
-                hit.stage1_persistent != plan->host.tcopt.stage1_persistent)
+                hit.stage1_persistent != plan->host.tcopt.stage1_persistent ||
+                hit.stage1_narrow != plan->host.tcopt.stage1_narrow)
                 st = apply_tc_options(plan, hit);
             if (st != TK_OK) return st;
-            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles, hit.combine_warps, hit.stage1_persistent};
+            out->chosen = {hit.tall_max_mtiles, hit.fuse_max_ntiles, hit.combine_warps, hit.stage1_persistent,
+                           hit.stage1_narrow};
             out->from_cache = 1;
             return TK_OK;
         }
@@ -1010,12 +1015,14 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
     if (st != TK_OK) return st;
     cudaStream_t s = plan->stream;
     TK_CUDA(launch_fill_start_vector(plan->hx.p, n, s));
-    // candidate schedules; a candidate whose tables come out the same as an
-    // earlier one's is not timed again.  The combine as persistent warps or one
+    // candidate schedules (each stage-1 form with 64- and 32-wide K chunks); a
+    // candidate whose tables and launch forms come out the same as an earlier
+    // one's is not timed again.  The combine as persistent warps or one
     // warp per job and the fused stage 3 stay settable (tk_heff2_set_tc_options)
     // but are not timed here: 1.3-3.5x slower than the default on the Hubbard
     // D=2048 bond, and every candidate costs a table rebuild inside a sweep
-    const TcOptions cand[] = {{3, 0, 0, 0}, {3, 0, 3, 0}, {3, 0, 0, 1}, {1 << 30, 0, 0, 0}, {1, 0, 0, 0}};
+    const TcOptions cand[] = {{3, 0, 0, 0, 0}, {3, 0, 0, 0, 1}, {3, 0, 3, 0, 0}, {3, 0, 3, 0, 1},
+                              {3, 0, 0, 1, 0}, {1 << 30, 0, 0, 0, 0}, {1, 0, 0, 0, 0}};
     std::vector<std::vector<size_t>> shapes;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TK_CUDA(cudaEventCreate(&e0));
@@ -1034,7 +1041,8 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         const TcTables& C = plan->host.tc;
         std::vector<size_t> shape = {C.tiles1.size(), C.tiles1x.size(), C.split.size(), C.tiles3.size(),
                                      C.tiles3f.size(), C.jobs.size(), C.jobs.empty() ? 0u : (size_t)c.combine_warps,
-                                     C.tiles1.empty() ? 0u : (size_t)c.stage1_persistent};
+                                     C.tiles1.empty() ? 0u : (size_t)c.stage1_persistent,
+                                     C.tiles1.empty() || c.stage1_persistent ? 0u : (size_t)c.stage1_narrow};
         if (std::find(shapes.begin(), shapes.end(), shape) != shapes.end()) continue;
         shapes.push_back(shape);
         for (int w = 0; w < 2; ++w)
@@ -1050,7 +1058,7 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         ms /= (float)reps;
         if (out->n_candidates < 8) {
             out->candidates[out->n_candidates] = {c.tall_max_mtiles, c.fuse_max_ntiles, c.combine_warps,
-                                                  c.stage1_persistent};
+                                                  c.stage1_persistent, c.stage1_narrow};
             out->candidate_ms[out->n_candidates] = ms;
             ++out->n_candidates;
         }
@@ -1064,7 +1072,8 @@ extern "C" tk_status tk_heff2_autotune(tk_heff2_plan* plan, int32_t reps, int32_
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache[key] = best;
     }
-    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles, best.combine_warps, best.stage1_persistent};
+    out->chosen = {best.tall_max_mtiles, best.fuse_max_ntiles, best.combine_warps, best.stage1_persistent,
+                   best.stage1_narrow};
     out->chosen_ms = best_ms;
     return TK_OK;
 }

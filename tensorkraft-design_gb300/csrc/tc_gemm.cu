@@ -110,6 +110,18 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     return d;
 }
 
+// The same for K-major rows of 64 bytes (32 bf16) with the 64-byte swizzle:
+// 8-row core groups 512 bytes apart, layout type 4.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)(512u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;
+    return d;
+}
+
 // Instruction descriptor, kind::f16: fp32 accumulate, bf16 A and B, both
 // K-major, N>>3 at bit 17, M>>4 at bit 24.  N is chosen per tile.
 __device__ __forceinline__ uint32_t make_idesc(int n) {
@@ -399,31 +411,49 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const TcTile* __restric
 
 
 // Stage 1 with the psi operand built in shared memory.  The L stack (A) comes
-// in by TMA as in tc_gemm_kernel; the B tile (n_mma columns x 64 K) is read
+// in by TMA as in tc_gemm_kernel; the B tile (n_mma columns x KW K) is read
 // from the fp64 vector by all 128 threads (column n of the tile is
 // psi[xsrc[n] + k * xstride[n]], zero past the stack's K), split into bf16
-// hi / lo and written in the layout a 128-byte-swizzled TMA load would give:
-// row n at n * 128 bytes, its 16-byte chunk j at position j ^ (n % 8).  A
-// proxy fence and a block barrier hand the tile to the MMA thread.  Loop trip
-// counts stay block-uniform (bounded waits are combined with
-// __syncthreads_and) so no thread can be left at a barrier.
-template <int NST>
-__global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restrict__ tiles,
+// hi / lo and written in the layout a swizzled TMA load would give: KW = 64,
+// row n at n * 128 bytes, its 16-byte chunk j at position j ^ (n % 8)
+// (128-byte swizzle); KW = 32, row n at n * 64 bytes, chunk j at
+// j ^ ((n / 2) % 4) (64-byte swizzle).  A proxy fence and a block barrier
+// hand the tile to the MMA thread.  Loop trip counts stay block-uniform
+// (bounded waits are combined with __syncthreads_and) so no thread can be
+// left at a barrier.
+//
+// KW = 32 (TcOptions::stage1_narrow) takes the K of a stack in 32-wide
+// chunks: chunk c is the half c % 2 of the plan's 64-wide chunk c / 2 (TMA
+// box 32 x 128 rows at x = 32 * (c % 2)), so a stage holds 24 KB instead of
+// 48, and with one stage, at most 64 registers a thread and 64 TMEM columns a
+// CTA, eight CTAs share an SM instead of four.  The MMAs are the same ones in
+// the same order, so T1 is bit-identical to KW = 64.
+template <int KW>
+constexpr int s1_stage_bytes() { return 2 * kTcBM * KW * 2 + 2 * kTcBN * KW * 2; }
+template <int KW>
+constexpr int s1_smem_bytes(int nst) { return nst * s1_stage_bytes<KW>() + 1024 + 256; }
+
+template <int NST, int KW>
+__global__ void __launch_bounds__(128, KW == 64 ? 4 : 8) tc_gemm1_kernel(const TcTile* __restrict__ tiles,
                                                           const __grid_constant__ CUtensorMap mAh,
                                                           const __grid_constant__ CUtensorMap mAl,
                                                           const double* __restrict__ x,
                                                           const int64_t* __restrict__ xsrc,
                                                           const int32_t* __restrict__ xstride, const OutMap om,
                                                           int* err) {
+    static_assert(KW == 64 || KW == 32, "stage-1 K chunk of 64 or 32");
+    constexpr int A_B = kTcBM * KW * 2, B_B = kTcBN * KW * 2, SB = s1_stage_bytes<KW>();
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* full = (uint64_t*)(smem + NST * STAGE_BYTES);
+    uint64_t* full = (uint64_t*)(smem + NST * SB);
     uint64_t* empty = full + NST;
     uint64_t* done = empty + NST;
     uint32_t* tslot = (uint32_t*)(done + 1);
     const TcTile t = tiles[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     grid_dep_launch();
+    // K chunks of this tile (the plan counts 64-wide ones)
+    const int kch = KW == 64 ? t.kch : (t.k_valid + KW - 1) / KW;
 
     if (t.kch == 0) {
         grid_dep_wait();
@@ -469,38 +499,40 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
         }
     // the L operand (a plan constant) of the first chunks goes out before the
     // dependency wait, overlapping the previous kernel's tail
-    const int npre = min(NST, t.kch);
+    const int npre = min(NST, kch);
     if (threadIdx.x == 0)
         for (int c = 0; c < npre; ++c) {
-            uint8_t* st = smem + c * STAGE_BYTES;
-            mbar_expect_tx(&full[c], 2 * A_BYTES);
-            const int ya = t.a_row + c * t.a_cs;
-            tma_load_2d(st, &mAh, 0, ya, &full[c]);
-            tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[c]);
+            uint8_t* st = smem + c * SB;
+            mbar_expect_tx(&full[c], 2 * A_B);
+            const int xa = KW == 64 ? 0 : (c & 1) * KW;
+            const int ya = t.a_row + (KW == 64 ? c : c >> 1) * t.a_cs;
+            tma_load_2d(st, &mAh, xa, ya, &full[c]);
+            tma_load_2d(st + A_B, &mAl, xa, ya, &full[c]);
         }
     grid_dep_wait();
-    for (int c = 0; c < t.kch; ++c) {
+    for (int c = 0; c < kch; ++c) {
         const int s = c % NST;
         bool good = true;
         if (c >= NST) good = mbar_wait(&empty[s], ((c / NST) - 1) & 1, err, ERR_EMPTY_TIMEOUT);
         if (!__syncthreads_and(good)) break;
-        uint8_t* st = smem + s * STAGE_BYTES;
+        uint8_t* st = smem + s * SB;
         if (threadIdx.x == 0 && c >= npre) {
-            mbar_expect_tx(&full[s], 2 * A_BYTES);
-            const int ya = t.a_row + c * t.a_cs;
-            tma_load_2d(st, &mAh, 0, ya, &full[s]);
-            tma_load_2d(st + A_BYTES, &mAl, 0, ya, &full[s]);
+            mbar_expect_tx(&full[s], 2 * A_B);
+            const int xa = KW == 64 ? 0 : (c & 1) * KW;
+            const int ya = t.a_row + (KW == 64 ? c : c >> 1) * t.a_cs;
+            tma_load_2d(st, &mAh, xa, ya, &full[s]);
+            tma_load_2d(st + A_B, &mAl, xa, ya, &full[s]);
         }
-        uint8_t* bh = st + 2 * A_BYTES;
-        uint8_t* bl = bh + B_BYTES;
-        const int kbase = c * kTcBK;
+        uint8_t* bh = st + 2 * A_B;
+        uint8_t* bl = bh + B_B;
+        const int kbase = c * KW;
         // 16-wide K steps that hold data: only those are filled and multiplied
-        const int ksteps = min(kTcBK / 16, (t.k_valid - kbase + 15) / 16);
+        const int ksteps = min(KW / 16, (t.k_valid - kbase + 15) / 16);
         const int nkp = 8 * ksteps;  // k pairs holding data in this chunk
         if (fill_col >= 0) {
-            // a thread owns at most kFillPairs k pairs of a chunk (nkp <= 32,
+            // a thread owns at most kFillPairs k pairs of a chunk (nkp <= KW / 2,
             // fill_step >= 2): every load of the chunk is in flight at once
-            constexpr int kFillPairs = kTcBK / 2 / 2;
+            constexpr int kFillPairs = KW / 2 / 2;
             double v[kFillPairs][2];
 #pragma unroll
             for (int u = 0; u < kFillPairs; ++u) {
@@ -519,7 +551,8 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
                 split2x2(v[u][0], v[u][1], hw, lw);
                 const int n = fill_col, k = 2 * kq;
                 const uint32_t off =
-                    (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u;
+                    KW == 64 ? (uint32_t)n * 128u + ((uint32_t)((k >> 3) ^ (n & 7)) << 4) + (uint32_t)(k & 7) * 2u
+                             : (uint32_t)n * 64u + ((uint32_t)((k >> 3) ^ ((n >> 1) & 3)) << 4) + (uint32_t)(k & 7) * 2u;
                 *reinterpret_cast<uint32_t*>(bh + off) = hw;
                 *reinterpret_cast<uint32_t*>(bl + off) = lw;
             }
@@ -530,8 +563,9 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
             if (mbar_wait(&full[s], (c / NST) & 1, err, ERR_FULL_TIMEOUT)) {
                 fence_after();
                 const uint32_t sa = smem_u32(st);
-                const uint64_t ah = sw128_desc(sa), al = sw128_desc(sa + A_BYTES);
-                const uint64_t bhd = sw128_desc(sa + 2 * A_BYTES), bld = sw128_desc(sa + 2 * A_BYTES + B_BYTES);
+                auto desc = [](uint32_t a) { return KW == 64 ? sw128_desc(a) : sw64_desc(a); };
+                const uint64_t ah = desc(sa), al = desc(sa + A_B);
+                const uint64_t bhd = desc(sa + 2 * A_B), bld = desc(sa + 2 * A_B + B_B);
                 for (int q = 0; q < ksteps; ++q) {
                     const uint64_t adv = (uint64_t)((q * 32) >> 4);
                     mma_bf16(tmem, ah + adv, bhd + adv, idesc, (c | q) != 0);
@@ -547,7 +581,7 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
     const bool have = mbar_wait(done, 0, err, ERR_DONE_TIMEOUT);
     fence_after();
     const bool go = __all_sync(0xffffffffu, have);
-    if (go) {
+    if (go && KW == 64) {
         float (*stile)[kTcBN + 1] = reinterpret_cast<float (*)[kTcBN + 1]>(smem);
         const int row = threadIdx.x;
         const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
@@ -558,6 +592,30 @@ __global__ void __launch_bounds__(128, 4) tc_gemm1_kernel(const TcTile* __restri
 #pragma unroll
             for (int h = 0; h < 2; ++h)
                 if (lane + 32 * h < t.n_valid) om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane + 32 * h];
+    } else if (go) {
+        // 32 columns at a time through a 128 x 33 transpose buffer (17 KB of
+        // the 24 KB stage), 16 TMEM columns per load: 64 registers a thread
+        float (*stile)[33] = reinterpret_cast<float (*)[33]>(smem);
+        const int row = threadIdx.x;
+        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+        const int rend = min(t.m_valid, warp * 32 + 32);
+        for (int h = 0; h < 2; ++h) {
+            if (32 * h >= t.n_mma) break;  // block-uniform
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                if (32 * h + 16 * q >= t.n_mma) break;
+                uint32_t r16[16];
+                tmem_ld16_nowait(tbase + (uint32_t)(32 * h + 16 * q), r16);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int i = 0; i < 16; ++i) stile[row][16 * q + i] = __uint_as_float(r16[i]);
+            }
+            __syncwarp();
+            if (lane + 32 * h < t.n_valid)
+                for (int r = warp * 32; r < rend; ++r)
+                    om.out32[cb[h] + (int64_t)(t.ldc + r) * cs[h]] = stile[r][lane];
+            __syncwarp();
+        }
     }
     fence_before();
     __syncthreads();
@@ -1353,17 +1411,20 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn(std::string& err) {
     return fn;
 }
 
-bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string& err) {
+// A 2D map over an operand of 64-element rows; box_k = 64 (128-byte swizzle)
+// or 32 (half a row, 64-byte swizzle: the narrow stage-1 chunks).
+bool make_map(CUtensorMap* m, void* ptr, int64_t rows, int box_rows, std::string& err, int box_k = kTcBK) {
     std::memset(m, 0, sizeof(*m));
     if (rows <= 0) return true;
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn(err);
     if (!enc) return false;
     cuuint64_t dims[2] = {(cuuint64_t)kTcBK, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)kTcBK * 2};
-    cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
-                                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                        CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                        box_k == kTcBK ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         err = "cuTensorMapEncodeTiled failed with CUresult " + std::to_string((int)r);
@@ -1382,6 +1443,7 @@ struct TcPlan {
     int n3f = 0;
     int comb_form = 0;  // TcOptions::combine_warps: 0 CTA per job, 1 warps, 2 warp per job, 3 64-thread CTA per job
     bool p1 = false;                    // stage 1 as the persistent kernel (TcOptions::stage1_persistent)
+    bool narrow1 = false;               // stage 1 in 32-wide K chunks (TcOptions::stage1_narrow)
     int p1_ctas = 0;                    // its resident CTAs per SM x SMs
     bool t1_wide = false;               // T1 holds 2^31 elements or more (64-bit combine offsets)
     __nv_bfloat16 *lh = nullptr, *ll = nullptr, *rh = nullptr, *rl = nullptr;
@@ -1403,6 +1465,7 @@ struct TcPlan {
     int64_t x_cut[kTcPsiPieces + 1] = {};
     int nst1 = 1, nst1x = 2, nst3 = 2;  // pipeline stages of the GEMM launches
     CUtensorMap mLh, mLl, mTh, mTl, mRh, mRl, mXh, mXl;
+    CUtensorMap mLh32, mLl32;  // the L operand in 32-wide K boxes (narrow stage 1)
     ~TcPlan() {
         void* ps[] = {lh,    ll,    rh,   rl,         th,           tl,   xh,      xl,  t1, tiles1, tiles1x,
                       tiles3, split, jobs, terms, yrow, t1col_base, t1col_stride, xsrc, xstride, err,
@@ -1459,6 +1522,7 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n3f = (int)C.tiles3f.size();
     p->comb_form = host.tcopt.combine_warps;
     p->p1 = host.tcopt.stage1_persistent != 0;
+    p->narrow1 = !p->p1 && host.tcopt.stage1_narrow != 0;
     p->t1_wide = C.t1_total > INT32_MAX;
     if (p->comb_form == 2 && C.t1_total > INT32_MAX) p->comb_form = 0;  // form 2 indexes T1 rows in 32 bits
     p->nsplit = (int)C.split.size();
@@ -1469,16 +1533,19 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     if (!make_map(&p->mLh, p->lh, C.lq_rows, kTcBM, err) || !make_map(&p->mLl, p->ll, C.lq_rows, kTcBM, err) ||
         !make_map(&p->mXh, p->xh, C.xq_rows, 16, err) || !make_map(&p->mXl, p->xl, C.xq_rows, 16, err) ||
         !make_map(&p->mTh, p->th, C.t2q_rows, kTcBM, err) || !make_map(&p->mTl, p->tl, C.t2q_rows, kTcBM, err) ||
-        !make_map(&p->mRh, p->rh, C.rq_rows, 16, err) || !make_map(&p->mRl, p->rl, C.rq_rows, 16, err))
+        !make_map(&p->mRh, p->rh, C.rq_rows, 16, err) || !make_map(&p->mRl, p->rl, C.rq_rows, 16, err) ||
+        !make_map(&p->mLh32, p->lh, C.lq_rows, kTcBM, err, 32) || !make_map(&p->mLl32, p->ll, C.lq_rows, kTcBM, err, 32))
         return TK_ERR_CUDA;
     if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
             cudaSuccess ||
         (e = cudaFuncSetAttribute(tc_gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
             cudaSuccess ||
-        (e = cudaFuncSetAttribute(tc_gemm1_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1))) !=
-            cudaSuccess ||
-        (e = cudaFuncSetAttribute(tc_gemm1_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
-            cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1_kernel<1, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  s1_smem_bytes<64>(1))) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1_kernel<2, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  s1_smem_bytes<64>(2))) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(tc_gemm1_kernel<1, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  s1_smem_bytes<32>(1))) != cudaSuccess ||
         (e = cudaFuncSetAttribute(tc_gemm3f_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2))) !=
             cudaSuccess ||
         (e = cudaFuncSetAttribute(tc_gemm1p_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1551,11 +1618,14 @@ void launch_stage1_fused(TcPlan& tc, const double* x, int first, int count, cuda
                        (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
         return;
     }
-    if (tc.nst1 == 1)
-        launch_pdl(tc_gemm1_kernel<1>, count, 128, smem_bytes(1), s, tiles, tc.mLh, tc.mLl, x,
+    if (tc.narrow1)  // one 24 KB stage whatever the tiles' K: the chunks of a tile run one after another
+        launch_pdl(tc_gemm1_kernel<1, 32>, count, 128, s1_smem_bytes<32>(1), s, tiles, tc.mLh32, tc.mLl32, x,
+                   (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
+    else if (tc.nst1 == 1)
+        launch_pdl(tc_gemm1_kernel<1, 64>, count, 128, s1_smem_bytes<64>(1), s, tiles, tc.mLh, tc.mLl, x,
                    (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
     else
-        launch_pdl(tc_gemm1_kernel<2>, count, 128, smem_bytes(2), s, tiles, tc.mLh, tc.mLl, x,
+        launch_pdl(tc_gemm1_kernel<2, 64>, count, 128, s1_smem_bytes<64>(2), s, tiles, tc.mLh, tc.mLl, x,
                    (const int64_t*)tc.xsrc, (const int32_t*)tc.xstride, om, tc.err);
 }
 

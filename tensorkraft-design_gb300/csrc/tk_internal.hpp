@@ -259,11 +259,15 @@ struct TcTables {
 //     64-thread CTA per job, eight elements per thread (3).
 //   stage1_persistent: the in-kernel-split stage 1 as a persistent,
 //     warp-specialised kernel (1) or one CTA per tile (0).
+//   stage1_narrow: the one-CTA-per-tile stage 1 in 32-wide K chunks with a
+//     single 24 KB stage, eight CTAs per SM (1), or 64-wide chunks, four CTAs
+//     per SM (0); the same MMAs in the same order either way.
 struct TcOptions {
     int32_t tall_max_mtiles = 3;
     int32_t fuse_max_ntiles = 0;
     int32_t combine_warps = 0;
     int32_t stage1_persistent = 0;
+    int32_t stage1_narrow = 0;
 };
 
 // The sector structure the split-precision tables are built from, kept with

@@ -83,7 +83,7 @@ class tk_mat_mut(C.Structure):
 
 class tk_tc_options(C.Structure):
     _fields_ = [("tall_max_mtiles", C.c_int32), ("fuse_max_ntiles", C.c_int32), ("combine_warps", C.c_int32),
-                ("stage1_persistent", C.c_int32)]
+                ("stage1_persistent", C.c_int32), ("stage1_narrow", C.c_int32)]
 
 
 class tk_autotune_result(C.Structure):

@@ -248,15 +248,16 @@ class Heff2Plan:
         self.precision = precision
 
     def set_tc_options(self, tall_max_mtiles: int = 3, fuse_max_ntiles: int = 0, combine_warps: int = 0,
-                       stage1_persistent: int = 0):
+                       stage1_persistent: int = 0, stage1_narrow: int = 0):
         """tk_heff2_set_tc_options: the split-precision schedule (see tk_heff.h)."""
-        o = _abi.tk_tc_options(tall_max_mtiles, fuse_max_ntiles, combine_warps, stage1_persistent)
+        o = _abi.tk_tc_options(tall_max_mtiles, fuse_max_ntiles, combine_warps, stage1_persistent, stage1_narrow)
         check(self._lib.tk_heff2_set_tc_options(self._h, C.byref(o)))
 
     @staticmethod
     def _opts(o) -> dict:
         return {"tall_max_mtiles": o.tall_max_mtiles, "fuse_max_ntiles": o.fuse_max_ntiles,
-                "combine_warps": o.combine_warps, "stage1_persistent": o.stage1_persistent}
+                "combine_warps": o.combine_warps, "stage1_persistent": o.stage1_persistent,
+                "stage1_narrow": o.stage1_narrow}
 
     def tc_options(self) -> dict:
         o = _abi.tk_tc_options()
