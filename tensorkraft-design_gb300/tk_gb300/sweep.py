@@ -264,7 +264,10 @@ class _SingleThreadBlas:
     small LAPACK calls side by side without oversubscribing the cores (the
     per-charge matrices of a truncation are too small for BLAS threading to
     pay).  Finds the library among the loaded shared objects and calls its
-    thread-count setter; a no-op when there is none."""
+    thread-count setter; a no-op when there is none.  scipy's wheels carry an
+    OpenBLAS of their own: while the block is active, `set_second(k)` gives
+    that one k threads (numpy's stays on one), so one large factorisation can
+    run threaded through scipy.linalg beside single-threaded numpy calls."""
 
     _fns = None
 
@@ -272,6 +275,10 @@ class _SingleThreadBlas:
     def _setters(cls):
         if cls._fns is None:
             cls._fns = []
+            try:
+                import scipy.linalg  # noqa: F401  (loads scipy's own OpenBLAS, if it has one)
+            except ImportError:
+                pass
             try:
                 paths = {ln.split()[-1] for ln in open("/proc/self/maps") if "openblas" in ln.lower()}
             except OSError:
@@ -290,13 +297,24 @@ class _SingleThreadBlas:
                             continue
                         get_fn.restype = C.c_int
                         set_fn.argtypes = [C.c_int]
-                        cls._fns.append((set_fn, get_fn))
+                        cls._fns.append((set_fn, get_fn, "numpy" in path))
                         break
         return cls._fns
 
+    @property
+    def has_second(self) -> bool:
+        """Whether a BLAS other than numpy's (scipy's) is loaded and settable."""
+        fns = self._setters()
+        return any(not is_np for _, _, is_np in fns) and any(is_np for _, _, is_np in fns)
+
+    def set_second(self, k: int):
+        for set_fn, _, is_np in self._setters():
+            if not is_np:
+                set_fn(int(k))
+
     def __enter__(self):
         self._saved = []
-        for set_fn, get_fn in self._setters():
+        for set_fn, get_fn, _ in self._setters():
             self._saved.append((set_fn, int(get_fn())))
             set_fn(1)
         return self
@@ -308,15 +326,78 @@ class _SingleThreadBlas:
 
 
 _POOL = None
+# Speed-up of LAPACK's gesdd on k threads for the largest block of a
+# truncation, as the share of its one-thread time: a 750 x 740 block on the
+# 16-core Grace host of a GB300 takes 192 ms on one thread, 137 / 124 / 120 ms
+# on 4 / 8 / 12 (about 126 ms on 8 beside eight single-threaded factorisations).
+_BIG_SPEEDUP = ((4, 0.71), (8, 0.65), (12, 0.63))
+
+
+def _big_block_threads(costs: list, workers: int) -> int:
+    """BLAS threads for the largest factorisation of a truncation (0: every
+    block on one thread): the k that minimises max(the largest block on k
+    threads, the other blocks on workers - k single-threaded workers),
+    from the blocks' flop counts m n min(m, n), largest first."""
+    if len(costs) < 2 or workers < 6:
+        return 0
+    big, rest = float(costs[0]), float(sum(costs[1:]))
+    best_k, best_t = 0, max(big, rest / (workers - 1))
+    for k, f in _BIG_SPEEDUP:
+        if k > workers - 2:
+            break
+        t = max(big * f, rest / (workers - k))
+        if t < 0.95 * best_t:
+            best_k, best_t = k, t
+    return best_k
+
+
+def _factor_blocks(block, order: list, costs: list) -> dict:
+    """{i: numpy.linalg.svd(block(i), full_matrices=False)} over `order`
+    (largest first) on the host thread pool, one BLAS thread per call; when
+    the largest block would set the wall time alone (_big_block_threads), it
+    is factored by scipy.linalg (gesdd, its own OpenBLAS on k threads) while
+    the others run on the remaining workers."""
+    import threading
+
+    workers = _pool_size()
+    with _SingleThreadBlas() as blas:
+        k = _big_block_threads(costs, workers) if blas.has_second else 0
+        if k == 0:
+            return dict(_pool().map(lambda i: (i, np.linalg.svd(block(i), full_matrices=False)), order))
+        import scipy.linalg as sl
+
+        blas.set_second(k)
+        big = order[0]
+        big_fut = _pool().submit(lambda: sl.svd(block(big), full_matrices=False, lapack_driver="gesdd"))
+        out, rest, lock = {}, iter(order[1:]), threading.Lock()
+
+        def worker():
+            while True:
+                with lock:
+                    i = next(rest, None)
+                if i is None:
+                    return
+                out[i] = np.linalg.svd(block(i), full_matrices=False)
+
+        futs = [_pool().submit(worker) for _ in range(workers - k)]
+        for f in futs:
+            f.result()
+        out[big] = big_fut.result()
+    return out
+
+
+def _pool_size() -> int:
+    import os
+
+    return max(1, min(32, os.cpu_count() or 1))
 
 
 def _pool():
     global _POOL
     if _POOL is None:
-        import os
         from concurrent.futures import ThreadPoolExecutor
 
-        _POOL = ThreadPoolExecutor(max(1, min(32, os.cpu_count() or 1)))
+        _POOL = ThreadPoolExecutor(_pool_size())
     return _POOL
 
 
@@ -610,13 +691,11 @@ def split_two_site_device(kind, psi_dev, keys, offs, legs, max_bond: int, cutoff
             mq = mbufs[0][moff[i]:moff[i + 1]].reshape(rows[i], cols[i])
             return mq + 1j * mbufs[1][moff[i]:moff[i + 1]].reshape(rows[i], cols[i]) if cplx else mq
 
-        def svd(i):
-            return i, np.linalg.svd(block(i), full_matrices=False)
-
-        # largest factorisations first on the pool (one BLAS thread each)
-        order = sorted(range(nq), key=lambda i: -int(rows[i] * cols[i] * min(rows[i], cols[i])))
-        with _SingleThreadBlas():
-            usv = dict(_pool().map(svd, order))
+        # largest factorisations first on the pool (one BLAS thread each, or a
+        # few for the largest block when it would set the wall time alone)
+        cost = [int(rows[i] * cols[i] * min(rows[i], cols[i])) for i in range(nq)]
+        order = sorted(range(nq), key=lambda i: -cost[i])
+        usv = _factor_blocks(block, order, [cost[i] for i in order])
         kept, disc, norm = _select([usv[i][1] for i in range(nq)], max_bond, cutoff, min_bond)
         nbi, ti, nbj, tj = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
         check(lib.tk_split_set_kept(h, _abi.i64ptr(kept), C.byref(nbi), C.byref(ti), C.byref(nbj), C.byref(tj)))

@@ -233,3 +233,40 @@ def test_rank_deficient_charges_match_a_dense_svd():
         A, B = _rebuild(Ai, Aj, nb, P, QA, QB)
         rec = np.einsum("sab,tbc->stac", A, B) * np.linalg.norm(psi)
         assert np.allclose(rec, T, atol=1e-12)
+
+
+def test_threads_for_the_largest_block():
+    """The largest factorisation of a truncation gets several BLAS threads only
+    when it would otherwise set the wall time alone."""
+    from tk_gb300.sweep import _big_block_threads
+
+    assert _big_block_threads([100.0] + [1.0] * 30, 16) > 0  # one dominant block
+    assert _big_block_threads([1.0] * 40, 16) == 0  # balanced: every block on one thread
+    assert _big_block_threads([100.0, 1.0], 4) == 0  # too few cores to share
+    assert _big_block_threads([5.0], 16) == 0
+
+
+def test_factor_blocks_matches_numpy():
+    """_factor_blocks: every block's thin SVD, whichever BLAS and thread count
+    factor it (the dominant block through scipy.linalg on several threads)."""
+    from tk_gb300 import sweep
+
+    rng = np.random.default_rng(3)
+    shapes = [(160, 150)] + [(rng.integers(2, 30), rng.integers(2, 30)) for _ in range(12)] + [(1, 5), (7, 1)]
+    blocks = [rng.standard_normal(s) for s in shapes]
+    for workers in (1, 8, 16):
+        saved = sweep._pool_size
+        sweep._pool_size = lambda w=workers: w
+        try:
+            cost = [m * n * min(m, n) for m, n in shapes]
+            order = sorted(range(len(blocks)), key=lambda i: -cost[i])
+            out = sweep._factor_blocks(lambda i: blocks[i], order, [cost[i] for i in order])
+        finally:
+            sweep._pool_size = saved
+        assert sorted(out) == list(range(len(blocks)))
+        for i, (U, s, Vt) in out.items():
+            ref = np.linalg.svd(blocks[i], compute_uv=False)
+            assert np.allclose(s, ref, rtol=1e-12, atol=1e-13)
+            assert np.allclose((U * s) @ Vt, blocks[i], atol=1e-12)
+            k = len(s)
+            assert np.allclose(U.T @ U, np.eye(k), atol=1e-12) and np.allclose(Vt @ Vt.T, np.eye(k), atol=1e-12)
