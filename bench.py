@@ -76,6 +76,10 @@ def parse():
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: time the split-precision schedule candidates and keep the fastest; 0: the default "
                          "schedule (for profiler launch lists)")
+    ap.add_argument("--tc-options", default=None, metavar="T,F,W,P,N",
+                    help="with --autotune 0: this split-precision schedule (tk_tc_options: tall_max_mtiles, "
+                         "fuse_max_ntiles, combine_warps, stage1_persistent, stage1_narrow), e.g. the autotuner's "
+                         "choice for a profiler launch list")
     ap.add_argument("--tdvp-steps", type=int, default=0, metavar="K",
                     help="also time K real-time TDVP steps of the impurity Green's function (Anderson chain, "
                          "16 sites, D=1024, dt=0.05, Krylov 16) after a split-precision DMRG ground state")
@@ -606,6 +610,9 @@ def run_ours(args):
         # the autotuner times the candidate schedules on this workload and keeps the fastest
         if args.autotune:
             tune = plan.autotune(reps=10, use_cache=False)
+        elif args.tc_options:
+            plan.set_tc_options(*[int(v) for v in args.tc_options.split(",")])
+            tune = {"chosen": plan.tc_options(), "set_by": "--tc-options"}
     n = plan.block_dim
     flops_total, alg_bytes = plan.cost()
     launches_per_matvec = plan.launches()
