@@ -487,7 +487,24 @@ tk_status tk_heff2_inject_error_word(tk_heff2_plan* plan, int32_t code) {
 // CUDA graphs hold the old kernels' tables and are dropped.
 static tk_status apply_tc_options(tk_heff2_plan* plan, const TcOptions& o) {
     std::string err;
-    tk_status st = rebuild_tc_tables(plan->host, o, err);
+    tk_status st;
+    const TcOptions cur = plan->host.tcopt;
+    if (plan->host.tc_built && o.tall_max_mtiles == cur.tall_max_mtiles && o.fuse_max_ntiles == cur.fuse_max_ntiles) {
+        // only launch forms change (combine form, persistent or narrow stage
+        // 1): the split tables and operands stay; the cached graphs go
+        if (plan->tc && (st = tc_set_launch_forms(*plan->tc, o, err)) != TK_OK) {
+            set_error("tc options: " + err);
+            return st;
+        }
+        plan->host.tcopt = o;
+        if (plan->host_exec) {
+            cudaGraphExecDestroy(plan->host_exec);
+            plan->host_exec = nullptr;
+        }
+        plan->lz_graph.reset();
+        return TK_OK;
+    }
+    st = rebuild_tc_tables(plan->host, o, err);
     if (st != TK_OK) {
         set_error("tc options: " + err);
         return st;

@@ -1520,11 +1520,7 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
     p->n1x = (int)C.tiles1x.size();
     p->n3 = (int)C.tiles3.size();
     p->n3f = (int)C.tiles3f.size();
-    p->comb_form = host.tcopt.combine_warps;
-    p->p1 = host.tcopt.stage1_persistent != 0;
-    p->narrow1 = !p->p1 && host.tcopt.stage1_narrow != 0;
     p->t1_wide = C.t1_total > INT32_MAX;
-    if (p->comb_form == 2 && C.t1_total > INT32_MAX) p->comb_form = 0;  // form 2 indexes T1 rows in 32 bits
     p->nsplit = (int)C.split.size();
     p->njobs = (int)C.jobs.size();
     p->nst1 = C.max_kch1 <= 1 ? 1 : 2;
@@ -1555,20 +1551,31 @@ tk_status tc_plan_create(const Heff2Tables& host, const double*, const double*,
         err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return TK_ERR_CUDA;
     }
-    if (p->p1) {
+    tk_status st = tc_set_launch_forms(*p, host.tcopt, err);
+    if (st != TK_OK) return st;
+    out = std::move(p);
+    return TK_OK;
+}
+
+tk_status tc_set_launch_forms(TcPlan& p, const TcOptions& o, std::string& err) {
+    p.comb_form = o.combine_warps;
+    if (p.comb_form == 2 && p.t1_wide) p.comb_form = 0;  // form 2 indexes T1 rows in 32 bits
+    p.p1 = o.stage1_persistent != 0;
+    p.narrow1 = !p.p1 && o.stage1_narrow != 0;
+    if (p.p1 && p.p1_ctas == 0) {
         int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
             (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-            (e = p->nst1 == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_gemm1p_kernel<1>, kP1Threads,
-                                                                              p1_smem_bytes(1))
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_gemm1p_kernel<2>, kP1Threads,
-                                                                              p1_smem_bytes(2))) != cudaSuccess) {
+            (e = p.nst1 == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_gemm1p_kernel<1>, kP1Threads,
+                                                                             p1_smem_bytes(1))
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_gemm1p_kernel<2>, kP1Threads,
+                                                                             p1_smem_bytes(2))) != cudaSuccess) {
             err = std::string("persistent stage-1 occupancy: ") + cudaGetErrorString(e);
             return TK_ERR_CUDA;
         }
-        p->p1_ctas = std::max(1, per_sm) * std::max(1, sms);
+        p.p1_ctas = std::max(1, per_sm) * std::max(1, sms);
     }
-    out = std::move(p);
     return TK_OK;
 }
 

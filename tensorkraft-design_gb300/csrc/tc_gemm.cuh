@@ -18,6 +18,9 @@ struct TcPlanDeleter {
 // tile tables of both GEMM stages.
 tk_status tc_plan_create(const Heff2Tables& host, const double* d_lbuf, const double* d_rbuf,
                          std::unique_ptr<TcPlan, TcPlanDeleter>& out, std::string& err);
+// The launch forms of a built plan (combine form, persistent or narrow stage
+// 1): the options that do not shape the split tables, applied in place.
+tk_status tc_set_launch_forms(TcPlan& p, const TcOptions& o, std::string& err);
 
 // One split-precision matvec, stream-ordered.
 cudaError_t tc_apply(TcPlan& tc, const Heff2Tables& host, const CombJob* d_jobs, int n_jobs,
