@@ -249,3 +249,98 @@ class BlockSparseTensor:
             sl = tuple(slice(ix.offset_of(q), ix.offset_of(q) + ix.dim_of(q)) for ix, q in zip(self.indices, qns))
             out[sl] += blk
         return out
+
+    def get_block(self, qns):
+        """The block of sector `qns`, or None when the tensor stores none
+        (block_sparse.rs:284-290)."""
+        return self.blocks.get(key_pack(self.kind, qns))
+
+    def permute(self, perm) -> "BlockSparseTensor":
+        """Legs, directions and every block's axes reordered by `perm`, keys
+        re-packed (block_sparse.rs:400-431).  Blocks are copied."""
+        perm = [int(p) for p in perm]
+        if sorted(perm) != list(range(self.rank)):
+            raise ValueError(f"permute: {perm} is not a permutation of {self.rank} legs")
+        out = BlockSparseTensor([self.indices[i] for i in perm], self.flux, [self.dirs[i] for i in perm])
+        for qns, blk in self.iter_blocks():
+            out.blocks[key_pack(self.kind, [qns[i] for i in perm])] = np.ascontiguousarray(blk.transpose(perm))
+        return out
+
+    def fuse_legs(self, start: int, end: int) -> "BlockSparseTensor":
+        """Legs [start, end) fused into one Incoming leg (block_sparse.rs:444-611):
+        its sectors are the fused charges of the sub-legs' sector combinations
+        (each leg's charge dualised when Outgoing), ascending, and within one
+        fused charge the combinations lie back to back in product order (first
+        sub-leg slowest).  A block's fused axis takes the row-major merge of
+        its sub-axes at the combination's offset."""
+        if not 0 <= start < end <= self.rank:
+            raise ValueError(f"fuse_legs: invalid range {start}..{end} for a rank-{self.rank} tensor")
+        if end - start == 1:
+            out = BlockSparseTensor(list(self.indices), self.flux, list(self.dirs))
+            out.blocks = {k: b.copy() for k, b in self.blocks.items()}
+            return out
+        fused, where = fuse_map(self.kind, self.indices[start:end], self.dirs[start:end])
+        out = BlockSparseTensor(self.indices[:start] + [fused] + self.indices[end:], self.flux,
+                                self.dirs[:start] + [INCOMING] + self.dirs[end:])
+        for qns, blk in self.iter_blocks():
+            fq, off = where[tuple(qns[start:end])]
+            new_q = list(qns[:start]) + [fq] + list(qns[end:])
+            key = key_pack(self.kind, new_q)
+            dst = out.blocks.get(key)
+            if dst is None:
+                dst = out.blocks[key] = np.zeros(out.block_shape(new_q))
+            d = blk.shape
+            width = int(np.prod(d[start:end]))
+            dst[(slice(None),) * start + (slice(off, off + width),)] = blk.reshape(d[:start] + (width,) + d[end:])
+        return out
+
+    def split_leg(self, leg: int, original_indices, original_dirs) -> "BlockSparseTensor":
+        """The inverse of fuse_legs (block_sparse.rs:622-793): leg `leg` split
+        back into sub-legs with these QIndices and directions; every
+        combination of sub-sectors that fuses to a stored block's charge
+        becomes a block of its own (zero where the fused block held zeros)."""
+        if not 0 <= leg < self.rank:
+            raise ValueError(f"split_leg: leg {leg} out of range")
+        original_indices, original_dirs = list(original_indices), list(original_dirs)
+        if len(original_indices) != len(original_dirs):
+            raise ValueError("split_leg: indices and directions length mismatch")
+        if len(original_indices) <= 1:
+            out = BlockSparseTensor(list(self.indices), self.flux, list(self.dirs))
+            out.blocks = {k: b.copy() for k, b in self.blocks.items()}
+            return out
+        _, where = fuse_map(self.kind, original_indices, original_dirs)
+        parts = {}
+        for sub, (fq, off) in where.items():
+            parts.setdefault(fq, []).append((sub, off))
+        out = BlockSparseTensor(self.indices[:leg] + original_indices + self.indices[leg + 1:], self.flux,
+                                self.dirs[:leg] + original_dirs + self.dirs[leg + 1:])
+        for qns, blk in self.iter_blocks():
+            for sub, off in parts.get(tuple(qns[leg]), []):
+                dims = tuple(ix.dim_of(q) for ix, q in zip(original_indices, sub))
+                width = int(np.prod(dims))
+                piece = blk[(slice(None),) * leg + (slice(off, off + width),)]
+                new_q = list(qns[:leg]) + list(sub) + list(qns[leg + 1:])
+                out.blocks[key_pack(self.kind, new_q)] = np.ascontiguousarray(piece).reshape(
+                    blk.shape[:leg] + dims + blk.shape[leg + 1:])
+        return out
+
+
+def fuse_map(kind: int, indices, dirs):
+    """The fused leg of `indices` (with their directions) and where each
+    combination of sub-sector charges lands in it: (QIndex, {charges tuple:
+    (fused charge, offset)}), the layout fuse_legs and split_leg share."""
+    combos = [((), identity(kind), 1)]
+    for ix, d in zip(indices, dirs):
+        combos = [(qs + (q,), fuse(kind, part, q if d == INCOMING else dual(kind, q)), dim * n)
+                  for qs, part, dim in combos for q, n in ix.sectors]
+    groups = {}
+    for qs, fq, dim in combos:
+        groups.setdefault(fq, []).append((qs, dim))
+    sectors, where = [], {}
+    for fq in sorted(groups):
+        off = 0
+        for qs, dim in groups[fq]:
+            where[qs] = (fq, off)
+            off += dim
+        sectors.append((fq, off))
+    return QIndex(kind, sectors), where
