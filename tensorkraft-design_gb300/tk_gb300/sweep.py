@@ -840,6 +840,23 @@ def _plan_to_site(kind, psi: np.ndarray, keys, offs, legs) -> dict:
     return out
 
 
+def mps_energy(model, sites: list, bonds: list, device: int = 0) -> complex:
+    """<psi|H|psi> of a block-sparse device MPS under the model's chain MPO
+    (mps_energy, tk-dmrg/src/mps/mod.rs:277-337): the left environment grown
+    from the 1x1x1 boundary across every site by tk_env_grow_left (the growth
+    the sweeps use), then the trace of the last environment over its bra = ket
+    index and MPO channel.  Not divided by <psi|psi>, as in the reference; the
+    value keeps its sign and phase (the reference returns its modulus).
+    Returns a float for a real MPS, else a complex number."""
+    W = model.chain(len(sites)).tensors
+    env = DeviceEnv.boundary(model.kind, bonds[0], W[0].indices[2], device)
+    for A, Wi in zip(sites, W):
+        env = grow_left(env, A, Wi, device=device)
+    T = env.to_dense()
+    e = sum(T[i, w, i] for i in range(min(T.shape[0], T.shape[2])) for w in range(T.shape[1]))
+    return complex(e) if np.iscomplexobj(T) else float(e)
+
+
 def mps_overlap(bra: list, ket: list) -> complex:
     """<bra|ket> of two block-sparse MPS on the same sites (bond bases may differ):
     the left transfer matrix is kept per bond charge, E_q (D_q^bra x D_q^ket), and

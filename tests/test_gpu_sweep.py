@@ -184,3 +184,23 @@ def test_device_sweeps_split_matches_fp64(lib_built):
             assert rec.fp64_matvecs < rec.matvecs
     assert abs(e[PREC_FP64] - e[PREC_BF16X3]) < 1e-10
     assert abs(e[PREC_FP64] - ed_heisenberg(10)) < 1e-9
+
+
+def test_mps_energy_matches_the_dense_contraction_and_the_sweep(lib_built):
+    """mps_energy (mps/mod.rs:277-337) on device site tensors: against the
+    dense host transfer (dmrg.grow_left over dense tensors) for a random
+    MPS, and equal to the last two-site eigenvalue after an untruncated
+    FP64 sweep (the state is then the normalised ground-state estimate)."""
+    n = 8
+    m, mps = _chain("heisenberg", n, 16, seed=6)
+    sites = _sites(m, mps)
+    W = m.chain(n).tensors
+    L = np.ones((1, 1, 1))
+    for i in range(n):
+        L = dmrg.grow_left(L, mps.tensors[i], W[i].to_dense())
+    e = sweep.mps_energy(m, sites, mps.bonds)
+    assert isinstance(e, float)
+    assert abs(e - float(L[0, 0, 0])) < 1e-12 * max(1.0, abs(float(L[0, 0, 0])))
+    dev = sweep.DeviceDMRG.from_dense_mps(m, mps, precision=PREC_FP64, solver="davidson", tol=1e-11)
+    rec = dev.run(16, 1)
+    assert abs(sweep.mps_energy(m, dev.sites, dev.bonds) - rec.energies[-1]) < 1e-9
