@@ -552,13 +552,16 @@ def split_two_site(kind, psi: np.ndarray, keys, offs, legs, max_bond: int, cutof
     if svd_charges:
         # the singular values (and vectors) of those charges from an SVD of M_q itself,
         # as truncate_svd takes them (truncation/mod.rs:68 through svd_truncated)
-        def svd(bi):
-            return bi, np.linalg.svd(M[charges[bi]], full_matrices=False)
+        def cost(bi):
+            m_, n_ = M[charges[bi]].shape
+            return m_ * n_ * min(m_, n_)
 
-        with _SingleThreadBlas():
-            for bi, (U, s, Vh) in _pool().map(svd, svd_charges):
-                svs[bi] = s
-                eig[charges[bi]] = (U, s, Vh)
+        todo = sorted(svd_charges, key=lambda bi: -cost(bi))
+        done = _factor_blocks(lambda bi: M[charges[bi]], todo, [cost(bi) for bi in todo])
+        for bi in todo:
+            U, s, Vh = done[bi]
+            svs[bi] = s
+            eig[charges[bi]] = (U, s, Vh)
     # every singular value of every charge, ordered by (-sigma, charge, position)
     sv = np.concatenate(svs) if svs else np.zeros(0)
     sv_charge = np.repeat(np.arange(len(svs)), [len(x) for x in svs])
